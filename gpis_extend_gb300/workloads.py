@@ -1,0 +1,164 @@
+"""Seeded synthetic flight workloads.
+
+The sphere workload: origins uniform on a radius-3 sphere, each aimed at a
+uniform point of the unit ball, clipped to the cube |x|,|y|,|z| <= 1.5 (the
+bounding primitive that carries the medium), through the field whose mean is
+the signed distance to the unit sphere.  The same generator feeds the GPU
+path, the oracle and the benchmark, so every consumer sees identical inputs.
+
+Random numbers come from a counter-based generator: value(seed, index, dim)
+is a splitmix64 finaliser of a linear combination of the three, so any
+subset of flights can be regenerated independently.
+"""
+import numpy as np
+
+from . import abi
+
+M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _mix64(x):
+    x = x.astype(np.uint64)
+    x ^= x >> np.uint64(30)
+    x *= np.uint64(0xBF58476D1CE4E5B9)
+    x ^= x >> np.uint64(27)
+    x *= np.uint64(0x94D049BB133111EB)
+    x ^= x >> np.uint64(31)
+    return x
+
+
+def counter_uniform(seed, index, dim):
+    """U[0,1) doubles (53-bit) from (seed, index, dim)."""
+    with np.errstate(over="ignore"):
+        idx = np.asarray(index, np.uint64)
+        x = (np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15)
+             + idx * np.uint64(0xD1B54A32D192ED03)
+             + np.uint64(dim) * np.uint64(0x8CB92BA72F3D8DD7)
+             + np.uint64(0x632BE59BD9B4E019))
+        x = _mix64(x)
+    return (x >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def counter_float32_unit(seed, index, dim):
+    """U[0,1) float32 values from 24 high bits (never rounds up to 1)."""
+    u = counter_uniform(seed, index, dim)
+    return (np.floor(u * 16777216.0) / 16777216.0).astype(np.float32)
+
+
+def _unit_sphere(u, v):
+    z = 1.0 - 2.0 * u
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    phi = 2.0 * np.pi * v
+    return np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=-1)
+
+
+def clip_to_cube(o, d, half):
+    """Slab intersection of rays o + t d with the cube [-half, half]^3 (float64)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        inv = 1.0 / d
+        t0 = (-half - o) * inv
+        t1 = (half - o) * inv
+    tmin = np.max(np.minimum(t0, t1), axis=-1)
+    tmax = np.min(np.maximum(t0, t1), axis=-1)
+    return tmin, tmax
+
+
+def sphere_medium(one_d=True, context=abi.CTX_RENEWAL_PLUS, sigma=0.05, length_scale=0.1,
+                  impulse_density=8.0, seed=1, step_size=0.01, min_step=8, **kw):
+    """The stationary SE field over the unit-sphere SDF: sigma 0.05, l 0.1, localScale 3,
+    8 impulses per cell, cell hash seeded 1; 1D sampling with Renewal+ by default
+    (the batched-flight microbenchmark), 3D world-space noise with Renewal for the
+    image configuration."""
+    return abi.make_medium(sigma=sigma, length_scale=length_scale, kernel_scale=3.0,
+                           impulse_density=impulse_density, seed=seed, one_d_sampling=int(one_d),
+                           correlation_context=context, step_size=step_size, min_step=min_step,
+                           mean_kind=abi.MEAN_SPHERE, mean_params=(0, 0, 0, 1),
+                           sigma_s=0.8, sigma_a=0.2, **kw)
+
+
+def pss_seeds(desc, pss, scene_seed=1):
+    """Vectorised noise/normal seeds (computeSeed / prepareGpisSegment formulas)."""
+    from .hashing import xxhash32_4, xxhash32_1
+    pss = np.asarray(pss, np.uint32)
+    w = pss[:, 3].copy()
+    if desc.correlation_context == abi.CTX_GLOBAL:
+        w[:] = 0
+    scene = xxhash32_1(np.full(len(pss), scene_seed, np.uint32))
+    with np.errstate(over="ignore"):
+        noise = np.full(len(pss), desc.seed, np.uint32)
+        if not desc.single_realization:
+            noise = noise + xxhash32_4(pss[:, 0], pss[:, 1], pss[:, 2], w) + scene
+        normal = xxhash32_4(pss[:, 0], pss[:, 1], pss[:, 2], pss[:, 3]) + scene + np.uint32(1)
+    return noise.astype(np.uint32), normal.astype(np.uint32)
+
+
+def sphere_flights(n, desc, seed=7, half=1.5, bounce=0, scene_seed=1):
+    """Primary flights of the sphere workload: returns a FlightBatch of n flights.
+
+    Origin = entry point of the ray into the cube, nearT = 0, farT = chord length;
+    jitter from the same counter stream; path coordinates pss = (i mod 2048,
+    i div 2048, 0, bounce)."""
+    i = np.arange(n, dtype=np.uint64)
+    o = 3.0 * _unit_sphere(counter_uniform(seed, i, 0), counter_uniform(seed, i, 1))
+    tgt = _unit_sphere(counter_uniform(seed, i, 2), counter_uniform(seed, i, 3))
+    tgt *= np.cbrt(counter_uniform(seed, i, 4))[:, None]
+    d = tgt - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d32 = d.astype(np.float32)
+    tmin, tmax = clip_to_cube(o, d, half)
+    entry = (o + d * tmin[:, None]).astype(np.float32)
+    # pull the entry point onto the cube face exactly where rounding pushed it outside
+    entry = np.clip(entry, -half, half).astype(np.float32)
+    b = abi.FlightBatch(n)
+    b.origin_near[:, :3] = entry
+    b.origin_near[:, 3] = 0.0
+    b.dir_far[:, :3] = d32
+    b.dir_far[:, 3] = (tmax - tmin).astype(np.float32)
+    pss = np.stack([(i % 2048).astype(np.uint32), (i // 2048).astype(np.uint32),
+                    np.zeros(n, np.uint32), np.full(n, bounce, np.uint32)], axis=1)
+    ns, nm = pss_seeds(desc, pss, scene_seed)
+    b.seeds[:, 0] = ns
+    b.seeds[:, 1] = nm
+    b.seeds[:, 2] = abi.FLAG_FIRST_SCATTER
+    b.set_jitter(counter_float32_unit(seed, i, 5))
+    b.pss = pss
+    return b
+
+
+def secondary_flights(primary, rec, desc, seed=7, half=1.5, scene_seed=1):
+    """Conditioned secondary flights from the hits of a primary pass: origin = hit
+    point, direction = mirror reflection about the sampled normal, prevValue = 0,
+    prevGradient = sampled gradient (Renewal+ birth), bounce = 1.  Returns
+    (batch, index of the primary flight of each secondary flight)."""
+    res = abi.unpack_results(rec)
+    ok = res["hit"] & (res["status"] == abi.FLIGHT_OK)
+    g = res["grad"].astype(np.float64)
+    gn = np.linalg.norm(g, axis=1)
+    ok &= np.isfinite(gn) & (gn > 1e-12)
+    idx = np.nonzero(ok)[0]
+    o = primary.origin_near[idx, :3].astype(np.float64)
+    d = primary.dir_far[idx, :3].astype(np.float64)
+    t = res["t"][idx].astype(np.float64)
+    p = o + d * t[:, None]
+    nrm = g[idx] / gn[idx, None]
+    r = d - 2.0 * np.sum(d * nrm, axis=1, keepdims=True) * nrm
+    r /= np.linalg.norm(r, axis=1, keepdims=True)
+    p = np.clip(p, -half, half)
+    _, tmax = clip_to_cube(p, r, half)
+    b = abi.FlightBatch(len(idx))
+    b.origin_near[:, :3] = p.astype(np.float32)
+    b.origin_near[:, 3] = 0.0
+    b.dir_far[:, :3] = r.astype(np.float32)
+    b.dir_far[:, 3] = np.maximum(tmax, 1e-4).astype(np.float32)
+    i = idx.astype(np.uint64)
+    pss = np.stack([(i % 2048).astype(np.uint32), (i // 2048).astype(np.uint32),
+                    np.zeros(len(idx), np.uint32), np.ones(len(idx), np.uint32)], axis=1)
+    ns, nm = pss_seeds(desc, pss, scene_seed)
+    b.seeds[:, 0] = ns
+    b.seeds[:, 1] = nm
+    b.seeds[:, 2] = 0
+    b.set_jitter(counter_float32_unit(seed, i, 6))
+    b.prev[:, 0] = 0.0
+    b.prev[:, 1:4] = res["grad"][idx]
+    b.pss = pss
+    return b, idx

@@ -1,0 +1,239 @@
+/*
+ * gpis.h -- C ABI of the GB300 GPIS ray-flight library (libgpis_gb300.so).
+ *
+ * One "ray-flight" is one sparse-convolution-noise medium segment query:
+ * Renewal / Renewal+ conditioning at the segment origin, the fixed-step march
+ * for the first sign change of the field, the regula-falsi back-off
+ * refinement, and the gradient sample at the end point.  It is the unit of
+ * work behind SparseConvolutionNoiseMedium::intersectGP
+ * (src/core/media/SparseConvolutionNoiseMedium.cpp:188-347) and the
+ * GpRayBatchBackend request/reply pair
+ * (src/core/media/GpRayBatchBackend.hpp:15-40).
+ *
+ * All signatures use plain pointers and sizes.  Device pointers are CUDA
+ * device addresses; "host" entry points take ordinary (preferably pinned)
+ * host arrays.  Every function returns an int status (GPIS_OK = 0, otherwise
+ * a positive errno-style code) and gpis_last_error() describes the last
+ * failure of the calling thread.
+ *
+ * Threading: a context is not thread-safe; use one context (or one stream)
+ * per host thread.  Contexts own their device-side medium tables; callers
+ * own every flight/result buffer.
+ */
+#ifndef GPIS_GB300_H_
+#define GPIS_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GPIS_OK        0
+#define GPIS_EIO       5    /* a CUDA runtime call failed                    */
+#define GPIS_ENOMEM   12    /* device or host allocation failed             */
+#define GPIS_ENODEV   19    /* no CUDA device                               */
+#define GPIS_EINVAL   22    /* invalid argument or medium description       */
+#define GPIS_ERANGE   34    /* a size exceeds a documented maximum          */
+#define GPIS_ENOTSUP  95    /* medium feature not supported by this build   */
+
+/* ---- per-flight status (RaySegmentStatus, src/gpu/cuda/RaySegmentBatch.hpp:55-59) */
+#define GPIS_FLIGHT_OK             0u
+#define GPIS_FLIGHT_INVALID_INPUT  1u
+#define GPIS_FLIGHT_STEP_LIMIT     2u
+#define GPIS_FLIGHT_PROPOSAL_MISS  3u  /* learned proposal rejected; plain march answered */
+
+/* ---- enumerations (values equal the reference enums) ------------------- */
+/* GPCorrelationContext, src/core/math/GaussianProcess.hpp:26-31 */
+#define GPIS_CTX_GLOBAL        0u
+#define GPIS_CTX_RENEWAL_PLUS  1u
+#define GPIS_CTX_RENEWAL       2u
+#define GPIS_CTX_NONE          3u
+/* SparseConv1DSamplingScheme, src/core/media/Medium.hpp:42-46 */
+#define GPIS_SCHEME_UNI        0u
+#define GPIS_SCHEME_NEE        1u
+#define GPIS_SCHEME_MIS        2u
+
+/* Mean functions (src/core/math/GPFunctions.hpp:915-996, GPFunctions.cpp:165-299). */
+#define GPIS_MEAN_SPHERE       0u  /* |p-c| - r            params: cx cy cz r            */
+#define GPIS_MEAN_HOMOGENEOUS  1u  /* offset               params: offset                */
+#define GPIS_MEAN_GRID         2u  /* dense trilinear grid (TabulatedMean baked to a grid) */
+#define GPIS_MEAN_PLANE        3u  /* n.p - d              params: nx ny nz d            */
+#define GPIS_MEAN_TORUS        4u  /* torus about y        params: cx cy cz R r          */
+#define GPIS_MEAN_TORUS_PLANE  5u  /* min(torus, y - h)    params: cx cy cz R r h; GP id 0 torus, 1 plane */
+
+/* Length-scale fields of a nonstationary SE covariance
+ * (ProceduralNonstationaryCovariance, src/core/math/GPFunctions.cpp:1600-1758). */
+#define GPIS_LS_CONSTANT       0u  /* ls(p) = 1                                       */
+#define GPIS_LS_SINCOS         1u  /* ls(p) = a + b*sin(fx*x)*cos(fz*z); ls_max given  */
+
+/* Flight flag bits (word 2 of the seed stream). */
+#define GPIS_FLAG_FIRST_SCATTER  1u  /* no preceding GPIS event: no conditioning      */
+#define GPIS_FLAG_SHADOW         2u  /* transmittance query: no gradient on a miss     */
+
+/* ---- dense mean grid (HostMeanGrid, src/gpu/cuda/RaySegmentBatch.hpp:21-30) */
+typedef struct gpis_mean_grid {
+    const float *voxels;        /* host array, x fastest, then y, then z          */
+    int32_t origin[3];
+    int32_t dims[3];            /* each >= 2                                     */
+    float world_to_index[12];   /* row-major 3x4 affine                          */
+    float clamp_min[3];
+    float clamp_max[3];
+    float offset;               /* mean = (trilinear + offset) * scale            */
+    float scale;
+} gpis_mean_grid;
+
+/* ---- medium description ------------------------------------------------
+ * Field names follow the scene-JSON keys of the "sparse_conv_noise" medium
+ * (SparseConvolutionNoiseMedium::fromJson, SparseConvolutionNoiseMedium.cpp:102-118;
+ * GaussianProcessMedium::fromJson, GaussianProcessMedium.cpp:98-127) and of the
+ * squared-exponential covariance (GPFunctions.cpp:657-685).
+ * gpis_medium_desc_init() fills the reference defaults.                       */
+typedef struct gpis_medium_desc {
+    /* squared-exponential covariance */
+    float sigma;                /* "sigma" (noise amplitude)                      */
+    float length_scale;         /* "lengthScale"                                   */
+    float aniso[3];             /* "aniso" (diagonal anisotropy)                  */
+    float kernel_scale;         /* "localScale": truncation radius in conv units  */
+    /* nonstationary length scale (1.0 everywhere for GPIS_LS_CONSTANT) */
+    uint32_t ls_kind;
+    float ls_params[4];         /* a, b, fx, fz                                   */
+    float ls_max;               /* supremum of ls(p); cell size follows it        */
+    uint32_t multires;          /* 2-level multi-resolution blend (base 2.5)      */
+    /* octaves: f = mean + sum_k octave_sigma[k] * noise_k; n_octaves = 1 means the
+       single reference realization with amplitude "sigma" */
+    uint32_t n_octaves;         /* 1..4                                           */
+    float octave_sigma[4];
+    float octave_scale[4];      /* length-scale multiplier of octave k            */
+    uint32_t octave_seed[4];    /* seed offset of octave k                        */
+    /* mean */
+    uint32_t mean_kind;
+    float mean_params[8];
+    const gpis_mean_grid *grid; /* GPIS_MEAN_GRID only (host memory)             */
+    /* sparse_conv_noise keys */
+    float step_size;            /* "step_size"                                     */
+    uint32_t min_step;          /* "min_step"                                      */
+    uint32_t seed;              /* "seed" (global seed)                            */
+    float impulse_density;      /* "impulse_density" (truncated to an integer)    */
+    uint32_t single_realization;    /* "single_realization"                       */
+    uint32_t isotropic_3d_sampling; /* "isotropic_3D_sampling"                    */
+    uint32_t one_d_sampling;        /* "1D_sampling"                              */
+    uint32_t sampling_scheme;       /* "1D_sampling_scheme"                       */
+    uint32_t correlation_xy;        /* "1D_gradient_correlationXY"                */
+    /* gaussian process medium keys */
+    uint32_t correlation_context;   /* "correlation_context"                      */
+    float sigma_a, sigma_s, density;
+    /* device-side limits */
+    uint32_t max_steps;         /* march give-up bound (StepLimit); 0 = 16384     */
+    uint32_t impulse_xyz_order; /* 0: z drawn first (right-to-left argument
+                                   evaluation of next3D, GCC/MSVC x86-64);
+                                   1: x drawn first                               */
+} gpis_medium_desc;
+
+/* ---- flight streams (structure of arrays, 16-byte records) ---------------
+ * Record i of each stream belongs to flight i.  Requests follow
+ * GpRaySegmentRequest (GpRayBatchBackend.hpp:15-29).                         */
+typedef struct gpis_flight_soa {
+    const float *origin_near;   /* n x {ox, oy, oz, nearT}                         */
+    const float *dir_far;       /* n x {dx, dy, dz, farT}  (unit direction)         */
+    const uint32_t *seeds;      /* n x {noiseSeed, normalSeed, flags, jitter bits}  */
+    const float *prev;          /* n x {previousValue, gx, gy, gz} (world gradient) */
+    const uint32_t *medium;     /* n medium indices, or NULL for medium 0           */
+} gpis_flight_soa;
+
+/* Results: two 16-byte records per flight.
+ *   rec0 = {t, value, gx, gy}, rec1 = {gz, transmittance, steps(u32), status(u32)}
+ * value is 0 at a hit and the field value at farT on a miss (lastVal);
+ * (gx,gy,gz) is the sampled world gradient at the end point (at a hit, and at
+ * farT for a distance miss; previous gradient for a shadow miss).
+ * status = GPIS_FLIGHT_* | (gp_id << 8).                                     */
+typedef struct gpis_result_soa {
+    float *rec;                 /* n x 8 words                                      */
+} gpis_result_soa;
+
+/* Device counter block, summed over all flights since the last reset. */
+typedef struct gpis_counters {
+    uint64_t flights;
+    uint64_t steps;             /* march steps (field evaluations in the march)    */
+    uint64_t refine_evals;      /* field evaluations in the refinement             */
+    uint64_t hits;
+    uint64_t step_limit;
+    uint64_t invalid;
+    uint64_t cell_refills;      /* impulse-cache cell regenerations                */
+    uint64_t reserved;
+} gpis_counters;
+
+typedef struct gpis_ctx gpis_ctx;
+
+/* Reference defaults: SparseConvolutionNoiseMedium() (SparseConvolutionNoiseMedium.cpp:62-79),
+ * GaussianProcessMedium() (GaussianProcessMedium.cpp:87-96), SE covariance with
+ * localScale 3 (GPFunctions.hpp:1816) and a unit sphere mean.                 */
+void gpis_medium_desc_init(gpis_medium_desc *desc);
+
+/* Parse a Tungsten "sparse_conv_noise" medium JSON object (with an inline
+ * "gaussian_process" {"mean", "covariance"}) into desc.  Replaces
+ * SparseConvolutionNoiseMedium::fromJson for the supported subset.           */
+int gpis_medium_desc_from_json(const char *json, gpis_medium_desc *desc);
+
+/* Create a context on the current CUDA device with n_media medium tables
+ * (replaces Se1DRayBatcher::setMeanGrid + SeBatchBackend set-up,
+ * src/gpu/cuda/RaySegmentBatch.cpp:16-62, PathTracerSeBatchBackend.cpp:402-416). */
+int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out);
+void gpis_ctx_destroy(gpis_ctx *ctx);
+
+/* Asynchronous flight batch on a CUDA stream; all stream pointers are device
+ * pointers (replaces launchSe1DRaySegments, RaySegmentBatch.cu:305-331).
+ * Returns after enqueueing.  n == 0 is a successful no-op.                   */
+int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in,
+                        const gpis_result_soa *out, uint32_t n, void *cuda_stream);
+
+/* Blocking flight batch on host arrays: copies in, traces, copies out and
+ * synchronizes once (replaces Se1DRayBatcher::trace, RaySegmentBatch.hpp:124-126
+ * and GpRayBatchBackend::trace, GpRayBatchBackend.hpp:43-47).                */
+int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in,
+                            const gpis_result_soa *out, uint32_t n);
+
+/* Read (and optionally reset) the device counter block. */
+int gpis_status(gpis_ctx *ctx, gpis_counters *out, int reset);
+
+/* Seeds of a flight from its path coordinates (computeSeed,
+ * SparseConvolutionNoise.cpp:57-66, and the request seeds of
+ * prepareGpisSegment, SparseConvolutionNoiseMedium.cpp:235-238).             */
+void gpis_flight_seeds(const gpis_medium_desc *desc, const uint32_t pixel_sample_segment[4],
+                       uint32_t scene_seed, uint32_t *noise_seed, uint32_t *normal_seed);
+
+/* ---- unit-level device entry points (used by the parity tests) ---------- */
+/* Impulses of n 1D cells (cell index, seed) on the device: pos[n*k], weight[n*k],
+ * k = impulses per cell (cell1D, SparseConvolutionNoise.cpp:465-485).
+ * All pointers are device pointers; synchronous.                             */
+int gpis_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n,
+                        uint32_t impulses, float *pos, float *weight);
+/* Impulses of n 3D cells: cells = n x {i, j, k}; pos = n*k x {x,y,z}.        */
+int gpis_debug_cells_3d(const int32_t *cells, const uint32_t *seeds, uint32_t n,
+                        uint32_t impulses, uint32_t xyz_order, float *pos, float *weight);
+
+/* Field evaluation at n points (device pointers): points/dirs n x 4 floats,
+ * seeds n x 4 words as in the flight seed stream, prev n x 4 floats.  The
+ * conditioning of each point's flight is built from (origin = points of the
+ * "origins" stream) exactly as a flight would.  out = n x 4 floats
+ * {noise value (normalized), dnoise/dz (1D) or unused, field value, mean}.   */
+int gpis_debug_field(gpis_ctx *ctx, const float *origins, const float *points,
+                     const float *dirs, const uint32_t *seeds, const float *prev,
+                     uint32_t n, float *out);
+
+/* Elementwise squared-exponential splat (launchKernel1D / seSplat1D,
+ * src/gpu/cuda/Kernel1D.hpp:26-29, SeSplat1D.cu:12-44): device pointers,
+ * asynchronous on the stream; local_scale must be finite and > 0.            */
+int gpis_se_splat_1d(const float *queries, const float *centers, float *values,
+                     float *derivatives, size_t count, float local_scale, void *cuda_stream);
+
+/* Last error message of the calling thread ("" when none). */
+const char *gpis_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPIS_GB300_H_ */

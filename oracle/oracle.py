@@ -1,0 +1,181 @@
+"""ctypes wrapper of the oracle (oracle/gpis_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by
+bench.py's CPU-baseline leg, always as the checker.  Builds
+oracle/_build/libgpis_oracle.so on first use (gcc, a few seconds).
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+from gpis_extend_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgpis_oracle.so")
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (no reference sources needed)."""
+    src = [os.path.join(HERE, "gpis_oracle.c"), os.path.join(HERE, "gpis_oracle.h"),
+           os.path.join(os.path.dirname(HERE), "include", "gpis.h")]
+    stale = not os.path.exists(LIB_PATH) or any(
+        os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in src)
+    if force or stale:
+        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(LIB_PATH)
+            u32, vp, c_int = ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int
+            P = ctypes.POINTER
+            M = P(abi.MediumDesc)
+            sigs = {
+                "gor_xxhash32_1": (u32, [u32]),
+                "gor_xxhash32_2": (u32, [u32, u32]),
+                "gor_xxhash32_4": (u32, [u32, u32, u32, u32]),
+                "gor_pcg_stream": (None, [ctypes.c_uint64, u32, vp, vp]),
+                "gor_normal_pair": (None, [ctypes.c_uint64, u32, vp]),
+                "gor_cell_1d": (None, [u32, u32, u32, vp, vp]),
+                "gor_cell_3d": (None, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, u32, u32, u32, vp, vp]),
+                "gor_field": (c_int, [M, vp, vp, vp, vp, vp, c_int, vp]),
+                "gor_gradient": (c_int, [M, vp, vp, vp, ctypes.c_float, vp, vp, vp]),
+                "gor_trace_flights": (c_int, [M, c_int, P(abi.FlightSoA), P(abi.ResultSoA), u32, c_int]),
+                "gor_flight_seeds": (None, [M, vp, u32, vp, vp]),
+                "gor_transverse_moments": (c_int, [M, vp, vp, vp, vp, vp, c_int, vp, vp]),
+                "gor_nee": (c_int, [M, vp, vp, vp, vp, ctypes.c_float, vp, vp, vp, vp]),
+                "gor_sampling_scheme": (c_int, [M, vp, vp, vp]),
+                "gor_se_splat_1d": (None, [vp, vp, u32, ctypes.c_float, vp, vp]),
+            }
+            for k, (r, a) in sigs.items():
+                f = getattr(L, k)
+                f.restype = r
+                f.argtypes = a
+            _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data
+
+
+def _f3(v):
+    return np.ascontiguousarray(v, np.float32).reshape(-1)
+
+
+def trace_flights(media, batch, n_threads=0):
+    """Float-mode flights on the CPU; returns the (n, 8) result records."""
+    if isinstance(media, abi.MediumDesc):
+        media = [media]
+    arr = (abi.MediumDesc * len(media))(*media)
+    rec = abi.new_results(batch.n)
+    rc = lib().gor_trace_flights(arr, len(media), ctypes.byref(batch.soa()),
+                                 ctypes.byref(abi.result_soa(rec)), batch.n, n_threads)
+    if rc:
+        raise abi.GpisError(f"oracle trace failed: {rc}", rc)
+    return rec
+
+
+def field(desc, origin, direction, p, seeds, prev=(0, 0, 0, 0), double_mode=False):
+    o, d, q = _f3(origin), _f3(direction), _f3(p)
+    s = np.ascontiguousarray(seeds, np.uint32)
+    pv = np.ascontiguousarray(prev, np.float32)
+    out = np.zeros(6, np.float64)
+    rc = lib().gor_field(ctypes.byref(desc), _p(o), _p(d), _p(q), _p(s), _p(pv), int(double_mode), _p(out))
+    if rc:
+        raise abi.GpisError(f"oracle field failed: {rc}", rc)
+    return out
+
+
+def gradient(desc, origin, direction, p, t_segment, seeds, prev=(0, 0, 0, 0)):
+    o, d, q = _f3(origin), _f3(direction), _f3(p)
+    s = np.ascontiguousarray(seeds, np.uint32)
+    pv = np.ascontiguousarray(prev, np.float32)
+    out = np.zeros(3, np.float32)
+    rc = lib().gor_gradient(ctypes.byref(desc), _p(o), _p(d), _p(q), float(t_segment), _p(s), _p(pv), _p(out))
+    if rc:
+        raise abi.GpisError(f"oracle gradient failed: {rc}", rc)
+    return out
+
+
+def transverse_moments(desc, origin, direction, p, seeds, prev, conditioning=True):
+    o, d, q = _f3(origin), _f3(direction), _f3(p)
+    s = np.ascontiguousarray(seeds, np.uint32)
+    pv = np.ascontiguousarray(prev, np.float32)
+    mean = np.zeros(2, np.float64)
+    var = np.zeros(1, np.float64)
+    ok = lib().gor_transverse_moments(ctypes.byref(desc), _p(o), _p(d), _p(q), _p(s), _p(pv),
+                                      int(conditioning), _p(mean), _p(var))
+    return bool(ok), mean, float(var[0])
+
+
+def nee(desc, origin, direction, p, normal, t_segment, seeds, prev):
+    o, d, q, nr = _f3(origin), _f3(direction), _f3(p), _f3(normal)
+    s = np.ascontiguousarray(seeds, np.uint32)
+    pv = np.ascontiguousarray(prev, np.float32)
+    pdf = np.zeros(1, np.float32)
+    g = np.zeros(3, np.float32)
+    rc = lib().gor_nee(ctypes.byref(desc), _p(o), _p(d), _p(q), _p(nr), float(t_segment), _p(s),
+                       _p(pv), _p(pdf), _p(g))
+    if rc:
+        raise abi.GpisError(f"oracle nee failed: {rc}", rc)
+    return float(pdf[0]), g
+
+
+def sampling_scheme(desc, origin, p, seeds):
+    o, q = _f3(origin), _f3(p)
+    s = np.ascontiguousarray(seeds, np.uint32)
+    return lib().gor_sampling_scheme(ctypes.byref(desc), _p(o), _p(q), _p(s))
+
+
+def cell_1d(cell, seed, impulses):
+    pos = np.zeros(impulses, np.float32)
+    w = np.zeros(impulses, np.float32)
+    lib().gor_cell_1d(cell & 0xFFFFFFFF, seed & 0xFFFFFFFF, impulses, _p(pos), _p(w))
+    return pos, w
+
+
+def cell_3d(i, j, k, seed, impulses, order=0):
+    pos = np.zeros((impulses, 3), np.float32)
+    w = np.zeros(impulses, np.float32)
+    lib().gor_cell_3d(i, j, k, seed & 0xFFFFFFFF, impulses, order, _p(pos), _p(w))
+    return pos, w
+
+
+def pcg_stream(state, n):
+    f = np.zeros(n, np.float32)
+    r = np.zeros(n, np.uint32)
+    lib().gor_pcg_stream(state, n, _p(f), _p(r))
+    return f, r
+
+
+def normal_pairs(state, pairs):
+    out = np.zeros(2 * pairs, np.float64)
+    lib().gor_normal_pair(state, pairs, _p(out))
+    return out
+
+
+def flight_seeds(desc, pss, scene_seed):
+    p = np.ascontiguousarray(pss, np.uint32)
+    a = np.zeros(1, np.uint32)
+    b = np.zeros(1, np.uint32)
+    lib().gor_flight_seeds(ctypes.byref(desc), _p(p), scene_seed, _p(a), _p(b))
+    return int(a[0]), int(b[0])
+
+
+def se_splat_1d(q, c, scale):
+    q = np.ascontiguousarray(q, np.float32)
+    c = np.ascontiguousarray(c, np.float32)
+    v = np.zeros(len(q), np.float64)
+    d = np.zeros(len(q), np.float64)
+    lib().gor_se_splat_1d(_p(q), _p(c), len(q), float(scale), _p(v), _p(d))
+    return v, d
