@@ -1,0 +1,327 @@
+// device_common.cuh -- device-side building blocks of the GPIS flight kernels:
+// the medium table, cell hash, jump-ahead PCG32, tangent frame, means and the
+// float-float march parameter.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gpis {
+
+// Maximum impulses per cell the library accepts (RaySegmentBatch.cu:317-318 caps
+// impulseDensity at 64).
+constexpr int kMaxImpulses = 64;
+// PCG draws a cell can consume: 2 warm-up + 4 per 3D impulse.
+constexpr int kMaxDraws = 2 + 4 * kMaxImpulses;
+
+// Medium flags.
+enum : uint32_t {
+    MF_ONE_D = 1u << 0,          // 1D sampling in isotropic ray space
+    MF_COND = 1u << 1,           // Renewal / Renewal+ conditioning active
+    MF_RENEWAL_PLUS = 1u << 2,   // gradient conditioning
+    MF_CORR_XY = 1u << 3,        // 1D_gradient_correlationXY
+    MF_TRANSVERSE = 1u << 4,     // exact SE transverse law applies
+    MF_XYZ_ORDER = 1u << 5,      // next3D drawn x first
+};
+
+// Per-medium constants derived on the host (all float values are rounded as the
+// reference's float expressions round them).
+struct DevMedium {
+    float sigma;            // noise amplitude
+    float l_inv[3];         // world -> isotropic (diagonal of _world_to_local)
+    float l_aniso[3];       // isotropic -> world (diagonal of _local_to_world)
+    float kr_iso;           // cell size of 1D noise in isotropic units (localScale)
+    float kr_world;         // cell size of 3D world noise
+    float inv_norm1d;       // 1 / sqrt(sparseConvNoiseVariance1D)
+    float inv_norm3d;       // 1 / sqrt(sparseConvNoiseVariance3D)
+    float kexp1d;           // exp(-(kr*d)^2/2) = ex2(kexp1d * d * d)
+    float kexp3d[3];        // 3D splat: ex2(sum_c kexp3d[c] * (kr*d_c)^2)
+    float m3[3];            // 3D splat inverse covariance diagonal (isCov = false)
+    float m3c[3];           // 3D conditioning inverse covariance diagonal (isCov = true)
+    float d2inv3[3];        // 3D Renewal+: 1 / (-2 * 0.25 * l_inv^2)
+    uint32_t n_imp;         // impulses per cell
+    uint32_t flags;
+    uint32_t seed_pad;
+    uint32_t mean_kind;
+    float mean_params[8];
+    const float *grid;      // device voxels (GPIS_MEAN_GRID)
+    int32_t grid_origin[3];
+    int32_t grid_dims[3];
+    float grid_w2i[12];
+    float grid_cmin[3];
+    float grid_cmax[3];
+    float grid_offset;
+    float grid_scale;
+    float step_size;
+    uint32_t min_step;
+    uint32_t max_steps;
+    uint32_t scheme;
+};
+
+struct PcgJump {
+    uint32_t alo, ahi;      // multiplier M^k
+    uint32_t clo, chi;      // increment sum_{j<k} M^j
+};
+
+// ---- hashing (MathUtil::xxhash32, src/core/math/MathUtil.hpp:179-224) -------
+__device__ __forceinline__ uint32_t rotl17(uint32_t h) { return __funnelshift_l(h, h, 17); }
+
+__device__ __forceinline__ uint32_t xx_finish(uint32_t h)
+{
+    h = 2246822519u * (h ^ (h >> 15));
+    h = 3266489917u * (h ^ (h >> 13));
+    return h ^ (h >> 16);
+}
+
+__device__ __forceinline__ uint32_t xxhash2(uint32_t x, uint32_t y)
+{
+    uint32_t h = y + 374761393u + x * 3266489917u;
+    h = 668265263u * rotl17(h);
+    return xx_finish(h);
+}
+
+__device__ __forceinline__ uint32_t xxhash4(uint32_t x, uint32_t y, uint32_t z, uint32_t w)
+{
+    uint32_t h = w + 374761393u + x * 3266489917u;
+    h = 668265263u * rotl17(h);
+    h += y * 3266489917u;
+    h = 668265263u * rotl17(h);
+    h += z * 3266489917u;
+    h = 668265263u * rotl17(h);
+    return xx_finish(h);
+}
+
+// ---- PCG32 output of a 64-bit state (UniformSampler::nextI, UniformSampler.hpp:41-48)
+__device__ __forceinline__ uint32_t pcg_output(uint32_t lo, uint32_t hi)
+{
+    // ((old >> 18) ^ old) >> 27 truncated to 32 bits == (old >> 27) ^ (old >> 45)
+    const uint32_t xs = __funnelshift_r(lo, hi, 27) ^ (hi >> 13);
+    return __funnelshift_r(xs, xs, hi >> 27);
+}
+
+// State k of the stream that set_state(s) starts: M^k * s + C_k (s < 2^32).
+__device__ __forceinline__ uint32_t pcg_draw(const PcgJump &j, uint32_t s)
+{
+    const uint64_t prod = (uint64_t)j.alo * s + (((uint64_t)j.chi << 32) | j.clo);
+    const uint32_t lo = (uint32_t)prod;
+    const uint32_t hi = (uint32_t)(prod >> 32) + j.ahi * s;
+    return pcg_output(lo, hi);
+}
+
+// BitManip::normalizedUint (BitManip.hpp:47-50)
+__device__ __forceinline__ float unit_float(uint32_t r)
+{
+    return __fsub_rn(__uint_as_float((r >> 9) | 0x3F800000u), 1.0f);
+}
+
+// ---- exact IEEE float helpers (no contraction) --------------------------------
+__device__ __forceinline__ float dot3_rn(float a0, float a1, float a2, float b0, float b1, float b2)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)), __fmul_rn(a2, b2));
+}
+
+__device__ __forceinline__ void normalize3_rn(float &x, float &y, float &z)
+{
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3_rn(x, y, z, x, y, z)));
+    x = __fmul_rn(x, inv);
+    y = __fmul_rn(y, inv);
+    z = __fmul_rn(z, inv);
+}
+
+// TangentFrame(n) (TangentFrame.hpp:74-98), IEEE-rounded like the reference.
+struct Frame {
+    float n[3], t[3], b[3];
+};
+
+__device__ __forceinline__ void make_frame(float nx, float ny, float nz, Frame &f)
+{
+    normalize3_rn(nx, ny, nz);
+    f.n[0] = nx; f.n[1] = ny; f.n[2] = nz;
+    const float sign = copysignf(1.0f, nz);
+    const float a = __fdiv_rn(-1.0f, __fadd_rn(sign, nz));
+    const float b = __fmul_rn(__fmul_rn(nx, ny), a);
+    float tx = __fadd_rn(1.0f, __fmul_rn(__fmul_rn(__fmul_rn(sign, nx), nx), a));
+    float ty = __fmul_rn(sign, b);
+    float tz = -__fmul_rn(sign, nx);
+    float bx = b;
+    float by = __fadd_rn(sign, __fmul_rn(__fmul_rn(ny, ny), a));
+    float bz = -ny;
+    normalize3_rn(tx, ty, tz);
+    normalize3_rn(bx, by, bz);
+    f.t[0] = tx; f.t[1] = ty; f.t[2] = tz;
+    f.b[0] = bx; f.b[1] = by; f.b[2] = bz;
+}
+
+// ---- float-float march parameter ----------------------------------------------
+// t = hi + lo represents the reference's double t exactly for the march grid
+// t_k = t0 + k*step (t0, step floats).
+__device__ __forceinline__ float two_sum(float a, float b, float &err)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float b)
+{
+    float e;
+    const float s = two_sum(hi, b, e);
+    const float l = __fadd_rn(lo, e);
+    hi = __fadd_rn(s, l);
+    lo = __fsub_rn(l, __fsub_rn(hi, s));
+}
+
+// float(o + t*d) with o, d floats and t = hi + lo, rounded as the double
+// expression Vec3f(Vec3d(o) + t * Vec3d(d)).
+__device__ __forceinline__ float ff_point(float o, float d, float hi, float lo)
+{
+    const float a = __fmul_rn(hi, d);
+    const float ae = __fmaf_rn(hi, d, -a);
+    const float b = __fmul_rn(lo, d);
+    float se;
+    const float s = two_sum(o, a, se);
+    const float r = __fadd_rn(se, __fadd_rn(ae, b));
+    return __fadd_rn(s, r);
+}
+
+// double-precision point (refinement and gradient points are rare).
+__device__ __forceinline__ float dd_point(float o, float d, double t)
+{
+    return (float)__dadd_rn((double)o, __dmul_rn(t, (double)d));
+}
+
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// ---- means (MeanFunction::mean / dmean_da) -------------------------------------
+__device__ __forceinline__ float grid_voxel(const DevMedium &m, int x, int y, int z)
+{
+    x = min(max(x - m.grid_origin[0], 0), m.grid_dims[0] - 1);
+    y = min(max(y - m.grid_origin[1], 0), m.grid_dims[1] - 1);
+    z = min(max(z - m.grid_origin[2], 0), m.grid_dims[2] - 1);
+    const size_t idx = ((size_t)z * (size_t)m.grid_dims[1] + (size_t)y) * (size_t)m.grid_dims[0] + (size_t)x;
+    return __ldg(m.grid + idx);
+}
+
+// Dense trilinear grid mean (RaySegmentBatch.cu:73-95 semantics).
+__device__ __forceinline__ float grid_mean(const DevMedium &m, float px, float py, float pz)
+{
+    float q[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        float v = __fmul_rn(m.grid_w2i[4 * r + 0], px);
+        v = __fadd_rn(v, __fmul_rn(m.grid_w2i[4 * r + 1], py));
+        v = __fadd_rn(v, __fmul_rn(m.grid_w2i[4 * r + 2], pz));
+        v = __fadd_rn(v, m.grid_w2i[4 * r + 3]);
+        q[r] = fminf(fmaxf(v, m.grid_cmin[r]), m.grid_cmax[r]);
+    }
+    const int x = (int)floorf(q[0]), y = (int)floorf(q[1]), z = (int)floorf(q[2]);
+    const float fx = q[0] - (float)x, fy = q[1] - (float)y, fz = q[2] - (float)z;
+    float layer[2];
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz) {
+        float row[2];
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+            const float a = grid_voxel(m, x, y + dy, z + dz);
+            const float b = grid_voxel(m, x + 1, y + dy, z + dz);
+            row[dy] = a + fx * (b - a);
+        }
+        layer[dz] = row[0] + fy * (row[1] - row[0]);
+    }
+    return (layer[0] + fz * (layer[1] - layer[0]) + m.grid_offset) * m.grid_scale;
+}
+
+__device__ __forceinline__ float torus_sdf(const float *q, float x, float y, float z)
+{
+    x -= q[0]; y -= q[1]; z -= q[2];
+    const float rxz = sqrtf(x * x + z * z) - q[3];
+    return sqrtf(rxz * rxz + y * y) - q[4];
+}
+
+// mean_weight_space: value and GP id (0 unless the union picks its second surface).
+__device__ __forceinline__ float mean_value(const DevMedium &m, float x, float y, float z, int &id)
+{
+    const float *q = m.mean_params;
+    id = 0;
+    switch (m.mean_kind) {
+    case 0: {  // sphere
+        const float dx = x - q[0], dy = y - q[1], dz = z - q[2];
+        return sqrtf(dx * dx + dy * dy + dz * dz) - q[3];
+    }
+    case 1:
+        return q[0];
+    case 2:
+        return grid_mean(m, x, y, z);
+    case 3:
+        return q[0] * x + q[1] * y + q[2] * z - q[3];
+    case 4:
+        return torus_sdf(q, x, y, z);
+    case 5: {
+        const float t = torus_sdf(q, x, y, z);
+        const float pl = y - q[5];
+        if (pl < t) { id = 1; return pl; }
+        return t;
+    }
+    default:
+        return 0.0f;
+    }
+}
+
+// Mean gradient in double where the reference evaluates it in double.
+__device__ __forceinline__ void mean_grad(const DevMedium &m, float x, float y, float z, float g[3])
+{
+    const float *q = m.mean_params;
+    int id;
+    switch (m.mean_kind) {
+    case 0: {
+        const double dx = (double)x - q[0], dy = (double)y - q[1], dz = (double)z - q[2];
+        const double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+        g[0] = (float)(dx * inv); g[1] = (float)(dy * inv); g[2] = (float)(dz * inv);
+        return;
+    }
+    case 1:
+        g[0] = g[1] = g[2] = 0.0f;
+        return;
+    case 2: {  // TabulatedMean::dmean_da forward difference, eps 0.001 in double
+        const double eps = 0.001;
+        const float v0 = grid_mean(m, x, y, z);
+        const float vx = grid_mean(m, (float)((double)x + eps), y, z);
+        const float vy = grid_mean(m, x, (float)((double)y + eps), z);
+        const float vz = grid_mean(m, x, y, (float)((double)z + eps));
+        g[0] = (float)(((double)vx - v0) / eps);
+        g[1] = (float)(((double)vy - v0) / eps);
+        g[2] = (float)(((double)vz - v0) / eps);
+        return;
+    }
+    case 3:
+        g[0] = q[0]; g[1] = q[1]; g[2] = q[2];
+        return;
+    case 4:
+    case 5: {
+        (void)mean_value(m, x, y, z, id);
+        if (m.mean_kind == 5 && id == 1) {
+            g[0] = 0.0f; g[1] = 1.0f; g[2] = 0.0f;
+            return;
+        }
+        const float px = x - q[0], py = y - q[1], pz = z - q[2];
+        const float rxz = sqrtf(px * px + pz * pz);
+        const float s = rxz - q[3];
+        const float len = sqrtf(s * s + py * py);
+        const float dr = s / len;
+        g[0] = rxz > 0.0f ? dr * px / rxz : 0.0f;
+        g[1] = py / len;
+        g[2] = rxz > 0.0f ? dr * pz / rxz : 0.0f;
+        return;
+    }
+    default:
+        g[0] = g[1] = g[2] = 0.0f;
+    }
+}
+
+}  // namespace gpis

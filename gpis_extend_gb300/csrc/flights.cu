@@ -1,0 +1,1001 @@
+// flights.cu -- sm_103a kernels of the GPIS ray-flight path.
+//
+// One batch of flights runs as three kernels on one stream:
+//   k_prepare  Renewal / Renewal+ conditioning at the origin of every
+//              secondary flight (SparseConvolutionNoise.cpp:488-656), one thread
+//              per flight, coefficients to a scratch record;
+//   k_march    the first-sign-change march and regula-falsi back-off
+//              (SparseConvolutionNoiseMedium.cpp:287-346): persistent warps pull
+//              flights from a device work counter and refill finished lanes, so
+//              flights of very uneven length keep every lane busy; value-only
+//              field evaluations; the 1D variant keeps the impulses of the three
+//              cells around the query in registers and regenerates a cell only
+//              when the query crosses a cell boundary;
+//   k_finish   the gradient sample at the end point (evaluateGradient,
+//              SparseConvolutionNoise.cpp:133-296), one thread per flight.
+//
+// Bit-exactness: cell hashes and PCG draws are integer-exact; the march
+// parameter t is a float-float pair equal to the reference's double t; the point,
+// the isotropic transform, the ray-space coordinate and the cell decomposition
+// are evaluated op-for-op in IEEE float without contraction, so the set of
+// impulses inside the truncated kernel is the reference's.  The splat values
+// use ex2.approx and agree with an FP64 evaluation to ~1e-6 relative.
+#include <cfloat>
+#include <climits>
+
+#include "flights.cuh"
+
+namespace gpis {
+
+__constant__ PcgJump c_jump[kMaxDraws];
+
+cudaError_t upload_pcg_table()
+{
+    PcgJump h[kMaxDraws];
+    uint64_t a = 1, c = 0;
+    const uint64_t M = 6364136223846793005ULL;
+    for (int k = 0; k < kMaxDraws; ++k) {
+        h[k].alo = (uint32_t)a; h[k].ahi = (uint32_t)(a >> 32);
+        h[k].clo = (uint32_t)c; h[k].chi = (uint32_t)(c >> 32);
+        a = a * M;
+        c = c * M + 1ULL;
+    }
+    return cudaMemcpyToSymbol(c_jump, h, sizeof(h));
+}
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr float LOG2E = 1.4426950408889634f;
+
+// Conditioning kernels of the 1D Renewal(+) update (GPFunctions.cpp:850-875):
+// exp(-d^2/4), its first and second derivative and the transverse factor.
+struct Cov1D { float k0, k1, k2, k3; };
+
+__device__ __forceinline__ Cov1D cov1d(float d)
+{
+    Cov1D c;
+    c.k0 = ex2_approx((-0.25f * LOG2E) * d * d);
+    c.k1 = -0.5f * d * c.k0;
+    c.k2 = (0.25f * d * d - 0.5f) * c.k0;
+    c.k3 = -0.5f * c.k0;
+    return c;
+}
+
+// World -> isotropic ray-space direction frame of a flight.
+__device__ __forceinline__ void ray_frame(const DevMedium &m, float dx, float dy, float dz, Frame &f)
+{
+    float ix = __fmul_rn(m.l_inv[0], dx), iy = __fmul_rn(m.l_inv[1], dy), iz = __fmul_rn(m.l_inv[2], dz);
+    normalize3_rn(ix, iy, iz);
+    make_frame(ix, iy, iz, f);
+}
+
+// Isotropic ray-space coordinate p_iso_ray.z (SparseConvolutionNoise.cpp:381-384).
+__device__ __forceinline__ float ray_coord(const float *li, const float *n, float px, float py, float pz)
+{
+    return dot3_rn(n[0], n[1], n[2], __fmul_rn(li[0], px), __fmul_rn(li[1], py), __fmul_rn(li[2], pz));
+}
+
+// ---- 1D noise, generic impulse count (no cache) --------------------------------
+// Returns the raw (unnormalized) sum and its derivative w.r.t. the iso coordinate.
+template <bool DERIV>
+__device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, float &v, float &dv)
+{
+    const float tg = __fdiv_rn(z, m.kr_iso);
+    const float fl = floorf(tg);
+    const float frac = __fsub_rn(tg, fl);
+    const int ci = (int)fl;
+    float sv = 0.0f, sd = 0.0f;
+    for (int dx = -1; dx <= 1; ++dx) {
+        const float tl = __fsub_rn(frac, (float)dx);
+        const uint32_t s = xxhash2((uint32_t)(ci + dx), seed) + 1u;
+        for (uint32_t k = 0; k < m.n_imp; ++k) {
+            const float ti = unit_float(pcg_draw(c_jump[2 + 2 * k], s));
+            const uint32_t wr = pcg_draw(c_jump[3 + 2 * k], s);
+            const float tp = __fsub_rn(tl, ti);
+            if (fabsf(tp) < 1.0f) {
+                const float e = ex2_approx(m.kexp1d * (tp * tp));
+                const float w = (wr >> 31) ? 1.0f : -1.0f;
+                sv += w * e;
+                if (DERIV) sd += w * (-(m.kr_iso * tp) * e);
+            }
+        }
+    }
+    v = sv;
+    dv = sd;
+}
+
+// ---- 3D world-space noise, generic (no cache) ----------------------------------
+// Raw sum and gradient (world units), noise3D + cell3D (SparseConvolutionNoise.cpp:419-452).
+template <bool GRAD>
+__device__ void noise3d_generic(const DevMedium &m, float px, float py, float pz, uint32_t seed,
+                                float &v, float g[3])
+{
+    const float kr = m.kr_world;
+    const float p[3] = {px, py, pz};
+    float fr[3];
+    int ijk[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float q = __fdiv_rn(p[i], kr);
+        const float fl = floorf(q);
+        fr[i] = __fsub_rn(q, fl);
+        ijk[i] = (int)fl;
+    }
+    const bool xfirst = (m.flags & MF_XYZ_ORDER) != 0;
+    float sv = 0.0f, s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz) {
+                const float t0 = __fsub_rn(fr[0], (float)dx), t1 = __fsub_rn(fr[1], (float)dy),
+                            t2 = __fsub_rn(fr[2], (float)dz);
+                const uint32_t s = xxhash4((uint32_t)(ijk[2] + dz), (uint32_t)(ijk[1] + dy),
+                                           (uint32_t)(ijk[0] + dx), seed) + 1u;
+                for (uint32_t k = 0; k < m.n_imp; ++k) {
+                    const int b = 2 + 4 * (int)k;
+                    const float r0 = unit_float(pcg_draw(c_jump[b], s));
+                    const float r1 = unit_float(pcg_draw(c_jump[b + 1], s));
+                    const float r2 = unit_float(pcg_draw(c_jump[b + 2], s));
+                    const uint32_t wr = pcg_draw(c_jump[b + 3], s);
+                    const float ix = xfirst ? r0 : r2, iy = r1, iz = xfirst ? r2 : r0;
+                    const float a0 = __fsub_rn(t0, ix), a1 = __fsub_rn(t1, iy), a2 = __fsub_rn(t2, iz);
+                    const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(a0, a0), __fmul_rn(a1, a1)), __fmul_rn(a2, a2));
+                    if (l2 < 1.0f) {
+                        const float ab0 = kr * a0, ab1 = kr * a1, ab2 = kr * a2;
+                        const float e = ex2_approx(m.kexp3d[0] * ab0 * ab0 + m.kexp3d[1] * ab1 * ab1 +
+                                                   m.kexp3d[2] * ab2 * ab2);
+                        const float w = (wr >> 31) ? 1.0f : -1.0f;
+                        sv += w * e;
+                        if (GRAD) {
+                            s0 += w * (-2.0f * (ab0 * m.m3[0]) * e);
+                            s1 += w * (-2.0f * (ab1 * m.m3[1]) * e);
+                            s2 += w * (-2.0f * (ab2 * m.m3[2]) * e);
+                        }
+                    }
+                }
+            }
+    v = sv;
+    if (GRAD) { g[0] = s0; g[1] = s1; g[2] = s2; }
+}
+
+// 3D conditioning splat (value and gradient) of the coefficients c at p.
+__device__ __forceinline__ void cond3d(const DevMedium &m, const CondRec &c, const float o[3],
+                                       const float p[3], float &v, float g[3])
+{
+    float ab[3], dp[3];
+    float absq = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        ab[i] = p[i] - o[i];
+        absq += ab[i] * m.m3c[i] * ab[i];
+    }
+    const float f = ex2_approx(-LOG2E * absq);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dp[i] = -2.0f * (ab[i] * m.m3c[i]);
+    v = f * c.vs;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) g[j] = dp[j] * f * c.vs;
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+        v += dp[cc] * f * c.gs[cc];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) g[j] += (dp[cc] * dp[j] - (cc == j ? 2.0f * m.m3c[cc] : 0.0f)) * f * c.gs[cc];
+    }
+}
+
+// Box-Muller pair (Gaussian.cpp:23-35) from two PCG outputs, in float.
+__device__ __forceinline__ void normal_pair(uint32_t r1, uint32_t r2, float &z0, float &z1)
+{
+    const float u1 = unit_float(r1), u2 = unit_float(r2);
+    const float rad = sqrtf(-2.0f * logf(1.0f - u1));
+    float sn, cs;
+    sincosf(6.28318548f * u2, &sn, &cs);
+    z0 = rad * cs;
+    z1 = rad * sn;
+}
+
+// The normal-seed stream: set_state(normalSeed) then draws 2.. (after the 2 warm-ups).
+__device__ __forceinline__ void normal_draws(uint32_t seed, int pair, float &z0, float &z1)
+{
+    normal_pair(pcg_draw(c_jump[2 + 2 * pair], seed), pcg_draw(c_jump[3 + 2 * pair], seed), z0, z1);
+}
+
+// correlatedGradientMoments (SparseConvolutionNoise.cpp:13-22)
+__device__ __forceinline__ void corr_moments(float dist, float &factor, float &variance)
+{
+    const float x = 0.5f * dist * dist;
+    factor = 0.5f * expf(-0.5f * x) * (1.0f - x);
+    variance = x < 1.0f ? 0.5f * (-expm1f(-x) + expf(-x) * x * (2.0f - x)) : 0.5f - 2.0f * factor * factor;
+}
+
+struct FlightIn {
+    float o[3], d[3], near_t, far_t, jitter;
+    uint32_t noise_seed, normal_seed, flags;
+    float prev_v, prev_g[3];
+};
+
+__device__ __forceinline__ FlightIn load_flight(const FlightArgs &a, uint32_t i)
+{
+    FlightIn f;
+    const float4 on = a.origin_near[i];
+    const float4 df = a.dir_far[i];
+    const uint4 sd = a.seeds[i];
+    f.o[0] = on.x; f.o[1] = on.y; f.o[2] = on.z; f.near_t = on.w;
+    f.d[0] = df.x; f.d[1] = df.y; f.d[2] = df.z; f.far_t = df.w;
+    f.noise_seed = sd.x; f.normal_seed = sd.y; f.flags = sd.z; f.jitter = __uint_as_float(sd.w);
+    if (a.prev) {
+        const float4 pv = a.prev[i];
+        f.prev_v = pv.x; f.prev_g[0] = pv.y; f.prev_g[1] = pv.z; f.prev_g[2] = pv.w;
+    } else {
+        f.prev_v = 0.0f; f.prev_g[0] = f.prev_g[1] = f.prev_g[2] = 0.0f;
+    }
+    return f;
+}
+
+// Input validation of RaySegmentBatch.cu:198-206.
+__device__ __forceinline__ bool flight_valid(const FlightIn &f)
+{
+    const bool first = (f.flags & GPIS_FLAG_FIRST_SCATTER) != 0;
+    bool ok = isfinite(f.near_t) && isfinite(f.far_t) && f.far_t > f.near_t && isfinite(f.jitter) &&
+              f.jitter >= 0.0f && f.jitter < 1.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) ok = ok && isfinite(f.o[i]) && isfinite(f.d[i]);
+    if (!first)
+        ok = ok && isfinite(f.prev_v) && isfinite(f.prev_g[0]) && isfinite(f.prev_g[1]) && isfinite(f.prev_g[2]);
+    const float dd = f.d[0] * f.d[0] + f.d[1] * f.d[1] + f.d[2] * f.d[2];
+    return ok && fabsf(dd - 1.0f) <= 0.001f;
+}
+
+__device__ __forceinline__ const DevMedium *medium_of(const FlightArgs &a, uint32_t i, bool &ok)
+{
+    const uint32_t mi = a.medium ? a.medium[i] : 0u;
+    ok = mi < (uint32_t)a.n_media;
+    return a.media + (ok ? mi : 0u);
+}
+
+__device__ __forceinline__ bool conditioned(const DevMedium &m, const FlightIn &f)
+{
+    return (m.flags & MF_COND) && !(f.flags & GPIS_FLAG_FIRST_SCATTER);
+}
+
+// Transverse moments of the exact SE law (seTransverseGradientMoments, :78-99).
+__device__ void transverse_moments(const DevMedium &m, const CondRec &c, const float o[3],
+                                   const float p[3], const Frame &f, bool cond, float &m0, float &m1, float &var)
+{
+    m0 = m1 = 0.0f;
+    var = 0.5f;
+    if (cond && c.has_obs) {
+        float dl[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) dl[i] = __fmul_rn(m.l_inv[i], __fsub_rn(p[i], o[i]));
+        const double q2 = 0.5 * ((double)dl[0] * dl[0] + (double)dl[1] * dl[1] + (double)dl[2] * dl[2]);
+        const float rho = (float)exp(-0.5 * q2);
+        var = (float)(-0.5 * expm1(-q2));
+        float og[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) og[i] = m.l_aniso[i] * c.tgn[i];
+        const float ox = dot3_rn(f.t[0], f.t[1], f.t[2], og[0], og[1], og[2]);
+        const float oy = dot3_rn(f.b[0], f.b[1], f.b[2], og[0], og[1], og[2]);
+        m0 = rho * ox;
+        m1 = rho * oy;
+    }
+}
+
+// World gradient of the noise of one flight at p (evaluateGradientNoise1D /
+// evaluateNoise3D gradient).  cond: conditioning splats active.
+__device__ void noise_gradient(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
+                               const float p[3], float t_segment, float &value, float g[3])
+{
+    if (!(m.flags & MF_ONE_D)) {
+        float v, gg[3];
+        noise3d_generic<true>(m, p[0], p[1], p[2], fl.noise_seed, v, gg);
+        value = v * m.inv_norm3d;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) g[i] = gg[i] * m.inv_norm3d;
+        if (cond) {
+            float cv, cg[3];
+            cond3d(m, c, fl.o, p, cv, cg);
+            value += cv;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) g[i] += cg[i];
+        }
+        return;
+    }
+    Frame f;
+    ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+    const float z = ray_coord(m.l_inv, f.n, p[0], p[1], p[2]);
+    float v, dv;
+    noise1d_generic<true>(m, z, fl.noise_seed, v, dv);
+    v *= m.inv_norm1d;
+    dv *= m.inv_norm1d;
+    float gcx = 0.0f, gcy = 0.0f;
+    if (cond) {
+        const float oz = ray_coord(m.l_inv, f.n, fl.o[0], fl.o[1], fl.o[2]);
+        const Cov1D k = cov1d(z - oz);
+        v += c.vs * k.k0 + c.gs[2] * k.k1;
+        dv += c.vs * k.k1 + c.gs[2] * k.k2;
+        if (m.flags & MF_CORR_XY) {
+            gcx = c.gs[0] * k.k3;
+            gcy = c.gs[1] * k.k3;
+        }
+    }
+    value = v;
+    float gl[3];
+    if (m.flags & MF_TRANSVERSE) {
+        float m0, m1, var, z0, z1;
+        transverse_moments(m, c, fl.o, p, f, cond, m0, m1, var);
+        normal_draws(fl.normal_seed, 0, z0, z1);
+        const float s = sqrtf(var);
+        gl[0] = m0 + s * z0;
+        gl[1] = m1 + s * z1;
+        gl[2] = dv;
+    } else {
+        float z0, z1;
+        normal_draws(fl.normal_seed, 0, z0, z1);
+        const float inv_s2 = 1.0f / 1.41421354f;
+        float x1 = z0 * inv_s2, y1 = z1 * inv_s2;
+        if (t_segment == 0.0f) {
+            gl[0] = x1 + gcx;
+            gl[1] = y1 + gcy;
+        } else if (!((m.flags & MF_RENEWAL_PLUS) && (m.flags & MF_CORR_XY))) {
+            float z2, z3;
+            normal_draws(fl.normal_seed, 1, z2, z3);
+            gl[0] = z2 * inv_s2 + gcx;
+            gl[1] = z3 * inv_s2 + gcy;
+        } else {
+            float fac, cv, z2, z3;
+            corr_moments(t_segment, fac, cv);
+            normal_draws(fl.normal_seed, 1, z2, z3);
+            const float sc = sqrtf(cv);
+            gl[0] = (z2 * sc + fac * 2.0f * x1) + gcx;
+            gl[1] = (z3 * sc + fac * 2.0f * y1) + gcy;
+        }
+        gl[2] = dv;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float gi = f.t[i] * gl[0] + f.b[i] * gl[1] + f.n[i] * gl[2];
+        g[i] = m.l_inv[i] * gi;
+    }
+}
+
+__device__ __forceinline__ void write_status(const FlightArgs &a, uint32_t i, float t, float value,
+                                             float trans, uint32_t steps, uint32_t status)
+{
+    a.out[2 * i] = make_float4(t, value, 0.0f, 0.0f);
+    a.out[2 * i + 1] = make_float4(0.0f, trans, __uint_as_float(steps), __uint_as_float(status));
+}
+
+// ---------------------------------------------------------------------------
+// k_prepare: conditioning coefficients at the origin of secondary flights.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_prepare(FlightArgs a)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    bool mok;
+    const DevMedium &m = *medium_of(a, i, mok);
+    const FlightIn fl = load_flight(a, i);
+    CondRec c = {};
+    if (!mok || !conditioned(m, fl) || !flight_valid(fl) || m.sigma == 0.0f) {
+        a.cond[i] = c;
+        return;
+    }
+    const float *p = fl.o;
+    int id;
+    const float mean = mean_value(m, p[0], p[1], p[2], id);
+    const float amp = m.sigma;
+    float v, g[3];
+    CondRec none = {};
+    noise_gradient(m, fl, none, false, p, 0.0f, v, g);
+    c.vs = (fl.prev_v - mean) / amp - v;
+    if (m.flags & MF_RENEWAL_PLUS) {
+        float mg[3];
+        mean_grad(m, p[0], p[1], p[2], mg);
+        float delta[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) delta[k] = (fl.prev_g[k] - mg[k]) / amp - g[k];
+        if (m.flags & MF_ONE_D) {
+            Frame f;
+            ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+            float gi[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) gi[k] = m.l_aniso[k] * delta[k];
+            const float gx = dot3_rn(f.t[0], f.t[1], f.t[2], gi[0], gi[1], gi[2]);
+            const float gy = dot3_rn(f.b[0], f.b[1], f.b[2], gi[0], gi[1], gi[2]);
+            const float gz = dot3_rn(f.n[0], f.n[1], f.n[2], gi[0], gi[1], gi[2]);
+            const bool xy = (m.flags & MF_CORR_XY) != 0;
+            c.gs[0] = xy ? -2.0f * gx : 0.0f;
+            c.gs[1] = xy ? -2.0f * gy : 0.0f;
+            c.gs[2] = -2.0f * gz;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) c.tgn[k] = (fl.prev_g[k] - mg[k]) / amp;
+            c.has_obs = 1u;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) c.gs[k] = delta[k] * m.d2inv3[k];
+        }
+    }
+    a.cond[i] = c;
+}
+
+// ---------------------------------------------------------------------------
+// Field evaluators used by the march.
+// ---------------------------------------------------------------------------
+// Registers of one lane's flight that the evaluators read.
+struct LaneField {
+    const DevMedium *m;
+    float n[3];             // ray-space frame normal (1D)
+    float li[3];
+    float kr, kexp, inv_norm, sigma;
+    uint32_t seed;
+    float vs, gsz, ozc;     // 1D conditioning
+    bool cond;
+    CondRec c3;             // 3D conditioning
+    float o[3];
+};
+
+// Generic evaluator: recomputes every impulse (any impulse count, 1D or 3D).
+struct EvalGeneric {
+    __device__ __forceinline__ void reset() {}
+    __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
+                                           int &id, uint32_t &refills)
+    {
+        const DevMedium &m = *L.m;
+        float noise;
+        if (m.flags & MF_ONE_D) {
+            const float z = ray_coord(L.li, L.n, px, py, pz);
+            float v, dv;
+            noise1d_generic<false>(m, z, L.seed, v, dv);
+            noise = v * L.inv_norm;
+            if (L.cond) {
+                const Cov1D k = cov1d(z - L.ozc);
+                noise += L.vs * k.k0 + L.gsz * k.k1;
+            }
+        } else {
+            float v, g[3];
+            noise3d_generic<false>(m, px, py, pz, L.seed, v, g);
+            noise = v * m.inv_norm3d;
+            if (L.cond) {
+                float cv, cg[3];
+                const float p[3] = {px, py, pz};
+                cond3d(m, L.c3, L.o, p, cv, cg);
+                noise += cv;
+            }
+        }
+        refills += 1;
+        return L.sigma * noise + mean_value(m, px, py, pz, id);
+    }
+};
+
+// 1D evaluator with the three-cell impulse window in registers.  Each cached
+// impulse is its position t_i in [0,1) with the sign of its weight in the sign bit.
+template <int NMAX>
+struct EvalCached1D {
+    float cache[3][NMAX];
+    int base;
+    bool valid;
+
+    __device__ __forceinline__ void reset() { valid = false; base = 0; }
+
+    __device__ __forceinline__ void gen(float (&dst)[NMAX], int cell, uint32_t seed, uint32_t n_imp)
+    {
+        const uint32_t s = xxhash2((uint32_t)cell, seed) + 1u;
+#pragma unroll
+        for (int k = 0; k < NMAX; ++k) {
+            if ((uint32_t)k < n_imp) {
+                const uint32_t r1 = pcg_draw(c_jump[2 + 2 * k], s);
+                const uint32_t r2 = pcg_draw(c_jump[3 + 2 * k], s);
+                const float t = unit_float(r1);
+                dst[k] = __uint_as_float(__float_as_uint(t) | (~r2 & 0x80000000u));
+            } else {
+                dst[k] = __int_as_float(0x7f800000);
+            }
+        }
+    }
+
+    __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
+                                           int &id, uint32_t &refills)
+    {
+        const float z = ray_coord(L.li, L.n, px, py, pz);
+        const float tg = __fdiv_rn(z, L.kr);
+        const float fl = floorf(tg);
+        const float frac = __fsub_rn(tg, fl);
+        const int ci = (int)fl;
+        if (!valid || ci != base) {
+            const uint32_t n_imp = L.m->n_imp;
+            if (valid && ci == base + 1) {
+#pragma unroll
+                for (int k = 0; k < NMAX; ++k) { cache[0][k] = cache[1][k]; cache[1][k] = cache[2][k]; }
+                gen(cache[2], ci + 1, L.seed, n_imp);
+                refills += 1;
+            } else if (valid && ci == base - 1) {
+#pragma unroll
+                for (int k = 0; k < NMAX; ++k) { cache[2][k] = cache[1][k]; cache[1][k] = cache[0][k]; }
+                gen(cache[0], ci - 1, L.seed, n_imp);
+                refills += 1;
+            } else {
+                gen(cache[0], ci - 1, L.seed, n_imp);
+                gen(cache[1], ci, L.seed, n_imp);
+                gen(cache[2], ci + 1, L.seed, n_imp);
+                refills += 3;
+            }
+            base = ci;
+            valid = true;
+        }
+        float acc0 = 0.0f, acc1 = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float tl = __fsub_rn(frac, (float)(c - 1));
+#pragma unroll
+            for (int k = 0; k < NMAX; ++k) {
+                const float s = cache[c][k];
+                const float tp = __fsub_rn(tl, fabsf(s));
+                const float e = ex2_approx(L.kexp * (tp * tp));
+                const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(s) & 0x80000000u));
+                if (k & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
+                else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
+            }
+        }
+        float noise = (acc0 + acc1) * L.inv_norm;
+        if (L.cond) {
+            const Cov1D k = cov1d(z - L.ozc);
+            noise += L.vs * k.k0 + L.gsz * k.k1;
+        }
+        return L.sigma * noise + mean_value(*L.m, px, py, pz, id);
+    }
+};
+
+enum : int { PH_IDLE = 0, PH_F0, PH_MARCH, PH_REFINE, PH_FAR };
+
+__device__ __forceinline__ bool t_less(float hi, float lo, float far_t)
+{
+    return hi < far_t || (hi == far_t && lo < 0.0f);
+}
+
+__device__ __forceinline__ double lerp_d(double a, double b, double r)
+{
+    return __dadd_rn(__dmul_rn(a, __dsub_rn(1.0, r)), __dmul_rn(b, r));
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(uint32_t v)
+{
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// k_march: persistent warps with per-lane refill.
+// ---------------------------------------------------------------------------
+template <class Eval>
+__global__ void __launch_bounds__(256) k_march(FlightArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    Eval ev;
+    ev.reset();
+    LaneField L;
+    L.m = a.media;
+    int phase = PH_IDLE;
+    bool drained = false, first = true;
+    uint32_t fid = 0, steps = 0, max_steps = 1;
+    float d[3] = {0, 0, 0}, near_t = 0, far_t = 0, step = 0, t0 = 0, th = 0, tl = 0, pf = 0;
+    int sign0 = 1, gpid = 0;
+    double ta = 0, tb = 0, fac = 0, tprev = 0, ttest = 0;
+    uint32_t refine_iter = 0;
+    uint32_t c_flights = 0, c_steps = 0, c_refine = 0, c_hits = 0, c_limit = 0, c_invalid = 0, c_refills = 0;
+
+    for (;;) {
+        const bool need = phase == PH_IDLE && !drained;
+        const unsigned need_mask = __ballot_sync(FULL, need);
+        if (need_mask) {
+            const int leader = __ffs(need_mask) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.work, (uint32_t)__popc(need_mask));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const uint32_t idx = base + (uint32_t)__popc(need_mask & lt_mask);
+                if (idx >= a.n) {
+                    drained = true;
+                } else {
+                    fid = idx;
+                    c_flights++;
+                    bool mok;
+                    L.m = medium_of(a, idx, mok);
+                    const DevMedium &m = *L.m;
+                    const FlightIn fl = load_flight(a, idx);
+                    if (!mok || !flight_valid(fl)) {
+                        write_status(a, idx, 0.0f, 0.0f, 1.0f, 0u, GPIS_FLIGHT_INVALID_INPUT);
+                        a.t_end[idx] = 0.0;
+                        c_invalid++;
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) { L.o[k] = fl.o[k]; d[k] = fl.d[k]; L.li[k] = m.l_inv[k]; }
+                        near_t = fl.near_t;
+                        far_t = fl.far_t;
+                        first = (fl.flags & GPIS_FLAG_FIRST_SCATTER) != 0;
+                        L.seed = fl.noise_seed;
+                        L.sigma = m.sigma;
+                        L.cond = conditioned(m, fl);
+                        L.vs = L.gsz = L.ozc = 0.0f;
+                        if (m.flags & MF_ONE_D) {
+                            Frame f;
+                            ray_frame(m, d[0], d[1], d[2], f);
+                            L.n[0] = f.n[0]; L.n[1] = f.n[1]; L.n[2] = f.n[2];
+                            L.kr = m.kr_iso;
+                            L.kexp = m.kexp1d;
+                            L.inv_norm = m.inv_norm1d;
+                            if (L.cond) {
+                                const CondRec c = a.cond[idx];
+                                L.vs = c.vs;
+                                L.gsz = c.gs[2];
+                                L.ozc = ray_coord(L.li, L.n, L.o[0], L.o[1], L.o[2]);
+                            }
+                        } else if (L.cond) {
+                            L.c3 = a.cond[idx];
+                        }
+                        step = __fdiv_rn(__fsub_rn(far_t, near_t), (float)m.min_step);
+                        if (m.step_size < step) step = m.step_size;
+                        t0 = __fadd_rn(near_t, __fmul_rn(step, fl.jitter));
+                        max_steps = m.max_steps;
+                        th = near_t;
+                        tl = 0.0f;
+                        steps = 0;
+                        ev.reset();
+                        phase = PH_F0;
+                    }
+                }
+            }
+        }
+        const bool live = phase != PH_IDLE;
+        if (!__any_sync(FULL, live)) {
+            if (__all_sync(FULL, drained)) break;
+            continue;
+        }
+        if (!live) continue;
+
+        float p[3];
+        if (phase == PH_REFINE) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) p[k] = dd_point(L.o[k], d[k], ttest);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], th, tl);
+        }
+        int id;
+        const float f = ev.value(L, p[0], p[1], p[2], id, c_refills);
+        gpid = id;
+        const int sg = f < 0.0f ? -1 : 1;
+        bool done = false;
+        float t_out = 0.0f, v_out = 0.0f, trans = 1.0f;
+        double t_end = 0.0;
+        uint32_t status = GPIS_FLIGHT_OK;
+
+        if (!isfinite(f)) {
+            // a non-finite field value ends the flight (RaySegmentBatch.cu:228-229, 238-239)
+            done = true;
+            status = GPIS_FLIGHT_INVALID_INPUT;
+            c_invalid++;
+        } else if (phase == PH_F0) {
+            sign0 = sg;
+            pf = f;
+            th = t0;
+            tl = 0.0f;
+            if (t_less(th, tl, far_t)) {
+                phase = PH_MARCH;
+            } else {
+                phase = PH_FAR;
+                th = far_t;
+            }
+        } else if (phase == PH_MARCH) {
+            steps++;
+            c_steps++;
+            bool crossed = false;
+            if (!first && steps == 1) {
+                sign0 = sg;
+            } else if (sg != sign0) {
+                crossed = true;
+                const double tc = (double)th + (double)tl;
+                ta = __dsub_rn(tc, (double)step);
+                tb = tc;
+                fac = __ddiv_rn((double)pf, __dsub_rn((double)pf, (double)f));
+                ttest = lerp_d(ta, tb, fac);
+                tprev = ttest;
+                refine_iter = 0;
+                phase = PH_REFINE;
+            }
+            if (!crossed) {
+                pf = f;
+                ff_add(th, tl, step);
+                if (!t_less(th, tl, far_t)) {
+                    phase = PH_FAR;
+                    th = far_t;
+                    tl = 0.0f;
+                } else if (steps >= max_steps) {
+                    done = true;
+                    status = GPIS_FLIGHT_STEP_LIMIT;
+                    t_out = far_t;
+                    t_end = far_t;
+                    c_limit++;
+                }
+            }
+        } else if (phase == PH_REFINE) {
+            c_refine++;
+            refine_iter++;
+            bool hit = false;
+            if (sg == sign0) {
+                hit = true;
+            } else {
+                fac = __dmul_rn(fac, 0.9);
+                // 0.9^44 < 0.01: the back-off ends within 44 evaluations for any
+                // factor <= 1; the explicit bound also covers a non-finite factor.
+                if (fac <= 0.01 || !(fac == fac) || refine_iter >= 64) {
+                    tprev = 0.0;
+                    hit = true;
+                } else {
+                    tprev = ttest;
+                    ttest = lerp_d(ta, tb, fac);
+                }
+            }
+            if (hit) {
+                done = true;
+                t_end = tprev;
+                t_out = (float)tprev;
+                v_out = 0.0f;
+                trans = 0.0f;
+                c_hits++;
+            }
+        } else {  // PH_FAR
+            done = true;
+            t_out = far_t;
+            t_end = far_t;
+            v_out = f;
+        }
+        if (done) {
+            write_status(a, fid, t_out, v_out, trans, steps, status | ((uint32_t)gpid << 8));
+            a.t_end[fid] = t_end;
+            phase = PH_IDLE;
+        }
+    }
+    // counters: one atomic per warp
+    const unsigned long long s0 = warp_sum(c_flights), s1 = warp_sum(c_steps), s2 = warp_sum(c_refine),
+                             s3 = warp_sum(c_hits), s4 = warp_sum(c_limit), s5 = warp_sum(c_invalid),
+                             s6 = warp_sum(c_refills);
+    if (lane == 0 && a.counters) {
+        atomicAdd(a.counters + 0, s0);
+        atomicAdd(a.counters + 1, s1);
+        atomicAdd(a.counters + 2, s2);
+        atomicAdd(a.counters + 3, s3);
+        atomicAdd(a.counters + 4, s4);
+        atomicAdd(a.counters + 5, s5);
+        atomicAdd(a.counters + 6, s6);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_finish: gradient sample at the end point.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_finish(FlightArgs a)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    float4 r0 = a.out[2 * i];
+    float4 r1 = a.out[2 * i + 1];
+    const uint32_t status = __float_as_uint(r1.w) & 0xFFu;
+    bool mok;
+    const DevMedium &m = *medium_of(a, i, mok);
+    const FlightIn fl = load_flight(a, i);
+    const bool hit = r1.y == 0.0f;
+    const bool shadow = (fl.flags & GPIS_FLAG_SHADOW) != 0;
+    if (status != GPIS_FLIGHT_OK || (!hit && shadow) || !mok) {
+        const bool keep = status != GPIS_FLIGHT_INVALID_INPUT;
+        r0.z = keep ? fl.prev_g[0] : 0.0f;
+        r0.w = keep ? fl.prev_g[1] : 0.0f;
+        r1.x = keep ? fl.prev_g[2] : 0.0f;
+        a.out[2 * i] = r0;
+        a.out[2 * i + 1] = r1;
+        return;
+    }
+    const double t = a.t_end[i];
+    // ro + normalize(rd) * t in double (GaussianProcessMedium.cpp:307, 401)
+    const double dx = fl.d[0], dy = fl.d[1], dz = fl.d[2];
+    const double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+    float p[3];
+    p[0] = (float)((double)fl.o[0] + dx * inv * t);
+    p[1] = (float)((double)fl.o[1] + dy * inv * t);
+    p[2] = (float)((double)fl.o[2] + dz * inv * t);
+    const bool cond = conditioned(m, fl);
+    CondRec c = {};
+    if (cond) c = a.cond[i];
+    float v, g[3], mg[3];
+    noise_gradient(m, fl, c, cond, p, (float)t, v, g);
+    mean_grad(m, p[0], p[1], p[2], mg);
+    r0.z = m.sigma * g[0] + mg[0];
+    r0.w = m.sigma * g[1] + mg[1];
+    r1.x = m.sigma * g[2] + mg[2];
+    a.out[2 * i] = r0;
+    a.out[2 * i + 1] = r1;
+}
+
+// ---------------------------------------------------------------------------
+// Unit-level kernels.
+// ---------------------------------------------------------------------------
+__global__ void k_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n,
+                                 uint32_t imp, float *pos, float *weight)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t s = xxhash2(cells[i], seeds[i]) + 1u;
+    for (uint32_t k = 0; k < imp; ++k) {
+        pos[(size_t)i * imp + k] = unit_float(pcg_draw(c_jump[2 + 2 * k], s));
+        weight[(size_t)i * imp + k] = (pcg_draw(c_jump[3 + 2 * k], s) >> 31) ? 1.0f : -1.0f;
+    }
+}
+
+__global__ void k_debug_cells_3d(const int32_t *cells, const uint32_t *seeds, uint32_t n, uint32_t imp,
+                                 uint32_t order, float *pos, float *weight)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t s = xxhash4((uint32_t)cells[3 * i + 2], (uint32_t)cells[3 * i + 1], (uint32_t)cells[3 * i],
+                               seeds[i]) + 1u;
+    for (uint32_t k = 0; k < imp; ++k) {
+        const int b = 2 + 4 * (int)k;
+        const float r0 = unit_float(pcg_draw(c_jump[b], s));
+        const float r1 = unit_float(pcg_draw(c_jump[b + 1], s));
+        const float r2 = unit_float(pcg_draw(c_jump[b + 2], s));
+        const size_t o = ((size_t)i * imp + k) * 3;
+        pos[o + 0] = order ? r0 : r2;
+        pos[o + 1] = r1;
+        pos[o + 2] = order ? r2 : r0;
+        weight[(size_t)i * imp + k] = (pcg_draw(c_jump[b + 3], s) >> 31) ? 1.0f : -1.0f;
+    }
+}
+
+// Field at arbitrary points: conditioning of the point's flight (as k_prepare),
+// then the noise value/gradient and the field value.
+__global__ void k_debug_field(const DevMedium *mp, const float4 *origins, const float4 *points,
+                              const float4 *dirs, const uint4 *seeds, const float4 *prev,
+                              uint32_t n, float4 *out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DevMedium &m = *mp;
+    FlightIn fl;
+    const float4 o = origins[i], d = dirs[i], pp = points[i], pv = prev[i];
+    const uint4 sd = seeds[i];
+    fl.o[0] = o.x; fl.o[1] = o.y; fl.o[2] = o.z; fl.near_t = 0.0f;
+    fl.d[0] = d.x; fl.d[1] = d.y; fl.d[2] = d.z; fl.far_t = 1.0f;
+    fl.noise_seed = sd.x; fl.normal_seed = sd.y; fl.flags = sd.z; fl.jitter = 0.0f;
+    fl.prev_v = pv.x; fl.prev_g[0] = pv.y; fl.prev_g[1] = pv.z; fl.prev_g[2] = pv.w;
+    CondRec c = {};
+    const bool cond = conditioned(m, fl) && m.sigma != 0.0f;
+    if (cond) {
+        // same coefficients as k_prepare
+        int id;
+        const float mean = mean_value(m, fl.o[0], fl.o[1], fl.o[2], id);
+        float v, g[3];
+        CondRec none = {};
+        noise_gradient(m, fl, none, false, fl.o, 0.0f, v, g);
+        c.vs = (fl.prev_v - mean) / m.sigma - v;
+        if (m.flags & MF_RENEWAL_PLUS) {
+            float mg[3], delta[3];
+            mean_grad(m, fl.o[0], fl.o[1], fl.o[2], mg);
+            for (int k = 0; k < 3; ++k) delta[k] = (fl.prev_g[k] - mg[k]) / m.sigma - g[k];
+            if (m.flags & MF_ONE_D) {
+                Frame f;
+                ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+                float gi[3];
+                for (int k = 0; k < 3; ++k) gi[k] = m.l_aniso[k] * delta[k];
+                const bool xy = (m.flags & MF_CORR_XY) != 0;
+                c.gs[0] = xy ? -2.0f * dot3_rn(f.t[0], f.t[1], f.t[2], gi[0], gi[1], gi[2]) : 0.0f;
+                c.gs[1] = xy ? -2.0f * dot3_rn(f.b[0], f.b[1], f.b[2], gi[0], gi[1], gi[2]) : 0.0f;
+                c.gs[2] = -2.0f * dot3_rn(f.n[0], f.n[1], f.n[2], gi[0], gi[1], gi[2]);
+                for (int k = 0; k < 3; ++k) c.tgn[k] = (fl.prev_g[k] - mg[k]) / m.sigma;
+                c.has_obs = 1u;
+            } else {
+                for (int k = 0; k < 3; ++k) c.gs[k] = delta[k] * m.d2inv3[k];
+            }
+        }
+    }
+    const float p[3] = {pp.x, pp.y, pp.z};
+    float v, g[3];
+    // value and derivative parts of the noise (the 1D xy entries are the conditioning splats)
+    if (m.flags & MF_ONE_D) {
+        Frame f;
+        ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+        const float z = ray_coord(m.l_inv, f.n, p[0], p[1], p[2]);
+        float dv;
+        noise1d_generic<true>(m, z, fl.noise_seed, v, dv);
+        v *= m.inv_norm1d;
+        dv *= m.inv_norm1d;
+        g[0] = g[1] = 0.0f;
+        if (cond) {
+            const float oz = ray_coord(m.l_inv, f.n, fl.o[0], fl.o[1], fl.o[2]);
+            const Cov1D k = cov1d(z - oz);
+            v += c.vs * k.k0 + c.gs[2] * k.k1;
+            dv += c.vs * k.k1 + c.gs[2] * k.k2;
+            if (m.flags & MF_CORR_XY) { g[0] = c.gs[0] * k.k3; g[1] = c.gs[1] * k.k3; }
+        }
+        g[2] = dv;
+    } else {
+        noise_gradient(m, fl, c, cond, p, 1.0f, v, g);
+    }
+    int id;
+    const float mean = mean_value(m, p[0], p[1], p[2], id);
+    out[2 * i] = make_float4(v, g[0], g[1], g[2]);
+    out[2 * i + 1] = make_float4(m.sigma * v + mean, mean, 0.0f, 0.0f);
+}
+
+__global__ void k_se_splat_1d(const float *q, const float *c, float *v, float *d, size_t n, float scale)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float delta = q[i] - c[i];
+    const float inv = 1.0f / (scale * scale);
+    const float e = expf(-0.5f * delta * delta * inv);
+    v[i] = e;
+    d[i] = -delta * inv * e;
+}
+
+}  // namespace
+
+cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream)
+{
+    if (a.n == 0) return cudaSuccess;
+    const uint32_t blocks = (a.n + 127) / 128;
+    if (a.any_cond) k_prepare<<<blocks, 128, 0, stream>>>(a);
+    cudaError_t err = cudaMemsetAsync(a.work, 0, sizeof(uint32_t), stream);
+    if (err != cudaSuccess) return err;
+    // persistent grid: a few resident CTAs per SM, never more warps than flights
+    const uint32_t warps_needed = (a.n + 31) / 32;
+    uint32_t ctas = (uint32_t)num_sms * 4u;
+    const uint32_t ctas_needed = (warps_needed + 7) / 8;
+    if (ctas > ctas_needed) ctas = ctas_needed;
+    if (ctas == 0) ctas = 1;
+    if (a.one_d && a.max_imp <= 8)
+        k_march<EvalCached1D<8>><<<ctas, 256, 0, stream>>>(a);
+    else
+        k_march<EvalGeneric><<<ctas, 256, 0, stream>>>(a);
+    k_finish<<<blocks, 128, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n,
+                                  uint32_t impulses, float *pos, float *weight, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_debug_cells_1d<<<(n + 127) / 128, 128, 0, s>>>(cells, seeds, n, impulses, pos, weight);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_cells_3d(const int32_t *cells, const uint32_t *seeds, uint32_t n,
+                                  uint32_t impulses, uint32_t order, float *pos, float *weight,
+                                  cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_debug_cells_3d<<<(n + 127) / 128, 128, 0, s>>>(cells, seeds, n, impulses, order, pos, weight);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_field(const DevMedium *m, const float4 *origins, const float4 *points,
+                               const float4 *dirs, const uint4 *seeds, const float4 *prev,
+                               uint32_t n, float4 *out, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_debug_field<<<(n + 127) / 128, 128, 0, s>>>(m, origins, points, dirs, seeds, prev, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_se_splat_1d(const float *q, const float *c, float *v, float *d, size_t n,
+                               float scale, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    const size_t blocks = (n + 255) / 256;
+    k_se_splat_1d<<<(unsigned)blocks, 256, 0, s>>>(q, c, v, d, n, scale);
+    return cudaGetLastError();
+}
+
+}  // namespace gpis

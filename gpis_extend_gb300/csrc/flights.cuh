@@ -1,0 +1,60 @@
+// flights.cuh -- launch interface between the C ABI (gpis_abi.cu) and the
+// flight kernels (flights.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gpis.h"
+#include "device_common.cuh"
+
+namespace gpis {
+
+// Per-flight conditioning coefficients (SparseConvConditioningCoefficients1D/3D,
+// SparseConvolutionNoise.hpp:7-24), written by the prepare kernel.
+struct CondRec {
+    float vs;               // value_scale
+    float gs[3];            // gradient_scale (iso-ray space for 1D, world for 3D)
+    float tgn[3];           // target_gradient_noise (1D transverse law)
+    uint32_t has_obs;       // has_gradient_observation
+};
+
+struct FlightArgs {
+    const float4 *origin_near;
+    const float4 *dir_far;
+    const uint4 *seeds;
+    const float4 *prev;
+    const uint32_t *medium;     // may be null
+    float4 *out;                // 2 float4 per flight
+    const DevMedium *media;
+    int n_media;
+    uint32_t n;
+    CondRec *cond;              // scratch, n records
+    double *t_end;              // scratch, n values (double march parameter at the end point)
+    uint32_t *work;             // scratch, 1 work counter (zeroed before the march)
+    unsigned long long *counters;  // gpis_counters block (8 x u64)
+    int any_cond;               // some medium conditions (run the prepare kernel)
+    int one_d;                  // all media use 1D noise
+    int three_d;                // all media use 3D noise
+    uint32_t max_imp;           // max impulses per cell over the media
+};
+
+// Upload the jump-ahead PCG table to the current device (once per device).
+cudaError_t upload_pcg_table();
+
+// Enqueue the three flight kernels on the stream.
+cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream);
+
+// Unit-level kernels (synchronous wrappers live in gpis_abi.cu).
+cudaError_t launch_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n,
+                                  uint32_t impulses, float *pos, float *weight, cudaStream_t s);
+cudaError_t launch_debug_cells_3d(const int32_t *cells, const uint32_t *seeds, uint32_t n,
+                                  uint32_t impulses, uint32_t order, float *pos, float *weight,
+                                  cudaStream_t s);
+cudaError_t launch_debug_field(const DevMedium *m, const float4 *origins, const float4 *points,
+                               const float4 *dirs, const uint4 *seeds, const float4 *prev,
+                               uint32_t n, float4 *out, cudaStream_t s);
+cudaError_t launch_se_splat_1d(const float *q, const float *c, float *v, float *d, size_t n,
+                               float scale, cudaStream_t s);
+
+}  // namespace gpis

@@ -1,0 +1,459 @@
+// gpis_abi.cu -- the C ABI of libgpis_gb300.so (include/gpis.h): medium
+// tables, contexts, flight submission and the unit-level entry points.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gpis.h"
+#include "flights.cuh"
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    return fail(GPIS_EIO, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(expr, what)                                 \
+    do {                                                     \
+        cudaError_t _e = (expr);                             \
+        if (_e != cudaSuccess) return cuda_fail(_e, what);   \
+    } while (0)
+
+bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+// Host derivation of the device medium constants.  Float expressions follow
+// the reference's rounding: _l_conv = l * sqrt(2.f) / 2 (GPFunctions.cpp:661),
+// _l_aniso_inv = 1 / (l_conv * aniso) with inf -> 0 (GPFunctions.hpp:153-162),
+// kernel radii (GPFunctions.cpp:706-719) and the noise variances (:751-770).
+int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
+{
+    std::memset(&m, 0, sizeof(m));
+    if (!(std::isfinite(d.length_scale) && d.length_scale > 0.0f))
+        return fail(GPIS_EINVAL, "length_scale must be finite and > 0");
+    if (!(std::isfinite(d.kernel_scale) && d.kernel_scale > 0.0f))
+        return fail(GPIS_EINVAL, "kernel_scale (localScale) must be finite and > 0");
+    if (!(std::isfinite(d.impulse_density) && d.impulse_density > 0.0f && d.impulse_density <= 64.0f))
+        return fail(GPIS_EINVAL, "impulse_density must be in (0, 64]");
+    if (!(std::isfinite(d.step_size) && d.step_size > 0.0f))
+        return fail(GPIS_EINVAL, "step_size must be finite and > 0");
+    if (!std::isfinite(d.sigma) || !finite3(d.aniso))
+        return fail(GPIS_EINVAL, "sigma and aniso must be finite");
+    if (d.correlation_context > GPIS_CTX_NONE) return fail(GPIS_EINVAL, "unknown correlation_context");
+    if (d.sampling_scheme > GPIS_SCHEME_MIS) return fail(GPIS_EINVAL, "unknown 1D_sampling_scheme");
+    for (int i = 0; i < 8; ++i)
+        if (!std::isfinite(d.mean_params[i])) return fail(GPIS_EINVAL, "mean parameters must be finite");
+    if (d.ls_kind != GPIS_LS_CONSTANT || d.n_octaves != 1 || d.multires)
+        return fail(GPIS_ENOTSUP, "nonstationary / multi-octave / multi-resolution fields are not supported");
+    if (d.isotropic_3d_sampling && !d.one_d_sampling)
+        return fail(GPIS_ENOTSUP, "isotropic_3D_sampling is not supported");
+    if (d.mean_kind > GPIS_MEAN_TORUS_PLANE) return fail(GPIS_EINVAL, "unknown mean kind");
+    if (d.mean_kind == GPIS_MEAN_GRID) {
+        const gpis_mean_grid *g = d.grid;
+        if (!g || !g->voxels || g->dims[0] < 2 || g->dims[1] < 2 || g->dims[2] < 2)
+            return fail(GPIS_EINVAL, "grid mean needs voxels and dims >= 2");
+    }
+
+    const float lc = d.length_scale * std::sqrt(2.f) / 2;
+    for (int i = 0; i < 3; ++i) {
+        m.l_aniso[i] = lc * d.aniso[i];
+        float inv = 1.0f / m.l_aniso[i];
+        if (std::isinf(inv) || std::isnan(inv)) inv = 0.0f;
+        m.l_inv[i] = inv;
+    }
+    const float mtx = std::max(std::max(m.l_aniso[0], m.l_aniso[1]), m.l_aniso[2]);
+    m.kr_iso = d.kernel_scale;
+    m.kr_world = d.kernel_scale * 1.0f * mtx;
+    m.sigma = d.sigma;
+    m.n_imp = (uint32_t)d.impulse_density;
+    const float var1 = (float)((double)(d.impulse_density / m.kr_iso) * (std::sqrt(M_PI) * 1.0));
+    m.inv_norm1d = 1.0f / std::sqrt(var1);
+    const float kr = m.kr_world;
+    const float ud = d.impulse_density / (kr * kr * kr);
+    const float det = m.l_aniso[0] * m.l_aniso[1] * m.l_aniso[2];
+    const float var3 = (float)((double)ud * (std::pow(M_PI, 1.5) * (double)det));
+    m.inv_norm3d = 1.0f / std::sqrt(var3);
+    const double log2e = 1.4426950408889634;
+    m.kexp1d = (float)(-0.5 * (double)m.kr_iso * (double)m.kr_iso * log2e);
+    for (int i = 0; i < 3; ++i) {
+        const float inv2 = m.l_inv[i] * m.l_inv[i];
+        m.m3[i] = inv2 * 0.5f;
+        m.m3c[i] = (inv2 * 0.5f) * 0.5f;
+        m.kexp3d[i] = (float)(-(double)m.m3[i] * log2e);
+        m.d2inv3[i] = inv2 > 0.0f ? 1.0f / (-2.0f * (inv2 * 0.25f)) : 0.0f;
+    }
+    const bool activate = !d.single_realization &&
+        (d.correlation_context == GPIS_CTX_RENEWAL || d.correlation_context == GPIS_CTX_RENEWAL_PLUS);
+    uint32_t flags = 0;
+    if (d.one_d_sampling) flags |= gpis::MF_ONE_D;
+    if (activate) flags |= gpis::MF_COND;
+    if (d.correlation_context == GPIS_CTX_RENEWAL_PLUS) flags |= gpis::MF_RENEWAL_PLUS;
+    if (d.correlation_xy) flags |= gpis::MF_CORR_XY;
+    if (d.one_d_sampling && d.correlation_xy && d.correlation_context == GPIS_CTX_RENEWAL_PLUS && !d.multires)
+        flags |= gpis::MF_TRANSVERSE;
+    if (d.impulse_xyz_order) flags |= gpis::MF_XYZ_ORDER;
+    m.flags = flags;
+    m.mean_kind = d.mean_kind;
+    std::memcpy(m.mean_params, d.mean_params, sizeof(m.mean_params));
+    if (d.mean_kind == GPIS_MEAN_GRID) {
+        const gpis_mean_grid *g = d.grid;
+        std::memcpy(m.grid_origin, g->origin, sizeof(m.grid_origin));
+        std::memcpy(m.grid_dims, g->dims, sizeof(m.grid_dims));
+        std::memcpy(m.grid_w2i, g->world_to_index, sizeof(m.grid_w2i));
+        std::memcpy(m.grid_cmin, g->clamp_min, sizeof(m.grid_cmin));
+        std::memcpy(m.grid_cmax, g->clamp_max, sizeof(m.grid_cmax));
+        m.grid_offset = g->offset;
+        m.grid_scale = g->scale;
+    }
+    m.step_size = d.step_size;
+    m.min_step = d.min_step;
+    m.max_steps = d.max_steps ? d.max_steps : 16384u;
+    m.scheme = (!d.single_realization && d.one_d_sampling) ? d.sampling_scheme : GPIS_SCHEME_UNI;
+    return GPIS_OK;
+}
+
+}  // namespace
+
+struct gpis_ctx {
+    int device = 0;
+    int num_sms = 1;
+    int n_media = 0;
+    gpis::DevMedium *d_media = nullptr;
+    std::vector<float *> d_grids;
+    bool any_cond = false, all_one_d = true, all_three_d = true;
+    uint32_t max_imp = 0;
+    // scratch of the flight kernels
+    gpis::CondRec *d_cond = nullptr;
+    double *d_tend = nullptr;
+    uint32_t *d_work = nullptr;
+    unsigned long long *d_counters = nullptr;
+    size_t cap = 0;
+    // staging of the host entry point
+    char *d_stage = nullptr;
+    size_t stage_cap = 0;
+    cudaStream_t stream = nullptr;
+};
+
+namespace {
+
+void release(gpis_ctx *c)
+{
+    if (!c) return;
+    cudaFree(c->d_media);
+    for (float *g : c->d_grids) cudaFree(g);
+    cudaFree(c->d_cond);
+    cudaFree(c->d_tend);
+    cudaFree(c->d_work);
+    cudaFree(c->d_counters);
+    cudaFree(c->d_stage);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int ensure_scratch(gpis_ctx *c, size_t n)
+{
+    if (n <= c->cap) return GPIS_OK;
+    size_t cap = std::max<size_t>(n, 1024);
+    cudaFree(c->d_cond);
+    cudaFree(c->d_tend);
+    c->d_cond = nullptr;
+    c->d_tend = nullptr;
+    c->cap = 0;
+    CUDA_TRY(cudaMalloc(&c->d_cond, cap * sizeof(gpis::CondRec)), "allocate conditioning scratch");
+    CUDA_TRY(cudaMalloc(&c->d_tend, cap * sizeof(double)), "allocate end-parameter scratch");
+    c->cap = cap;
+    return GPIS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+__attribute__((visibility("hidden"))) int gpis_internal_set_error(int code, const char *msg)
+{
+    g_error = msg ? msg : "";
+    return code;
+}
+
+void gpis_medium_desc_init(gpis_medium_desc *d)
+{
+    if (!d) return;
+    std::memset(d, 0, sizeof(*d));
+    d->sigma = 1.0f;
+    d->length_scale = 1.0f;
+    d->aniso[0] = d->aniso[1] = d->aniso[2] = 1.0f;
+    d->kernel_scale = 3.0f;
+    d->ls_kind = GPIS_LS_CONSTANT;
+    d->ls_params[0] = 1.0f;
+    d->ls_max = 1.0f;
+    d->n_octaves = 1;
+    d->octave_sigma[0] = 1.0f;
+    for (int i = 0; i < 4; ++i) d->octave_scale[i] = 1.0f;
+    d->mean_kind = GPIS_MEAN_SPHERE;
+    d->mean_params[3] = 1.0f;
+    d->step_size = 0.01f;
+    d->min_step = 8;
+    d->seed = 0;
+    d->impulse_density = 3.0f;
+    d->correlation_context = GPIS_CTX_RENEWAL_PLUS;
+    d->sampling_scheme = GPIS_SCHEME_UNI;
+    d->density = 1.0f;
+}
+
+const char *gpis_last_error(void) { return g_error.c_str(); }
+
+int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
+{
+    if (!out) return fail(GPIS_EINVAL, "out is null");
+    *out = nullptr;
+    if (!media || n_media <= 0) return fail(GPIS_EINVAL, "need at least one medium");
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return fail(GPIS_ENODEV, "no CUDA device");
+    std::vector<gpis::DevMedium> host((size_t)n_media);
+    for (int i = 0; i < n_media; ++i) {
+        int rc = derive_medium(media[i], host[(size_t)i]);
+        if (rc) return fail(rc, "medium %d: %s", i, g_error.c_str());
+    }
+    gpis_ctx *c = new (std::nothrow) gpis_ctx();
+    if (!c) return fail(GPIS_ENOMEM, "out of host memory");
+    cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    c->n_media = n_media;
+    int rc = GPIS_OK;
+    do {
+        if ((e = gpis::upload_pcg_table()) != cudaSuccess) { rc = cuda_fail(e, "upload PCG table"); break; }
+        for (int i = 0; i < n_media; ++i) {
+            gpis::DevMedium &m = host[(size_t)i];
+            if (m.mean_kind == GPIS_MEAN_GRID) {
+                const gpis_mean_grid *g = media[i].grid;
+                const size_t cnt = (size_t)g->dims[0] * g->dims[1] * g->dims[2];
+                float *dg = nullptr;
+                if ((e = cudaMalloc(&dg, cnt * sizeof(float))) != cudaSuccess) { rc = cuda_fail(e, "allocate grid"); break; }
+                c->d_grids.push_back(dg);
+                if ((e = cudaMemcpy(dg, g->voxels, cnt * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess) {
+                    rc = cuda_fail(e, "upload grid");
+                    break;
+                }
+                m.grid = dg;
+            }
+            c->any_cond = c->any_cond || (m.flags & gpis::MF_COND);
+            c->all_one_d = c->all_one_d && (m.flags & gpis::MF_ONE_D);
+            c->all_three_d = c->all_three_d && !(m.flags & gpis::MF_ONE_D);
+            c->max_imp = std::max(c->max_imp, m.n_imp);
+        }
+        if (rc) break;
+        if ((e = cudaMalloc(&c->d_media, host.size() * sizeof(gpis::DevMedium))) != cudaSuccess) { rc = cuda_fail(e, "allocate media"); break; }
+        if ((e = cudaMemcpy(c->d_media, host.data(), host.size() * sizeof(gpis::DevMedium), cudaMemcpyHostToDevice)) != cudaSuccess) {
+            rc = cuda_fail(e, "upload media");
+            break;
+        }
+        if ((e = cudaMalloc(&c->d_work, sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(e, "allocate work counter"); break; }
+        if ((e = cudaMalloc(&c->d_counters, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "allocate counters"); break; }
+        if ((e = cudaMemset(c->d_counters, 0, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "clear counters"); break; }
+        if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(e, "create stream"); break; }
+    } while (false);
+    if (rc) {
+        release(c);
+        return rc;
+    }
+    *out = c;
+    return GPIS_OK;
+}
+
+void gpis_ctx_destroy(gpis_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaDeviceSynchronize();
+    release(ctx);
+}
+
+int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa *out, uint32_t n,
+                        void *cuda_stream)
+{
+    if (!ctx || !in || !out) return fail(GPIS_EINVAL, "null argument");
+    if (n == 0) return GPIS_OK;
+    if (!in->origin_near || !in->dir_far || !in->seeds || !out->rec)
+        return fail(GPIS_EINVAL, "flight streams origin_near, dir_far, seeds and rec are required");
+    if (ctx->any_cond && !in->prev) return fail(GPIS_EINVAL, "conditioning media need the prev stream");
+    int rc = ensure_scratch(ctx, n);
+    if (rc) return rc;
+    gpis::FlightArgs a;
+    a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
+    a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
+    a.seeds = reinterpret_cast<const uint4 *>(in->seeds);
+    a.prev = reinterpret_cast<const float4 *>(in->prev);
+    a.medium = in->medium;
+    a.out = reinterpret_cast<float4 *>(out->rec);
+    a.media = ctx->d_media;
+    a.n_media = ctx->n_media;
+    a.n = n;
+    a.cond = ctx->d_cond;
+    a.t_end = ctx->d_tend;
+    a.work = ctx->d_work;
+    a.counters = ctx->d_counters;
+    a.any_cond = ctx->any_cond;
+    a.one_d = ctx->all_one_d;
+    a.three_d = ctx->all_three_d;
+    a.max_imp = ctx->max_imp;
+    for (const void *p : {(const void *)in->origin_near, (const void *)in->dir_far, (const void *)in->seeds,
+                          (const void *)in->prev, (const void *)out->rec})
+        if (p && (reinterpret_cast<uintptr_t>(p) & 15u))
+            return fail(GPIS_EINVAL, "flight and result streams must be 16-byte aligned");
+    CUDA_TRY(gpis::launch_flights(a, ctx->num_sms, static_cast<cudaStream_t>(cuda_stream)), "launch flights");
+    return GPIS_OK;
+}
+
+int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa *out, uint32_t n)
+{
+    if (!ctx || !in || !out) return fail(GPIS_EINVAL, "null argument");
+    if (n == 0) return GPIS_OK;
+    if (!in->origin_near || !in->dir_far || !in->seeds || !out->rec)
+        return fail(GPIS_EINVAL, "flight streams origin_near, dir_far, seeds and rec are required");
+    const size_t rec16 = (size_t)n * 16;
+    const size_t need = rec16 * 4 + (size_t)n * 4 + 64 + rec16 * 2;
+    if (need > ctx->stage_cap) {
+        cudaFree(ctx->d_stage);
+        ctx->d_stage = nullptr;
+        ctx->stage_cap = 0;
+        CUDA_TRY(cudaMalloc(&ctx->d_stage, need), "allocate staging");
+        ctx->stage_cap = need;
+    }
+    char *base = ctx->d_stage;
+    gpis_flight_soa din;
+    din.origin_near = reinterpret_cast<float *>(base);
+    din.dir_far = reinterpret_cast<float *>(base + rec16);
+    din.seeds = reinterpret_cast<uint32_t *>(base + 2 * rec16);
+    din.prev = reinterpret_cast<float *>(base + 3 * rec16);
+    char *med = base + 4 * rec16;
+    din.medium = in->medium ? reinterpret_cast<uint32_t *>(med) : nullptr;
+    char *outp = base + ((4 * rec16 + (size_t)n * 4 + 63) & ~(size_t)63);
+    gpis_result_soa dout;
+    dout.rec = reinterpret_cast<float *>(outp);
+    cudaStream_t s = ctx->stream;
+    CUDA_TRY(cudaMemcpyAsync((void *)din.origin_near, in->origin_near, rec16, cudaMemcpyHostToDevice, s), "copy origins");
+    CUDA_TRY(cudaMemcpyAsync((void *)din.dir_far, in->dir_far, rec16, cudaMemcpyHostToDevice, s), "copy directions");
+    CUDA_TRY(cudaMemcpyAsync((void *)din.seeds, in->seeds, rec16, cudaMemcpyHostToDevice, s), "copy seeds");
+    if (in->prev)
+        CUDA_TRY(cudaMemcpyAsync((void *)din.prev, in->prev, rec16, cudaMemcpyHostToDevice, s), "copy prev");
+    else
+        CUDA_TRY(cudaMemsetAsync((void *)din.prev, 0, rec16, s), "clear prev");
+    if (in->medium)
+        CUDA_TRY(cudaMemcpyAsync((void *)din.medium, in->medium, (size_t)n * 4, cudaMemcpyHostToDevice, s), "copy media");
+    int rc = gpis_flights_submit(ctx, &din, &dout, n, s);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(out->rec, dout.rec, rec16 * 2, cudaMemcpyDeviceToHost, s), "copy results");
+    CUDA_TRY(cudaStreamSynchronize(s), "synchronize flights");
+    return GPIS_OK;
+}
+
+int gpis_status(gpis_ctx *ctx, gpis_counters *out, int reset)
+{
+    if (!ctx || !out) return fail(GPIS_EINVAL, "null argument");
+    CUDA_TRY(cudaDeviceSynchronize(), "synchronize");
+    CUDA_TRY(cudaMemcpy(out, ctx->d_counters, sizeof(gpis_counters), cudaMemcpyDeviceToHost), "read counters");
+    if (reset) CUDA_TRY(cudaMemset(ctx->d_counters, 0, sizeof(gpis_counters)), "reset counters");
+    return GPIS_OK;
+}
+
+static uint32_t h_xx1(uint32_t p)
+{
+    uint32_t h = p + 374761393u;
+    h = 668265263u * ((h << 17) | (h >> 15));
+    h = 2246822519u * (h ^ (h >> 15));
+    h = 3266489917u * (h ^ (h >> 13));
+    return h ^ (h >> 16);
+}
+
+static uint32_t h_xx4(uint32_t x, uint32_t y, uint32_t z, uint32_t w)
+{
+    uint32_t h = w + 374761393u + x * 3266489917u;
+    h = 668265263u * ((h << 17) | (h >> 15));
+    h += y * 3266489917u;
+    h = 668265263u * ((h << 17) | (h >> 15));
+    h += z * 3266489917u;
+    h = 668265263u * ((h << 17) | (h >> 15));
+    h = 2246822519u * (h ^ (h >> 15));
+    h = 3266489917u * (h ^ (h >> 13));
+    return h ^ (h >> 16);
+}
+
+void gpis_flight_seeds(const gpis_medium_desc *d, const uint32_t pss[4], uint32_t scene_seed,
+                       uint32_t *noise_seed, uint32_t *normal_seed)
+{
+    if (!d || !pss) return;
+    const uint32_t w = d->correlation_context == GPIS_CTX_GLOBAL ? 0u : pss[3];
+    uint32_t seed = d->seed;
+    if (!d->single_realization) seed += h_xx4(pss[0], pss[1], pss[2], w) + h_xx1(scene_seed);
+    if (noise_seed) *noise_seed = seed;
+    if (normal_seed) *normal_seed = h_xx4(pss[0], pss[1], pss[2], pss[3]) + h_xx1(scene_seed) + 1u;
+}
+
+int gpis_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n, uint32_t impulses,
+                        float *pos, float *weight)
+{
+    if (impulses > (uint32_t)gpis::kMaxImpulses) return fail(GPIS_ERANGE, "at most %d impulses", gpis::kMaxImpulses);
+    if (n && (!cells || !seeds || !pos || !weight)) return fail(GPIS_EINVAL, "null argument");
+    CUDA_TRY(gpis::upload_pcg_table(), "upload PCG table");
+    CUDA_TRY(gpis::launch_debug_cells_1d(cells, seeds, n, impulses, pos, weight, 0), "launch");
+    CUDA_TRY(cudaDeviceSynchronize(), "synchronize");
+    return GPIS_OK;
+}
+
+int gpis_debug_cells_3d(const int32_t *cells, const uint32_t *seeds, uint32_t n, uint32_t impulses,
+                        uint32_t xyz_order, float *pos, float *weight)
+{
+    if (impulses > (uint32_t)gpis::kMaxImpulses) return fail(GPIS_ERANGE, "at most %d impulses", gpis::kMaxImpulses);
+    if (n && (!cells || !seeds || !pos || !weight)) return fail(GPIS_EINVAL, "null argument");
+    CUDA_TRY(gpis::upload_pcg_table(), "upload PCG table");
+    CUDA_TRY(gpis::launch_debug_cells_3d(cells, seeds, n, impulses, xyz_order, pos, weight, 0), "launch");
+    CUDA_TRY(cudaDeviceSynchronize(), "synchronize");
+    return GPIS_OK;
+}
+
+int gpis_debug_field(gpis_ctx *ctx, const float *origins, const float *points, const float *dirs,
+                     const uint32_t *seeds, const float *prev, uint32_t n, float *out)
+{
+    if (!ctx) return fail(GPIS_EINVAL, "null context");
+    if (n && (!origins || !points || !dirs || !seeds || !prev || !out)) return fail(GPIS_EINVAL, "null argument");
+    CUDA_TRY(gpis::launch_debug_field(ctx->d_media, reinterpret_cast<const float4 *>(origins),
+                                      reinterpret_cast<const float4 *>(points), reinterpret_cast<const float4 *>(dirs),
+                                      reinterpret_cast<const uint4 *>(seeds), reinterpret_cast<const float4 *>(prev), n,
+                                      reinterpret_cast<float4 *>(out), 0),
+             "launch");
+    CUDA_TRY(cudaDeviceSynchronize(), "synchronize");
+    return GPIS_OK;
+}
+
+int gpis_se_splat_1d(const float *queries, const float *centers, float *values, float *derivatives, size_t count,
+                     float local_scale, void *cuda_stream)
+{
+    if (!(std::isfinite(local_scale) && local_scale > 0.0f)) return fail(GPIS_EINVAL, "local_scale must be finite and > 0");
+    if (count == 0) return GPIS_OK;
+    if (!queries || !centers || !values || !derivatives) return fail(GPIS_EINVAL, "null argument");
+    CUDA_TRY(gpis::launch_se_splat_1d(queries, centers, values, derivatives, count, local_scale,
+                                      static_cast<cudaStream_t>(cuda_stream)),
+             "launch");
+    return GPIS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,163 @@
+"""Context objects over the C ABI (gpis_ctx_*), with torch tensors as device memory.
+
+``Context.trace_host`` is the blocking host-array entry (gpis_flights_trace_host);
+``Context.submit`` enqueues a batch whose streams already live in HBM
+(gpis_flights_submit).  Both raise :class:`abi.GpisError` on any failure; there is
+no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import abi
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class DeviceFlights:
+    """Flight streams and result records resident on the GPU (torch tensors)."""
+
+    def __init__(self, batch, device="cuda"):
+        torch = _torch()
+        self.n = batch.n
+        self.origin_near = torch.from_numpy(batch.origin_near).to(device)
+        self.dir_far = torch.from_numpy(batch.dir_far).to(device)
+        self.seeds = torch.from_numpy(batch.seeds.view(np.int32)).to(device)
+        self.prev = torch.from_numpy(batch.prev).to(device)
+        self.medium = None
+        if batch.medium is not None:
+            self.medium = torch.from_numpy(batch.medium.view(np.int32)).to(device)
+        self.rec = torch.zeros((self.n, 8), dtype=torch.float32, device=device)
+
+    def soa(self):
+        s = abi.FlightSoA()
+        s.origin_near = self.origin_near.data_ptr()
+        s.dir_far = self.dir_far.data_ptr()
+        s.seeds = self.seeds.data_ptr()
+        s.prev = self.prev.data_ptr()
+        s.medium = self.medium.data_ptr() if self.medium is not None else None
+        return s
+
+    def result_soa(self):
+        r = abi.ResultSoA()
+        r.rec = self.rec.data_ptr()
+        return r
+
+    def results(self):
+        return self.rec.cpu().numpy()
+
+
+class Context:
+    """A gpis_ctx over one or more media on the current CUDA device."""
+
+    def __init__(self, media):
+        if isinstance(media, abi.MediumDesc):
+            media = [media]
+        self.lib = abi.load_library()
+        self._media = list(media)
+        arr = (abi.MediumDesc * len(media))(*media)
+        h = ctypes.c_void_p()
+        abi.check(self.lib.gpis_ctx_create(arr, len(media), ctypes.byref(h)), "gpis_ctx_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.gpis_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def trace_host(self, batch, rec=None):
+        if rec is None:
+            rec = abi.new_results(batch.n)
+        soa = batch.soa()
+        res = abi.result_soa(rec)
+        abi.check(self.lib.gpis_flights_trace_host(self.h, ctypes.byref(soa), ctypes.byref(res), batch.n),
+                  "gpis_flights_trace_host")
+        return rec
+
+    def submit(self, dev, stream=None):
+        """Enqueue a DeviceFlights batch on a CUDA stream (torch stream or None)."""
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        soa = dev.soa()
+        res = dev.result_soa()
+        abi.check(self.lib.gpis_flights_submit(self.h, ctypes.byref(soa), ctypes.byref(res), dev.n,
+                                               ctypes.c_void_p(s.cuda_stream)), "gpis_flights_submit")
+
+    def counters(self, reset=False):
+        c = abi.Counters()
+        abi.check(self.lib.gpis_status(self.h, ctypes.byref(c), int(reset)), "gpis_status")
+        return {k: int(getattr(c, k)) for k, _ in abi.Counters._fields_}
+
+    def debug_field(self, origins, points, dirs, seeds, prev):
+        """Field/noise at points on the device; returns (n, 8) float32."""
+        torch = _torch()
+        n = len(points)
+
+        def dev4(a, dt=np.float32):
+            x = np.zeros((n, 4), dt)
+            a = np.asarray(a)
+            x[:, :a.shape[1]] = a
+            if dt == np.uint32:
+                x = x.view(np.int32)
+            return torch.from_numpy(x).cuda()
+
+        o, p, d = dev4(origins), dev4(points), dev4(dirs)
+        s, pv = dev4(seeds, np.uint32), dev4(prev)
+        out = torch.zeros((n, 8), dtype=torch.float32, device="cuda")
+        abi.check(self.lib.gpis_debug_field(self.h, o.data_ptr(), p.data_ptr(), d.data_ptr(), s.data_ptr(),
+                                            pv.data_ptr(), n, out.data_ptr()), "gpis_debug_field")
+        return out.cpu().numpy()
+
+
+def debug_cells_1d(cells, seeds, impulses):
+    torch = _torch()
+    lib = abi.load_library()
+    n = len(cells)
+    c = torch.from_numpy(np.asarray(cells, np.uint32).view(np.int32)).cuda()
+    s = torch.from_numpy(np.asarray(seeds, np.uint32).view(np.int32)).cuda()
+    pos = torch.zeros(n * impulses, dtype=torch.float32, device="cuda")
+    w = torch.zeros(n * impulses, dtype=torch.float32, device="cuda")
+    abi.check(lib.gpis_debug_cells_1d(c.data_ptr(), s.data_ptr(), n, impulses, pos.data_ptr(), w.data_ptr()),
+              "gpis_debug_cells_1d")
+    return pos.cpu().numpy().reshape(n, impulses), w.cpu().numpy().reshape(n, impulses)
+
+
+def debug_cells_3d(cells, seeds, impulses, order=0):
+    torch = _torch()
+    lib = abi.load_library()
+    n = len(cells)
+    c = torch.from_numpy(np.ascontiguousarray(cells, np.int32)).cuda()
+    s = torch.from_numpy(np.asarray(seeds, np.uint32).view(np.int32)).cuda()
+    pos = torch.zeros(n * impulses * 3, dtype=torch.float32, device="cuda")
+    w = torch.zeros(n * impulses, dtype=torch.float32, device="cuda")
+    abi.check(lib.gpis_debug_cells_3d(c.data_ptr(), s.data_ptr(), n, impulses, order, pos.data_ptr(),
+                                      w.data_ptr()), "gpis_debug_cells_3d")
+    return pos.cpu().numpy().reshape(n, impulses, 3), w.cpu().numpy().reshape(n, impulses)
+
+
+def se_splat_1d(q, c, scale):
+    torch = _torch()
+    lib = abi.load_library()
+    qd = torch.from_numpy(np.ascontiguousarray(q, np.float32)).cuda()
+    cd = torch.from_numpy(np.ascontiguousarray(c, np.float32)).cuda()
+    v = torch.zeros_like(qd)
+    dv = torch.zeros_like(qd)
+    abi.check(lib.gpis_se_splat_1d(qd.data_ptr(), cd.data_ptr(), v.data_ptr(), dv.data_ptr(), len(q),
+                                   float(scale), None), "gpis_se_splat_1d")
+    torch.cuda.synchronize()
+    return v.cpu().numpy(), dv.cpu().numpy()

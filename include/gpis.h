@@ -217,8 +217,10 @@ int gpis_debug_cells_3d(const int32_t *cells, const uint32_t *seeds, uint32_t n,
 /* Field evaluation at n points (device pointers): points/dirs n x 4 floats,
  * seeds n x 4 words as in the flight seed stream, prev n x 4 floats.  The
  * conditioning of each point's flight is built from (origin = points of the
- * "origins" stream) exactly as a flight would.  out = n x 4 floats
- * {noise value (normalized), dnoise/dz (1D) or unused, field value, mean}.   */
+ * "origins" stream) exactly as a flight would.  out = n x 8 floats:
+ * {noise value (normalized), n1, n2, n3, field value, mean, 0, 0} where
+ * (n1, n2, n3) is, for 1D noise, (conditioning x splat, conditioning y splat,
+ * dnoise/dz) and, for 3D noise, the world gradient of the normalized noise. */
 int gpis_debug_field(gpis_ctx *ctx, const float *origins, const float *points,
                      const float *dirs, const uint32_t *seeds, const float *prev,
                      uint32_t n, float *out);
