@@ -1,0 +1,341 @@
+"""Benchmark of the GPIS ray-flight path on GB300.
+
+Workload (one "step"): the batched flight microbenchmark -- 2^22 primary flights
+through the stationary SE field over the unit-sphere SDF (sigma 0.05, l 0.1,
+localScale 3, 8 impulses per cell, cell hash seeded 1, 1D noise, Renewal+,
+step 0.01, min_step 8), origins on a radius-3 sphere aimed at uniform points of
+the unit ball (seed 7), clipped to the cube |x|,|y|,|z| <= 1.5; followed by the
+conditioned secondary flights reflected at every primary hit.  Inputs are
+seeded synthetic data generated once; every step re-traces all flights.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  `value` is device-resident throughput (flights/s,
+inputs already in HBM, 512 MiB of flight streams > L2 so no flush is needed);
+`e2e` is the same metric through gpis_flights_trace_host from pinned host
+buffers (copies inside the timed region); `roofline` is the march kernel's
+algorithmic FP32 rate against cuBLAS SGEMM measured in the same run;
+`cpu_baseline` is the oracle (CPU restatement) on all host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GPIS ray-flights/s on 1 GB300: plain vs learned proposal at equal image RMSE"
+UNIT = "flights/s"
+WORKLOAD = ("batched sphere-field flights: 2^22 primary (seed 7, radius-3 origins, cube 1.5) + "
+            "conditioned secondary reflections, 1D SE Renewal+, sigma 0.05, l 0.1, N 8, step 0.01")
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi SM clock and throttle-reason samples during a timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        self.lines += [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def sgemm_peak_tflops(torch):
+    """FP32 FFMA peak as cuBLAS SGEMM delivers it (TF32 off), best of 5, 8192^3."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        for _ in range(2):
+            torch.mm(a, b)
+        best = None
+        for _ in range(5):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            torch.mm(a, b)
+            e.record()
+            torch.cuda.synchronize()
+            ms = s.elapsed_time(e)
+            best = ms if best is None else min(best, ms)
+        del a, b
+        return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def load_traffic():
+    """Per-flight DRAM bytes of the march kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "march_dram.json")
+    if not os.path.exists(p):
+        return None
+    try:
+        return json.load(open(p))
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(desc, prim, sec, target_s=8.0):
+    """The oracle on all host cores over a bounded sample of the same flights."""
+    from oracle import oracle
+    cores = os.cpu_count() or 1
+    m = 4096
+    t0 = time.perf_counter()
+    oracle.trace_flights(desc, prim.subset(np.arange(m)), n_threads=0)
+    oracle.trace_flights(desc, sec.subset(np.arange(min(m, sec.n))), n_threads=0)
+    dt = time.perf_counter() - t0
+    rate = (m + min(m, sec.n)) / dt
+    m2 = int(min(prim.n, max(4096, rate * target_s / 2)))
+    s2 = min(m2, sec.n)
+    t0 = time.perf_counter()
+    oracle.trace_flights(desc, prim.subset(np.arange(m2)), n_threads=0)
+    oracle.trace_flights(desc, sec.subset(np.arange(s2)), n_threads=0)
+    dt = time.perf_counter() - t0
+    return {"value": (m2 + s2) / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {m2} primary + first {s2} secondary flights of the workload, "
+                      f"oracle (C restatement, float mode) on {cores} threads, {dt:.1f} s"}
+
+
+def run_reference(args, world, rank):
+    """The reference arm: the reference's CPU path for this workload, timed on the
+    host cores.  The reference CPU library does not build here (Boost, TBB,
+    OpenVDB, OpenEXR absent), so the arm runs the oracle port with all threads."""
+    if rank != 0:
+        return
+    from gpis_extend_gb300 import abi, workloads
+    from oracle import oracle
+    desc = workloads.sphere_medium()
+    n = args.flights
+    prim = workloads.sphere_flights(n, desc)
+    # secondary flights come from the oracle's own primary hits on the sampled range
+    cores = os.cpu_count() or 1
+    per_step = args.ref_sample
+    prim_s = prim.subset(np.arange(per_step))
+    rec = oracle.trace_flights(desc, prim_s)
+    sec_s, _ = workloads.secondary_flights(prim_s, rec, desc)
+    for _ in range(args.warmup):
+        oracle.trace_flights(desc, prim_s)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.trace_flights(desc, prim_s)
+        oracle.trace_flights(desc, sec_s)
+    dt = time.perf_counter() - t0
+    flights = args.steps * (prim_s.n + sec_s.n)
+    value = flights / dt
+    sample = (f"per step the first {prim_s.n} primary flights of the workload and their "
+              f"{sec_s.n} conditioned secondaries, oracle port on {cores} threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "arm": "reference CPU path (oracle port: the reference "
+                   "CPU library needs Boost/TBB/OpenVDB/OpenEXR, absent on this image)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--flights", type=int, default=1 << 22)
+    ap.add_argument("--ref-sample", type=int, default=1 << 16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    world, rank, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    from gpis_extend_gb300 import abi, build, roofline, runtime, workloads
+
+    build.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
+    desc = workloads.sphere_medium()
+    n = args.flights
+    prim = workloads.sphere_flights(n, desc, index_offset=rank * n)
+    ctx = runtime.Context(desc)
+    rec = ctx.trace_host(prim)
+    sec, _ = workloads.secondary_flights(prim, rec, desc)
+    dev_p = runtime.DeviceFlights(prim)
+    dev_s = runtime.DeviceFlights(sec)
+    flights_per_step = prim.n + sec.n
+    stream = torch.cuda.current_stream()
+
+    # ---- device-resident throughput --------------------------------------------
+    for _ in range(args.warmup):
+        ctx.submit(dev_p, stream)
+        ctx.submit(dev_s, stream)
+    torch.cuda.synchronize()
+    ctx.counters(reset=True)
+    ctx.profile_read(reset=True)
+    ctx.profile(True)
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        ctx.submit(dev_p, stream)
+        ctx.submit(dev_s, stream)
+    end.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = start.elapsed_time(end)
+    ctx.profile(False)
+    kms, klaunch = ctx.profile_read(reset=True)
+    cnt = ctx.counters(reset=True)
+    ms_max = max_over_ranks(ms)
+    total_flights = sum_over_ranks(float(flights_per_step * args.steps))
+    value = total_flights / (ms_max * 1e-3)
+
+    # ---- end to end through the host entry point -------------------------------
+    pin_p = runtime.PinnedFlights(prim)
+    pin_s = runtime.PinnedFlights(sec)
+    ctx.trace_pinned(pin_p)
+    ctx.trace_pinned(pin_s)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.trace_pinned(pin_p)
+        ctx.trace_pinned(pin_s)
+    t_e2e = time.perf_counter() - t0
+    barrier()
+    clocks.stop()
+    e2e_value = sum_over_ranks(float(flights_per_step * args.steps)) / max_over_ranks(t_e2e)
+    h2d = roofline.BYTES_IN_PER_FLIGHT * flights_per_step
+    d2h = roofline.BYTES_OUT_PER_FLIGHT * flights_per_step
+
+    # ---- roofline of the march kernel ------------------------------------------
+    march_launches = max(1, klaunch[1])
+    march_ms = kms[1] / march_launches
+    evals_march = cnt["steps"] + cnt["refine_evals"] + cnt["flights"] + (cnt["flights"] - cnt["hits"])
+    flops = evals_march * roofline.flops_per_eval_1d(8) / march_launches
+    achieved = flops / (march_ms * 1e-3) / 1e12
+    peak = sgemm_peak_tflops(torch) if rank == 0 else None
+    traffic = None
+    tr = load_traffic()
+    if tr and tr.get("bytes_per_flight"):
+        traffic = tr["bytes_per_flight"] * flights_per_step / 2.0
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": (achieved / peak) if peak else None, "traffic": traffic,
+            "kernel": "k_march<EvalCached1D<8>>",
+            "march_ms_per_launch": march_ms,
+            "kernel_ms_per_step": [k / max(1, args.steps) for k in kms],
+            "flops_per_eval": roofline.flops_per_eval_1d(8),
+            "evals_per_launch": evals_march / march_launches,
+            "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, best of 5, measured in this run"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "arm": "plain", "flights_per_step_per_gpu": flights_per_step,
+                   "primary": prim.n, "secondary": sec.n, "l2": "inputs 512 MiB > L2 (no flush)",
+                   "parallelism": f"replicas x{world} (disjoint flight ranges)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps * 2 * 3,
+        "roofline": roof,
+        "counters": {k: v for k, v in cnt.items() if k != "reserved"},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(desc, prim, sec)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -272,6 +272,8 @@ def load_library(path=None):
         "gpis_flights_submit": (c_int, [vp, P(FlightSoA), P(ResultSoA), c_u32, vp]),
         "gpis_flights_trace_host": (c_int, [vp, P(FlightSoA), P(ResultSoA), c_u32]),
         "gpis_status": (c_int, [vp, P(Counters), c_int]),
+        "gpis_profile_enable": (c_int, [vp, c_int]),
+        "gpis_profile_read": (c_int, [vp, P(ctypes.c_double), P(ctypes.c_uint64), c_int]),
         "gpis_flight_seeds": (None, [P(MediumDesc), P(c_u32), c_u32, P(c_u32), P(c_u32)]),
         "gpis_debug_cells_1d": (c_int, [vp, vp, c_u32, c_u32, vp, vp]),
         "gpis_debug_cells_3d": (c_int, [vp, vp, c_u32, c_u32, c_u32, vp, vp]),

@@ -34,6 +34,9 @@ struct DevMedium {
     float kr_world;         // cell size of 3D world noise
     float inv_norm1d;       // 1 / sqrt(sparseConvNoiseVariance1D)
     float inv_norm3d;       // 1 / sqrt(sparseConvNoiseVariance3D)
+    float norm1d;           // sqrt(sparseConvNoiseVariance1D) as the reference rounds it
+    float norm3d;           // sqrt(sparseConvNoiseVariance3D)
+    float cov_den2;         // 2 * sqr(float(sqrt(2))): covarianceKernel1DVal denominator
     float kexp1d;           // exp(-(kr*d)^2/2) = ex2(kexp1d * d * d)
     float kexp3d[3];        // 3D splat: ex2(sum_c kexp3d[c] * (kr*d_c)^2)
     float m3[3];            // 3D splat inverse covariance diagonal (isCov = false)
@@ -183,6 +186,77 @@ __device__ __forceinline__ float ff_point(float o, float d, float hi, float lo)
     const float s = two_sum(o, a, se);
     const float r = __fadd_rn(se, __fadd_rn(ae, b));
     return __fadd_rn(s, r);
+}
+
+// ---- float-float arithmetic (about 48 significant bits) -------------------------
+struct FF {
+    float h, l;
+};
+
+__device__ __forceinline__ FF ff_norm(float h, float l)
+{
+    const float s = __fadd_rn(h, l);
+    return {s, __fsub_rn(l, __fsub_rn(s, h))};
+}
+
+__device__ __forceinline__ FF ff_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    float e;
+    const float s = two_sum(a.h, b.h, e);
+    return ff_norm(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+
+__device__ __forceinline__ FF ff_add_f(FF a, float b)
+{
+    float e;
+    const float s = two_sum(a.h, b, e);
+    return ff_norm(s, __fadd_rn(e, a.l));
+}
+
+__device__ __forceinline__ FF ff_mul(FF a, FF b)
+{
+    FF p = ff_prod(a.h, b.h);
+    return ff_norm(p.h, __fadd_rn(p.l, __fadd_rn(__fmul_rn(a.h, b.l), __fmul_rn(a.l, b.h))));
+}
+
+__device__ __forceinline__ FF ff_mul_f(FF a, float b)
+{
+    FF p = ff_prod(a.h, b);
+    return ff_norm(p.h, __fadd_rn(p.l, __fmul_rn(a.l, b)));
+}
+
+__device__ __forceinline__ FF ff_sq(FF a)
+{
+    FF p = ff_prod(a.h, a.h);
+    return ff_norm(p.h, __fadd_rn(p.l, __fmul_rn(2.0f * a.h, a.l)));
+}
+
+__device__ __forceinline__ FF ff_sqrt(FF a)
+{
+    const float r = __fsqrt_rn(a.h);
+    const FF r2 = ff_prod(r, r);
+    const float e = __fadd_rn(__fsub_rn(__fsub_rn(a.h, r2.h), r2.l), a.l);
+    return ff_norm(r, __fdiv_rn(e, __fmul_rn(2.0f, r)));
+}
+
+// a / b for floats a, b as a float-float quotient.
+__device__ __forceinline__ FF ff_div_ff(float a, FF b)
+{
+    const float q = __fdiv_rn(a, b.h);
+    const float r = __fsub_rn(__fmaf_rn(-q, b.h, a), __fmul_rn(q, b.l));
+    return ff_norm(q, __fdiv_rn(r, b.h));
+}
+
+// a <= c for a float-float a and the double c = ch + cl.
+__device__ __forceinline__ bool ff_le(FF a, float ch, float cl)
+{
+    return a.h < ch || (a.h == ch && a.l <= cl);
 }
 
 // double-precision point (refinement and gradient points are rare).

@@ -435,6 +435,147 @@ struct LaneField {
     float o[3];
 };
 
+// ---- precise evaluation ------------------------------------------------------
+// The reference's float formulation op for op: every splat as
+// expf(-((kr*t - kr*t_i)^2 / 2)) (GPFunctions.cpp:845-848), cell sums in impulse
+// order, cells summed in order, division by the rounded normalisation, the
+// conditioning splats of evaluateNoise1DNormalized, and the mean in double
+// (emulated in float-float for the sphere) added as
+// float(double(amplitude * noise) + mean) (SparseConvolutionNoise.cpp:114-130).
+// The march uses it wherever a sign decision is close: the crossing step, the
+// step before it and every refinement point.
+
+__device__ float noise1d_precise(const DevMedium &m, float z, uint32_t seed)
+{
+    const float kr = m.kr_iso;
+    const float tg = __fdiv_rn(z, kr);
+    const float fl = floorf(tg);
+    const float frac = __fsub_rn(tg, fl);
+    const int ci = (int)fl;
+    float sv = 0.0f;
+    for (int dx = -1; dx <= 1; ++dx) {
+        const float tl = __fsub_rn(frac, (float)dx);
+        const float a = __fmul_rn(kr, tl);
+        const uint32_t s = xxhash2((uint32_t)(ci + dx), seed) + 1u;
+        float cv = 0.0f;
+        for (uint32_t k = 0; k < m.n_imp; ++k) {
+            const float ti = unit_float(pcg_draw(c_jump[2 + 2 * k], s));
+            const uint32_t wr = pcg_draw(c_jump[3 + 2 * k], s);
+            const float tp = __fsub_rn(tl, ti);
+            if (fabsf(tp) < 1.0f) {
+                const float ab = __fsub_rn(a, __fmul_rn(kr, ti));
+                const float e = expf(-__fmul_rn(__fmul_rn(ab, ab), 0.5f));
+                cv = __fadd_rn(cv, (wr >> 31) ? e : -e);
+            }
+        }
+        sv = __fadd_rn(sv, cv);
+    }
+    return __fdiv_rn(sv, m.norm1d);
+}
+
+__device__ float noise3d_precise(const DevMedium &m, float px, float py, float pz, uint32_t seed)
+{
+    const float kr = m.kr_world;
+    const float p[3] = {px, py, pz};
+    float fr[3];
+    int ijk[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float q = __fdiv_rn(p[i], kr);
+        const float fl = floorf(q);
+        fr[i] = __fsub_rn(q, fl);
+        ijk[i] = (int)fl;
+    }
+    const bool xfirst = (m.flags & MF_XYZ_ORDER) != 0;
+    float sv = 0.0f;
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz) {
+                const float t0 = __fsub_rn(fr[0], (float)dx), t1 = __fsub_rn(fr[1], (float)dy),
+                            t2 = __fsub_rn(fr[2], (float)dz);
+                const uint32_t s = xxhash4((uint32_t)(ijk[2] + dz), (uint32_t)(ijk[1] + dy),
+                                           (uint32_t)(ijk[0] + dx), seed) + 1u;
+                float cv = 0.0f;
+                for (uint32_t k = 0; k < m.n_imp; ++k) {
+                    const int b = 2 + 4 * (int)k;
+                    const float r0 = unit_float(pcg_draw(c_jump[b], s));
+                    const float r1 = unit_float(pcg_draw(c_jump[b + 1], s));
+                    const float r2 = unit_float(pcg_draw(c_jump[b + 2], s));
+                    const uint32_t wr = pcg_draw(c_jump[b + 3], s);
+                    const float ix = xfirst ? r0 : r2, iy = r1, iz = xfirst ? r2 : r0;
+                    const float a0 = __fsub_rn(t0, ix), a1 = __fsub_rn(t1, iy), a2 = __fsub_rn(t2, iz);
+                    const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(a0, a0), __fmul_rn(a1, a1)), __fmul_rn(a2, a2));
+                    if (l2 < 1.0f) {
+                        const float b0 = __fsub_rn(__fmul_rn(kr, t0), __fmul_rn(kr, ix));
+                        const float b1 = __fsub_rn(__fmul_rn(kr, t1), __fmul_rn(kr, iy));
+                        const float b2 = __fsub_rn(__fmul_rn(kr, t2), __fmul_rn(kr, iz));
+                        float q = __fmul_rn(__fmul_rn(b0, m.m3[0]), b0);
+                        q = __fadd_rn(q, __fmul_rn(__fmul_rn(b1, m.m3[1]), b1));
+                        q = __fadd_rn(q, __fmul_rn(__fmul_rn(b2, m.m3[2]), b2));
+                        const float e = expf(-q);
+                        cv = __fadd_rn(cv, (wr >> 31) ? e : -e);
+                    }
+                }
+                sv = __fadd_rn(sv, cv);
+            }
+    return __fdiv_rn(sv, m.norm3d);
+}
+
+// float(double(an) + mean(p)) with the mean evaluated as the reference does in
+// double; the sphere's distance is emulated in float-float.
+__device__ float mean_plus_precise(const DevMedium &m, float an, float x, float y, float z, int &id)
+{
+    const float *q = m.mean_params;
+    id = 0;
+    if (m.mean_kind == 0) {
+        float e0, e1, e2;
+        const float h0 = two_sum(x, -q[0], e0), h1 = two_sum(y, -q[1], e1), h2 = two_sum(z, -q[2], e2);
+        FF s = ff_add(ff_add(ff_sq({h0, e0}), ff_sq({h1, e1})), ff_sq({h2, e2}));
+        FF len = ff_sqrt(s);
+        FF mean = ff_add_f(len, -q[3]);
+        FF tot = ff_add_f(mean, an);
+        return __fadd_rn(tot.h, tot.l);
+    }
+    if (m.mean_kind == 3) {
+        FF d = ff_add(ff_add(ff_prod(q[0], x), ff_prod(q[1], y)), ff_prod(q[2], z));
+        FF tot = ff_add_f(ff_add_f(d, -q[3]), an);
+        return __fadd_rn(tot.h, tot.l);
+    }
+    const float mv = mean_value(m, x, y, z, id);
+    float e;
+    const float s = two_sum(an, mv, e);
+    return __fadd_rn(s, e);
+}
+
+__device__ float field_precise(const LaneField &L, float px, float py, float pz, int &id)
+{
+    const DevMedium &m = *L.m;
+    float noise;
+    if (m.flags & MF_ONE_D) {
+        const float z = ray_coord(L.li, L.n, px, py, pz);
+        noise = noise1d_precise(m, z, L.seed);
+        if (L.cond) {
+            // covarianceKernel1D / 1DGrad value parts (GPFunctions.cpp:850-862)
+            const float d = __fsub_rn(z, L.ozc);
+            const float k0 = expf(-__fdiv_rn(__fmul_rn(d, d), m.cov_den2));
+            const float k1 = -2.0f * d / m.cov_den2 * k0;
+            const float vs0 = __fmul_rn(L.vs, k0);
+            const float gz0 = __fmul_rn(__fmul_rn(1.0f, L.gsz), k1);
+            noise = __fadd_rn(noise, __fmul_rn(1.0f, __fadd_rn(vs0, gz0)));
+        }
+    } else {
+        noise = noise3d_precise(m, px, py, pz, L.seed);
+        if (L.cond) {
+            float cv, cg[3];
+            const float p[3] = {px, py, pz};
+            cond3d(m, L.c3, L.o, p, cv, cg);
+            noise = __fadd_rn(noise, cv);
+        }
+    }
+    return mean_plus_precise(m, __fmul_rn(L.sigma, noise), px, py, pz, id);
+}
+
+// ---- fast evaluators ----------------------------------------------------------
 // Generic evaluator: recomputes every impulse (any impulse count, 1D or 3D).
 struct EvalGeneric {
     __device__ __forceinline__ void reset() {}
@@ -546,16 +687,18 @@ struct EvalCached1D {
     }
 };
 
-enum : int { PH_IDLE = 0, PH_F0, PH_MARCH, PH_REFINE, PH_FAR };
+// Phases of a lane's flight.  The fast evaluator marches; a precise evaluation
+// re-decides every step whose fast value is within the band of zero or changed
+// sign, evaluates the step before a crossing (when that one was fast) and every
+// refinement point.
+enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE, PH_FAR };
+
+// Fast values farther than this from zero have the sign of the precise value.
+constexpr float kPreciseBand = 1e-5f;
 
 __device__ __forceinline__ bool t_less(float hi, float lo, float far_t)
 {
     return hi < far_t || (hi == far_t && lo < 0.0f);
-}
-
-__device__ __forceinline__ double lerp_d(double a, double b, double r)
-{
-    return __dadd_rn(__dmul_rn(a, __dsub_rn(1.0, r)), __dmul_rn(b, r));
 }
 
 __device__ __forceinline__ unsigned long long warp_sum(uint32_t v)
@@ -574,17 +717,19 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
 {
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
+    // 0.9 and 0.01 as float-float pairs (the reference's double constants)
+    const FF kNine = {0.9f, -2.38418579e-08f};
+    const float kHundredthH = 0.01f, kHundredthL = -2.23517418e-10f;
     Eval ev;
     ev.reset();
     LaneField L;
     L.m = a.media;
     int phase = PH_IDLE;
-    bool drained = false, first = true;
-    uint32_t fid = 0, steps = 0, max_steps = 1;
-    float d[3] = {0, 0, 0}, near_t = 0, far_t = 0, step = 0, t0 = 0, th = 0, tl = 0, pf = 0;
+    bool drained = false, first = true, pf_precise = false;
+    uint32_t fid = 0, steps = 0, max_steps = 1, refine_iter = 0;
+    float d[3] = {0, 0, 0}, near_t = 0, far_t = 0, step = 0, t0 = 0, th = 0, tl = 0, pf = 0, fb = 0;
     int sign0 = 1, gpid = 0;
-    double ta = 0, tb = 0, fac = 0, tprev = 0, ttest = 0;
-    uint32_t refine_iter = 0;
+    FF ta = {0, 0}, fac = {0, 0}, tprev = {0, 0}, ttest = {0, 0};
     uint32_t c_flights = 0, c_steps = 0, c_refine = 0, c_hits = 0, c_limit = 0, c_invalid = 0, c_refills = 0;
 
     for (;;) {
@@ -656,21 +801,21 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
         }
         if (!live) continue;
 
+        // evaluation point of this phase
+        float eh = th, el = tl;
+        if (phase == PH_REFINE) { eh = ttest.h; el = ttest.l; }
+        if (phase == PH_PF) { eh = ta.h; el = ta.l; }
         float p[3];
-        if (phase == PH_REFINE) {
 #pragma unroll
-            for (int k = 0; k < 3; ++k) p[k] = dd_point(L.o[k], d[k], ttest);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], th, tl);
-        }
+        for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], eh, el);
         int id;
-        const float f = ev.value(L, p[0], p[1], p[2], id, c_refills);
+        const bool precise = phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE;
+        const float f = precise ? field_precise(L, p[0], p[1], p[2], id) : ev.value(L, p[0], p[1], p[2], id, c_refills);
         gpid = id;
         const int sg = f < 0.0f ? -1 : 1;
         bool done = false;
         float t_out = 0.0f, v_out = 0.0f, trans = 1.0f;
-        double t_end = 0.0;
+        FF t_end = {0.0f, 0.0f};
         uint32_t status = GPIS_FLIGHT_OK;
 
         if (!isfinite(f)) {
@@ -678,9 +823,12 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
             done = true;
             status = GPIS_FLIGHT_INVALID_INPUT;
             c_invalid++;
-        } else if (phase == PH_F0) {
+        } else if (phase == PH_F0 && fabsf(f) < kPreciseBand) {
+            phase = PH_F0_P;
+        } else if (phase == PH_F0 || phase == PH_F0_P) {
             sign0 = sg;
             pf = f;
+            pf_precise = phase == PH_F0_P;
             th = t0;
             tl = 0.0f;
             if (t_less(th, tl, far_t)) {
@@ -689,7 +837,10 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                 phase = PH_FAR;
                 th = far_t;
             }
-        } else if (phase == PH_MARCH) {
+        } else if (phase == PH_MARCH && (fabsf(f) < kPreciseBand || (sg != sign0 && (first || steps != 0)))) {
+            // close to zero or a candidate crossing: decide on the precise value
+            phase = PH_MARCH_P;
+        } else if (phase == PH_MARCH || phase == PH_MARCH_P) {
             steps++;
             c_steps++;
             bool crossed = false;
@@ -697,18 +848,27 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                 sign0 = sg;
             } else if (sg != sign0) {
                 crossed = true;
-                const double tc = (double)th + (double)tl;
-                ta = __dsub_rn(tc, (double)step);
-                tb = tc;
-                fac = __ddiv_rn((double)pf, __dsub_rn((double)pf, (double)f));
-                ttest = lerp_d(ta, tb, fac);
-                tprev = ttest;
-                refine_iter = 0;
-                phase = PH_REFINE;
             }
-            if (!crossed) {
+            if (crossed) {
+                // tb = t, ta = t - step (exact); the back-off starts at the regula-falsi point
+                ta = ff_add_f(ff_norm(th, tl), -step);
+                fb = f;
+                if (!pf_precise) {
+                    phase = PH_PF;  // re-evaluate the step before the crossing precisely first
+                } else {
+                    float e;
+                    const float dh = two_sum(pf, -fb, e);
+                    fac = ff_div_ff(pf, {dh, e});
+                    ttest = ff_add(ta, ff_mul_f(fac, step));
+                    tprev = ttest;
+                    refine_iter = 0;
+                    phase = PH_REFINE;
+                }
+            } else {
                 pf = f;
+                pf_precise = phase == PH_MARCH_P;
                 ff_add(th, tl, step);
+                phase = PH_MARCH;
                 if (!t_less(th, tl, far_t)) {
                     phase = PH_FAR;
                     th = far_t;
@@ -717,10 +877,20 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                     done = true;
                     status = GPIS_FLIGHT_STEP_LIMIT;
                     t_out = far_t;
-                    t_end = far_t;
+                    t_end = {far_t, 0.0f};
                     c_limit++;
                 }
             }
+        } else if (phase == PH_PF) {
+            // f: precise value at ta; fb: precise value at tb
+            pf = f;
+            float e;
+            const float dh = two_sum(pf, -fb, e);
+            fac = ff_div_ff(pf, {dh, e});
+            ttest = ff_add(ta, ff_mul_f(fac, step));
+            tprev = ttest;
+            refine_iter = 0;
+            phase = PH_REFINE;
         } else if (phase == PH_REFINE) {
             c_refine++;
             refine_iter++;
@@ -728,21 +898,21 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
             if (sg == sign0) {
                 hit = true;
             } else {
-                fac = __dmul_rn(fac, 0.9);
+                fac = ff_mul(fac, kNine);
                 // 0.9^44 < 0.01: the back-off ends within 44 evaluations for any
                 // factor <= 1; the explicit bound also covers a non-finite factor.
-                if (fac <= 0.01 || !(fac == fac) || refine_iter >= 64) {
-                    tprev = 0.0;
+                if (ff_le(fac, kHundredthH, kHundredthL) || !(fac.h == fac.h) || refine_iter >= 64) {
+                    tprev = {0.0f, 0.0f};
                     hit = true;
                 } else {
                     tprev = ttest;
-                    ttest = lerp_d(ta, tb, fac);
+                    ttest = ff_add(ta, ff_mul_f(fac, step));
                 }
             }
             if (hit) {
                 done = true;
                 t_end = tprev;
-                t_out = (float)tprev;
+                t_out = __fadd_rn(tprev.h, tprev.l);
                 v_out = 0.0f;
                 trans = 0.0f;
                 c_hits++;
@@ -750,12 +920,12 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
         } else {  // PH_FAR
             done = true;
             t_out = far_t;
-            t_end = far_t;
+            t_end = {far_t, 0.0f};
             v_out = f;
         }
         if (done) {
             write_status(a, fid, t_out, v_out, trans, steps, status | ((uint32_t)gpid << 8));
-            a.t_end[fid] = t_end;
+            a.t_end[fid] = (double)t_end.h + (double)t_end.l;
             phase = PH_IDLE;
         }
     }
@@ -942,11 +1112,13 @@ __global__ void k_se_splat_1d(const float *q, const float *c, float *v, float *d
 
 }  // namespace
 
-cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream)
+cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream, cudaEvent_t *ev)
 {
     if (a.n == 0) return cudaSuccess;
     const uint32_t blocks = (a.n + 127) / 128;
+    if (ev) cudaEventRecord(ev[0], stream);
     if (a.any_cond) k_prepare<<<blocks, 128, 0, stream>>>(a);
+    if (ev) cudaEventRecord(ev[1], stream);
     cudaError_t err = cudaMemsetAsync(a.work, 0, sizeof(uint32_t), stream);
     if (err != cudaSuccess) return err;
     // persistent grid: a few resident CTAs per SM, never more warps than flights
@@ -955,11 +1127,15 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     const uint32_t ctas_needed = (warps_needed + 7) / 8;
     if (ctas > ctas_needed) ctas = ctas_needed;
     if (ctas == 0) ctas = 1;
+    if (ev) cudaEventRecord(ev[2], stream);
     if (a.one_d && a.max_imp <= 8)
         k_march<EvalCached1D<8>><<<ctas, 256, 0, stream>>>(a);
     else
         k_march<EvalGeneric><<<ctas, 256, 0, stream>>>(a);
+    if (ev) cudaEventRecord(ev[3], stream);
+    if (ev) cudaEventRecord(ev[4], stream);
     k_finish<<<blocks, 128, 0, stream>>>(a);
+    if (ev) cudaEventRecord(ev[5], stream);
     return cudaGetLastError();
 }
 

@@ -42,8 +42,9 @@ struct FlightArgs {
 // Upload the jump-ahead PCG table to the current device (once per device).
 cudaError_t upload_pcg_table();
 
-// Enqueue the three flight kernels on the stream.
-cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream);
+// Enqueue the three flight kernels on the stream.  ev, when not null, holds
+// start/stop events for the prepare, march and finish kernels (ev[2k], ev[2k+1]).
+cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream, cudaEvent_t *ev = nullptr);
 
 // Unit-level kernels (synchronous wrappers live in gpis_abi.cu).
 cudaError_t launch_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n,

@@ -86,12 +86,19 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
     m.sigma = d.sigma;
     m.n_imp = (uint32_t)d.impulse_density;
     const float var1 = (float)((double)(d.impulse_density / m.kr_iso) * (std::sqrt(M_PI) * 1.0));
-    m.inv_norm1d = 1.0f / std::sqrt(var1);
+    m.norm1d = std::sqrt(var1);
+    m.inv_norm1d = 1.0f / m.norm1d;
+    {
+        // covarianceKernel1DVal(ab, 1) = exp(-(ab*ab / (2 * sqr(float(1 * sqrt(2)))))), GPFunctions.cpp:845-852
+        const float s2 = (float)(1.0 * std::sqrt(2.0));
+        m.cov_den2 = (float)(2.0 * (double)(s2 * s2));
+    }
     const float kr = m.kr_world;
     const float ud = d.impulse_density / (kr * kr * kr);
     const float det = m.l_aniso[0] * m.l_aniso[1] * m.l_aniso[2];
     const float var3 = (float)((double)ud * (std::pow(M_PI, 1.5) * (double)det));
-    m.inv_norm3d = 1.0f / std::sqrt(var3);
+    m.norm3d = std::sqrt(var3);
+    m.inv_norm3d = 1.0f / m.norm3d;
     const double log2e = 1.4426950408889634;
     m.kexp1d = (float)(-0.5 * (double)m.kr_iso * (double)m.kr_iso * log2e);
     for (int i = 0; i < 3; ++i) {
@@ -151,6 +158,12 @@ struct gpis_ctx {
     char *d_stage = nullptr;
     size_t stage_cap = 0;
     cudaStream_t stream = nullptr;
+    // per-kernel event timing (gpis_profile_*)
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;      // free events
+    std::vector<cudaEvent_t> ev_pending;   // groups of 6 recorded events
+    double prof_ms[3] = {0, 0, 0};
+    uint64_t prof_launches[3] = {0, 0, 0};
 };
 
 namespace {
@@ -165,6 +178,8 @@ void release(gpis_ctx *c)
     cudaFree(c->d_work);
     cudaFree(c->d_counters);
     cudaFree(c->d_stage);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->ev_pending) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -319,7 +334,57 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_res
                           (const void *)in->prev, (const void *)out->rec})
         if (p && (reinterpret_cast<uintptr_t>(p) & 15u))
             return fail(GPIS_EINVAL, "flight and result streams must be 16-byte aligned");
-    CUDA_TRY(gpis::launch_flights(a, ctx->num_sms, static_cast<cudaStream_t>(cuda_stream)), "launch flights");
+    cudaEvent_t *ev = nullptr;
+    cudaEvent_t evs[6];
+    if (ctx->profiling) {
+        for (int k = 0; k < 6; ++k) {
+            if (ctx->ev_pool.empty()) {
+                cudaEvent_t e;
+                CUDA_TRY(cudaEventCreate(&e), "create profiling event");
+                ctx->ev_pool.push_back(e);
+            }
+            evs[k] = ctx->ev_pool.back();
+            ctx->ev_pool.pop_back();
+            ctx->ev_pending.push_back(evs[k]);
+        }
+        ev = evs;
+    }
+    CUDA_TRY(gpis::launch_flights(a, ctx->num_sms, static_cast<cudaStream_t>(cuda_stream), ev), "launch flights");
+    if (ctx->profiling) {
+        ctx->prof_launches[0] += a.any_cond ? 1 : 0;
+        ctx->prof_launches[1] += 1;
+        ctx->prof_launches[2] += 1;
+    }
+    return GPIS_OK;
+}
+
+int gpis_profile_enable(gpis_ctx *ctx, int on)
+{
+    if (!ctx) return fail(GPIS_EINVAL, "null context");
+    ctx->profiling = on != 0;
+    return GPIS_OK;
+}
+
+int gpis_profile_read(gpis_ctx *ctx, double ms[3], uint64_t launches[3], int reset)
+{
+    if (!ctx || !ms || !launches) return fail(GPIS_EINVAL, "null argument");
+    for (size_t g = 0; g + 6 <= ctx->ev_pending.size(); g += 6) {
+        for (int k = 0; k < 3; ++k) {
+            CUDA_TRY(cudaEventSynchronize(ctx->ev_pending[g + 2 * k + 1]), "synchronize profiling event");
+            float t = 0.0f;
+            CUDA_TRY(cudaEventElapsedTime(&t, ctx->ev_pending[g + 2 * k], ctx->ev_pending[g + 2 * k + 1]),
+                     "read profiling event");
+            ctx->prof_ms[k] += t;
+        }
+    }
+    for (cudaEvent_t e : ctx->ev_pending) ctx->ev_pool.push_back(e);
+    ctx->ev_pending.clear();
+    for (int k = 0; k < 3; ++k) {
+        ms[k] = ctx->prof_ms[k];
+        launches[k] = ctx->prof_launches[k];
+    }
+    if (reset)
+        for (int k = 0; k < 3; ++k) { ctx->prof_ms[k] = 0.0; ctx->prof_launches[k] = 0; }
     return GPIS_OK;
 }
 

@@ -1,0 +1,36 @@
+"""Algorithmic work of one field evaluation, for the roofline of the march kernel.
+
+Counted once from the reference formulation of the 1D noise evaluation
+(evaluateNoise1DNormalized + noise1D + cell1D, SparseConvolutionNoise.cpp:379-485)
+with FMA = 2 flops and exp = 1 op, independent of how the kernel computes it:
+
+* impulses inside the truncated kernel per evaluation: 3 cells x N impulses x 2/3
+  (uniform impulse positions, support of half-width one cell) = 2N;
+* per inside impulse: difference, square, scale, exp, weighted accumulate of the
+  value and the derivative (2 FMA) = 1 + 1 + 1 + 1 + 4 = 8 flops, rounded up to 9 to
+  count the inside test;
+* per evaluation: 40 flops of frame transform, coordinate, normalisation,
+  conditioning splats and mean.
+
+The integer work of the cell hash and the PCG draws (3 hashes, 6 warm-up draws
+and 6N draws per evaluation in the reference) is not counted as flops.
+"""
+
+FLOPS_PER_INSIDE_IMPULSE = 9
+FLOPS_PER_EVAL_OVERHEAD = 40
+
+
+def flops_per_eval_1d(impulses_per_cell):
+    return 2 * impulses_per_cell * FLOPS_PER_INSIDE_IMPULSE + FLOPS_PER_EVAL_OVERHEAD
+
+
+def flops_per_eval_3d(impulses_per_cell):
+    # 27 cells x N impulses x (4 pi / 3) / 27 inside; ~20 flops per inside impulse
+    # (3 differences, quadratic form, exp, value + gradient accumulate) + 60 overhead.
+    inside = 27 * impulses_per_cell * 0.155
+    return inside * 20 + 60
+
+
+# Flight record traffic: 4 input streams of 16 B and 2 result records of 16 B.
+BYTES_IN_PER_FLIGHT = 64
+BYTES_OUT_PER_FLIGHT = 32

@@ -50,6 +50,33 @@ class DeviceFlights:
         return self.rec.cpu().numpy()
 
 
+class PinnedFlights:
+    """Flight streams and result records in pinned host memory (torch tensors)."""
+
+    def __init__(self, batch):
+        torch = _torch()
+        self.n = batch.n
+
+        def pin(a):
+            t = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32,
+                            pin_memory=True)
+            t.numpy()[...] = a.view(np.float32 if a.dtype == np.float32 else np.int32)
+            return t
+
+        self.origin_near = pin(batch.origin_near)
+        self.dir_far = pin(batch.dir_far)
+        self.seeds = pin(batch.seeds)
+        self.prev = pin(batch.prev)
+        self.medium = pin(batch.medium) if batch.medium is not None else None
+        self.rec = torch.zeros((self.n, 8), dtype=torch.float32, pin_memory=True)
+
+    soa = DeviceFlights.soa
+    result_soa = DeviceFlights.result_soa
+
+    def results(self):
+        return self.rec.numpy()
+
+
 class Context:
     """A gpis_ctx over one or more media on the current CUDA device."""
 
@@ -89,6 +116,13 @@ class Context:
                   "gpis_flights_trace_host")
         return rec
 
+    def trace_pinned(self, pinned):
+        """gpis_flights_trace_host on PinnedFlights (host -> device -> host, synchronous)."""
+        soa = pinned.soa()
+        res = pinned.result_soa()
+        abi.check(self.lib.gpis_flights_trace_host(self.h, ctypes.byref(soa), ctypes.byref(res), pinned.n),
+                  "gpis_flights_trace_host")
+
     def submit(self, dev, stream=None):
         """Enqueue a DeviceFlights batch on a CUDA stream (torch stream or None)."""
         torch = _torch()
@@ -97,6 +131,16 @@ class Context:
         res = dev.result_soa()
         abi.check(self.lib.gpis_flights_submit(self.h, ctypes.byref(soa), ctypes.byref(res), dev.n,
                                                ctypes.c_void_p(s.cuda_stream)), "gpis_flights_submit")
+
+    def profile(self, on=True):
+        abi.check(self.lib.gpis_profile_enable(self.h, int(on)), "gpis_profile_enable")
+
+    def profile_read(self, reset=False):
+        """Accumulated (ms, launches) of the prepare, march and finish kernels."""
+        ms = (ctypes.c_double * 3)()
+        ln = (ctypes.c_uint64 * 3)()
+        abi.check(self.lib.gpis_profile_read(self.h, ms, ln, int(reset)), "gpis_profile_read")
+        return list(ms), list(ln)
 
     def counters(self, reset=False):
         c = abi.Counters()

@@ -92,13 +92,13 @@ def pss_seeds(desc, pss, scene_seed=1):
     return noise.astype(np.uint32), normal.astype(np.uint32)
 
 
-def sphere_flights(n, desc, seed=7, half=1.5, bounce=0, scene_seed=1):
+def sphere_flights(n, desc, seed=7, half=1.5, bounce=0, scene_seed=1, index_offset=0):
     """Primary flights of the sphere workload: returns a FlightBatch of n flights.
 
     Origin = entry point of the ray into the cube, nearT = 0, farT = chord length;
     jitter from the same counter stream; path coordinates pss = (i mod 2048,
     i div 2048, 0, bounce)."""
-    i = np.arange(n, dtype=np.uint64)
+    i = np.arange(n, dtype=np.uint64) + np.uint64(index_offset)
     o = 3.0 * _unit_sphere(counter_uniform(seed, i, 0), counter_uniform(seed, i, 1))
     tgt = _unit_sphere(counter_uniform(seed, i, 2), counter_uniform(seed, i, 3))
     tgt *= np.cbrt(counter_uniform(seed, i, 4))[:, None]
@@ -122,6 +122,7 @@ def sphere_flights(n, desc, seed=7, half=1.5, bounce=0, scene_seed=1):
     b.seeds[:, 2] = abi.FLAG_FIRST_SCATTER
     b.set_jitter(counter_float32_unit(seed, i, 5))
     b.pss = pss
+    b.index_offset = int(index_offset)
     return b
 
 
@@ -150,7 +151,7 @@ def secondary_flights(primary, rec, desc, seed=7, half=1.5, scene_seed=1):
     b.origin_near[:, 3] = 0.0
     b.dir_far[:, :3] = r.astype(np.float32)
     b.dir_far[:, 3] = np.maximum(tmax, 1e-4).astype(np.float32)
-    i = idx.astype(np.uint64)
+    i = idx.astype(np.uint64) + np.uint64(getattr(primary, "index_offset", 0))
     pss = np.stack([(i % 2048).astype(np.uint32), (i // 2048).astype(np.uint32),
                     np.zeros(len(idx), np.uint32), np.ones(len(idx), np.uint32)], axis=1)
     ns, nm = pss_seeds(desc, pss, scene_seed)

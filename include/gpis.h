@@ -198,6 +198,14 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in,
 /* Read (and optionally reset) the device counter block. */
 int gpis_status(gpis_ctx *ctx, gpis_counters *out, int reset);
 
+/* Per-kernel timing with CUDA events recorded on the launch stream of every
+ * gpis_flights_submit while enabled.  gpis_profile_read synchronizes on the
+ * recorded events and returns the accumulated milliseconds and launch counts
+ * of the prepare (0), march (1) and finish (2) kernels.  Replaces the
+ * TUNGSTEN_GPIS_PROFILE counters (SparseConvolutionNoiseMedium.cpp:23-60). */
+int gpis_profile_enable(gpis_ctx *ctx, int on);
+int gpis_profile_read(gpis_ctx *ctx, double ms[3], uint64_t launches[3], int reset);
+
 /* Seeds of a flight from its path coordinates (computeSeed,
  * SparseConvolutionNoise.cpp:57-66, and the request seeds of
  * prepareGpisSegment, SparseConvolutionNoiseMedium.cpp:235-238).             */

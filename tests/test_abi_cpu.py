@@ -32,7 +32,7 @@ def declared_symbols():
 
 def test_library_exports_every_declared_symbol(lib):
     names = declared_symbols()
-    assert len(names) >= 13
+    assert len(names) >= 15
     for n in sorted(names):
         assert hasattr(lib, n), n
 
