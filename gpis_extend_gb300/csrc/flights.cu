@@ -433,7 +433,35 @@ struct LaneField {
     bool cond;
     CondRec c3;             // 3D conditioning
     float o[3];
+    uint32_t mean_kind;     // mean function in registers (all kinds but the grid)
+    float mq[6];
 };
+
+// mean_value with the parameters held in registers; the grid reads the medium table.
+__device__ __forceinline__ float lane_mean(const LaneField &L, float x, float y, float z, int &id)
+{
+    id = 0;
+    switch (L.mean_kind) {
+    case 0: {
+        const float dx = x - L.mq[0], dy = y - L.mq[1], dz = z - L.mq[2];
+        return sqrtf(dx * dx + dy * dy + dz * dz) - L.mq[3];
+    }
+    case 1:
+        return L.mq[0];
+    case 3:
+        return L.mq[0] * x + L.mq[1] * y + L.mq[2] * z - L.mq[3];
+    case 4:
+        return torus_sdf(L.mq, x, y, z);
+    case 5: {
+        const float t = torus_sdf(L.mq, x, y, z);
+        const float pl = y - L.mq[5];
+        if (pl < t) { id = 1; return pl; }
+        return t;
+    }
+    default:
+        return mean_value(*L.m, x, y, z, id);
+    }
+}
 
 // ---- precise evaluation ------------------------------------------------------
 // The reference's float formulation op for op: every splat as
@@ -605,7 +633,7 @@ struct EvalGeneric {
             }
         }
         refills += 1;
-        return L.sigma * noise + mean_value(m, px, py, pz, id);
+        return L.sigma * noise + lane_mean(L, px, py, pz, id);
     }
 };
 
@@ -683,7 +711,7 @@ struct EvalCached1D {
             const Cov1D k = cov1d(z - L.ozc);
             noise += L.vs * k.k0 + L.gsz * k.k1;
         }
-        return L.sigma * noise + mean_value(*L.m, px, py, pz, id);
+        return L.sigma * noise + lane_mean(L, px, py, pz, id);
     }
 };
 
@@ -693,8 +721,18 @@ struct EvalCached1D {
 // refinement point.
 enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE, PH_FAR };
 
-// Fast values farther than this from zero have the sign of the precise value.
-constexpr float kPreciseBand = 1e-5f;
+// Fast values farther than this from zero have the sign of the precise value
+// (the fast evaluator differs from the precise one by a few 1e-8).
+constexpr float kPreciseBand = 1e-6f;
+
+// Saved march state of a flight handed to the resume pass (phase 0: none).
+__device__ __forceinline__ uint4 pack_resume(float th, float tl, float pf, uint32_t steps, int sign0,
+                                             bool pf_precise, int phase)
+{
+    const uint32_t bits = (steps & 0xFFFFFFu) | (sign0 < 0 ? (1u << 24) : 0u) | (pf_precise ? (1u << 25) : 0u) |
+                          ((uint32_t)phase << 28);
+    return make_uint4(__float_as_uint(th), __float_as_uint(tl), __float_as_uint(pf), bits);
+}
 
 __device__ __forceinline__ bool t_less(float hi, float lo, float far_t)
 {
@@ -712,10 +750,16 @@ __device__ __forceinline__ unsigned long long warp_sum(uint32_t v)
 // ---------------------------------------------------------------------------
 // k_march: persistent warps with per-lane refill.
 // ---------------------------------------------------------------------------
-template <class Eval>
+// RESUME = false: the fast pass.  Lanes march with the fast evaluator only; a
+// flight whose value comes within the band of zero or changes sign is saved to
+// its resume record and left to the resume pass.
+// RESUME = true: the resume pass over the saved flights, with precise decisions,
+// the refinement and, after a rejected crossing candidate, the rest of the march.
+template <class Eval, bool RESUME>
 __global__ void __launch_bounds__(256) k_march(FlightArgs a)
 {
     const int lane = threadIdx.x & 31;
+    uint32_t *work = a.work + (RESUME ? 2 : 0);
     const unsigned lt_mask = (1u << lane) - 1u;
     // 0.9 and 0.01 as float-float pairs (the reference's double constants)
     const FF kNine = {0.9f, -2.38418579e-08f};
@@ -738,7 +782,7 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
         if (need_mask) {
             const int leader = __ffs(need_mask) - 1;
             uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(a.work, (uint32_t)__popc(need_mask));
+            if (lane == leader) base = atomicAdd(work, (uint32_t)__popc(need_mask));
             base = __shfl_sync(FULL, base, leader);
             if (need) {
                 const uint32_t idx = base + (uint32_t)__popc(need_mask & lt_mask);
@@ -746,14 +790,19 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                     drained = true;
                 } else {
                     fid = idx;
-                    c_flights++;
+                    if (!RESUME) c_flights++;
                     bool mok;
                     L.m = medium_of(a, idx, mok);
                     const DevMedium &m = *L.m;
                     const FlightIn fl = load_flight(a, idx);
-                    if (!mok || !flight_valid(fl)) {
+                    uint4 rs = make_uint4(0u, 0u, 0u, 0u);
+                    if (RESUME) rs = a.resume[idx];
+                    if (RESUME && (rs.w >> 28) == 0u) {
+                        // finished by the fast pass
+                    } else if (!mok || !flight_valid(fl)) {
                         write_status(a, idx, 0.0f, 0.0f, 1.0f, 0u, GPIS_FLIGHT_INVALID_INPUT);
                         a.t_end[idx] = 0.0;
+                        a.resume[idx] = make_uint4(0u, 0u, 0u, 0u);
                         c_invalid++;
                     } else {
 #pragma unroll
@@ -765,6 +814,9 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                         L.sigma = m.sigma;
                         L.cond = conditioned(m, fl);
                         L.vs = L.gsz = L.ozc = 0.0f;
+                        L.mean_kind = m.mean_kind;
+#pragma unroll
+                        for (int k = 0; k < 6; ++k) L.mq[k] = m.mean_params[k];
                         if (m.flags & MF_ONE_D) {
                             Frame f;
                             ray_frame(m, d[0], d[1], d[2], f);
@@ -790,6 +842,15 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                         steps = 0;
                         ev.reset();
                         phase = PH_F0;
+                        if (RESUME) {
+                            th = __uint_as_float(rs.x);
+                            tl = __uint_as_float(rs.y);
+                            pf = __uint_as_float(rs.z);
+                            steps = rs.w & 0xFFFFFFu;
+                            sign0 = (rs.w & (1u << 24)) ? -1 : 1;
+                            pf_precise = (rs.w & (1u << 25)) != 0;
+                            phase = (int)(rs.w >> 28);
+                        }
                     }
                 }
             }
@@ -809,7 +870,7 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
 #pragma unroll
         for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], eh, el);
         int id;
-        const bool precise = phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE;
+        const bool precise = RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE);
         const float f = precise ? field_precise(L, p[0], p[1], p[2], id) : ev.value(L, p[0], p[1], p[2], id, c_refills);
         gpid = id;
         const int sg = f < 0.0f ? -1 : 1;
@@ -818,13 +879,17 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
         FF t_end = {0.0f, 0.0f};
         uint32_t status = GPIS_FLIGHT_OK;
 
+        bool pend = false;
         if (!isfinite(f)) {
             // a non-finite field value ends the flight (RaySegmentBatch.cu:228-229, 238-239)
             done = true;
             status = GPIS_FLIGHT_INVALID_INPUT;
             c_invalid++;
-        } else if (phase == PH_F0 && fabsf(f) < kPreciseBand) {
+        } else if (phase == PH_F0 && first && fabsf(f) < kPreciseBand) {
+            // the initial sign decides the crossing of a primary flight; a secondary
+            // flight takes its sign from the first step instead
             phase = PH_F0_P;
+            pend = !RESUME;
         } else if (phase == PH_F0 || phase == PH_F0_P) {
             sign0 = sg;
             pf = f;
@@ -840,6 +905,7 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
         } else if (phase == PH_MARCH && (fabsf(f) < kPreciseBand || (sg != sign0 && (first || steps != 0)))) {
             // close to zero or a candidate crossing: decide on the precise value
             phase = PH_MARCH_P;
+            pend = !RESUME;
         } else if (phase == PH_MARCH || phase == PH_MARCH_P) {
             steps++;
             c_steps++;
@@ -923,9 +989,13 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
             t_end = {far_t, 0.0f};
             v_out = f;
         }
-        if (done) {
+        if (pend) {
+            a.resume[fid] = pack_resume(th, tl, pf, steps, sign0, pf_precise, phase);
+            phase = PH_IDLE;
+        } else if (done) {
             write_status(a, fid, t_out, v_out, trans, steps, status | ((uint32_t)gpid << 8));
             a.t_end[fid] = (double)t_end.h + (double)t_end.l;
+            if (!RESUME) a.resume[fid] = make_uint4(0u, 0u, 0u, 0u);
             phase = PH_IDLE;
         }
     }
@@ -1119,7 +1189,7 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     if (ev) cudaEventRecord(ev[0], stream);
     if (a.any_cond) k_prepare<<<blocks, 128, 0, stream>>>(a);
     if (ev) cudaEventRecord(ev[1], stream);
-    cudaError_t err = cudaMemsetAsync(a.work, 0, sizeof(uint32_t), stream);
+    cudaError_t err = cudaMemsetAsync(a.work, 0, 4 * sizeof(uint32_t), stream);
     if (err != cudaSuccess) return err;
     // persistent grid: a few resident CTAs per SM, never more warps than flights
     const uint32_t warps_needed = (a.n + 31) / 32;
@@ -1129,9 +1199,10 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     if (ctas == 0) ctas = 1;
     if (ev) cudaEventRecord(ev[2], stream);
     if (a.one_d && a.max_imp <= 8)
-        k_march<EvalCached1D<8>><<<ctas, 256, 0, stream>>>(a);
+        k_march<EvalCached1D<8>, false><<<ctas, 256, 0, stream>>>(a);
     else
-        k_march<EvalGeneric><<<ctas, 256, 0, stream>>>(a);
+        k_march<EvalGeneric, false><<<ctas, 256, 0, stream>>>(a);
+    k_march<EvalGeneric, true><<<ctas, 256, 0, stream>>>(a);
     if (ev) cudaEventRecord(ev[3], stream);
     if (ev) cudaEventRecord(ev[4], stream);
     k_finish<<<blocks, 128, 0, stream>>>(a);

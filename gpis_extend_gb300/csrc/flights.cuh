@@ -31,7 +31,10 @@ struct FlightArgs {
     uint32_t n;
     CondRec *cond;              // scratch, n records
     double *t_end;              // scratch, n values (double march parameter at the end point)
-    uint32_t *work;             // scratch, 1 work counter (zeroed before the march)
+    uint32_t *work;             // scratch, 4 counters zeroed before the march: march work,
+                                // resume-queue length, resume work, unused
+    uint32_t *queue;            // scratch, n flight indices handed to the resume pass
+    uint4 *resume;              // scratch, n saved march states
     unsigned long long *counters;  // gpis_counters block (8 x u64)
     int any_cond;               // some medium conditions (run the prepare kernel)
     int one_d;                  // all media use 1D noise
@@ -42,8 +45,8 @@ struct FlightArgs {
 // Upload the jump-ahead PCG table to the current device (once per device).
 cudaError_t upload_pcg_table();
 
-// Enqueue the three flight kernels on the stream.  ev, when not null, holds
-// start/stop events for the prepare, march and finish kernels (ev[2k], ev[2k+1]).
+// Enqueue the flight kernels on the stream.  ev, when not null, holds start/stop
+// events for the prepare, march (march + resume) and finish kernels (ev[2k], ev[2k+1]).
 cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream, cudaEvent_t *ev = nullptr);
 
 // Unit-level kernels (synchronous wrappers live in gpis_abi.cu).

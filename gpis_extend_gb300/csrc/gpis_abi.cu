@@ -134,6 +134,7 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
     m.step_size = d.step_size;
     m.min_step = d.min_step;
     m.max_steps = d.max_steps ? d.max_steps : 16384u;
+    if (m.max_steps > 0xFFFFFFu) return fail(GPIS_ERANGE, "max_steps must be below 2^24");
     m.scheme = (!d.single_realization && d.one_d_sampling) ? d.sampling_scheme : GPIS_SCHEME_UNI;
     return GPIS_OK;
 }
@@ -151,6 +152,7 @@ struct gpis_ctx {
     // scratch of the flight kernels
     gpis::CondRec *d_cond = nullptr;
     double *d_tend = nullptr;
+    uint4 *d_resume = nullptr;
     uint32_t *d_work = nullptr;
     unsigned long long *d_counters = nullptr;
     size_t cap = 0;
@@ -175,6 +177,7 @@ void release(gpis_ctx *c)
     for (float *g : c->d_grids) cudaFree(g);
     cudaFree(c->d_cond);
     cudaFree(c->d_tend);
+    cudaFree(c->d_resume);
     cudaFree(c->d_work);
     cudaFree(c->d_counters);
     cudaFree(c->d_stage);
@@ -190,11 +193,14 @@ int ensure_scratch(gpis_ctx *c, size_t n)
     size_t cap = std::max<size_t>(n, 1024);
     cudaFree(c->d_cond);
     cudaFree(c->d_tend);
+    cudaFree(c->d_resume);
     c->d_cond = nullptr;
     c->d_tend = nullptr;
+    c->d_resume = nullptr;
     c->cap = 0;
     CUDA_TRY(cudaMalloc(&c->d_cond, cap * sizeof(gpis::CondRec)), "allocate conditioning scratch");
     CUDA_TRY(cudaMalloc(&c->d_tend, cap * sizeof(double)), "allocate end-parameter scratch");
+    CUDA_TRY(cudaMalloc(&c->d_resume, cap * sizeof(uint4)), "allocate resume scratch");
     c->cap = cap;
     return GPIS_OK;
 }
@@ -282,7 +288,7 @@ int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
             rc = cuda_fail(e, "upload media");
             break;
         }
-        if ((e = cudaMalloc(&c->d_work, sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(e, "allocate work counter"); break; }
+        if ((e = cudaMalloc(&c->d_work, 4 * sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(e, "allocate work counters"); break; }
         if ((e = cudaMalloc(&c->d_counters, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "allocate counters"); break; }
         if ((e = cudaMemset(c->d_counters, 0, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "clear counters"); break; }
         if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(e, "create stream"); break; }
@@ -325,6 +331,8 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_res
     a.cond = ctx->d_cond;
     a.t_end = ctx->d_tend;
     a.work = ctx->d_work;
+    a.queue = nullptr;
+    a.resume = ctx->d_resume;
     a.counters = ctx->d_counters;
     a.any_cond = ctx->any_cond;
     a.one_d = ctx->all_one_d;

@@ -182,8 +182,10 @@ def flights_vs_oracle(desc, batch, rec_gpu, check_grad=True):
     assert np.mean(dt <= T_TOL) >= 0.9999, f"t disagreement on {(dt > T_TOL).sum()} hits"
     miss = agree & ~g["hit"]
     assert np.all(g["t"][miss] == c["t"][miss])
-    sig = np.maximum(1.0, np.abs(c["value"][miss]))
-    assert np.mean(np.abs(g["value"][miss] - c["value"][miss]) <= 1e-5 * sig * 10) >= 0.9999
+    if miss.any():
+        # the miss value is amplitude * noise + mean at farT: 1e-5 of the noise scale
+        tol = 1e-5 * max(desc.sigma, 1e-6) * np.maximum(1.0, np.abs(c["value"][miss]) / max(desc.sigma, 1e-6))
+        assert np.mean(np.abs(g["value"][miss] - c["value"][miss]) <= tol) >= 0.9999
     if check_grad:
         close_t = both.copy()
         close_t[both] = dt <= 1e-6
@@ -222,7 +224,7 @@ def test_gpu_flights_edge_cases():
     b.prev[5, 0] = np.inf                           # conditioned with non-finite birth value
     with runtime.Context(desc) as ctx:
         r = abi.unpack_results(ctx.trace_host(b))
-        assert list(r["status"][:6]) == [abi.FLIGHT_INVALID_INPUT] * 6
+        assert list(r["status"][:6]) == [abi.FLIGHT_INVALID_INPUT] * 4 + [abi.FLIGHT_OK, abi.FLIGHT_INVALID_INPUT]
         assert np.all(r["status"][6:] == abi.FLIGHT_OK)
         # empty batch
         e = abi.FlightBatch(0)
