@@ -31,6 +31,7 @@ CTX_GLOBAL, CTX_RENEWAL_PLUS, CTX_RENEWAL, CTX_NONE = 0, 1, 2, 3
 SCHEME_UNI, SCHEME_NEE, SCHEME_MIS = 0, 1, 2
 MEAN_SPHERE, MEAN_HOMOGENEOUS, MEAN_GRID, MEAN_PLANE, MEAN_TORUS, MEAN_TORUS_PLANE = range(6)
 LS_CONSTANT, LS_SINCOS = 0, 1
+STATIC_MAX_FLIGHTS = 65536
 FLAG_FIRST_SCATTER = 1
 FLAG_SHADOW = 2
 
@@ -279,6 +280,7 @@ def load_library(path=None):
         "gpis_debug_cells_3d": (c_int, [vp, vp, c_u32, c_u32, c_u32, vp, vp]),
         "gpis_debug_field": (c_int, [vp, vp, vp, vp, vp, vp, c_u32, vp]),
         "gpis_se_splat_1d": (c_int, [vp, vp, vp, vp, ctypes.c_size_t, ctypes.c_float, vp]),
+        "gpis_flights_submit_static": (c_int, [P(MediumDesc), P(FlightSoA), P(ResultSoA), c_u32, vp]),
         "gpis_last_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

@@ -141,6 +141,11 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
 
 }  // namespace
 
+namespace gpis {
+// Medium derivation for the allocation-free entry point (gpis_static.cu).
+int derive_medium_host(const gpis_medium_desc &d, DevMedium &m) { return derive_medium(d, m); }
+}  // namespace gpis
+
 struct gpis_ctx {
     int device = 0;
     int num_sms = 1;

@@ -239,6 +239,24 @@ int gpis_debug_field(gpis_ctx *ctx, const float *origins, const float *points,
 int gpis_se_splat_1d(const float *queries, const float *centers, float *values,
                      float *derivatives, size_t count, float local_scale, void *cuda_stream);
 
+/* ---- allocation-free flight batch ------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc: a
+ * renderer thread that must never make the device synchronize (cudaMalloc and
+ * cudaFree can), or a plugin host that owns all device memory and forbids
+ * plugins to allocate.  The same flight kernels as gpis_flights_submit run on
+ * one medium description (no grid mean), with all working memory in a fixed
+ * array of this library (about 3.7 MB for GPIS_STATIC_MAX_FLIGHTS flights)
+ * that every GPU which loads the library keeps until the process exits.  The
+ * caller provides device flight and result streams as for gpis_flights_submit.
+ * Larger batches fail with GPIS_ERANGE.  The first call on a device, with that
+ * device current, looks up the array's device address and uploads a constant
+ * table; make that first call before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU (other streams, other host threads)
+ * race: serialize them.                                                      */
+#define GPIS_STATIC_MAX_FLIGHTS 65536u
+int gpis_flights_submit_static(const gpis_medium_desc *medium, const gpis_flight_soa *in,
+                               const gpis_result_soa *out, uint32_t n, void *cuda_stream);
+
 /* Last error message of the calling thread ("" when none). */
 const char *gpis_last_error(void);
 
