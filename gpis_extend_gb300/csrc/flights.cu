@@ -435,7 +435,26 @@ struct LaneField {
     float o[3];
     uint32_t mean_kind;     // mean function in registers (all kinds but the grid)
     float mq[6];
+    uint32_t n_imp;         // impulses per cell
 };
+
+// Safe contents for a lane without a flight (collective evaluators run every lane).
+__device__ __forceinline__ void lane_field_idle(LaneField &L, const DevMedium *m0)
+{
+    L.m = m0;
+    L.n[0] = 0.0f; L.n[1] = 0.0f; L.n[2] = 1.0f;
+    L.li[0] = L.li[1] = L.li[2] = 1.0f;
+    L.kr = 1.0f; L.kexp = -1.0f; L.inv_norm = 1.0f; L.sigma = 0.0f;
+    L.seed = 0u;
+    L.vs = L.gsz = L.ozc = 0.0f;
+    L.cond = false;
+    L.c3 = CondRec{};
+    L.o[0] = L.o[1] = L.o[2] = 0.0f;
+    L.mean_kind = 1u;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) L.mq[k] = 0.0f;
+    L.n_imp = 0u;
+}
 
 // mean_value with the parameters held in registers; the grid reads the medium table.
 __device__ __forceinline__ float lane_mean(const LaneField &L, float x, float y, float z, int &id)
@@ -606,9 +625,11 @@ __device__ float field_precise(const LaneField &L, float px, float py, float pz,
 // ---- fast evaluators ----------------------------------------------------------
 // Generic evaluator: recomputes every impulse (any impulse count, 1D or 3D).
 struct EvalGeneric {
+    static constexpr bool kCollective = false;
     __device__ __forceinline__ void reset() {}
+    __device__ __forceinline__ void bind(const PcgJump *) {}
     __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
-                                           int &id, uint32_t &refills)
+                                           int &id, uint32_t &refills, bool)
     {
         const DevMedium &m = *L.m;
         float noise;
@@ -641,11 +662,13 @@ struct EvalGeneric {
 // impulse is its position t_i in [0,1) with the sign of its weight in the sign bit.
 template <int NMAX>
 struct EvalCached1D {
+    static constexpr bool kCollective = false;
     float cache[3][NMAX];
     int base;
     bool valid;
 
     __device__ __forceinline__ void reset() { valid = false; base = 0; }
+    __device__ __forceinline__ void bind(const PcgJump *) {}
 
     __device__ __forceinline__ void gen(float (&dst)[NMAX], int cell, uint32_t seed, uint32_t n_imp)
     {
@@ -664,7 +687,7 @@ struct EvalCached1D {
     }
 
     __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
-                                           int &id, uint32_t &refills)
+                                           int &id, uint32_t &refills, bool)
     {
         const float z = ray_coord(L.li, L.n, px, py, pz);
         const float tg = __fdiv_rn(z, L.kr);
@@ -691,6 +714,114 @@ struct EvalCached1D {
             }
             base = ci;
             valid = true;
+        }
+        float acc0 = 0.0f, acc1 = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float tl = __fsub_rn(frac, (float)(c - 1));
+#pragma unroll
+            for (int k = 0; k < NMAX; ++k) {
+                const float s = cache[c][k];
+                const float tp = __fsub_rn(tl, fabsf(s));
+                const float e = ex2_approx(L.kexp * (tp * tp));
+                const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(s) & 0x80000000u));
+                if (k & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
+                else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
+            }
+        }
+        float noise = (acc0 + acc1) * L.inv_norm;
+        if (L.cond) {
+            const Cov1D k = cov1d(z - L.ozc);
+            noise += L.vs * k.k0 + L.gsz * k.k1;
+        }
+        return L.sigma * noise + lane_mean(L, px, py, pz, id);
+    }
+};
+
+
+// 1D evaluator with the three-cell impulse window in registers and a
+// warp-cooperative refill: the lanes whose query entered a new cell are
+// gathered by a ballot and the whole warp generates their cells, one impulse per
+// lane (the jump-ahead PCG draws any impulse of a cell independently), 32/NMAX
+// cells per pass; shuffles deliver each cell into its owner's registers.  Every
+// lane of the warp must call value() (idle lanes pass live = false).
+template <int NMAX>
+struct EvalCoop1D {
+    static constexpr bool kCollective = true;
+    float cache[3][NMAX];
+    int base;
+    bool valid;
+    const PcgJump *sj;      // the jump table in shared memory
+
+    __device__ __forceinline__ void reset() { valid = false; base = 0; }
+    __device__ __forceinline__ void bind(const PcgJump *t) { sj = t; }
+
+    template <int S>
+    __device__ __forceinline__ void fill_slot(bool need, int cell, const LaneField &L, int lane)
+    {
+        unsigned mask = __ballot_sync(FULL, need);
+        const int rq = lane / NMAX;
+        const int k = lane % NMAX;
+        while (mask) {
+            unsigned pass = 0u, m = mask;
+#pragma unroll
+            for (int r = 0; r < 32 / NMAX; ++r) {
+                pass |= m & (0u - m);
+                m &= m - 1u;
+            }
+            mask = m;
+            // the request this lane produces an impulse for
+            unsigned pm = pass;
+            for (int r = 0; r < rq; ++r) pm &= pm - 1u;
+            const int owner = pm ? __ffs(pm) - 1 : 0;
+            const int ocell = __shfl_sync(FULL, cell, owner);
+            const uint32_t oseed = __shfl_sync(FULL, L.seed, owner);
+            const uint32_t onimp = __shfl_sync(FULL, L.n_imp, owner);
+            float v = __int_as_float(0x7f800000);
+            if (pm != 0u && (uint32_t)k < onimp) {
+                const uint32_t s = xxhash2((uint32_t)ocell, oseed) + 1u;
+                const uint32_t r1 = pcg_draw(sj[2 + 2 * k], s);
+                const uint32_t r2 = pcg_draw(sj[3 + 2 * k], s);
+                v = __uint_as_float(__float_as_uint(unit_float(r1)) | (~r2 & 0x80000000u));
+            }
+            const bool mine = (pass >> lane) & 1u;
+            const int myrq = __popc(pass & ((1u << lane) - 1u));
+#pragma unroll
+            for (int kk = 0; kk < NMAX; ++kk) {
+                const float x = __shfl_sync(FULL, v, myrq * NMAX + kk);
+                if (mine) cache[S][kk] = x;
+            }
+        }
+    }
+
+    __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
+                                           int &id, uint32_t &refills, bool live)
+    {
+        const int lane = threadIdx.x & 31;
+        const float z = ray_coord(L.li, L.n, px, py, pz);
+        const float tg = __fdiv_rn(z, L.kr);
+        const float fl = floorf(tg);
+        const float frac = __fsub_rn(tg, fl);
+        const int ci = (int)fl;
+        const bool changed = live && (!valid || ci != base);
+        const bool up = changed && valid && ci == base + 1;
+        const bool down = changed && valid && ci == base - 1;
+        const bool full = changed && !up && !down;
+        if (up) {
+#pragma unroll
+            for (int k = 0; k < NMAX; ++k) { cache[0][k] = cache[1][k]; cache[1][k] = cache[2][k]; }
+        }
+        if (down) {
+#pragma unroll
+            for (int k = 0; k < NMAX; ++k) { cache[2][k] = cache[1][k]; cache[1][k] = cache[0][k]; }
+        }
+        fill_slot<0>(full || down, ci - 1, L, lane);
+        fill_slot<1>(full, ci, L, lane);
+        fill_slot<2>(full || up, ci + 1, L, lane);
+        if (changed) {
+            base = ci;
+            valid = true;
+            refills += full ? 3u : 1u;
         }
         float acc0 = 0.0f, acc1 = 0.0f;
 #pragma unroll
@@ -764,10 +895,14 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
     // 0.9 and 0.01 as float-float pairs (the reference's double constants)
     const FF kNine = {0.9f, -2.38418579e-08f};
     const float kHundredthH = 0.01f, kHundredthL = -2.23517418e-10f;
+    __shared__ PcgJump s_jump[2 + 2 * 8];
+    if (threadIdx.x < 2 + 2 * 8) s_jump[threadIdx.x] = c_jump[threadIdx.x];
+    __syncthreads();
     Eval ev;
     ev.reset();
+    ev.bind(s_jump);
     LaneField L;
-    L.m = a.media;
+    lane_field_idle(L, a.media);
     int phase = PH_IDLE;
     bool drained = false, first = true, pf_precise = false;
     uint32_t fid = 0, steps = 0, max_steps = 1, refine_iter = 0;
@@ -817,6 +952,7 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                         L.mean_kind = m.mean_kind;
 #pragma unroll
                         for (int k = 0; k < 6; ++k) L.mq[k] = m.mean_params[k];
+                        L.n_imp = m.n_imp;
                         if (m.flags & MF_ONE_D) {
                             Frame f;
                             ray_frame(m, d[0], d[1], d[2], f);
@@ -860,7 +996,7 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
             if (__all_sync(FULL, drained)) break;
             continue;
         }
-        if (!live) continue;
+        if (!Eval::kCollective && !live) continue;
 
         // evaluation point of this phase
         float eh = th, el = tl;
@@ -871,7 +1007,9 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
         for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], eh, el);
         int id;
         const bool precise = RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE);
-        const float f = precise ? field_precise(L, p[0], p[1], p[2], id) : ev.value(L, p[0], p[1], p[2], id, c_refills);
+        const float f = precise ? field_precise(L, p[0], p[1], p[2], id)
+                                : ev.value(L, p[0], p[1], p[2], id, c_refills, live);
+        if (Eval::kCollective && !live) continue;
         gpid = id;
         const int sg = f < 0.0f ? -1 : 1;
         bool done = false;
@@ -1191,18 +1329,30 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     if (ev) cudaEventRecord(ev[1], stream);
     cudaError_t err = cudaMemsetAsync(a.work, 0, 4 * sizeof(uint32_t), stream);
     if (err != cudaSuccess) return err;
-    // persistent grid: a few resident CTAs per SM, never more warps than flights
+    // persistent grids: exactly the CTAs that are resident at once, never more
+    // warps than flights
     const uint32_t warps_needed = (a.n + 31) / 32;
-    uint32_t ctas = (uint32_t)num_sms * 4u;
     const uint32_t ctas_needed = (warps_needed + 7) / 8;
-    if (ctas > ctas_needed) ctas = ctas_needed;
-    if (ctas == 0) ctas = 1;
+    auto grid = [&](const void *fn) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        uint32_t c = (uint32_t)num_sms * (uint32_t)per_sm;
+        if (c > ctas_needed) c = ctas_needed;
+        return c == 0 ? 1u : c;
+    };
     if (ev) cudaEventRecord(ev[2], stream);
-    if (a.one_d && a.max_imp <= 8)
-        k_march<EvalCached1D<8>, false><<<ctas, 256, 0, stream>>>(a);
-    else
-        k_march<EvalGeneric, false><<<ctas, 256, 0, stream>>>(a);
-    k_march<EvalGeneric, true><<<ctas, 256, 0, stream>>>(a);
+    if (a.one_d && a.max_imp <= 8) {
+        const void *fn = (const void *)k_march<EvalCoop1D<8>, false>;
+        k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(a);
+    } else {
+        const void *fn = (const void *)k_march<EvalGeneric, false>;
+        k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(a);
+    }
+    {
+        const void *fn = (const void *)k_march<EvalGeneric, true>;
+        k_march<EvalGeneric, true><<<grid(fn), 256, 0, stream>>>(a);
+    }
     if (ev) cudaEventRecord(ev[3], stream);
     if (ev) cudaEventRecord(ev[4], stream);
     k_finish<<<blocks, 128, 0, stream>>>(a);
