@@ -93,7 +93,40 @@ class MediumDesc(ctypes.Structure):
         ("density", ctypes.c_float),
         ("max_steps", ctypes.c_uint32),
         ("impulse_xyz_order", ctypes.c_uint32),
+        ("max_bounces", ctypes.c_int32),
+        ("reserved_", ctypes.c_uint32),
     ]
+
+
+class Ray(ctypes.Structure):
+    _fields_ = [("pos", ctypes.c_float * 3), ("dir", ctypes.c_float * 3), ("near_t", ctypes.c_float),
+                ("far_t", ctypes.c_float)]
+
+
+class MediumState(ctypes.Structure):
+    _fields_ = [("pixel_sample_segment", ctypes.c_uint32 * 4), ("scene_seed", ctypes.c_uint32),
+                ("first_scatter", ctypes.c_uint32), ("bounce", ctypes.c_int32), ("last_gp_id", ctypes.c_int32),
+                ("last_val", ctypes.c_float), ("last_aniso", ctypes.c_float * 3), ("info_t", ctypes.c_double),
+                ("sampling_scheme", ctypes.c_uint32), ("reserved_", ctypes.c_uint32)]
+
+
+class MediumSample(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_float), ("p", ctypes.c_float * 3), ("weight", ctypes.c_float * 3),
+                ("pdf", ctypes.c_float), ("aniso", ctypes.c_float * 3), ("continued_t", ctypes.c_float),
+                ("continued_weight", ctypes.c_float * 3), ("exited", ctypes.c_int32), ("gp_id", ctypes.c_int32),
+                ("status", ctypes.c_int32), ("sampling_scheme", ctypes.c_uint32), ("reserved_", ctypes.c_uint32)]
+
+
+# numpy views of the structures (same layout, for batches)
+RAY_DTYPE = np.dtype([("pos", np.float32, 3), ("dir", np.float32, 3), ("near_t", np.float32), ("far_t", np.float32)])
+STATE_DTYPE = np.dtype([("pss", np.uint32, 4), ("scene_seed", np.uint32), ("first_scatter", np.uint32),
+                        ("bounce", np.int32), ("last_gp_id", np.int32), ("last_val", np.float32),
+                        ("last_aniso", np.float32, 3), ("info_t", np.float64), ("sampling_scheme", np.uint32),
+                        ("reserved_", np.uint32)])
+SAMPLE_DTYPE = np.dtype([("t", np.float32), ("p", np.float32, 3), ("weight", np.float32, 3), ("pdf", np.float32),
+                         ("aniso", np.float32, 3), ("continued_t", np.float32), ("continued_weight", np.float32, 3),
+                         ("exited", np.int32), ("gp_id", np.int32), ("status", np.int32),
+                         ("sampling_scheme", np.uint32), ("reserved_", np.uint32)])
 
 
 class FlightSoA(ctypes.Structure):
@@ -149,6 +182,7 @@ def medium_defaults():
     d.density = 1.0
     d.max_steps = 0
     d.impulse_xyz_order = 0
+    d.max_bounces = 1024
     return d
 
 
@@ -281,6 +315,8 @@ def load_library(path=None):
         "gpis_debug_field": (c_int, [vp, vp, vp, vp, vp, vp, c_u32, vp]),
         "gpis_se_splat_1d": (c_int, [vp, vp, vp, vp, ctypes.c_size_t, ctypes.c_float, vp]),
         "gpis_flights_submit_static": (c_int, [P(MediumDesc), P(FlightSoA), P(ResultSoA), c_u32, vp]),
+        "gpis_medium_sample_distance": (c_int, [vp, c_u32, vp, vp, vp, vp, c_u32]),
+        "gpis_medium_transmittance": (c_int, [vp, c_u32, vp, vp, vp, vp, c_u32]),
         "gpis_last_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

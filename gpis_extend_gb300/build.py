@@ -14,7 +14,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgpis_gb300.so")
 ROOT = os.path.dirname(HERE)
 
-SOURCES = ["flights.cu", "gpis_abi.cu", "gpis_static.cu", "medium_json.cpp"]
+SOURCES = ["flights.cu", "gpis_abi.cu", "gpis_static.cu", "medium_json.cpp", "medium_adapter.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -166,6 +166,7 @@ struct gpis_ctx {
     size_t stage_cap = 0;
     cudaStream_t stream = nullptr;
     // per-kernel event timing (gpis_profile_*)
+    std::vector<gpis_medium_desc> host_media;  // host copies for the medium queries
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;      // free events
     std::vector<cudaEvent_t> ev_pending;   // groups of 6 recorded events
@@ -220,6 +221,12 @@ __attribute__((visibility("hidden"))) int gpis_internal_set_error(int code, cons
     return code;
 }
 
+__attribute__((visibility("hidden"))) const gpis_medium_desc *gpis_internal_ctx_medium(gpis_ctx *ctx, uint32_t index)
+{
+    if (!ctx || index >= ctx->host_media.size()) return nullptr;
+    return &ctx->host_media[index];
+}
+
 void gpis_medium_desc_init(gpis_medium_desc *d)
 {
     if (!d) return;
@@ -243,6 +250,7 @@ void gpis_medium_desc_init(gpis_medium_desc *d)
     d->correlation_context = GPIS_CTX_RENEWAL_PLUS;
     d->sampling_scheme = GPIS_SCHEME_UNI;
     d->density = 1.0f;
+    d->max_bounces = 1024;
 }
 
 const char *gpis_last_error(void) { return g_error.c_str(); }
@@ -265,6 +273,7 @@ int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
     c->n_media = n_media;
+    c->host_media.assign(media, media + n_media);
     int rc = GPIS_OK;
     do {
         if ((e = gpis::upload_pcg_table()) != cudaSuccess) { rc = cuda_fail(e, "upload PCG table"); break; }

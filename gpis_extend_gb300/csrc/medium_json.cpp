@@ -210,6 +210,7 @@ extern "C" int gpis_medium_desc_from_json(const char *json, gpis_medium_desc *d)
         if (const Value *s = v.get("surf_vol_phase_separate"))
             if (num(*s, "surf_vol_phase_separate") != 0.0) bad(GPIS_ENOTSUP, "surf_vol_phase_separate is not supported");
         field(v, "max_steps", d->max_steps);
+        field(v, "max_bounces", d->max_bounces);
     } catch (const Err &e) {
         return gpis_internal_set_error(e.code, e.msg.c_str());
     } catch (const std::exception &e) {

@@ -142,6 +142,24 @@ class Context:
         abi.check(self.lib.gpis_profile_read(self.h, ms, ln, int(reset)), "gpis_profile_read")
         return list(ms), list(ln)
 
+    def sample_distance(self, medium, rays, states, jitter):
+        """Batched Medium::sampleDistance (gpis_medium_sample_distance); states update in place."""
+        samples = np.zeros(len(rays), abi.SAMPLE_DTYPE)
+        jit = np.ascontiguousarray(jitter, np.float32)
+        abi.check(self.lib.gpis_medium_sample_distance(self.h, medium, rays.ctypes.data, states.ctypes.data,
+                                                       jit.ctypes.data, samples.ctypes.data, len(rays)),
+                  "gpis_medium_sample_distance")
+        return samples
+
+    def transmittance(self, medium, rays, states, jitter):
+        """Batched Medium::transmittance (gpis_medium_transmittance)."""
+        tr = np.zeros(len(rays), np.float32)
+        jit = np.ascontiguousarray(jitter, np.float32)
+        abi.check(self.lib.gpis_medium_transmittance(self.h, medium, rays.ctypes.data, states.ctypes.data,
+                                                     jit.ctypes.data, tr.ctypes.data, len(rays)),
+                  "gpis_medium_transmittance")
+        return tr
+
     def counters(self, reset=False):
         c = abi.Counters()
         abi.check(self.lib.gpis_status(self.h, ctypes.byref(c), int(reset)), "gpis_status")

@@ -130,6 +130,8 @@ typedef struct gpis_medium_desc {
     uint32_t impulse_xyz_order; /* 0: z drawn first (right-to-left argument
                                    evaluation of next3D, GCC/MSVC x86-64);
                                    1: x drawn first                               */
+    int32_t max_bounces;        /* "max_bounces" (Medium::fromJson, Medium.cpp:37) */
+    uint32_t reserved_;
 } gpis_medium_desc;
 
 /* ---- flight streams (structure of arrays, 16-byte records) ---------------
@@ -167,6 +169,48 @@ typedef struct gpis_counters {
 
 typedef struct gpis_ctx gpis_ctx;
 
+/* ---- medium queries (GaussianProcessMedium state machines) -------------------
+ * A ray (Ray: pos, dir, nearT, farT; farT may be +inf).                       */
+typedef struct gpis_ray {
+    float pos[3];
+    float dir[3];
+    float near_t;
+    float far_t;
+} gpis_ray;
+
+/* The MediumState fields the GPIS medium reads and writes (Medium.hpp:70-108,
+ * RayInfo): path coordinates and scene seed, firstScatter, bounce, lastGPId,
+ * lastVal, lastAniso, info.t and the 1D sampling scheme of the last event.    */
+typedef struct gpis_medium_state {
+    uint32_t pixel_sample_segment[4];
+    uint32_t scene_seed;
+    uint32_t first_scatter;
+    int32_t bounce;
+    int32_t last_gp_id;
+    float last_val;
+    float last_aniso[3];
+    double info_t;
+    uint32_t sampling_scheme;
+    uint32_t reserved_;
+} gpis_medium_state;
+
+/* MediumSample fields set by sampleDistance (MediumSample.hpp; resumeDistance,
+ * GaussianProcessMedium.cpp:289-381).  status: 1 Finished, 0 Failed.       */
+typedef struct gpis_medium_sample {
+    float t;
+    float p[3];
+    float weight[3];
+    float pdf;
+    float aniso[3];
+    float continued_t;
+    float continued_weight[3];
+    int32_t exited;
+    int32_t gp_id;
+    int32_t status;
+    uint32_t sampling_scheme;
+    uint32_t reserved_;
+} gpis_medium_sample;
+
 /* Reference defaults: SparseConvolutionNoiseMedium() (SparseConvolutionNoiseMedium.cpp:62-79),
  * GaussianProcessMedium() (GaussianProcessMedium.cpp:87-96), SE covariance with
  * localScale 3 (GPFunctions.hpp:1816) and a unit sphere mean.                 */
@@ -194,6 +238,21 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in,
  * and GpRayBatchBackend::trace, GpRayBatchBackend.hpp:43-47).                */
 int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in,
                             const gpis_result_soa *out, uint32_t n);
+
+/* Batched Medium::sampleDistance for n rays of one medium of the context
+ * (GaussianProcessMedium::sampleDistance / beginDistance / resumeDistance /
+ * finishDistance, GaussianProcessMedium.cpp:222-381).  jitter[i] is the one
+ * PathSampleGenerator draw of ray i's segment (SparseConvolutionNoiseMedium.cpp:234).
+ * Host arrays; states are updated in place; blocking.                         */
+int gpis_medium_sample_distance(gpis_ctx *ctx, uint32_t medium, const gpis_ray *rays,
+                                gpis_medium_state *states, const float *jitter,
+                                gpis_medium_sample *samples, uint32_t n);
+
+/* Batched Medium::transmittance (GaussianProcessMedium.cpp:383-440): writes 0 or 1
+ * per ray and updates the states (lastAniso and firstScatter at a hit).      */
+int gpis_medium_transmittance(gpis_ctx *ctx, uint32_t medium, const gpis_ray *rays,
+                              gpis_medium_state *states, const float *jitter,
+                              float *transmittance, uint32_t n);
 
 /* Read (and optionally reset) the device counter block. */
 int gpis_status(gpis_ctx *ctx, gpis_counters *out, int reset);

@@ -1521,3 +1521,164 @@ void gor_se_splat_1d(const float *q, const float *c, uint32_t n, float scale,
         derivatives[i] = -delta / ((double)scale * scale) * values[i];
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Medium queries: GaussianProcessMedium state machines                      */
+/* ------------------------------------------------------------------------ */
+/* sampleDistance / beginDistance / resumeDistance / finishDistance
+ * (GaussianProcessMedium.cpp:222-381) and transmittance (:383-440), with the
+ * state updates of finishGpisSegment (SparseConvolutionNoiseMedium.cpp:265-347). */
+
+static void gm_flight(const gpis_medium_desc *d, const gpis_ray *r, float far_t, const gpis_medium_state *st,
+                      float jitter, int shadow, float rec[8])
+{
+    float on[4] = {r->pos[0], r->pos[1], r->pos[2], r->near_t};
+    float df[4] = {r->dir[0], r->dir[1], r->dir[2], far_t};
+    uint32_t sd[4], ns, nm, jb;
+    gor_flight_seeds(d, st->pixel_sample_segment, st->scene_seed, &ns, &nm);
+    memcpy(&jb, &jitter, 4);
+    int first = st->first_scatter != 0;
+    sd[0] = ns; sd[1] = nm; sd[2] = (first ? GPIS_FLAG_FIRST_SCATTER : 0u) | (shadow ? GPIS_FLAG_SHADOW : 0u); sd[3] = jb;
+    float pv[4] = {first ? 0.0f : st->last_val, first ? 0.0f : st->last_aniso[0], first ? 0.0f : st->last_aniso[1],
+                   first ? 0.0f : st->last_aniso[2]};
+    gpis_flight_soa in = {on, df, sd, pv, NULL};
+    gpis_result_soa out = {rec};
+    gor_trace_flights(d, 1, &in, &out, 1, 1);
+}
+
+static uint32_t gm_scheme(const gpis_medium_desc *d, int conditioned_rp, float t)
+{
+    if (d->single_realization || !d->one_d_sampling) return GPIS_SCHEME_UNI;
+    if (d->sigma < 1e-6f) return GPIS_SCHEME_UNI;
+    if (d->correlation_xy && conditioned_rp && t == 0.0f) return GPIS_SCHEME_UNI;
+    return d->sampling_scheme;
+}
+
+static void gm_finish_segment(const gpis_medium_desc *d, const float rec[8], gpis_medium_state *st)
+{
+    int rp = !d->single_realization && d->correlation_context == GPIS_CTX_RENEWAL_PLUS && st->first_scatter == 0;
+    uint32_t status;
+    memcpy(&status, &rec[7], 4);
+    if (rec[5] == 0.0f) {
+        st->last_gp_id = (int32_t)((status >> 8) & 0xFFu);
+        st->sampling_scheme = gm_scheme(d, rp, rec[0]);
+        st->last_val = 0.0f;
+    } else {
+        st->sampling_scheme = GPIS_SCHEME_UNI;
+        st->last_val = rec[1];
+    }
+}
+
+int gor_medium_sample_distance(const gpis_medium_desc *d, const gpis_ray *rays, gpis_medium_state *states,
+                               const float *jitter, gpis_medium_sample *samples, uint32_t n)
+{
+    float sa = d->sigma_a * d->density, ss = d->sigma_s * d->density, stt = sa + ss;
+    int absorption_only = ss == 0.0f;
+    for (uint32_t i = 0; i < n; ++i) {
+        const gpis_ray *r = &rays[i];
+        gpis_medium_sample *s = &samples[i];
+        gpis_medium_state *st = &states[i];
+        memset(s, 0, sizeof(*s));
+        float far_t = r->far_t;
+        if (!isfinite(far_t)) far_t = (float)((double)r->near_t + 2000);
+        float maxT = far_t;
+        if (st->bounce >= d->max_bounces) { s->status = 0; continue; }
+        if (maxT <= r->near_t) {
+            s->t = maxT;
+            s->weight[0] = s->weight[1] = s->weight[2] = 1.0f;
+            s->pdf = 1.0f; s->exited = 1;
+            for (int k = 0; k < 3; ++k) s->p[k] = r->pos[k] + s->t * r->dir[k];
+            s->sampling_scheme = GPIS_SCHEME_UNI; s->status = 1;
+            continue;
+        }
+        float rec[8];
+        if (absorption_only) {
+            gm_flight(d, r, far_t, st, jitter[i], 1, rec);
+            gm_finish_segment(d, rec, st);
+            float tr = rec[5] == 0.0f ? 0.0f : 1.0f;
+            if (rec[0] < far_t) {
+                st->last_aniso[0] = rec[2]; st->last_aniso[1] = rec[3]; st->last_aniso[2] = rec[4];
+                st->first_scatter = 0;
+            }
+            s->t = far_t;
+            s->weight[0] = s->weight[1] = s->weight[2] = tr;
+            s->pdf = 1.0f; s->exited = 1; s->sampling_scheme = GPIS_SCHEME_UNI;
+            for (int k = 0; k < 3; ++k) s->p[k] = r->pos[k] + s->t * r->dir[k];
+            s->gp_id = st->last_gp_id;
+            st->info_t += s->t;
+            s->status = 1;
+            continue;
+        }
+        gm_flight(d, r, far_t, st, jitter[i], 0, rec);
+        uint32_t fst;
+        memcpy(&fst, &rec[7], 4);
+        if ((fst & 0xFFu) != GPIS_FLIGHT_OK) { s->status = 0; continue; }
+        gm_finish_segment(d, rec, st);
+        double t = rec[0];
+        int hit = rec[5] == 0.0f;
+        s->exited = !hit;
+        if (t < maxT) {
+            s->aniso[0] = rec[2]; s->aniso[1] = rec[3]; s->aniso[2] = rec[4];
+            st->last_aniso[0] = rec[2]; st->last_aniso[1] = rec[3]; st->last_aniso[2] = rec[4];
+            st->first_scatter = 0;
+            if (!isfinite((rec[2] + rec[3] + rec[4]) / 3.0f)) {
+                s->aniso[0] = 1.0f; s->aniso[1] = s->aniso[2] = 0.0f;
+                s->status = 0;
+                continue;
+            }
+        }
+        if (hit) {
+            double dot = (double)s->aniso[0] * r->dir[0] + (double)s->aniso[1] * r->dir[1] + (double)s->aniso[2] * r->dir[2];
+            if (dot > 0) { s->status = 0; continue; }
+            double l2 = (double)s->aniso[0] * s->aniso[0] + (double)s->aniso[1] * s->aniso[1] + (double)s->aniso[2] * s->aniso[2];
+            if (l2 < 0.0000001f) {
+                s->aniso[0] = 1.0f; s->aniso[1] = s->aniso[2] = 0.0f;
+                s->status = 0;
+                continue;
+            }
+        } else {
+            s->aniso[0] = rec[2]; s->aniso[1] = rec[3]; s->aniso[2] = rec[4];
+        }
+        float ratio = ss / stt;
+        s->t = fminf((float)t, maxT);
+        s->continued_t = (float)t;
+        for (int k = 0; k < 3; ++k) { s->weight[k] = ratio; s->continued_weight[k] = ratio; }
+        s->pdf = 1.0f;
+        st->last_aniso[0] = s->aniso[0]; st->last_aniso[1] = s->aniso[1]; st->last_aniso[2] = s->aniso[2];
+        s->sampling_scheme = st->sampling_scheme;
+        st->first_scatter = 0;
+        st->bounce += 1;
+        st->sampling_scheme = GPIS_SCHEME_UNI;
+        for (int k = 0; k < 3; ++k) s->p[k] = r->pos[k] + s->t * r->dir[k];
+        s->gp_id = st->last_gp_id;
+        st->info_t += s->t;
+        s->status = 1;
+    }
+    return GPIS_OK;
+}
+
+int gor_medium_transmittance(const gpis_medium_desc *d, const gpis_ray *rays, gpis_medium_state *states,
+                             const float *jitter, float *transmittance, uint32_t n)
+{
+    for (uint32_t i = 0; i < n; ++i) {
+        const gpis_ray *r = &rays[i];
+        gpis_medium_state *st = &states[i];
+        transmittance[i] = 1.0f;
+        if (r->far_t <= r->near_t) continue;
+        float far_t = r->far_t;
+        if (!isfinite(far_t)) far_t = (float)((double)r->near_t + 2000);
+        float rec[8];
+        gm_flight(d, r, far_t, st, jitter[i], 1, rec);
+        uint32_t fst;
+        memcpy(&fst, &rec[7], 4);
+        if ((fst & 0xFFu) != GPIS_FLIGHT_OK) { transmittance[i] = 0.0f; continue; }
+        gm_finish_segment(d, rec, st);
+        if (rec[0] < far_t) {
+            st->last_aniso[0] = rec[2]; st->last_aniso[1] = rec[3]; st->last_aniso[2] = rec[4];
+            st->first_scatter = 0;
+            if (!isfinite((rec[2] + rec[3] + rec[4]) / 3.0f)) { transmittance[i] = 0.0f; continue; }
+        }
+        transmittance[i] = rec[5] == 0.0f ? 0.0f : 1.0f;
+    }
+    return GPIS_OK;
+}

@@ -83,6 +83,13 @@ int gor_nee(const gpis_medium_desc *desc, const float origin[3], const float dir
 int gor_sampling_scheme(const gpis_medium_desc *desc, const float origin[3], const float p[3],
                         const uint32_t seeds[4]);
 
+/* Medium queries over oracle flights (GaussianProcessMedium state machines,
+ * GaussianProcessMedium.cpp:222-440); single-threaded. */
+int gor_medium_sample_distance(const gpis_medium_desc *desc, const gpis_ray *rays, gpis_medium_state *states,
+                               const float *jitter, gpis_medium_sample *samples, uint32_t n);
+int gor_medium_transmittance(const gpis_medium_desc *desc, const gpis_ray *rays, gpis_medium_state *states,
+                             const float *jitter, float *transmittance, uint32_t n);
+
 /* Elementwise SE splat in FP64 (the SeSplat1DTest expectation, SeSplat1DTest.cpp:72-84). */
 void gor_se_splat_1d(const float *q, const float *c, uint32_t n, float scale,
                      double *values, double *derivatives);

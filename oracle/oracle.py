@@ -55,6 +55,8 @@ def lib():
                 "gor_nee": (c_int, [M, vp, vp, vp, vp, ctypes.c_float, vp, vp, vp, vp]),
                 "gor_sampling_scheme": (c_int, [M, vp, vp, vp]),
                 "gor_se_splat_1d": (None, [vp, vp, u32, ctypes.c_float, vp, vp]),
+                "gor_medium_sample_distance": (c_int, [M, vp, vp, vp, vp, u32]),
+                "gor_medium_transmittance": (c_int, [M, vp, vp, vp, vp, u32]),
             }
             for k, (r, a) in sigs.items():
                 f = getattr(L, k)
@@ -179,3 +181,22 @@ def se_splat_1d(q, c, scale):
     d = np.zeros(len(q), np.float64)
     lib().gor_se_splat_1d(_p(q), _p(c), len(q), float(scale), _p(v), _p(d))
     return v, d
+
+
+def medium_sample_distance(desc, rays, states, jitter):
+    """rays: RAY_DTYPE array; states: STATE_DTYPE array (updated in place)."""
+    samples = np.zeros(len(rays), abi.SAMPLE_DTYPE)
+    jit = np.ascontiguousarray(jitter, np.float32)
+    rc = lib().gor_medium_sample_distance(ctypes.byref(desc), _p(rays), _p(states), _p(jit), _p(samples), len(rays))
+    if rc:
+        raise abi.GpisError(f"oracle sample distance failed: {rc}", rc)
+    return samples
+
+
+def medium_transmittance(desc, rays, states, jitter):
+    tr = np.zeros(len(rays), np.float32)
+    jit = np.ascontiguousarray(jitter, np.float32)
+    rc = lib().gor_medium_transmittance(ctypes.byref(desc), _p(rays), _p(states), _p(jit), _p(tr), len(rays))
+    if rc:
+        raise abi.GpisError(f"oracle transmittance failed: {rc}", rc)
+    return tr
