@@ -143,6 +143,15 @@ class ResultSoA(ctypes.Structure):
     _fields_ = [("rec", ctypes.c_void_p)]
 
 
+class NeeSoA(ctypes.Structure):
+    """gpis_nee_soa: the realization's flight streams plus point_t and normal (float4 each)."""
+    _fields_ = [
+        ("flight", FlightSoA),
+        ("point_t", ctypes.c_void_p),
+        ("normal", ctypes.c_void_p),
+    ]
+
+
 class Counters(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint64) for name in
                 ("flights", "steps", "refine_evals", "hits", "step_limit", "invalid",
@@ -306,6 +315,8 @@ def load_library(path=None):
         "gpis_ctx_destroy": (None, [vp]),
         "gpis_flights_submit": (c_int, [vp, P(FlightSoA), P(ResultSoA), c_u32, vp]),
         "gpis_flights_trace_host": (c_int, [vp, P(FlightSoA), P(ResultSoA), c_u32]),
+        "gpis_nee_submit": (c_int, [vp, P(NeeSoA), vp, c_u32, vp]),
+        "gpis_nee_host": (c_int, [vp, P(NeeSoA), vp, c_u32]),
         "gpis_status": (c_int, [vp, P(Counters), c_int]),
         "gpis_profile_enable": (c_int, [vp, c_int]),
         "gpis_profile_read": (c_int, [vp, P(ctypes.c_double), P(ctypes.c_uint64), c_int]),

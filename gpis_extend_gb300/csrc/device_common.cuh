@@ -59,6 +59,16 @@ struct DevMedium {
     uint32_t min_step;
     uint32_t max_steps;
     uint32_t scheme;
+    // nonstationary length scale ls(p) = a + b*sin(fx*x)*cos(fz*z) (brute force)
+    uint32_t ls_kind;
+    float ls_params[4];
+    float ls_max;
+    float var1d_c;          // impulseDensity / kernelRadius as the reference rounds it
+    // octaves: noise = sum_k oct_sigma[k] * n_k with length scale x oct_scale[k]
+    uint32_t n_oct;
+    float oct_sigma[4];
+    float oct_scale[4];
+    uint32_t oct_seed[4];
 };
 
 struct PcgJump {

@@ -48,24 +48,69 @@ namespace {
 constexpr unsigned FULL = 0xffffffffu;
 constexpr float LOG2E = 1.4426950408889634f;
 
-// Conditioning kernels of the 1D Renewal(+) update (GPFunctions.cpp:850-875):
-// exp(-d^2/4), its first and second derivative and the transverse factor.
+// Conditioning kernels of the 1D Renewal(+) update (GPFunctions.cpp:850-875) for the
+// local scale a (1 when stationary; sqrt of the mean squared kernel scale of the
+// two points otherwise, getNonstationaryCovSplatCov1D, GPFunctions.cpp:1723-1734):
+// exp(-d^2/(4a^2)), its first and second derivative and the transverse factor.
 struct Cov1D { float k0, k1, k2, k3; };
 
-__device__ __forceinline__ Cov1D cov1d(float d)
+__device__ __forceinline__ Cov1D cov1d(float d, float a = 1.0f)
 {
     Cov1D c;
-    c.k0 = ex2_approx((-0.25f * LOG2E) * d * d);
-    c.k1 = -0.5f * d * c.k0;
-    c.k2 = (0.25f * d * d - 0.5f) * c.k0;
-    c.k3 = -0.5f * c.k0;
+    const float ia2 = 1.0f / (a * a);
+    c.k0 = ex2_approx((-0.25f * LOG2E) * ia2 * d * d);
+    c.k1 = -0.5f * ia2 * d * c.k0;
+    c.k2 = (0.25f * ia2 * ia2 * d * d - 0.5f * ia2) * c.k0;
+    c.k3 = -0.5f * ia2 * c.k0;
     return c;
 }
 
-// World -> isotropic ray-space direction frame of a flight.
+// ---- octaves and the nonstationary length scale --------------------------------
+__device__ __forceinline__ float oct_sigma(const DevMedium &m, int k) { return m.n_oct == 1 ? m.sigma : m.oct_sigma[k]; }
+__device__ __forceinline__ float oct_scale(const DevMedium &m, int k) { return m.n_oct == 1 ? 1.0f : m.oct_scale[k]; }
+__device__ __forceinline__ uint32_t oct_seed(const DevMedium &m, int k) { return m.n_oct == 1 ? 0u : m.oct_seed[k]; }
+__device__ __forceinline__ uint32_t oct_normal_seed(const DevMedium &m, uint32_t s, int k)
+{
+    return m.n_oct == 1 ? s : s + (uint32_t)k * 0x9E3779B9u;
+}
+
+// nonStationarySplattingKernelScale = ls(p) / ls_max (GPFunctions.cpp:1229-1235); 1 when stationary.
+__device__ __forceinline__ float ns_scale(const DevMedium &m, float x, float z)
+{
+    if (m.ls_kind == 0u) return 1.0f;
+    const float *q = m.ls_params;
+    return __fdiv_rn(q[0] + q[1] * sinf(q[2] * x) * cosf(q[3] * z), m.ls_max);
+}
+
+// The same with the procedural vector evaluated in double, as on Vec3d(p).
+__device__ __forceinline__ float ns_scale_precise(const DevMedium &m, float x, float z)
+{
+    if (m.ls_kind == 0u) return 1.0f;
+    const float *q = m.ls_params;
+    const double v = __dmul_rn(__dmul_rn((double)q[1], sin(__dmul_rn((double)q[2], (double)x))),
+                               cos(__dmul_rn((double)q[3], (double)z)));
+    const float ls = (float)__dadd_rn((double)q[0], v);
+    return __fdiv_rn(ls, m.ls_max);
+}
+
+// getNonstationaryCovSplatCov1D(pq, pc) for the isotropic field.
+__device__ __forceinline__ float splat_cov_1d(float sq, float sc)
+{
+    if (sq == 1.0f && sc == 1.0f) return 1.0f;
+    // (float)(0.5 * (double)x) is exactly 0.5f * x for normal x
+    return __fsqrt_rn(__fmul_rn(0.5f, __fadd_rn(__fmul_rn(sq, sq), __fmul_rn(sc, sc))));
+}
+
+// World -> isotropic ray-space direction frame of a flight (the nonstationary
+// transform divides by the maximum lateral scale before normalising).
 __device__ __forceinline__ void ray_frame(const DevMedium &m, float dx, float dy, float dz, Frame &f)
 {
     float ix = __fmul_rn(m.l_inv[0], dx), iy = __fmul_rn(m.l_inv[1], dy), iz = __fmul_rn(m.l_inv[2], dz);
+    if (m.ls_kind) {
+        ix = __fdiv_rn(ix, m.ls_max);
+        iy = __fdiv_rn(iy, m.ls_max);
+        iz = __fdiv_rn(iz, m.ls_max);
+    }
     normalize3_rn(ix, iy, iz);
     make_frame(ix, iy, iz, f);
 }
@@ -76,15 +121,41 @@ __device__ __forceinline__ float ray_coord(const float *li, const float *n, floa
     return dot3_rn(n[0], n[1], n[2], __fmul_rn(li[0], px), __fmul_rn(li[1], py), __fmul_rn(li[2], pz));
 }
 
+// The coordinate of octave k (length scale x sc) of a nonstationary or octave medium.
+__device__ __forceinline__ float ray_coord_oct(const DevMedium &m, const float *n, float px, float py, float pz, float sc)
+{
+    float x = __fmul_rn(m.l_inv[0], px), y = __fmul_rn(m.l_inv[1], py), z = __fmul_rn(m.l_inv[2], pz);
+    if (m.ls_kind) {
+        x = __fdiv_rn(x, m.ls_max);
+        y = __fdiv_rn(y, m.ls_max);
+        z = __fdiv_rn(z, m.ls_max);
+    }
+    if (sc != 1.0f) {
+        x = __fdiv_rn(x, sc);
+        y = __fdiv_rn(y, sc);
+        z = __fdiv_rn(z, sc);
+    }
+    return dot3_rn(n[0], n[1], n[2], x, y, z);
+}
+
+// 1 / sqrt(sparseConvNoiseVariance1D) at kernel scale ls.
+__device__ __forceinline__ float inv_norm_1d(const DevMedium &m, float ls)
+{
+    return ls == 1.0f ? m.inv_norm1d : m.inv_norm1d * rsqrtf(ls);
+}
+
 // ---- 1D noise, generic impulse count (no cache) --------------------------------
-// Returns the raw (unnormalized) sum and its derivative w.r.t. the iso coordinate.
+// Returns the raw (unnormalized) sum and its derivative w.r.t. the iso coordinate;
+// ls is the local kernel scale (splattingKernel1D takes it at the query point).
 template <bool DERIV>
-__device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, float &v, float &dv)
+__device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, float &v, float &dv, float ls = 1.0f)
 {
     const float tg = __fdiv_rn(z, m.kr_iso);
     const float fl = floorf(tg);
     const float frac = __fsub_rn(tg, fl);
     const int ci = (int)fl;
+    const float il2 = 1.0f / (ls * ls);
+    const float kexp = m.kexp1d * il2;
     float sv = 0.0f, sd = 0.0f;
     for (int dx = -1; dx <= 1; ++dx) {
         const float tl = __fsub_rn(frac, (float)dx);
@@ -94,10 +165,10 @@ __device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, floa
             const uint32_t wr = pcg_draw(c_jump[3 + 2 * k], s);
             const float tp = __fsub_rn(tl, ti);
             if (fabsf(tp) < 1.0f) {
-                const float e = ex2_approx(m.kexp1d * (tp * tp));
+                const float e = ex2_approx(kexp * (tp * tp));
                 const float w = (wr >> 31) ? 1.0f : -1.0f;
                 sv += w * e;
-                if (DERIV) sd += w * (-(m.kr_iso * tp) * e);
+                if (DERIV) sd += w * (-(m.kr_iso * tp) * il2 * e);
             }
         }
     }
@@ -172,14 +243,15 @@ __device__ __forceinline__ void cond3d(const DevMedium &m, const CondRec &c, con
     const float f = ex2_approx(-LOG2E * absq);
 #pragma unroll
     for (int i = 0; i < 3; ++i) dp[i] = -2.0f * (ab[i] * m.m3c[i]);
-    v = f * c.vs;
+    const CondOct &co = c.oct[0];
+    v = f * co.vs;
 #pragma unroll
-    for (int j = 0; j < 3; ++j) g[j] = dp[j] * f * c.vs;
+    for (int j = 0; j < 3; ++j) g[j] = dp[j] * f * co.vs;
 #pragma unroll
     for (int cc = 0; cc < 3; ++cc) {
-        v += dp[cc] * f * c.gs[cc];
+        v += dp[cc] * f * co.gs[cc];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) g[j] += (dp[cc] * dp[j] - (cc == j ? 2.0f * m.m3c[cc] : 0.0f)) * f * c.gs[cc];
+        for (int j = 0; j < 3; ++j) g[j] += (dp[cc] * dp[j] - (cc == j ? 2.0f * m.m3c[cc] : 0.0f)) * f * co.gs[cc];
     }
 }
 
@@ -281,10 +353,10 @@ __device__ void transverse_moments(const DevMedium &m, const CondRec &c, const f
     }
 }
 
-// World gradient of the noise of one flight at p (evaluateGradientNoise1D /
-// evaluateNoise3D gradient).  cond: conditioning splats active.
-__device__ void noise_gradient(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
-                               const float p[3], float t_segment, float &value, float g[3])
+// Noise of octave k at p with its world gradient (evaluateGradientNoise1D /
+// evaluateNoise3D gradient).  cond: the octave's conditioning splats are active.
+__device__ void noise_gradient_oct(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
+                                   const float p[3], float t_segment, int oc, float &value, float g[3])
 {
     if (!(m.flags & MF_ONE_D)) {
         float v, gg[3];
@@ -301,62 +373,77 @@ __device__ void noise_gradient(const DevMedium &m, const FlightIn &fl, const Con
         }
         return;
     }
+    const CondOct &co = c.oct[oc];
+    const float sc = oct_scale(m, oc);
     Frame f;
     ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
-    const float z = ray_coord(m.l_inv, f.n, p[0], p[1], p[2]);
+    const float z = ray_coord_oct(m, f.n, p[0], p[1], p[2], sc);
+    const float ls = ns_scale(m, p[0], p[2]);
     float v, dv;
-    noise1d_generic<true>(m, z, fl.noise_seed, v, dv);
-    v *= m.inv_norm1d;
-    dv *= m.inv_norm1d;
+    noise1d_generic<true>(m, z, fl.noise_seed + oct_seed(m, oc), v, dv, ls);
+    const float inrm = inv_norm_1d(m, ls);
+    v *= inrm;
+    dv *= inrm;
     float gcx = 0.0f, gcy = 0.0f;
     if (cond) {
-        const float oz = ray_coord(m.l_inv, f.n, fl.o[0], fl.o[1], fl.o[2]);
-        const Cov1D k = cov1d(z - oz);
-        v += c.vs * k.k0 + c.gs[2] * k.k1;
-        dv += c.vs * k.k1 + c.gs[2] * k.k2;
+        const float oz = ray_coord_oct(m, f.n, fl.o[0], fl.o[1], fl.o[2], sc);
+        const float a = splat_cov_1d(ls, ns_scale(m, fl.o[0], fl.o[2]));
+        const Cov1D k = cov1d(z - oz, a);
+        v += co.vs * k.k0 + (sc * co.gs[2]) * k.k1;
+        dv += co.vs * k.k1 + (sc * co.gs[2]) * k.k2;
         if (m.flags & MF_CORR_XY) {
-            gcx = c.gs[0] * k.k3;
-            gcy = c.gs[1] * k.k3;
+            gcx = (sc * co.gs[0]) * k.k3;
+            gcy = (sc * co.gs[1]) * k.k3;
         }
     }
     value = v;
+    const uint32_t nseed = oct_normal_seed(m, fl.normal_seed, oc);
     float gl[3];
-    if (m.flags & MF_TRANSVERSE) {
+    if ((m.flags & MF_TRANSVERSE) && m.ls_kind == 0u && m.n_oct == 1) {
         float m0, m1, var, z0, z1;
         transverse_moments(m, c, fl.o, p, f, cond, m0, m1, var);
-        normal_draws(fl.normal_seed, 0, z0, z1);
+        normal_draws(nseed, 0, z0, z1);
         const float s = sqrtf(var);
         gl[0] = m0 + s * z0;
         gl[1] = m1 + s * z1;
         gl[2] = dv;
     } else {
+        const float scx = splat_cov_1d(ls, ls);
+        const float xs = 1.0f / scx;
         float z0, z1;
-        normal_draws(fl.normal_seed, 0, z0, z1);
+        normal_draws(nseed, 0, z0, z1);
         const float inv_s2 = 1.0f / 1.41421354f;
-        float x1 = z0 * inv_s2, y1 = z1 * inv_s2;
+        const float x1 = z0 * inv_s2, y1 = z1 * inv_s2;
         if (t_segment == 0.0f) {
-            gl[0] = x1 + gcx;
-            gl[1] = y1 + gcy;
+            gl[0] = x1 * xs + gcx;
+            gl[1] = y1 * xs + gcy;
         } else if (!((m.flags & MF_RENEWAL_PLUS) && (m.flags & MF_CORR_XY))) {
             float z2, z3;
-            normal_draws(fl.normal_seed, 1, z2, z3);
-            gl[0] = z2 * inv_s2 + gcx;
-            gl[1] = z3 * inv_s2 + gcy;
+            normal_draws(nseed, 1, z2, z3);
+            gl[0] = z2 * inv_s2 * xs + gcx;
+            gl[1] = z3 * inv_s2 * xs + gcy;
         } else {
             float fac, cv, z2, z3;
             corr_moments(t_segment, fac, cv);
-            normal_draws(fl.normal_seed, 1, z2, z3);
-            const float sc = sqrtf(cv);
-            gl[0] = (z2 * sc + fac * 2.0f * x1) + gcx;
-            gl[1] = (z3 * sc + fac * 2.0f * y1) + gcy;
+            normal_draws(nseed, 1, z2, z3);
+            const float sq = sqrtf(cv);
+            gl[0] = (z2 * sq + fac * 2.0f * x1) + gcx;
+            gl[1] = (z3 * sq + fac * 2.0f * y1) + gcy;
         }
         gl[2] = dv;
     }
+    const float div = (m.ls_kind ? m.ls_max : 1.0f) * sc;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const float gi = f.t[i] * gl[0] + f.b[i] * gl[1] + f.n[i] * gl[2];
-        g[i] = m.l_inv[i] * gi;
+        g[i] = m.l_inv[i] * gi / div;
     }
+}
+
+__device__ __forceinline__ void noise_gradient(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
+                                               const float p[3], float t_segment, float &value, float g[3])
+{
+    noise_gradient_oct(m, fl, c, cond, p, t_segment, 0, value, g);
 }
 
 __device__ __forceinline__ void write_status(const FlightArgs &a, uint32_t i, float t, float value,
@@ -364,6 +451,88 @@ __device__ __forceinline__ void write_status(const FlightArgs &a, uint32_t i, fl
 {
     a.out[2 * i] = make_float4(t, value, 0.0f, 0.0f);
     a.out[2 * i + 1] = make_float4(0.0f, trans, __uint_as_float(steps), __uint_as_float(status));
+}
+
+// Conditioning coefficients of a flight at its origin (conditioning1D / 3D,
+// SparseConvolutionNoise.cpp:498-656).  With several octaves the residual of the
+// value (and of the gradient under Renewal+) is shared in proportion to each
+// octave's variance.
+__device__ CondRec make_condition(const DevMedium &m, const FlightIn &fl)
+{
+    CondRec c = {};
+    const float *p = fl.o;
+    int id;
+    const float mean = mean_value(m, p[0], p[1], p[2], id);
+    float mg[3] = {0.0f, 0.0f, 0.0f};
+    const bool rp = (m.flags & MF_RENEWAL_PLUS) != 0;
+    if (rp) mean_grad(m, p[0], p[1], p[2], mg);
+    CondRec none = {};
+    const int n = (m.flags & MF_ONE_D) ? (int)m.n_oct : 1;
+    float v[4], g[4][3];
+    for (int k = 0; k < n; ++k) noise_gradient_oct(m, fl, none, false, p, 0.0f, k, v[k], g[k]);
+    float tv[4], tg[4][3];
+    if (n == 1) {
+        tv[0] = fl.prev_v;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) tg[0][i] = fl.prev_g[i];
+    } else {
+        float total = 0.0f, sum_v = 0.0f, sum_g[3] = {0.0f, 0.0f, 0.0f};
+        for (int k = 0; k < n; ++k) {
+            const float sk = oct_sigma(m, k);
+            total += sk * sk;
+            sum_v += sk * v[k];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) sum_g[i] += sk * g[k][i];
+        }
+        const float resid = (fl.prev_v - mean) - sum_v;
+        float resid_g[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) resid_g[i] = (fl.prev_g[i] - mg[i]) - sum_g[i];
+        for (int k = 0; k < n; ++k) {
+            const float sk = oct_sigma(m, k);
+            const float share = sk * sk / total;
+            tv[k] = mean + sk * v[k] + share * resid;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) tg[k][i] = mg[i] + sk * g[k][i] + share * resid_g[i];
+        }
+    }
+    for (int k = 0; k < n; ++k) {
+        const float amp = oct_sigma(m, k);
+        if (amp == 0.0f) continue;
+        CondOct &co = c.oct[k];
+        co.vs = (tv[k] - mean) / amp - v[k];
+        if (!rp) continue;
+        float delta[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) delta[i] = (tg[k][i] - mg[i]) / amp - g[k][i];
+        if (m.flags & MF_ONE_D) {
+            Frame f;
+            ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+            // the octave's length multiplier enters where the splats are evaluated
+            const float mul = m.ls_kind ? m.ls_max : 1.0f;
+            float gi[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) gi[i] = (m.l_aniso[i] * delta[i]) * mul;
+            const float ls = ns_scale(m, p[0], p[2]);
+            const float s2 = splat_cov_1d(ls, ls) * splat_cov_1d(ls, ls);
+            const float gx = dot3_rn(f.t[0], f.t[1], f.t[2], gi[0], gi[1], gi[2]);
+            const float gy = dot3_rn(f.b[0], f.b[1], f.b[2], gi[0], gi[1], gi[2]);
+            const float gz = dot3_rn(f.n[0], f.n[1], f.n[2], gi[0], gi[1], gi[2]);
+            const bool xy = (m.flags & MF_CORR_XY) != 0;
+            co.gs[0] = xy ? -2.0f * gx * s2 : 0.0f;
+            co.gs[1] = xy ? -2.0f * gy * s2 : 0.0f;
+            co.gs[2] = -2.0f * gz * s2;
+            if (k == 0) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) c.tgn[i] = (tg[0][i] - mg[i]) / amp;
+                c.has_obs = 1u;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) co.gs[i] = delta[i] * m.d2inv3[i];
+        }
+    }
+    return c;
 }
 
 // ---------------------------------------------------------------------------
@@ -376,47 +545,11 @@ __global__ void __launch_bounds__(128) k_prepare(FlightArgs a)
     bool mok;
     const DevMedium &m = *medium_of(a, i, mok);
     const FlightIn fl = load_flight(a, i);
-    CondRec c = {};
-    if (!mok || !conditioned(m, fl) || !flight_valid(fl) || m.sigma == 0.0f) {
-        a.cond[i] = c;
+    if (!mok || !conditioned(m, fl) || !flight_valid(fl)) {
+        a.cond[i] = CondRec{};
         return;
     }
-    const float *p = fl.o;
-    int id;
-    const float mean = mean_value(m, p[0], p[1], p[2], id);
-    const float amp = m.sigma;
-    float v, g[3];
-    CondRec none = {};
-    noise_gradient(m, fl, none, false, p, 0.0f, v, g);
-    c.vs = (fl.prev_v - mean) / amp - v;
-    if (m.flags & MF_RENEWAL_PLUS) {
-        float mg[3];
-        mean_grad(m, p[0], p[1], p[2], mg);
-        float delta[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) delta[k] = (fl.prev_g[k] - mg[k]) / amp - g[k];
-        if (m.flags & MF_ONE_D) {
-            Frame f;
-            ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
-            float gi[3];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) gi[k] = m.l_aniso[k] * delta[k];
-            const float gx = dot3_rn(f.t[0], f.t[1], f.t[2], gi[0], gi[1], gi[2]);
-            const float gy = dot3_rn(f.b[0], f.b[1], f.b[2], gi[0], gi[1], gi[2]);
-            const float gz = dot3_rn(f.n[0], f.n[1], f.n[2], gi[0], gi[1], gi[2]);
-            const bool xy = (m.flags & MF_CORR_XY) != 0;
-            c.gs[0] = xy ? -2.0f * gx : 0.0f;
-            c.gs[1] = xy ? -2.0f * gy : 0.0f;
-            c.gs[2] = -2.0f * gz;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) c.tgn[k] = (fl.prev_g[k] - mg[k]) / amp;
-            c.has_obs = 1u;
-        } else {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) c.gs[k] = delta[k] * m.d2inv3[k];
-        }
-    }
-    a.cond[i] = c;
+    a.cond[i] = make_condition(m, fl);
 }
 
 // ---------------------------------------------------------------------------
@@ -436,6 +569,8 @@ struct LaneField {
     uint32_t mean_kind;     // mean function in registers (all kinds but the grid)
     float mq[6];
     uint32_t n_imp;         // impulses per cell
+    bool ns;                // nonstationary length scale
+    float ls_o;             // kernel scale at the origin (conditioning)
 };
 
 // Safe contents for a lane without a flight (collective evaluators run every lane).
@@ -454,6 +589,48 @@ __device__ __forceinline__ void lane_field_idle(LaneField &L, const DevMedium *m
 #pragma unroll
     for (int k = 0; k < 6; ++k) L.mq[k] = 0.0f;
     L.n_imp = 0u;
+    L.ns = false;
+    L.ls_o = 1.0f;
+}
+
+// A lane's registers for flight fl of medium m; cond points at its conditioning record.
+__device__ __forceinline__ void lane_field_setup(LaneField &L, const DevMedium &m, const FlightIn &fl,
+                                                 const CondRec *cond)
+{
+    L.m = &m;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { L.o[k] = fl.o[k]; L.li[k] = m.l_inv[k]; }
+    L.seed = fl.noise_seed;
+    L.sigma = m.sigma;
+    L.cond = conditioned(m, fl);
+    L.vs = L.gsz = L.ozc = 0.0f;
+    L.ns = m.ls_kind != 0u;
+    L.ls_o = 1.0f;
+    L.mean_kind = m.mean_kind;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) L.mq[k] = m.mean_params[k];
+    L.n_imp = m.n_imp;
+    if (m.flags & MF_ONE_D) {
+        Frame f;
+        ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+        L.n[0] = f.n[0]; L.n[1] = f.n[1]; L.n[2] = f.n[2];
+        L.kr = m.kr_iso;
+        L.kexp = m.kexp1d;
+        L.inv_norm = m.inv_norm1d;
+        if (L.cond) {
+            L.ls_o = ns_scale_precise(m, L.o[0], L.o[2]);
+            if (m.n_oct == 1) {
+                const CondOct c = cond->oct[0];
+                L.vs = c.vs;
+                L.gsz = c.gs[2];
+                L.ozc = ray_coord_oct(m, L.n, L.o[0], L.o[1], L.o[2], 1.0f);
+            } else {
+                L.c3 = *cond;
+            }
+        }
+    } else if (L.cond) {
+        L.c3 = *cond;
+    }
 }
 
 // mean_value with the parameters held in registers; the grid reads the medium table.
@@ -482,6 +659,23 @@ __device__ __forceinline__ float lane_mean(const LaneField &L, float x, float y,
     }
 }
 
+// Conditioning coefficients of octave k of a 1D lane: value scale, gradient
+// scale along the ray (times the octave's length multiplier) and the origin's
+// ray coordinate.  Single-octave flights keep them in registers.
+__device__ __forceinline__ void lane_cond_1d(const LaneField &L, int k, float sc, float &vs, float &gz, float &oz)
+{
+    if (L.m->n_oct == 1) {
+        vs = L.vs;
+        gz = L.gsz;
+        oz = L.ozc;
+        return;
+    }
+    const CondOct &co = L.c3.oct[k];
+    vs = co.vs;
+    gz = __fmul_rn(sc, co.gs[2]);
+    oz = ray_coord_oct(*L.m, L.n, L.o[0], L.o[1], L.o[2], sc);
+}
+
 // ---- precise evaluation ------------------------------------------------------
 // The reference's float formulation op for op: every splat as
 // expf(-((kr*t - kr*t_i)^2 / 2)) (GPFunctions.cpp:845-848), cell sums in impulse
@@ -492,13 +686,14 @@ __device__ __forceinline__ float lane_mean(const LaneField &L, float x, float y,
 // The march uses it wherever a sign decision is close: the crossing step, the
 // step before it and every refinement point.
 
-__device__ float noise1d_precise(const DevMedium &m, float z, uint32_t seed)
+__device__ float noise1d_precise(const DevMedium &m, float z, uint32_t seed, float ls = 1.0f)
 {
     const float kr = m.kr_iso;
     const float tg = __fdiv_rn(z, kr);
     const float fl = floorf(tg);
     const float frac = __fsub_rn(tg, fl);
     const int ci = (int)fl;
+    const float den = __fmul_rn(2.0f, __fmul_rn(ls, ls));
     float sv = 0.0f;
     for (int dx = -1; dx <= 1; ++dx) {
         const float tl = __fsub_rn(frac, (float)dx);
@@ -511,13 +706,16 @@ __device__ float noise1d_precise(const DevMedium &m, float z, uint32_t seed)
             const float tp = __fsub_rn(tl, ti);
             if (fabsf(tp) < 1.0f) {
                 const float ab = __fsub_rn(a, __fmul_rn(kr, ti));
-                const float e = expf(-__fmul_rn(__fmul_rn(ab, ab), 0.5f));
+                const float e = expf(-__fdiv_rn(__fmul_rn(ab, ab), den));
                 cv = __fadd_rn(cv, (wr >> 31) ? e : -e);
             }
         }
         sv = __fadd_rn(sv, cv);
     }
-    return __fdiv_rn(sv, m.norm1d);
+    if (ls == 1.0f) return __fdiv_rn(sv, m.norm1d);
+    // sparseConvNoiseVariance1D: impulseDensity/kernelRadius * sqrt(pi) * localScale
+    const float var = (float)((double)m.var1d_c * (1.7724538509055159 * (double)ls));
+    return __fdiv_rn(sv, __fsqrt_rn(var));
 }
 
 __device__ float noise3d_precise(const DevMedium &m, float px, float py, float pz, uint32_t seed)
@@ -588,6 +786,23 @@ __device__ float mean_plus_precise(const DevMedium &m, float an, float x, float 
         FF tot = ff_add_f(ff_add_f(d, -q[3]), an);
         return __fadd_rn(tot.h, tot.l);
     }
+    if (m.mean_kind == 4 || m.mean_kind == 5) {
+        // the torus (and the union with the plane y = q[5]) in double, uncontracted
+        const double dx = __dsub_rn((double)x, (double)q[0]);
+        const double dy = __dsub_rn((double)y, (double)q[1]);
+        const double dz = __dsub_rn((double)z, (double)q[2]);
+        const double rxz = __dsub_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dz, dz))), (double)q[3]);
+        double mean = __dsub_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(rxz, rxz), __dmul_rn(dy, dy))), (double)q[4]);
+        if (m.mean_kind == 5) {
+            const double pl = __dsub_rn((double)y, (double)q[5]);
+            if (pl < mean) {
+                id = 1;
+                mean = pl;
+            }
+        }
+        return (float)__dadd_rn((double)an, mean);
+    }
+    // float means (homogeneous, grid): (float)((double)an + mean) is the rounded exact sum
     const float mv = mean_value(m, x, y, z, id);
     float e;
     const float s = two_sum(an, mv, e);
@@ -597,29 +812,41 @@ __device__ float mean_plus_precise(const DevMedium &m, float an, float x, float 
 __device__ float field_precise(const LaneField &L, float px, float py, float pz, int &id)
 {
     const DevMedium &m = *L.m;
-    float noise;
-    if (m.flags & MF_ONE_D) {
-        const float z = ray_coord(L.li, L.n, px, py, pz);
-        noise = noise1d_precise(m, z, L.seed);
-        if (L.cond) {
-            // covarianceKernel1D / 1DGrad value parts (GPFunctions.cpp:850-862)
-            const float d = __fsub_rn(z, L.ozc);
-            const float k0 = expf(-__fdiv_rn(__fmul_rn(d, d), m.cov_den2));
-            const float k1 = -2.0f * d / m.cov_den2 * k0;
-            const float vs0 = __fmul_rn(L.vs, k0);
-            const float gz0 = __fmul_rn(__fmul_rn(1.0f, L.gsz), k1);
-            noise = __fadd_rn(noise, __fmul_rn(1.0f, __fadd_rn(vs0, gz0)));
-        }
-    } else {
-        noise = noise3d_precise(m, px, py, pz, L.seed);
+    if (!(m.flags & MF_ONE_D)) {
+        float noise = noise3d_precise(m, px, py, pz, L.seed);
         if (L.cond) {
             float cv, cg[3];
             const float p[3] = {px, py, pz};
             cond3d(m, L.c3, L.o, p, cv, cg);
             noise = __fadd_rn(noise, cv);
         }
+        return mean_plus_precise(m, __fmul_rn(L.sigma, noise), px, py, pz, id);
     }
-    return mean_plus_precise(m, __fmul_rn(L.sigma, noise), px, py, pz, id);
+    const float ls = ns_scale_precise(m, px, pz);
+    float an = 0.0f;
+    for (int k = 0; k < (int)m.n_oct; ++k) {
+        const float sc = oct_scale(m, k);
+        const float z = m.n_oct == 1 && m.ls_kind == 0u ? ray_coord(L.li, L.n, px, py, pz)
+                                                          : ray_coord_oct(m, L.n, px, py, pz, sc);
+        float noise = noise1d_precise(m, z, L.seed + oct_seed(m, k), ls);
+        if (L.cond) {
+            // covarianceKernel1DVal / 1stGrad (GPFunctions.cpp:850-862) at the local
+            // scale a: den2 = 2 (a sqrt2)^2 in float, the derivative in double
+            float vs, gz, oz;
+            lane_cond_1d(L, k, sc, vs, gz, oz);
+            const float a = splat_cov_1d(ls, L.ls_o);
+            const float s2 = (float)((double)a * 1.4142135623730951);
+            const float den2 = a == 1.0f ? m.cov_den2 : (float)(2.0 * (double)__fmul_rn(s2, s2));
+            const float d = __fsub_rn(z, oz);
+            const float k0 = expf(-__fdiv_rn(__fmul_rn(d, d), den2));
+            const float k1 = (float)(-2.0 * (double)d / (double)den2 * (double)k0);
+            const float vs0 = __fmul_rn(vs, k0);
+            const float gz0 = __fmul_rn(gz, k1);
+            noise = __fadd_rn(noise, __fmul_rn(1.0f, __fadd_rn(vs0, gz0)));
+        }
+        an = m.n_oct == 1 ? __fmul_rn(L.sigma, noise) : __fadd_rn(an, __fmul_rn(oct_sigma(m, k), noise));
+    }
+    return mean_plus_precise(m, an, px, py, pz, id);
 }
 
 // ---- fast evaluators ----------------------------------------------------------
@@ -634,26 +861,35 @@ struct EvalGeneric {
         const DevMedium &m = *L.m;
         float noise;
         if (m.flags & MF_ONE_D) {
-            const float z = ray_coord(L.li, L.n, px, py, pz);
-            float v, dv;
-            noise1d_generic<false>(m, z, L.seed, v, dv);
-            noise = v * L.inv_norm;
-            if (L.cond) {
-                const Cov1D k = cov1d(z - L.ozc);
-                noise += L.vs * k.k0 + L.gsz * k.k1;
+            const float ls = ns_scale(m, px, pz);
+            noise = 0.0f;
+            for (int k = 0; k < (int)m.n_oct; ++k) {
+                const float sc = oct_scale(m, k);
+                const float z = ray_coord_oct(m, L.n, px, py, pz, sc);
+                float v, dv;
+                noise1d_generic<false>(m, z, L.seed + oct_seed(m, k), v, dv, ls);
+                float nk = v * inv_norm_1d(m, ls);
+                if (L.cond) {
+                    float vs, gz, oz;
+                    lane_cond_1d(L, k, sc, vs, gz, oz);
+                    const Cov1D c = cov1d(z - oz, splat_cov_1d(ls, L.ls_o));
+                    nk += vs * c.k0 + gz * c.k1;
+                }
+                noise += oct_sigma(m, k) * nk;
+                refills += 3;
             }
-        } else {
-            float v, g[3];
-            noise3d_generic<false>(m, px, py, pz, L.seed, v, g);
-            noise = v * m.inv_norm3d;
-            if (L.cond) {
-                float cv, cg[3];
-                const float p[3] = {px, py, pz};
-                cond3d(m, L.c3, L.o, p, cv, cg);
-                noise += cv;
-            }
+            return noise + lane_mean(L, px, py, pz, id);
         }
-        refills += 1;
+        float v, g[3];
+        noise3d_generic<false>(m, px, py, pz, L.seed, v, g);
+        noise = v * m.inv_norm3d;
+        if (L.cond) {
+            float cv, cg[3];
+            const float p[3] = {px, py, pz};
+            cond3d(m, L.c3, L.o, p, cv, cg);
+            noise += cv;
+        }
+        refills += 27;
         return L.sigma * noise + lane_mean(L, px, py, pz, id);
     }
 };
@@ -798,7 +1034,18 @@ struct EvalCoop1D {
                                            int &id, uint32_t &refills, bool live)
     {
         const int lane = threadIdx.x & 31;
-        const float z = ray_coord(L.li, L.n, px, py, pz);
+        // nonstationary: coordinate in the ls_max-scaled space, kernel width,
+        // normalisation and conditioning scale at the query
+        float z, kexp = L.kexp, inv_norm = L.inv_norm, ca = 1.0f;
+        if (L.ns) {
+            const float ls = ns_scale(*L.m, px, pz);
+            z = ray_coord_oct(*L.m, L.n, px, py, pz, 1.0f);
+            kexp = L.kexp / (ls * ls);
+            inv_norm = inv_norm_1d(*L.m, ls);
+            ca = splat_cov_1d(ls, L.ls_o);
+        } else {
+            z = ray_coord(L.li, L.n, px, py, pz);
+        }
         const float tg = __fdiv_rn(z, L.kr);
         const float fl = floorf(tg);
         const float frac = __fsub_rn(tg, fl);
@@ -831,15 +1078,15 @@ struct EvalCoop1D {
             for (int k = 0; k < NMAX; ++k) {
                 const float s = cache[c][k];
                 const float tp = __fsub_rn(tl, fabsf(s));
-                const float e = ex2_approx(L.kexp * (tp * tp));
+                const float e = ex2_approx(kexp * (tp * tp));
                 const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(s) & 0x80000000u));
                 if (k & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
                 else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
             }
         }
-        float noise = (acc0 + acc1) * L.inv_norm;
+        float noise = (acc0 + acc1) * inv_norm;
         if (L.cond) {
-            const Cov1D k = cov1d(z - L.ozc);
+            const Cov1D k = cov1d(z - L.ozc, ca);
             noise += L.vs * k.k0 + L.gsz * k.k1;
         }
         return L.sigma * noise + lane_mean(L, px, py, pz, id);
@@ -941,34 +1188,11 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                         c_invalid++;
                     } else {
 #pragma unroll
-                        for (int k = 0; k < 3; ++k) { L.o[k] = fl.o[k]; d[k] = fl.d[k]; L.li[k] = m.l_inv[k]; }
+                        for (int k = 0; k < 3; ++k) d[k] = fl.d[k];
                         near_t = fl.near_t;
                         far_t = fl.far_t;
                         first = (fl.flags & GPIS_FLAG_FIRST_SCATTER) != 0;
-                        L.seed = fl.noise_seed;
-                        L.sigma = m.sigma;
-                        L.cond = conditioned(m, fl);
-                        L.vs = L.gsz = L.ozc = 0.0f;
-                        L.mean_kind = m.mean_kind;
-#pragma unroll
-                        for (int k = 0; k < 6; ++k) L.mq[k] = m.mean_params[k];
-                        L.n_imp = m.n_imp;
-                        if (m.flags & MF_ONE_D) {
-                            Frame f;
-                            ray_frame(m, d[0], d[1], d[2], f);
-                            L.n[0] = f.n[0]; L.n[1] = f.n[1]; L.n[2] = f.n[2];
-                            L.kr = m.kr_iso;
-                            L.kexp = m.kexp1d;
-                            L.inv_norm = m.inv_norm1d;
-                            if (L.cond) {
-                                const CondRec c = a.cond[idx];
-                                L.vs = c.vs;
-                                L.gsz = c.gs[2];
-                                L.ozc = ray_coord(L.li, L.n, L.o[0], L.o[1], L.o[2]);
-                            }
-                        } else if (L.cond) {
-                            L.c3 = a.cond[idx];
-                        }
+                        lane_field_setup(L, m, fl, a.cond + idx);
                         step = __fdiv_rn(__fsub_rn(far_t, near_t), (float)m.min_step);
                         if (m.step_size < step) step = m.step_size;
                         t0 = __fadd_rn(near_t, __fmul_rn(step, fl.jitter));
@@ -1000,8 +1224,7 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
 
         // evaluation point of this phase
         float eh = th, el = tl;
-        if (phase == PH_REFINE) { eh = ttest.h; el = ttest.l; }
-        if (phase == PH_PF) { eh = ta.h; el = ta.l; }
+        if (phase == PH_REFINE || phase == PH_PF) { eh = ttest.h; el = ttest.l; }
         float p[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], eh, el);
@@ -1058,7 +1281,11 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                 ta = ff_add_f(ff_norm(th, tl), -step);
                 fb = f;
                 if (!pf_precise) {
-                    phase = PH_PF;  // re-evaluate the step before the crossing precisely first
+                    // re-evaluate the previous value precisely first: it was taken at
+                    // t - step, or at nearT for the first step (where the reference's
+                    // interval [t - step, t] still starts at t - step)
+                    ttest = steps == 1 ? FF{near_t, 0.0f} : ta;
+                    phase = PH_PF;
                 } else {
                     float e;
                     const float dh = two_sum(pf, -fb, e);
@@ -1086,7 +1313,7 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                 }
             }
         } else if (phase == PH_PF) {
-            // f: precise value at ta; fb: precise value at tb
+            // f: precise value at the previous point; fb: precise value at tb
             pf = f;
             float e;
             const float dh = two_sum(pf, -fb, e);
@@ -1187,12 +1414,21 @@ __global__ void __launch_bounds__(128) k_finish(FlightArgs a)
     const bool cond = conditioned(m, fl);
     CondRec c = {};
     if (cond) c = a.cond[i];
-    float v, g[3], mg[3];
-    noise_gradient(m, fl, c, cond, p, (float)t, v, g);
+    // evaluateGradient (SparseConvolutionNoise.cpp:133-140): sum of the octaves'
+    // amplitude-weighted noise gradients plus the mean gradient
+    float gs[3] = {0.0f, 0.0f, 0.0f}, mg[3];
+    const int n_oct = (m.flags & MF_ONE_D) ? (int)m.n_oct : 1;
+    for (int k = 0; k < n_oct; ++k) {
+        float v, g[3];
+        noise_gradient_oct(m, fl, c, cond, p, (float)t, k, v, g);
+        const float amp = oct_sigma(m, k);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) gs[j] = __fadd_rn(gs[j], __fmul_rn(amp, g[j]));
+    }
     mean_grad(m, p[0], p[1], p[2], mg);
-    r0.z = m.sigma * g[0] + mg[0];
-    r0.w = m.sigma * g[1] + mg[1];
-    r1.x = m.sigma * g[2] + mg[2];
+    r0.z = __fadd_rn(gs[0], mg[0]);
+    r0.w = __fadd_rn(gs[1], mg[1]);
+    r1.x = __fadd_rn(gs[2], mg[2]);
     a.out[2 * i] = r0;
     a.out[2 * i + 1] = r1;
 }
@@ -1248,63 +1484,200 @@ __global__ void k_debug_field(const DevMedium *mp, const float4 *origins, const 
     fl.d[0] = d.x; fl.d[1] = d.y; fl.d[2] = d.z; fl.far_t = 1.0f;
     fl.noise_seed = sd.x; fl.normal_seed = sd.y; fl.flags = sd.z; fl.jitter = 0.0f;
     fl.prev_v = pv.x; fl.prev_g[0] = pv.y; fl.prev_g[1] = pv.z; fl.prev_g[2] = pv.w;
-    CondRec c = {};
-    const bool cond = conditioned(m, fl) && m.sigma != 0.0f;
-    if (cond) {
-        // same coefficients as k_prepare
-        int id;
-        const float mean = mean_value(m, fl.o[0], fl.o[1], fl.o[2], id);
-        float v, g[3];
-        CondRec none = {};
-        noise_gradient(m, fl, none, false, fl.o, 0.0f, v, g);
-        c.vs = (fl.prev_v - mean) / m.sigma - v;
-        if (m.flags & MF_RENEWAL_PLUS) {
-            float mg[3], delta[3];
-            mean_grad(m, fl.o[0], fl.o[1], fl.o[2], mg);
-            for (int k = 0; k < 3; ++k) delta[k] = (fl.prev_g[k] - mg[k]) / m.sigma - g[k];
-            if (m.flags & MF_ONE_D) {
-                Frame f;
-                ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
-                float gi[3];
-                for (int k = 0; k < 3; ++k) gi[k] = m.l_aniso[k] * delta[k];
-                const bool xy = (m.flags & MF_CORR_XY) != 0;
-                c.gs[0] = xy ? -2.0f * dot3_rn(f.t[0], f.t[1], f.t[2], gi[0], gi[1], gi[2]) : 0.0f;
-                c.gs[1] = xy ? -2.0f * dot3_rn(f.b[0], f.b[1], f.b[2], gi[0], gi[1], gi[2]) : 0.0f;
-                c.gs[2] = -2.0f * dot3_rn(f.n[0], f.n[1], f.n[2], gi[0], gi[1], gi[2]);
-                for (int k = 0; k < 3; ++k) c.tgn[k] = (fl.prev_g[k] - mg[k]) / m.sigma;
-                c.has_obs = 1u;
-            } else {
-                for (int k = 0; k < 3; ++k) c.gs[k] = delta[k] * m.d2inv3[k];
-            }
-        }
-    }
+    const bool cond = conditioned(m, fl);
+    const CondRec c = cond ? make_condition(m, fl) : CondRec{};
     const float p[3] = {pp.x, pp.y, pp.z};
-    float v, g[3];
-    // value and derivative parts of the noise (the 1D xy entries are the conditioning splats)
+    float v = 0.0f, g[3] = {0.0f, 0.0f, 0.0f}, fv_noise;
+    // value and derivative parts of the noise (the 1D xy entries are the
+    // conditioning splats); several octaves report amplitude-weighted sums
     if (m.flags & MF_ONE_D) {
         Frame f;
         ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
-        const float z = ray_coord(m.l_inv, f.n, p[0], p[1], p[2]);
-        float dv;
-        noise1d_generic<true>(m, z, fl.noise_seed, v, dv);
-        v *= m.inv_norm1d;
-        dv *= m.inv_norm1d;
-        g[0] = g[1] = 0.0f;
-        if (cond) {
-            const float oz = ray_coord(m.l_inv, f.n, fl.o[0], fl.o[1], fl.o[2]);
-            const Cov1D k = cov1d(z - oz);
-            v += c.vs * k.k0 + c.gs[2] * k.k1;
-            dv += c.vs * k.k1 + c.gs[2] * k.k2;
-            if (m.flags & MF_CORR_XY) { g[0] = c.gs[0] * k.k3; g[1] = c.gs[1] * k.k3; }
+        const float ls = ns_scale(m, p[0], p[2]);
+        const float a = splat_cov_1d(ls, ns_scale(m, fl.o[0], fl.o[2]));
+        for (int k = 0; k < (int)m.n_oct; ++k) {
+            const float sc = oct_scale(m, k);
+            const float z = ray_coord_oct(m, f.n, p[0], p[1], p[2], sc);
+            float vk, dv;
+            noise1d_generic<true>(m, z, fl.noise_seed + oct_seed(m, k), vk, dv, ls);
+            const float inrm = inv_norm_1d(m, ls);
+            vk *= inrm;
+            dv *= inrm;
+            float gx = 0.0f, gy = 0.0f;
+            if (cond) {
+                const CondOct &co = c.oct[k];
+                const float oz = ray_coord_oct(m, f.n, fl.o[0], fl.o[1], fl.o[2], sc);
+                const Cov1D kk = cov1d(z - oz, a);
+                vk += co.vs * kk.k0 + (sc * co.gs[2]) * kk.k1;
+                dv += co.vs * kk.k1 + (sc * co.gs[2]) * kk.k2;
+                if (m.flags & MF_CORR_XY) { gx = (sc * co.gs[0]) * kk.k3; gy = (sc * co.gs[1]) * kk.k3; }
+            }
+            const float w = m.n_oct == 1 ? 1.0f : oct_sigma(m, k);
+            v += w * vk;
+            g[0] += w * gx;
+            g[1] += w * gy;
+            g[2] += w * dv;
         }
-        g[2] = dv;
+        fv_noise = m.n_oct == 1 ? m.sigma * v : v;
     } else {
         noise_gradient(m, fl, c, cond, p, 1.0f, v, g);
+        fv_noise = m.sigma * v;
     }
     int id;
     const float mean = mean_value(m, p[0], p[1], p[2], id);
+    // the march's precise evaluator at p (the value its decisions near zero use)
+    LaneField L;
+    lane_field_idle(L, &m);
+    lane_field_setup(L, m, fl, &c);
+    int pid;
+    const float fp = field_precise(L, p[0], p[1], p[2], pid);
     out[2 * i] = make_float4(v, g[0], g[1], g[2]);
-    out[2 * i + 1] = make_float4(m.sigma * v + mean, mean, 0.0f, 0.0f);
+    out[2 * i + 1] = make_float4(fv_noise + mean, mean, fp, __int_as_float(pid));
+}
+
+// ---------------------------------------------------------------------------
+// k_nee: 1D specular next-event estimation on the realization of a flight
+// (neeShared / neeGrad / neePDF, SparseConvolutionNoise.cpp:662-821): the
+// gradient plane of the ray's 1D derivative, the gradient that makes the world
+// normal, and the solid-angle PDF of drawing it.  One thread per query; the
+// realization's conditioning is rebuilt from the flight as k_prepare does.
+// out = {pdf, gradient}; NaN pdf for media without 1D single-octave noise or
+// non-finite inputs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void inv3(const float A[9], float R[9])
+{
+    const float c00 = A[4] * A[8] - A[5] * A[7];
+    const float c01 = A[5] * A[6] - A[3] * A[8];
+    const float c02 = A[3] * A[7] - A[4] * A[6];
+    const float id = 1.0f / (A[0] * c00 + A[1] * c01 + A[2] * c02);
+    R[0] = c00 * id;
+    R[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+    R[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+    R[3] = c01 * id;
+    R[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+    R[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+    R[6] = c02 * id;
+    R[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+    R[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+}
+
+__global__ void __launch_bounds__(128) k_nee(FlightArgs a, const float4 *point_t, const float4 *normal, float4 *out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    bool mok;
+    const DevMedium &m = *medium_of(a, i, mok);
+    FlightIn fl = load_flight(a, i);
+    const float4 q = point_t[i], nv = normal[i];
+    const float p[3] = {q.x, q.y, q.z}, nw[3] = {nv.x, nv.y, nv.z};
+    const float t_seg = q.w;
+    bool ok = mok && (m.flags & MF_ONE_D) && m.n_oct == 1 && isfinite(t_seg);
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        ok = ok && isfinite(fl.o[k]) && isfinite(fl.d[k]) && isfinite(p[k]) && isfinite(nw[k]);
+    const bool cond = conditioned(m, fl);
+    if (cond) ok = ok && isfinite(fl.prev_v) && isfinite(fl.prev_g[0]) && isfinite(fl.prev_g[1]) && isfinite(fl.prev_g[2]);
+    if (!ok) {
+        out[i] = make_float4(__int_as_float(0x7fffffff), 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    const CondRec c = cond ? make_condition(m, fl) : CondRec{};
+    const float amp = m.sigma;
+    float mg[3];
+    mean_grad(m, p[0], p[1], p[2], mg);
+    Frame f;
+    ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+    // mtx_pt = amplitude * localToWorldInvTransposeMatrix(p) * [t b n]
+    float A[9], Ai[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float li = m.ls_kind ? __fdiv_rn(m.l_inv[r], m.ls_max) : m.l_inv[r];
+        const float al = __fmul_rn(amp, li);
+        A[3 * r + 0] = __fmul_rn(al, f.t[r]);
+        A[3 * r + 1] = __fmul_rn(al, f.b[r]);
+        A[3 * r + 2] = __fmul_rn(al, f.n[r]);
+    }
+    inv3(A, Ai);
+    // grad_constraint_3d: the conditioned 1D noise's splat parts at p
+    const float ls = ns_scale_precise(m, p[0], p[2]);
+    const float z = ray_coord_oct(m, f.n, p[0], p[1], p[2], 1.0f);
+    float v, dv;
+    noise1d_generic<true>(m, z, fl.noise_seed, v, dv, ls);
+    const float inrm = inv_norm_1d(m, ls);
+    dv *= inrm;
+    float gc[3] = {0.0f, 0.0f, 0.0f};
+    if (cond) {
+        const CondOct &co = c.oct[0];
+        const float oz = ray_coord_oct(m, f.n, fl.o[0], fl.o[1], fl.o[2], 1.0f);
+        const Cov1D kk = cov1d(z - oz, splat_cov_1d(ls, ns_scale_precise(m, fl.o[0], fl.o[2])));
+        dv += co.vs * kk.k1 + co.gs[2] * kk.k2;
+        if (m.flags & MF_CORR_XY) {
+            gc[0] = co.gs[0] * kk.k3;
+            gc[1] = co.gs[1] * kk.k3;
+        }
+    }
+    gc[2] = dv;
+    // the gradient plane and the gradient that points along the normal
+    float ppt[3], px[3], py[3], cr[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        ppt[r] = A[3 * r + 2] * gc[2] + mg[r];
+        px[r] = A[3 * r + 0];
+        py[r] = A[3 * r + 1];
+    }
+    cr[0] = px[1] * py[2] - px[2] * py[1];
+    cr[1] = px[2] * py[0] - px[0] * py[2];
+    cr[2] = px[0] * py[1] - px[1] * py[0];
+    const float jac = sqrtf(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    const float pn[3] = {cr[0] / jac, cr[1] / jac, cr[2] / jac};
+    const float npn = nw[0] * pn[0] + nw[1] * pn[1] + nw[2] * pn[2];
+    const float isect = (ppt[0] * pn[0] + ppt[1] * pn[1] + ppt[2] * pn[2]) / npn;
+    float g[3], gw[3], g3[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        g[r] = isect * nw[r];
+        gw[r] = g[r] - mg[r];
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) g3[r] = Ai[3 * r + 0] * gw[0] + Ai[3 * r + 1] * gw[1] + Ai[3 * r + 2] * gw[2];
+    float pdf = 0.0f;
+    if (!(isect < 0.0f)) {
+        const double two_pi = 6.283185307179586;
+        double pdf_area;
+        const uint32_t nseed = fl.normal_seed;
+        if (m.flags & MF_TRANSVERSE) {
+            float m0, m1, var;
+            transverse_moments(m, c, fl.o, p, f, cond, m0, m1, var);
+            if (!(var > 0.0f)) {
+                pdf_area = -1.0;
+            } else {
+                const double dx = (double)g3[0] - m0, dy = (double)g3[1] - m1;
+                pdf_area = exp(-0.5 * (dx * dx + dy * dy) / var) / (two_pi * var);
+            }
+        } else if (!((m.flags & MF_RENEWAL_PLUS) && (m.flags & MF_CORR_XY)) || t_seg == 0.0f) {
+            const float sc = splat_cov_1d(ls, ls);
+            const float sx = (float)((double)(g3[0] - gc[0]) * 1.4142135623730951 * sc);
+            const float sy = (float)((double)(g3[1] - gc[1]) * 1.4142135623730951 * sc);
+            pdf_area = exp(-(double)(sx * sx) / 2.0) * exp(-(double)(sy * sy) / 2.0) / two_pi * 2.0 * sc * sc;
+        } else {
+            float z0, z1, fac, cv;
+            normal_draws(nseed, 0, z0, z1);
+            corr_moments(t_seg, fac, cv);
+            const double s2 = 1.41421354;
+            const double x1 = z0 / s2, y1 = z1 / s2;
+            const double sq = sqrt((double)cv);
+            const float sx = (float)(((double)(g3[0] - gc[0]) - fac * 2.0 * x1) / sq);
+            const float sy = (float)(((double)(g3[1] - gc[1]) - fac * 2.0 * y1) / sq);
+            pdf_area = exp(-(double)(sx * sx) / 2.0) * exp(-(double)(sy * sy) / 2.0) / two_pi / cv;
+        }
+        if (pdf_area >= 0.0) {
+            const float cos_l = fabsf(npn);
+            const float pdf_n = (float)pdf_area * (isect * isect) / cos_l / jac;
+            const float ndr = -(nw[0] * fl.d[0] + nw[1] * fl.d[1] + nw[2] * fl.d[2]);
+            pdf = (float)(pdf_n / (4.0 * ndr));
+        }
+    }
+    out[i] = make_float4(pdf, g[0], g[1], g[2]);
 }
 
 __global__ void k_se_splat_1d(const float *q, const float *c, float *v, float *d, size_t n, float scale)
@@ -1342,7 +1715,7 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
         return c == 0 ? 1u : c;
     };
     if (ev) cudaEventRecord(ev[2], stream);
-    if (a.one_d && a.max_imp <= 8) {
+    if (a.one_d && a.max_imp <= 8 && a.max_oct == 1) {
         const void *fn = (const void *)k_march<EvalCoop1D<8>, false>;
         k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(a);
     } else {
@@ -1383,6 +1756,14 @@ cudaError_t launch_debug_field(const DevMedium *m, const float4 *origins, const 
 {
     if (n == 0) return cudaSuccess;
     k_debug_field<<<(n + 127) / 128, 128, 0, s>>>(m, origins, points, dirs, seeds, prev, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nee(const FlightArgs &a, const float4 *point_t, const float4 *normal, float4 *out,
+                       cudaStream_t stream)
+{
+    if (a.n == 0) return cudaSuccess;
+    k_nee<<<(a.n + 127) / 128, 128, 0, stream>>>(a, point_t, normal, out);
     return cudaGetLastError();
 }
 

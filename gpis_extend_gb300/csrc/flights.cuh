@@ -12,9 +12,14 @@ namespace gpis {
 
 // Per-flight conditioning coefficients (SparseConvConditioningCoefficients1D/3D,
 // SparseConvolutionNoise.hpp:7-24), written by the prepare kernel.
-struct CondRec {
+// One realization's coefficients; several octaves each have their own.
+struct CondOct {
     float vs;               // value_scale
     float gs[3];            // gradient_scale (iso-ray space for 1D, world for 3D)
+};
+
+struct CondRec {
+    CondOct oct[4];
     float tgn[3];           // target_gradient_noise (1D transverse law)
     uint32_t has_obs;       // has_gradient_observation
 };
@@ -40,6 +45,7 @@ struct FlightArgs {
     int one_d;                  // all media use 1D noise
     int three_d;                // all media use 3D noise
     uint32_t max_imp;           // max impulses per cell over the media
+    uint32_t max_oct;           // max octaves over the media
 };
 
 // Upload the jump-ahead PCG table to the current device (once per device).
@@ -48,6 +54,9 @@ cudaError_t upload_pcg_table();
 // Enqueue the flight kernels on the stream.  ev, when not null, holds start/stop
 // events for the prepare, march (march + resume) and finish kernels (ev[2k], ev[2k+1]).
 cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream, cudaEvent_t *ev = nullptr);
+// 1D specular NEE queries on the realizations of the flights in a (one thread each)
+cudaError_t launch_nee(const FlightArgs &a, const float4 *point_t, const float4 *normal, float4 *out,
+                       cudaStream_t stream);
 
 // Unit-level kernels (synchronous wrappers live in gpis_abi.cu).
 cudaError_t launch_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n,

@@ -62,8 +62,20 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
     if (d.sampling_scheme > GPIS_SCHEME_MIS) return fail(GPIS_EINVAL, "unknown 1D_sampling_scheme");
     for (int i = 0; i < 8; ++i)
         if (!std::isfinite(d.mean_params[i])) return fail(GPIS_EINVAL, "mean parameters must be finite");
-    if (d.ls_kind != GPIS_LS_CONSTANT || d.n_octaves != 1 || d.multires)
-        return fail(GPIS_ENOTSUP, "nonstationary / multi-octave / multi-resolution fields are not supported");
+    if (d.multires) return fail(GPIS_ENOTSUP, "multi-resolution fields are not supported");
+    if (d.n_octaves < 1 || d.n_octaves > 4) return fail(GPIS_EINVAL, "n_octaves must be in 1..4");
+    if (d.ls_kind > GPIS_LS_SINCOS) return fail(GPIS_EINVAL, "unknown ls_kind");
+    if ((d.ls_kind != GPIS_LS_CONSTANT || d.n_octaves != 1) && !d.one_d_sampling)
+        return fail(GPIS_ENOTSUP, "nonstationary and multi-octave fields need 1D_sampling");
+    if (d.ls_kind != GPIS_LS_CONSTANT) {
+        if (!(std::isfinite(d.ls_max) && d.ls_max > 0.0f)) return fail(GPIS_EINVAL, "ls_max must be finite and > 0");
+        for (int i = 0; i < 4; ++i)
+            if (!std::isfinite(d.ls_params[i])) return fail(GPIS_EINVAL, "ls parameters must be finite");
+    }
+    if (d.n_octaves > 1)
+        for (uint32_t k = 0; k < d.n_octaves; ++k)
+            if (!std::isfinite(d.octave_sigma[k]) || !(std::isfinite(d.octave_scale[k]) && d.octave_scale[k] > 0.0f))
+                return fail(GPIS_EINVAL, "octave sigma must be finite and octave scale finite and > 0");
     if (d.isotropic_3d_sampling && !d.one_d_sampling)
         return fail(GPIS_ENOTSUP, "isotropic_3D_sampling is not supported");
     if (d.mean_kind > GPIS_MEAN_TORUS_PLANE) return fail(GPIS_EINVAL, "unknown mean kind");
@@ -85,7 +97,8 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
     m.kr_world = d.kernel_scale * 1.0f * mtx;
     m.sigma = d.sigma;
     m.n_imp = (uint32_t)d.impulse_density;
-    const float var1 = (float)((double)(d.impulse_density / m.kr_iso) * (std::sqrt(M_PI) * 1.0));
+    m.var1d_c = d.impulse_density / m.kr_iso;
+    const float var1 = (float)((double)m.var1d_c * (std::sqrt(M_PI) * 1.0));
     m.norm1d = std::sqrt(var1);
     m.inv_norm1d = 1.0f / m.norm1d;
     {
@@ -115,7 +128,9 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
     if (activate) flags |= gpis::MF_COND;
     if (d.correlation_context == GPIS_CTX_RENEWAL_PLUS) flags |= gpis::MF_RENEWAL_PLUS;
     if (d.correlation_xy) flags |= gpis::MF_CORR_XY;
-    if (d.one_d_sampling && d.correlation_xy && d.correlation_context == GPIS_CTX_RENEWAL_PLUS && !d.multires)
+    // seTransverseGradientMoments applies to one stationary SE realization only
+    if (d.one_d_sampling && d.correlation_xy && d.correlation_context == GPIS_CTX_RENEWAL_PLUS && !d.multires &&
+        d.ls_kind == GPIS_LS_CONSTANT && d.n_octaves == 1)
         flags |= gpis::MF_TRANSVERSE;
     if (d.impulse_xyz_order) flags |= gpis::MF_XYZ_ORDER;
     m.flags = flags;
@@ -130,6 +145,16 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         std::memcpy(m.grid_cmax, g->clamp_max, sizeof(m.grid_cmax));
         m.grid_offset = g->offset;
         m.grid_scale = g->scale;
+    }
+    m.ls_kind = d.ls_kind;
+    for (int i = 0; i < 4; ++i) m.ls_params[i] = d.ls_params[i];
+    m.ls_max = d.ls_kind != GPIS_LS_CONSTANT ? d.ls_max : 1.0f;
+    m.n_oct = d.n_octaves;
+    for (int k = 0; k < 4; ++k) {
+        const bool on = (uint32_t)k < d.n_octaves && d.n_octaves > 1;
+        m.oct_sigma[k] = on ? d.octave_sigma[k] : 0.0f;
+        m.oct_scale[k] = on ? d.octave_scale[k] : 1.0f;
+        m.oct_seed[k] = on ? d.octave_seed[k] : 0u;
     }
     m.step_size = d.step_size;
     m.min_step = d.min_step;
@@ -153,7 +178,7 @@ struct gpis_ctx {
     gpis::DevMedium *d_media = nullptr;
     std::vector<float *> d_grids;
     bool any_cond = false, all_one_d = true, all_three_d = true;
-    uint32_t max_imp = 0;
+    uint32_t max_imp = 0, max_oct = 1;
     // scratch of the flight kernels
     gpis::CondRec *d_cond = nullptr;
     double *d_tend = nullptr;
@@ -295,6 +320,7 @@ int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
             c->all_one_d = c->all_one_d && (m.flags & gpis::MF_ONE_D);
             c->all_three_d = c->all_three_d && !(m.flags & gpis::MF_ONE_D);
             c->max_imp = std::max(c->max_imp, m.n_imp);
+            c->max_oct = std::max(c->max_oct, m.n_oct);
         }
         if (rc) break;
         if ((e = cudaMalloc(&c->d_media, host.size() * sizeof(gpis::DevMedium))) != cudaSuccess) { rc = cuda_fail(e, "allocate media"); break; }
@@ -352,6 +378,7 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_res
     a.one_d = ctx->all_one_d;
     a.three_d = ctx->all_three_d;
     a.max_imp = ctx->max_imp;
+    a.max_oct = ctx->max_oct;
     for (const void *p : {(const void *)in->origin_near, (const void *)in->dir_far, (const void *)in->seeds,
                           (const void *)in->prev, (const void *)out->rec})
         if (p && (reinterpret_cast<uintptr_t>(p) & 15u))
@@ -450,6 +477,78 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis
     if (rc) return rc;
     CUDA_TRY(cudaMemcpyAsync(out->rec, dout.rec, rec16 * 2, cudaMemcpyDeviceToHost, s), "copy results");
     CUDA_TRY(cudaStreamSynchronize(s), "synchronize flights");
+    return GPIS_OK;
+}
+
+int gpis_nee_submit(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n, void *cuda_stream)
+{
+    if (!ctx || !in || !out) return fail(GPIS_EINVAL, "null argument");
+    if (n == 0) return GPIS_OK;
+    const gpis_flight_soa &f = in->flight;
+    if (!f.origin_near || !f.dir_far || !f.seeds || !in->point_t || !in->normal)
+        return fail(GPIS_EINVAL, "streams origin_near, dir_far, seeds, point_t and normal are required");
+    if (ctx->any_cond && !f.prev) return fail(GPIS_EINVAL, "conditioning media need the prev stream");
+    for (const void *p : {(const void *)f.origin_near, (const void *)f.dir_far, (const void *)f.seeds,
+                          (const void *)f.prev, (const void *)in->point_t, (const void *)in->normal, (const void *)out})
+        if (p && (reinterpret_cast<uintptr_t>(p) & 15u)) return fail(GPIS_EINVAL, "NEE streams must be 16-byte aligned");
+    gpis::FlightArgs a = {};
+    a.origin_near = reinterpret_cast<const float4 *>(f.origin_near);
+    a.dir_far = reinterpret_cast<const float4 *>(f.dir_far);
+    a.seeds = reinterpret_cast<const uint4 *>(f.seeds);
+    a.prev = reinterpret_cast<const float4 *>(f.prev);
+    a.medium = f.medium;
+    a.media = ctx->d_media;
+    a.n_media = ctx->n_media;
+    a.n = n;
+    CUDA_TRY(gpis::launch_nee(a, reinterpret_cast<const float4 *>(in->point_t),
+                              reinterpret_cast<const float4 *>(in->normal), reinterpret_cast<float4 *>(out),
+                              static_cast<cudaStream_t>(cuda_stream)),
+             "launch NEE");
+    return GPIS_OK;
+}
+
+int gpis_nee_host(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n)
+{
+    if (!ctx || !in || !out) return fail(GPIS_EINVAL, "null argument");
+    if (n == 0) return GPIS_OK;
+    const gpis_flight_soa &f = in->flight;
+    if (!f.origin_near || !f.dir_far || !f.seeds || !in->point_t || !in->normal)
+        return fail(GPIS_EINVAL, "streams origin_near, dir_far, seeds, point_t and normal are required");
+    const size_t q16 = (size_t)n * 16;
+    const size_t need = q16 * 7 + (((size_t)n * 4 + 15) & ~(size_t)15);
+    if (need > ctx->stage_cap) {
+        cudaFree(ctx->d_stage);
+        ctx->d_stage = nullptr;
+        ctx->stage_cap = 0;
+        CUDA_TRY(cudaMalloc(&ctx->d_stage, need), "allocate staging");
+        ctx->stage_cap = need;
+    }
+    char *b = ctx->d_stage;
+    gpis_nee_soa d;
+    d.flight.origin_near = reinterpret_cast<float *>(b);
+    d.flight.dir_far = reinterpret_cast<float *>(b + q16);
+    d.flight.seeds = reinterpret_cast<uint32_t *>(b + 2 * q16);
+    d.flight.prev = reinterpret_cast<float *>(b + 3 * q16);
+    d.point_t = reinterpret_cast<float *>(b + 4 * q16);
+    d.normal = reinterpret_cast<float *>(b + 5 * q16);
+    float *dout = reinterpret_cast<float *>(b + 6 * q16);
+    d.flight.medium = f.medium ? reinterpret_cast<uint32_t *>(b + 7 * q16) : nullptr;
+    cudaStream_t s = ctx->stream;
+    CUDA_TRY(cudaMemcpyAsync((void *)d.flight.origin_near, f.origin_near, q16, cudaMemcpyHostToDevice, s), "copy origins");
+    CUDA_TRY(cudaMemcpyAsync((void *)d.flight.dir_far, f.dir_far, q16, cudaMemcpyHostToDevice, s), "copy directions");
+    CUDA_TRY(cudaMemcpyAsync((void *)d.flight.seeds, f.seeds, q16, cudaMemcpyHostToDevice, s), "copy seeds");
+    if (f.prev)
+        CUDA_TRY(cudaMemcpyAsync((void *)d.flight.prev, f.prev, q16, cudaMemcpyHostToDevice, s), "copy prev");
+    else
+        CUDA_TRY(cudaMemsetAsync((void *)d.flight.prev, 0, q16, s), "clear prev");
+    CUDA_TRY(cudaMemcpyAsync((void *)d.point_t, in->point_t, q16, cudaMemcpyHostToDevice, s), "copy points");
+    CUDA_TRY(cudaMemcpyAsync((void *)d.normal, in->normal, q16, cudaMemcpyHostToDevice, s), "copy normals");
+    if (f.medium)
+        CUDA_TRY(cudaMemcpyAsync((void *)d.flight.medium, f.medium, (size_t)n * 4, cudaMemcpyHostToDevice, s), "copy media");
+    int rc = gpis_nee_submit(ctx, &d, dout, n, s);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(out, dout, q16, cudaMemcpyDeviceToHost, s), "copy NEE results");
+    CUDA_TRY(cudaStreamSynchronize(s), "synchronize NEE");
     return GPIS_OK;
 }
 

@@ -126,6 +126,7 @@ extern "C" int gpis_flights_submit_static(const gpis_medium_desc *medium, const 
     a.one_d = (m.flags & gpis::MF_ONE_D) != 0;
     a.three_d = !a.one_d;
     a.max_imp = m.n_imp;
+    a.max_oct = m.n_oct;
     if (gpis::launch_flights(a, sms, s) != cudaSuccess) return fail(GPIS_EIO, "launching the flight kernels failed");
     return GPIS_OK;
 }

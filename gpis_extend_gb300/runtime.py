@@ -116,6 +116,20 @@ class Context:
                   "gpis_flights_trace_host")
         return rec
 
+    def nee(self, batch, points, t_segment, normals):
+        """1D specular NEE (gpis_nee_host) on the realizations of the flights in batch:
+        returns (n, 4) float32 {pdf, gradient}."""
+        n = batch.n
+        pt = np.zeros((n, 4), np.float32)
+        pt[:, :3] = points
+        pt[:, 3] = t_segment
+        nr = np.zeros((n, 4), np.float32)
+        nr[:, :3] = normals
+        out = np.zeros((n, 4), np.float32)
+        q = abi.NeeSoA(batch.soa(), pt.ctypes.data, nr.ctypes.data)
+        abi.check(self.lib.gpis_nee_host(self.h, ctypes.byref(q), out.ctypes.data, n), "gpis_nee_host")
+        return out
+
     def trace_pinned(self, pinned):
         """gpis_flights_trace_host on PinnedFlights (host -> device -> host, synchronous)."""
         soa = pinned.soa()

@@ -76,6 +76,27 @@ def sphere_medium(one_d=True, context=abi.CTX_RENEWAL_PLUS, sigma=0.05, length_s
                            sigma_s=0.8, sigma_a=0.2, **kw)
 
 
+def torus_plane_medium(nonstationary=True, octaves=3, context=abi.CTX_RENEWAL_PLUS, **kw):
+    """The nonstationary field over the union SDF of a torus (R 1, r 0.35, about the
+    y axis) and the plane y = -0.5: length scale 0.11 + 0.09 sin(3x) cos(2z)
+    (0.02 to 0.2; the cells follow the supremum 0.2), three octaves halving the
+    length scale with std 0.04 / 0.02 / 0.01, 1D sampling with Renewal+.
+    nonstationary=False keeps the length scale at 0.2; octaves=1 keeps one
+    realization with std 0.04."""
+    params = dict(sigma=0.04, length_scale=1.0 if nonstationary else 0.2, kernel_scale=3.0,
+                  impulse_density=8.0, seed=1, one_d_sampling=1, correlation_context=context,
+                  step_size=0.005, min_step=8, mean_kind=abi.MEAN_TORUS_PLANE,
+                  mean_params=(0, 0, 0, 1.0, 0.35, -0.5), sigma_s=0.8, sigma_a=0.2)
+    if nonstationary:
+        params.update(ls_kind=abi.LS_SINCOS, ls_params=(0.11, 0.09, 3.0, 2.0), ls_max=0.2)
+    if octaves > 1:
+        params.update(n_octaves=octaves, octave_sigma=[0.04 / 2 ** k for k in range(octaves)],
+                      octave_scale=[0.5 ** k for k in range(octaves)],
+                      octave_seed=[0x1F123BB5 * k for k in range(octaves)])
+    params.update(kw)
+    return abi.make_medium(**params)
+
+
 def pss_seeds(desc, pss, scene_seed=1):
     """Vectorised noise/normal seeds (computeSeed / prepareGpisSegment formulas)."""
     from .hashing import xxhash32_4, xxhash32_1

@@ -254,6 +254,28 @@ int gpis_medium_transmittance(gpis_ctx *ctx, uint32_t medium, const gpis_ray *ra
                               gpis_medium_state *states, const float *jitter,
                               float *transmittance, uint32_t n);
 
+/* ---- 1D specular next-event estimation ----------------------------------
+ * neeGrad / neePDF on the realization of a hit (SparseConvolutionNoiseRealization::
+ * neeShared / neeGrad / neePDF, SparseConvolutionNoise.cpp:662-821), as MirrorBsdf
+ * (MirrorBsdf.cpp:45, 69, 79, 109) and ConductorBsdf (ConductorBsdf.cpp:73, 97,
+ * 107, 137) call them.  Query i uses the realization of flight i of `flight`
+ * (origin, direction = the ray direction info->w, seeds, prev, medium; near,
+ * far and jitter are not read), the point and segment parameter
+ * point_t[i] = {p, info->t} and the world normal normal[i] = {n, unused}.
+ * out[i] = {pdf (neePDF), gradient (neeGrad, 3 floats)}.  Media must use 1D
+ * sampling with one octave; a query on another medium or with non-finite
+ * inputs gets a NaN pdf.  All streams 16-byte aligned.                      */
+typedef struct {
+    gpis_flight_soa flight;
+    const float *point_t;       /* float4 per query                           */
+    const float *normal;        /* float4 per query                           */
+} gpis_nee_soa;
+
+/* Asynchronous, device pointers, n == 0 is a no-op. */
+int gpis_nee_submit(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n, void *cuda_stream);
+/* Blocking, host pointers. */
+int gpis_nee_host(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n);
+
 /* Read (and optionally reset) the device counter block. */
 int gpis_status(gpis_ctx *ctx, gpis_counters *out, int reset);
 
@@ -285,9 +307,12 @@ int gpis_debug_cells_3d(const int32_t *cells, const uint32_t *seeds, uint32_t n,
  * seeds n x 4 words as in the flight seed stream, prev n x 4 floats.  The
  * conditioning of each point's flight is built from (origin = points of the
  * "origins" stream) exactly as a flight would.  out = n x 8 floats:
- * {noise value (normalized), n1, n2, n3, field value, mean, 0, 0} where
- * (n1, n2, n3) is, for 1D noise, (conditioning x splat, conditioning y splat,
- * dnoise/dz) and, for 3D noise, the world gradient of the normalized noise. */
+ * {noise value (normalized), n1, n2, n3, field value, mean, precise field
+ * value, GP id (int bits)} where (n1, n2, n3) is, for 1D noise, (conditioning
+ * x splat, conditioning y splat, dnoise/dz) and, for 3D noise, the world
+ * gradient of the normalized noise; with several octaves the noise entries are
+ * amplitude-weighted sums.  The precise value is the one the march decides
+ * crossings with (the reference's float formulation operation for operation). */
 int gpis_debug_field(gpis_ctx *ctx, const float *origins, const float *points,
                      const float *dirs, const uint32_t *seeds, const float *prev,
                      uint32_t n, float *out);
@@ -304,7 +329,7 @@ int gpis_se_splat_1d(const float *queries, const float *centers, float *values,
  * cudaFree can), or a plugin host that owns all device memory and forbids
  * plugins to allocate.  The same flight kernels as gpis_flights_submit run on
  * one medium description (no grid mean), with all working memory in a fixed
- * array of this library (about 3.7 MB for GPIS_STATIC_MAX_FLIGHTS flights)
+ * array of this library (about 6.8 MB for GPIS_STATIC_MAX_FLIGHTS flights)
  * that every GPU which loads the library keeps until the process exits.  The
  * caller provides device flight and result streams as for gpis_flights_submit.
  * Larger batches fail with GPIS_ERANGE.  The first call on a device, with that

@@ -219,6 +219,8 @@ static int om_init(om_t *m, const gpis_medium_desc *d)
     if (d->n_octaves < 1 || d->n_octaves > 4) return GPIS_EINVAL;
     if (d->mean_kind == GPIS_MEAN_GRID && (!d->grid || !d->grid->voxels)) return GPIS_EINVAL;
     if (d->multires) return GPIS_ENOTSUP;
+    if ((d->ls_kind != GPIS_LS_CONSTANT || d->n_octaves != 1) && !d->one_d_sampling) return GPIS_ENOTSUP;
+    if (d->ls_kind != GPIS_LS_CONSTANT && !(d->ls_max > 0.0f)) return GPIS_EINVAL;
     m->n_imp = (uint32_t)d->impulse_density;
     m->activate_cond = !d->single_realization &&
         (d->correlation_context == GPIS_CTX_RENEWAL || d->correlation_context == GPIS_CTX_RENEWAL_PLUS);
@@ -249,7 +251,9 @@ static inline float ls_field(const om_t *m, const float p[3])
 {
     if (!m->nonstationary) return 1.0f;
     const float *q = m->d.ls_params;
-    return q[0] + q[1] * sinf(q[2] * p[0]) * cosf(q[3] * p[2]);
+    /* a code-defined procedural vector evaluated on Vec3d(p), returned as float
+       (getKernelScale, GPFunctions.cpp:1738-1744) */
+    return (float)((double)q[0] + (double)q[1] * sin((double)q[2] * p[0]) * cos((double)q[3] * p[2]));
 }
 
 /* nonStationarySplattingKernelScale, GPFunctions.cpp:1229-1235 (brute force) */
@@ -803,8 +807,11 @@ static void corr_moments(float distance, double *factor, double *variance)
 
 static inline int transverse_law(const om_t *m)
 {
+    /* seTransverseGradientMoments needs a SquaredExponentialCovariance (a
+       nonstationary wrapper fails the dynamic_cast) and one realization */
     return m->d.one_d_sampling && m->d.correlation_xy &&
-           m->d.correlation_context == GPIS_CTX_RENEWAL_PLUS && !m->d.multires;
+           m->d.correlation_context == GPIS_CTX_RENEWAL_PLUS && !m->d.multires &&
+           !m->nonstationary && m->d.n_octaves == 1;
 }
 
 /* seTransverseGradientMoments (SparseConvolutionNoise.cpp:78-99) */
@@ -901,6 +908,9 @@ static void grad_noise_1d(const real_t *r, const float p[3], float t_segment, co
     float gi[3];
     frame_to_global(&f, gr, gi);
     l2w_grad(m, gi, 1.0f, out);
+    const float sc = oct_scale(m, r->octave);
+    if (sc != 1.0f)
+        for (int i = 0; i < 3; ++i) out[i] = out[i] / sc;
 }
 
 static void mean_grad_f(const om_t *m, const float p[3], float g[3])
@@ -942,6 +952,8 @@ static void conditioning_1d(real_t *r, const float p[3], const float dir[3], flo
         frame_t f;
         frame_make(dn, &f);
         float gi[3], gl[3];
+        /* the octave's length multiplier enters once, where the splats are
+           evaluated (noise1d_norm scales gs by it) */
         w2l_grad(m, delta, 1.0f, gi);
         frame_to_local(&f, gi, gl);
         float s = splat_cov_1d(m, p, p);
@@ -1076,21 +1088,32 @@ static void field_condition(field_t *F, const float p[3], float target_val, cons
         else conditioning_3d(&F->oct[0], p, target_val, target_grad, mean, mg);
         return;
     }
-    /* Octaves: the current value of the other octaves is folded into the mean. */
+    /* Octaves (1D): the residual of the value, and of the gradient under
+       Renewal+, is shared between the octaves in proportion to their variance
+       sigma_k^2, so that the summed field meets the birth value and gradient. */
     float total = 0.0f;
     for (int k = 0; k < F->n; ++k) total += oct_sigma(m, k) * oct_sigma(m, k);
     double cur[4][4];
-    for (int k = 0; k < F->n; ++k) oct_noise(F, k, p, 0, 0, cur[k]);
-    float sum_v = 0.0f;
-    for (int k = 0; k < F->n; ++k) sum_v += oct_sigma(m, k) * (float)cur[k][0];
+    float curg[4][3];
     for (int k = 0; k < F->n; ++k) {
-        float share = oct_sigma(m, k) * oct_sigma(m, k) / total;
-        float resid = (target_val - mean) - sum_v;
-        float tv = mean + oct_sigma(m, k) * (float)cur[k][0] + share * resid;
+        oct_noise(F, k, p, 0, 0, cur[k]);
+        grad_noise_1d(&F->oct[k], p, 0.0f, F->dir, 0, curg[k]);
+    }
+    float sum_v = 0.0f, sum_g[3] = {0.0f, 0.0f, 0.0f};
+    for (int k = 0; k < F->n; ++k) {
+        sum_v += oct_sigma(m, k) * (float)cur[k][0];
+        for (int i = 0; i < 3; ++i) sum_g[i] += oct_sigma(m, k) * curg[k][i];
+    }
+    const float resid = (target_val - mean) - sum_v;
+    float resid_g[3];
+    for (int i = 0; i < 3; ++i) resid_g[i] = (target_grad[i] - mg[i]) - sum_g[i];
+    for (int k = 0; k < F->n; ++k) {
+        const float sk = oct_sigma(m, k);
+        const float share = sk * sk / total;
+        const float tv = mean + sk * (float)cur[k][0] + share * resid;
         float tg[3];
-        for (int i = 0; i < 3; ++i) tg[i] = target_grad[i];
-        if (m->d.one_d_sampling) conditioning_1d(&F->oct[k], p, F->dir, tv, tg, mean, mg);
-        else conditioning_3d(&F->oct[k], p, tv, tg, mean, mg);
+        for (int i = 0; i < 3; ++i) tg[i] = mg[i] + sk * curg[k][i] + share * resid_g[i];
+        conditioning_1d(&F->oct[k], p, F->dir, tv, tg, mean, mg);
     }
 }
 
@@ -1432,7 +1455,8 @@ static void inv3(const float A[9], float R[9])
     R[8] = (A[0] * A[4] - A[1] * A[3]) * id;
 }
 
-/* neeShared / neeGrad / neePDF (SparseConvolutionNoise.cpp:662-821), stationary branch. */
+/* neeShared / neeGrad / neePDF (SparseConvolutionNoise.cpp:662-821), single-resolution
+ * branch, one octave (stationary or nonstationary length scale). */
 int gor_nee(const gpis_medium_desc *desc, const float origin[3], const float dir[3],
             const float p[3], const float normal[3], float t_segment, const uint32_t seeds[4],
             const float prev[4], float *pdf, float grad[3])
@@ -1451,12 +1475,15 @@ int gor_nee(const gpis_medium_desc *desc, const float origin[3], const float dir
     normalize3f(diso, dn);
     frame_t f;
     frame_make(dn, &f);
-    /* mtx_pt = amplitude * diag(l_inv) * [t b n] (row-major here) */
+    /* mtx_pt = amplitude * localToWorldInvTransposeMatrix(p) * [t b n] (row-major
+       here); the nonstationary matrix divides diag(l_inv) by the maximum lateral
+       scale (NonstationaryCovariance::localToWorldInvTransposeMatrix, GPFunctions.cpp:1291-1294) */
     float A[9];
     for (int i = 0; i < 3; ++i) {
-        A[3 * i + 0] = amp * m.l_inv[i] * f.t[i];
-        A[3 * i + 1] = amp * m.l_inv[i] * f.b[i];
-        A[3 * i + 2] = amp * m.l_inv[i] * f.n[i];
+        const float li = m.nonstationary ? m.l_inv[i] / m.ls_max : m.l_inv[i];
+        A[3 * i + 0] = amp * li * f.t[i];
+        A[3 * i + 1] = amp * li * f.b[i];
+        A[3 * i + 2] = amp * li * f.n[i];
     }
     float Ai[9];
     inv3(A, Ai);

@@ -5,7 +5,11 @@ Bars (tolerances written here):
   * noise values: |gpu - fp64| <= 1e-5 * max(1, |fp64|) (normalized noise units,
     i.e. an absolute floor of 1e-5 sigma in field units);
   * hit distances: |t_gpu - t_oracle| <= 1e-4 * 1.5 (the scene scale is the half
-    size of the bounding cube, 1.5);
+    size of the bounding cube, 1.5) on >= 99.99 % of hits; every hit outside that
+    bar must be a back-off case of the reference's refinement (one side returns
+    t = 0 after the x0.9 back-off of the regula-falsi factor reached 0.01,
+    SparseConvolutionNoiseMedium.cpp:309-330), which turns on the last bit of a
+    near-zero field value; such cases stay below 0.05 % of hits;
   * hit / miss (transmittance 0/1) agreement on >= 99.99 % of flights;
   * gradients of agreeing hits: relative L2 <= 2e-3 (float Box-Muller and
     ex2.approx splats against the reference's double Box-Muller).
@@ -179,7 +183,10 @@ def flights_vs_oracle(desc, batch, rec_gpu, check_grad=True):
     assert frac >= 0.9999 or (~agree).sum() <= 1, f"hit agreement {frac} ({(~agree).sum()} of {n})"
     both = agree & g["hit"]
     dt = np.abs(g["t"][both] - c["t"][both])
-    assert np.mean(dt <= T_TOL) >= 0.9999, f"t disagreement on {(dt > T_TOL).sum()} hits"
+    bad = dt > T_TOL
+    backoff = (g["t"][both] == 0) | (c["t"][both] == 0)
+    assert np.all(backoff[bad]), f"t disagreement outside the back-off cases on {(bad & ~backoff).sum()} hits"
+    assert bad.mean() <= 5e-4, f"back-off disagreement on {bad.sum()} of {both.sum()} hits"
     miss = agree & ~g["hit"]
     assert np.all(g["t"][miss] == c["t"][miss])
     if miss.any():

@@ -1,0 +1,154 @@
+"""Nonstationary length scale and octaves (the torus-union-plane field with
+ls(p) = 0.11 + 0.09 sin(3x) cos(2z) and three octaves).
+
+CPU: the oracle's conditioning meets the birth value and the along-ray birth
+gradient of the summed field exactly (up to float rounding), for one octave and
+for three, stationary and nonstationary.  GPU: noise values against the
+oracle's FP64 anchor and flights against the oracle, with the bars of the
+stationary parity tests (hit agreement >= 99.99 %, |dt| <= 1.5e-4 on >= 99.99 %
+of hits, gradient relative L2 <= 2e-3 on >= 99.9 % of coincident hits)."""
+import numpy as np
+import pytest
+
+from gpis_extend_gb300 import abi, workloads
+from oracle import oracle
+
+CASES = [(True, 1), (False, 3), (True, 3)]
+
+
+def birth_points(n, rng):
+    o = rng.uniform(-1.3, 1.3, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = d.astype(np.float32)
+    seeds = np.zeros((n, 4), np.uint32)
+    seeds[:, 0] = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    seeds[:, 1] = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    prev = np.zeros((n, 4), np.float32)
+    prev[:, 0] = rng.normal(scale=0.02, size=n)
+    prev[:, 1:] = rng.normal(size=(n, 3))
+    return o, d, seeds, prev
+
+
+@pytest.mark.parametrize("ns,octaves", CASES)
+def test_oracle_conditioning_meets_birth_state(ns, octaves):
+    desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves)
+    rng = np.random.default_rng(5 + octaves + 2 * ns)
+    o, d, seeds, prev = birth_points(200, rng)
+    for i in range(len(o)):
+        f = oracle.field(desc, o[i], d[i], o[i], seeds[i], prev[i])
+        assert abs(f[4] - prev[i, 0]) <= 2e-6 * (1 + abs(prev[i, 0])), (i, f[4], prev[i, 0])
+        g = oracle.gradient(desc, o[i], d[i], o[i], 0.0, seeds[i], prev[i])
+        want = float(np.dot(prev[i, 1:].astype(np.float64), d[i]))
+        got = float(np.dot(g.astype(np.float64), d[i]))
+        assert abs(got - want) <= 2e-4 * (1 + abs(want)), (i, got, want)
+
+
+def test_oracle_octaves_sum_of_realizations():
+    """An unconditioned three-octave field is the sum of three one-octave fields with
+    the octave's std, length-scale multiplier (folded into the length scale) and seed."""
+    base = dict(nonstationary=False, octaves=3)
+    desc = workloads.torus_plane_medium(**base)
+    rng = np.random.default_rng(2)
+    o, d, seeds, prev = birth_points(50, rng)
+    seeds[:, 2] = abi.FLAG_FIRST_SCATTER
+    for i in range(len(o)):
+        p = (o[i] + 0.3 * d[i]).astype(np.float32)
+        total = oracle.field(desc, o[i], d[i], p, seeds[i], prev[i])
+        acc = 0.0
+        for k in range(3):
+            one = workloads.torus_plane_medium(nonstationary=False, octaves=1,
+                                               sigma=desc.octave_sigma[k],
+                                               length_scale=0.2 * desc.octave_scale[k])
+            s = seeds[i].copy()
+            s[0] = (int(s[0]) + int(desc.octave_seed[k])) & 0xFFFFFFFF
+            acc += oracle.field(one, o[i], d[i], p, s, prev[i])[4] - oracle.field(one, o[i], d[i], p, s, prev[i])[5]
+        # the length multiplier is applied after the world-to-iso transform, so the
+        # coordinates differ by float rounding only
+        assert abs((total[4] - total[5]) - acc) <= 1e-5, (i, total[4] - total[5], acc)
+
+
+def test_oracle_rejects_unsupported_combinations():
+    d3 = workloads.torus_plane_medium(one_d_sampling=0)
+    with pytest.raises(abi.GpisError):
+        oracle.field(d3, [0, 0, 0], [0, 0, 1], [0, 0, 0.1], [1, 2, 1, 0])
+    bad = workloads.torus_plane_medium(ls_max=0.0)
+    with pytest.raises(abi.GpisError):
+        oracle.field(bad, [0, 0, 0], [0, 0, 1], [0, 0, 0.1], [1, 2, 1, 0])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ns,octaves", CASES)
+def test_gpu_nonstationary_noise_vs_fp64(ns, octaves):
+    from gpis_extend_gb300 import runtime
+    desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves)
+    rng = np.random.default_rng(17 + octaves + 2 * ns)
+    n = 1500
+    o, d, seeds, prev = birth_points(n, rng)
+    seeds[:, 2] = np.where(rng.random(n) < 0.5, abi.FLAG_FIRST_SCATTER, 0)
+    t = rng.uniform(0.0, 0.4, n)
+    p = (o.astype(np.float64) + d * t[:, None]).astype(np.float32)
+    with runtime.Context(desc) as ctx:
+        out = ctx.debug_field(o, p, d, seeds, prev)
+    amp = sum(desc.octave_sigma[:octaves]) if octaves > 1 else 1.0
+    for i in range(n):
+        ref = oracle.field(desc, o[i], d[i], p[i], seeds[i], prev[i], double_mode=True)
+        tol = 2e-5 * amp * max(1.0, abs(ref[0]) / amp)
+        assert abs(out[i, 0] - ref[0]) <= tol, (i, out[i, 0], ref[0])
+        assert abs(out[i, 4] - ref[4]) <= 2e-5 * max(1.0, abs(ref[4])) + tol * desc.sigma
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ns,octaves", CASES)
+def test_gpu_nonstationary_flights_vs_oracle(ns, octaves):
+    from gpis_extend_gb300 import runtime
+    from test_gpu_parity import flights_vs_oracle
+    desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves)
+    prim = workloads.sphere_flights(1 << 14, desc)
+    with runtime.Context(desc) as ctx:
+        rec = ctx.trace_host(prim)
+        flights_vs_oracle(desc, prim, rec)
+        rec_cpu = oracle.trace_flights(desc, prim)
+        sec, _ = workloads.secondary_flights(prim, rec_cpu, desc)
+        rec2 = ctx.trace_host(sec)
+        flights_vs_oracle(desc, sec, rec2)
+
+
+PRECISE_MEDIA = {
+    "sphere_1d": lambda: workloads.sphere_medium(),
+    "sphere_3d": lambda: workloads.sphere_medium(one_d=False, context=abi.CTX_RENEWAL),
+    "torus_ns": lambda: workloads.torus_plane_medium(nonstationary=True, octaves=1),
+    "torus_oct": lambda: workloads.torus_plane_medium(nonstationary=False, octaves=3),
+    "torus_ns_oct": lambda: workloads.torus_plane_medium(nonstationary=True, octaves=3),
+}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(PRECISE_MEDIA))
+def test_gpu_precise_field_matches_oracle_float_mode(name):
+    """The march's precise evaluator against the oracle's float-mode field value on
+    unconditioned points: within 8 ulp of the field scale everywhere and bit-exact
+    on most points (CUDA's expf is within 2 ulp, the C library's within about half
+    an ulp, so the 24 splats of a sum can move its last bits)."""
+    from gpis_extend_gb300 import runtime
+    desc = PRECISE_MEDIA[name]()
+    rng = np.random.default_rng(sum(map(ord, name)))
+    n = 4000 if desc.one_d_sampling else 800
+    o, d, seeds, prev = birth_points(n, rng)
+    seeds[:, 2] = abi.FLAG_FIRST_SCATTER
+    t = rng.uniform(0.0, 0.5, n)
+    p = (o.astype(np.float64) + d * t[:, None]).astype(np.float32)
+    with runtime.Context(desc) as ctx:
+        out = ctx.debug_field(o, p, d, seeds, prev)
+    ref = np.array([oracle.field(desc, o[i], d[i], p[i], seeds[i], prev[i])[4] for i in range(n)], np.float32)
+    exact = out[:, 6] == ref
+    ulp = np.spacing(np.maximum(np.abs(ref), np.float32(desc.sigma)))
+    err = np.abs(out[:, 6].astype(np.float64) - ref) / ulp
+    print(name, "bit-exact fraction", exact.mean(), "max ulp", err.max())
+    assert np.all(err <= 8), (name, err.max(), np.argmax(err))
+    assert exact.mean() >= 0.75, (name, exact.mean())
+    ids = out[:, 7].view(np.int32)
+    ref_id = np.array([oracle.field(desc, o[i], d[i], p[i], seeds[i], prev[i])[5] for i in range(n)])
+    if desc.mean_kind == abi.MEAN_TORUS_PLANE:
+        # the union picks the plane (GP id 1) where y + 0.5 is below the torus SDF
+        assert np.array_equal(ids == 1, np.isclose(ref_id, p[:, 1] + 0.5, atol=1e-6) & (ids == 1))
