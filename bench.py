@@ -308,7 +308,7 @@ def main():
         traffic = tr["bytes_per_flight"] * flights_per_step / 2.0
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if peak else None, "traffic": traffic,
-            "kernel": "k_march<EvalCached1D<8>>",
+            "kernel": "k_march<EvalCoop1D<8>> fast pass + k_march<EvalGeneric> resume pass",
             "march_ms_per_launch": march_ms,
             "kernel_ms_per_step": [k / max(1, args.steps) for k in kms],
             "flops_per_eval": roofline.flops_per_eval_1d(8),

@@ -55,6 +55,11 @@ struct DevMedium {
     float grid_cmax[3];
     float grid_offset;
     float grid_scale;
+    // corner table: the 8 (clamped) corner voxels of every reachable trilinear
+    // cell as two float4, cells lo..lo+n-1 per axis; null when not built
+    const float4 *grid_cells;
+    int32_t cell_lo[3];
+    int32_t cell_n[3];
     float step_size;
     uint32_t min_step;
     uint32_t max_steps;
@@ -292,8 +297,15 @@ __device__ __forceinline__ float grid_voxel(const DevMedium &m, int x, int y, in
     return __ldg(m.grid + idx);
 }
 
-// Dense trilinear grid mean (RaySegmentBatch.cu:73-95 semantics).
-__device__ __forceinline__ float grid_mean(const DevMedium &m, float px, float py, float pz)
+// The eight corner voxels of the trilinear cell of p and its fractions: the
+// loads of grid_mean, issued apart from the arithmetic so that a caller can
+// overlap their latency with other work.
+struct GridTap {
+    float v[8];
+    float fx, fy, fz;
+};
+
+__device__ __forceinline__ void grid_fetch(const DevMedium &m, float px, float py, float pz, GridTap &g)
 {
     float q[3];
 #pragma unroll
@@ -305,20 +317,56 @@ __device__ __forceinline__ float grid_mean(const DevMedium &m, float px, float p
         q[r] = fminf(fmaxf(v, m.grid_cmin[r]), m.grid_cmax[r]);
     }
     const int x = (int)floorf(q[0]), y = (int)floorf(q[1]), z = (int)floorf(q[2]);
-    const float fx = q[0] - (float)x, fy = q[1] - (float)y, fz = q[2] - (float)z;
+    g.fx = q[0] - (float)x;
+    g.fy = q[1] - (float)y;
+    g.fz = q[2] - (float)z;
+    if (m.grid_cells) {
+        // the clamps keep (x, y, z) inside the table: floor of [cmin, cmax]
+        const size_t c = ((size_t)(z - m.cell_lo[2]) * (size_t)m.cell_n[1] + (size_t)(y - m.cell_lo[1])) *
+                             (size_t)m.cell_n[0] + (size_t)(x - m.cell_lo[0]);
+        const float4 a = __ldg(m.grid_cells + 2 * c), b = __ldg(m.grid_cells + 2 * c + 1);
+        g.v[0] = a.x; g.v[1] = a.y; g.v[2] = a.z; g.v[3] = a.w;
+        g.v[4] = b.x; g.v[5] = b.y; g.v[6] = b.z; g.v[7] = b.w;
+        return;
+    }
+    // clamp each axis' two indices once (grid_voxel's rule), then 8 loads
+    const int nx = m.grid_dims[0], ny = m.grid_dims[1], nz = m.grid_dims[2];
+    const int x0 = min(max(x - m.grid_origin[0], 0), nx - 1), x1 = min(max(x + 1 - m.grid_origin[0], 0), nx - 1);
+    const int y0 = min(max(y - m.grid_origin[1], 0), ny - 1), y1 = min(max(y + 1 - m.grid_origin[1], 0), ny - 1);
+    const int z0 = min(max(z - m.grid_origin[2], 0), nz - 1), z1 = min(max(z + 1 - m.grid_origin[2], 0), nz - 1);
+    const float *r00 = m.grid + ((size_t)z0 * ny + y0) * nx;
+    const float *r01 = m.grid + ((size_t)z0 * ny + y1) * nx;
+    const float *r10 = m.grid + ((size_t)z1 * ny + y0) * nx;
+    const float *r11 = m.grid + ((size_t)z1 * ny + y1) * nx;
+    g.v[0] = __ldg(r00 + x0); g.v[1] = __ldg(r00 + x1);
+    g.v[2] = __ldg(r01 + x0); g.v[3] = __ldg(r01 + x1);
+    g.v[4] = __ldg(r10 + x0); g.v[5] = __ldg(r10 + x1);
+    g.v[6] = __ldg(r11 + x0); g.v[7] = __ldg(r11 + x1);
+}
+
+__device__ __forceinline__ float grid_combine(const DevMedium &m, const GridTap &g)
+{
     float layer[2];
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz) {
         float row[2];
 #pragma unroll
         for (int dy = 0; dy < 2; ++dy) {
-            const float a = grid_voxel(m, x, y + dy, z + dz);
-            const float b = grid_voxel(m, x + 1, y + dy, z + dz);
-            row[dy] = a + fx * (b - a);
+            const float a = g.v[4 * dz + 2 * dy + 0];
+            const float b = g.v[4 * dz + 2 * dy + 1];
+            row[dy] = a + g.fx * (b - a);
         }
-        layer[dz] = row[0] + fy * (row[1] - row[0]);
+        layer[dz] = row[0] + g.fy * (row[1] - row[0]);
     }
-    return (layer[0] + fz * (layer[1] - layer[0]) + m.grid_offset) * m.grid_scale;
+    return (layer[0] + g.fz * (layer[1] - layer[0]) + m.grid_offset) * m.grid_scale;
+}
+
+// Dense trilinear grid mean (RaySegmentBatch.cu:73-95 semantics).
+__device__ __forceinline__ float grid_mean(const DevMedium &m, float px, float py, float pz)
+{
+    GridTap g;
+    grid_fetch(m, px, py, pz, g);
+    return grid_combine(m, g);
 }
 
 __device__ __forceinline__ float torus_sdf(const float *q, float x, float y, float z)

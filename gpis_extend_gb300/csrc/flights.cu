@@ -57,7 +57,7 @@ struct Cov1D { float k0, k1, k2, k3; };
 __device__ __forceinline__ Cov1D cov1d(float d, float a = 1.0f)
 {
     Cov1D c;
-    const float ia2 = 1.0f / (a * a);
+    const float ia2 = a == 1.0f ? 1.0f : 1.0f / (a * a);
     c.k0 = ex2_approx((-0.25f * LOG2E) * ia2 * d * d);
     c.k1 = -0.5f * ia2 * d * c.k0;
     c.k2 = (0.25f * ia2 * ia2 * d * d - 0.5f * ia2) * c.k0;
@@ -355,7 +355,7 @@ __device__ void transverse_moments(const DevMedium &m, const CondRec &c, const f
 
 // Noise of octave k at p with its world gradient (evaluateGradientNoise1D /
 // evaluateNoise3D gradient).  cond: the octave's conditioning splats are active.
-__device__ void noise_gradient_oct(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
+__device__ __forceinline__ void noise_gradient_oct(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
                                    const float p[3], float t_segment, int oc, float &value, float g[3])
 {
     if (!(m.flags & MF_ONE_D)) {
@@ -453,84 +453,91 @@ __device__ __forceinline__ void write_status(const FlightArgs &a, uint32_t i, fl
     a.out[2 * i + 1] = make_float4(0.0f, trans, __uint_as_float(steps), __uint_as_float(status));
 }
 
-// Conditioning coefficients of a flight at its origin (conditioning1D / 3D,
-// SparseConvolutionNoise.cpp:498-656).  With several octaves the residual of the
-// value (and of the gradient under Renewal+) is shared in proportion to each
-// octave's variance.
-__device__ CondRec make_condition(const DevMedium &m, const FlightIn &fl)
+// One octave's coefficients from its target value and gradient at the origin
+// (conditioning1D / conditioning3D, SparseConvolutionNoise.cpp:498-656).
+__device__ __forceinline__ void condition_octave(const DevMedium &m, const FlightIn &fl, int k, float v,
+                                                 const float g[3], float tv, const float tg[3], float mean,
+                                                 const float mg[3], CondRec &c)
+{
+    const float amp = oct_sigma(m, k);
+    if (amp == 0.0f) return;
+    CondOct &co = c.oct[k];
+    co.vs = (tv - mean) / amp - v;
+    if (!(m.flags & MF_RENEWAL_PLUS)) return;
+    float delta[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) delta[i] = (tg[i] - mg[i]) / amp - g[i];
+    if (m.flags & MF_ONE_D) {
+        Frame f;
+        ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+        // the octave's length multiplier enters where the splats are evaluated
+        const float mul = m.ls_kind ? m.ls_max : 1.0f;
+        float gi[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) gi[i] = (m.l_aniso[i] * delta[i]) * mul;
+        const float ls = ns_scale(m, fl.o[0], fl.o[2]);
+        const float sc = splat_cov_1d(ls, ls);
+        const float s2 = sc * sc;
+        const float gx = dot3_rn(f.t[0], f.t[1], f.t[2], gi[0], gi[1], gi[2]);
+        const float gy = dot3_rn(f.b[0], f.b[1], f.b[2], gi[0], gi[1], gi[2]);
+        const float gz = dot3_rn(f.n[0], f.n[1], f.n[2], gi[0], gi[1], gi[2]);
+        const bool xy = (m.flags & MF_CORR_XY) != 0;
+        co.gs[0] = xy ? -2.0f * gx * s2 : 0.0f;
+        co.gs[1] = xy ? -2.0f * gy * s2 : 0.0f;
+        co.gs[2] = -2.0f * gz * s2;
+        if (k == 0) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) c.tgn[i] = (tg[i] - mg[i]) / amp;
+            c.has_obs = 1u;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) co.gs[i] = delta[i] * m.d2inv3[i];
+    }
+}
+
+// Conditioning coefficients of a flight at its origin (conditioning,
+// SparseConvolutionNoise.cpp:488-496).  With several octaves the residual of
+// the value (and of the gradient under Renewal+) is shared in proportion to
+// each octave's variance.
+__device__ __forceinline__ CondRec make_condition(const DevMedium &m, const FlightIn &fl)
 {
     CondRec c = {};
     const float *p = fl.o;
     int id;
     const float mean = mean_value(m, p[0], p[1], p[2], id);
     float mg[3] = {0.0f, 0.0f, 0.0f};
-    const bool rp = (m.flags & MF_RENEWAL_PLUS) != 0;
-    if (rp) mean_grad(m, p[0], p[1], p[2], mg);
-    CondRec none = {};
+    if (m.flags & MF_RENEWAL_PLUS) mean_grad(m, p[0], p[1], p[2], mg);
+    const CondRec none = {};
     const int n = (m.flags & MF_ONE_D) ? (int)m.n_oct : 1;
+    if (n == 1) {
+        float v, g[3];
+        noise_gradient_oct(m, fl, none, false, p, 0.0f, 0, v, g);
+        condition_octave(m, fl, 0, v, g, fl.prev_v, fl.prev_g, mean, mg, c);
+        return c;
+    }
     float v[4], g[4][3];
     for (int k = 0; k < n; ++k) noise_gradient_oct(m, fl, none, false, p, 0.0f, k, v[k], g[k]);
-    float tv[4], tg[4][3];
-    if (n == 1) {
-        tv[0] = fl.prev_v;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) tg[0][i] = fl.prev_g[i];
-    } else {
-        float total = 0.0f, sum_v = 0.0f, sum_g[3] = {0.0f, 0.0f, 0.0f};
-        for (int k = 0; k < n; ++k) {
-            const float sk = oct_sigma(m, k);
-            total += sk * sk;
-            sum_v += sk * v[k];
-#pragma unroll
-            for (int i = 0; i < 3; ++i) sum_g[i] += sk * g[k][i];
-        }
-        const float resid = (fl.prev_v - mean) - sum_v;
-        float resid_g[3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) resid_g[i] = (fl.prev_g[i] - mg[i]) - sum_g[i];
-        for (int k = 0; k < n; ++k) {
-            const float sk = oct_sigma(m, k);
-            const float share = sk * sk / total;
-            tv[k] = mean + sk * v[k] + share * resid;
-#pragma unroll
-            for (int i = 0; i < 3; ++i) tg[k][i] = mg[i] + sk * g[k][i] + share * resid_g[i];
-        }
-    }
+    float total = 0.0f, sum_v = 0.0f, sum_g[3] = {0.0f, 0.0f, 0.0f};
     for (int k = 0; k < n; ++k) {
-        const float amp = oct_sigma(m, k);
-        if (amp == 0.0f) continue;
-        CondOct &co = c.oct[k];
-        co.vs = (tv[k] - mean) / amp - v[k];
-        if (!rp) continue;
-        float delta[3];
+        const float sk = oct_sigma(m, k);
+        total += sk * sk;
+        sum_v += sk * v[k];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) delta[i] = (tg[k][i] - mg[i]) / amp - g[k][i];
-        if (m.flags & MF_ONE_D) {
-            Frame f;
-            ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
-            // the octave's length multiplier enters where the splats are evaluated
-            const float mul = m.ls_kind ? m.ls_max : 1.0f;
-            float gi[3];
+        for (int i = 0; i < 3; ++i) sum_g[i] += sk * g[k][i];
+    }
+    const float resid = (fl.prev_v - mean) - sum_v;
+    float resid_g[3];
 #pragma unroll
-            for (int i = 0; i < 3; ++i) gi[i] = (m.l_aniso[i] * delta[i]) * mul;
-            const float ls = ns_scale(m, p[0], p[2]);
-            const float s2 = splat_cov_1d(ls, ls) * splat_cov_1d(ls, ls);
-            const float gx = dot3_rn(f.t[0], f.t[1], f.t[2], gi[0], gi[1], gi[2]);
-            const float gy = dot3_rn(f.b[0], f.b[1], f.b[2], gi[0], gi[1], gi[2]);
-            const float gz = dot3_rn(f.n[0], f.n[1], f.n[2], gi[0], gi[1], gi[2]);
-            const bool xy = (m.flags & MF_CORR_XY) != 0;
-            co.gs[0] = xy ? -2.0f * gx * s2 : 0.0f;
-            co.gs[1] = xy ? -2.0f * gy * s2 : 0.0f;
-            co.gs[2] = -2.0f * gz * s2;
-            if (k == 0) {
+    for (int i = 0; i < 3; ++i) resid_g[i] = (fl.prev_g[i] - mg[i]) - sum_g[i];
+    for (int k = 0; k < n; ++k) {
+        const float sk = oct_sigma(m, k);
+        const float share = sk * sk / total;
+        const float tv = mean + sk * v[k] + share * resid;
+        float tg[3];
 #pragma unroll
-                for (int i = 0; i < 3; ++i) c.tgn[i] = (tg[0][i] - mg[i]) / amp;
-                c.has_obs = 1u;
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < 3; ++i) co.gs[i] = delta[i] * m.d2inv3[i];
-        }
+        for (int i = 0; i < 3; ++i) tg[i] = mg[i] + sk * g[k][i] + share * resid_g[i];
+        condition_octave(m, fl, k, v[k], g[k], tv, tg, mean, mg, c);
     }
     return c;
 }
@@ -594,6 +601,8 @@ __device__ __forceinline__ void lane_field_idle(LaneField &L, const DevMedium *m
 }
 
 // A lane's registers for flight fl of medium m; cond points at its conditioning record.
+// GENERAL = false: a stationary single-octave flight (the fast evaluator's case).
+template <bool GENERAL = true>
 __device__ __forceinline__ void lane_field_setup(LaneField &L, const DevMedium &m, const FlightIn &fl,
                                                  const CondRec *cond)
 {
@@ -618,8 +627,8 @@ __device__ __forceinline__ void lane_field_setup(LaneField &L, const DevMedium &
         L.kexp = m.kexp1d;
         L.inv_norm = m.inv_norm1d;
         if (L.cond) {
-            L.ls_o = ns_scale_precise(m, L.o[0], L.o[2]);
-            if (m.n_oct == 1) {
+            if (GENERAL) L.ls_o = ns_scale_precise(m, L.o[0], L.o[2]);
+            if (!GENERAL || m.n_oct == 1) {
                 const CondOct c = cond->oct[0];
                 L.vs = c.vs;
                 L.gsz = c.gs[2];
@@ -628,7 +637,7 @@ __device__ __forceinline__ void lane_field_setup(LaneField &L, const DevMedium &
                 L.c3 = *cond;
             }
         }
-    } else if (L.cond) {
+    } else if (GENERAL && L.cond) {
         L.c3 = *cond;
     }
 }
@@ -835,11 +844,20 @@ __device__ float field_precise(const LaneField &L, float px, float py, float pz,
             float vs, gz, oz;
             lane_cond_1d(L, k, sc, vs, gz, oz);
             const float a = splat_cov_1d(ls, L.ls_o);
-            const float s2 = (float)((double)a * 1.4142135623730951);
-            const float den2 = a == 1.0f ? m.cov_den2 : (float)(2.0 * (double)__fmul_rn(s2, s2));
+            float den2 = m.cov_den2;
+            if (a != 1.0f) {
+                const float s2 = (float)((double)a * 1.4142135623730951);
+                den2 = (float)(2.0 * (double)__fmul_rn(s2, s2));
+            }
             const float d = __fsub_rn(z, oz);
             const float k0 = expf(-__fdiv_rn(__fmul_rn(d, d), den2));
-            const float k1 = (float)(-2.0 * (double)d / (double)den2 * (double)k0);
+            // (float)(-2 d / den2 * k0) with the quotient and product carried in
+            // float-float: the double expression's rounding without FP64 division
+            const float r = -2.0f * d;
+            const float qh = __fdiv_rn(r, den2);
+            const float ql = __fdiv_rn(__fmaf_rn(-qh, den2, r), den2);
+            const float ph = __fmul_rn(qh, k0);
+            const float k1 = __fadd_rn(ph, __fmaf_rn(ql, k0, __fmaf_rn(qh, k0, -ph)));
             const float vs0 = __fmul_rn(vs, k0);
             const float gz0 = __fmul_rn(gz, k1);
             noise = __fadd_rn(noise, __fmul_rn(1.0f, __fadd_rn(vs0, gz0)));
@@ -853,6 +871,8 @@ __device__ float field_precise(const LaneField &L, float px, float py, float pz,
 // Generic evaluator: recomputes every impulse (any impulse count, 1D or 3D).
 struct EvalGeneric {
     static constexpr bool kCollective = false;
+    static constexpr int kMinBlocks = 2;
+    static constexpr bool kGeneral = true;
     __device__ __forceinline__ void reset() {}
     __device__ __forceinline__ void bind(const PcgJump *) {}
     __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
@@ -981,9 +1001,11 @@ struct EvalCached1D {
 // lane (the jump-ahead PCG draws any impulse of a cell independently), 32/NMAX
 // cells per pass; shuffles deliver each cell into its owner's registers.  Every
 // lane of the warp must call value() (idle lanes pass live = false).
-template <int NMAX>
+template <int NMAX, bool GRID = false, bool NS = false>
 struct EvalCoop1D {
     static constexpr bool kCollective = true;
+    static constexpr int kMinBlocks = 2;
+    static constexpr bool kGeneral = NS;   // stationary, single octave, 1D otherwise
     float cache[3][NMAX];
     int base;
     bool valid;
@@ -1034,10 +1056,14 @@ struct EvalCoop1D {
                                            int &id, uint32_t &refills, bool live)
     {
         const int lane = threadIdx.x & 31;
+        // a grid mean's voxel loads go first so that their latency overlaps the noise
+        GridTap tap;
+        const bool on_grid = GRID && L.mean_kind == GPIS_MEAN_GRID;
+        if (on_grid) grid_fetch(*L.m, px, py, pz, tap);
         // nonstationary: coordinate in the ls_max-scaled space, kernel width,
         // normalisation and conditioning scale at the query
         float z, kexp = L.kexp, inv_norm = L.inv_norm, ca = 1.0f;
-        if (L.ns) {
+        if (NS && L.ns) {
             const float ls = ns_scale(*L.m, px, pz);
             z = ray_coord_oct(*L.m, L.n, px, py, pz, 1.0f);
             kexp = L.kexp / (ls * ls);
@@ -1086,8 +1112,12 @@ struct EvalCoop1D {
         }
         float noise = (acc0 + acc1) * inv_norm;
         if (L.cond) {
-            const Cov1D k = cov1d(z - L.ozc, ca);
+            const Cov1D k = NS ? cov1d(z - L.ozc, ca) : cov1d(z - L.ozc);
             noise += L.vs * k.k0 + L.gsz * k.k1;
+        }
+        if (on_grid) {
+            id = 0;
+            return L.sigma * noise + grid_combine(*L.m, tap);
         }
         return L.sigma * noise + lane_mean(L, px, py, pz, id);
     }
@@ -1134,7 +1164,7 @@ __device__ __forceinline__ unsigned long long warp_sum(uint32_t v)
 // RESUME = true: the resume pass over the saved flights, with precise decisions,
 // the refinement and, after a rejected crossing candidate, the rest of the march.
 template <class Eval, bool RESUME>
-__global__ void __launch_bounds__(256) k_march(FlightArgs a)
+__global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
 {
     const int lane = threadIdx.x & 31;
     uint32_t *work = a.work + (RESUME ? 2 : 0);
@@ -1192,7 +1222,7 @@ __global__ void __launch_bounds__(256) k_march(FlightArgs a)
                         near_t = fl.near_t;
                         far_t = fl.far_t;
                         first = (fl.flags & GPIS_FLAG_FIRST_SCATTER) != 0;
-                        lane_field_setup(L, m, fl, a.cond + idx);
+                        lane_field_setup<Eval::kGeneral>(L, m, fl, a.cond + idx);
                         step = __fdiv_rn(__fsub_rn(far_t, near_t), (float)m.min_step);
                         if (m.step_size < step) step = m.step_size;
                         t0 = __fadd_rn(near_t, __fmul_rn(step, fl.jitter));
@@ -1680,6 +1710,27 @@ __global__ void __launch_bounds__(128) k_nee(FlightArgs a, const float4 *point_t
     out[i] = make_float4(pdf, g[0], g[1], g[2]);
 }
 
+// Corner table of a grid mean: cell c holds the 8 clamped corner voxels that
+// grid_fetch would load for any point whose trilinear cell is c.
+__global__ void k_pack_grid(DevMedium m, float4 *cells, size_t n)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int cx = m.cell_lo[0] + (int)(i % (size_t)m.cell_n[0]);
+    const int cy = m.cell_lo[1] + (int)((i / (size_t)m.cell_n[0]) % (size_t)m.cell_n[1]);
+    const int cz = m.cell_lo[2] + (int)(i / ((size_t)m.cell_n[0] * (size_t)m.cell_n[1]));
+    float v[8];
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+            v[4 * dz + 2 * dy + 0] = grid_voxel(m, cx, cy + dy, cz + dz);
+            v[4 * dz + 2 * dy + 1] = grid_voxel(m, cx + 1, cy + dy, cz + dz);
+        }
+    cells[2 * i] = make_float4(v[0], v[1], v[2], v[3]);
+    cells[2 * i + 1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+
 __global__ void k_se_splat_1d(const float *q, const float *c, float *v, float *d, size_t n, float scale)
 {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1715,7 +1766,14 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
         return c == 0 ? 1u : c;
     };
     if (ev) cudaEventRecord(ev[2], stream);
-    if (a.one_d && a.max_imp <= 8 && a.max_oct == 1) {
+    const bool coop = a.one_d && a.max_imp <= 8 && a.max_oct == 1;
+    if (coop && a.any_ns) {
+        const void *fn = (const void *)k_march<EvalCoop1D<8, false, true>, false>;
+        k_march<EvalCoop1D<8, false, true>, false><<<grid(fn), 256, 0, stream>>>(a);
+    } else if (coop && a.all_grid) {
+        const void *fn = (const void *)k_march<EvalCoop1D<8, true>, false>;
+        k_march<EvalCoop1D<8, true>, false><<<grid(fn), 256, 0, stream>>>(a);
+    } else if (coop) {
         const void *fn = (const void *)k_march<EvalCoop1D<8>, false>;
         k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(a);
     } else {
@@ -1764,6 +1822,15 @@ cudaError_t launch_nee(const FlightArgs &a, const float4 *point_t, const float4 
 {
     if (a.n == 0) return cudaSuccess;
     k_nee<<<(a.n + 127) / 128, 128, 0, stream>>>(a, point_t, normal, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_grid(const DevMedium &m, float4 *cells, size_t n, cudaStream_t stream)
+{
+    if (n == 0) return cudaSuccess;
+    DevMedium mm = m;
+    mm.grid_cells = nullptr;
+    k_pack_grid<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(mm, cells, n);
     return cudaGetLastError();
 }
 

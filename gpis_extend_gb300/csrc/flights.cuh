@@ -46,6 +46,8 @@ struct FlightArgs {
     int three_d;                // all media use 3D noise
     uint32_t max_imp;           // max impulses per cell over the media
     uint32_t max_oct;           // max octaves over the media
+    int all_grid;               // all media have a grid mean
+    int any_ns;                 // some medium has a nonstationary length scale
 };
 
 // Upload the jump-ahead PCG table to the current device (once per device).
@@ -54,6 +56,8 @@ cudaError_t upload_pcg_table();
 // Enqueue the flight kernels on the stream.  ev, when not null, holds start/stop
 // events for the prepare, march (march + resume) and finish kernels (ev[2k], ev[2k+1]).
 cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream, cudaEvent_t *ev = nullptr);
+// Fill the corner table of a grid mean (m holds the device voxel pointer and cell_lo/cell_n)
+cudaError_t launch_pack_grid(const DevMedium &m, float4 *cells, size_t n, cudaStream_t stream);
 // 1D specular NEE queries on the realizations of the flights in a (one thread each)
 cudaError_t launch_nee(const FlightArgs &a, const float4 *point_t, const float4 *normal, float4 *out,
                        cudaStream_t stream);

@@ -177,7 +177,7 @@ struct gpis_ctx {
     int n_media = 0;
     gpis::DevMedium *d_media = nullptr;
     std::vector<float *> d_grids;
-    bool any_cond = false, all_one_d = true, all_three_d = true;
+    bool any_cond = false, all_one_d = true, all_three_d = true, all_grid = true, any_ns = false;
     uint32_t max_imp = 0, max_oct = 1;
     // scratch of the flight kernels
     gpis::CondRec *d_cond = nullptr;
@@ -315,12 +315,38 @@ int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
                     break;
                 }
                 m.grid = dg;
+                // corner table over the cells the clamps can reach, when it stays
+                // small enough to live in L2 (32 MiB); a larger table would turn
+                // the L2 hits of a grid that fits there into DRAM reads
+                size_t cells = 1;
+                for (int k = 0; k < 3; ++k) {
+                    const double lo = std::floor((double)g->clamp_min[k]), hi = std::floor((double)g->clamp_max[k]);
+                    const double span = hi - lo + 1.0;
+                    if (!(span >= 1.0 && span < 2147483647.0 && lo > -2147483647.0)) { cells = 0; break; }
+                    m.cell_lo[k] = (int32_t)lo;
+                    m.cell_n[k] = (int32_t)span;
+                    cells *= (size_t)span;
+                }
+                const size_t table = cells * 2 * sizeof(float4);
+                if (cells && table <= ((size_t)32 << 20)) {
+                    float4 *dc = nullptr;
+                    if ((e = cudaMalloc(&dc, table)) != cudaSuccess) { rc = cuda_fail(e, "allocate grid corner table"); break; }
+                    c->d_grids.push_back(reinterpret_cast<float *>(dc));
+                    if ((e = gpis::launch_pack_grid(m, dc, cells, nullptr)) != cudaSuccess ||
+                        (e = cudaDeviceSynchronize()) != cudaSuccess) {
+                        rc = cuda_fail(e, "build grid corner table");
+                        break;
+                    }
+                    m.grid_cells = dc;
+                }
             }
             c->any_cond = c->any_cond || (m.flags & gpis::MF_COND);
             c->all_one_d = c->all_one_d && (m.flags & gpis::MF_ONE_D);
             c->all_three_d = c->all_three_d && !(m.flags & gpis::MF_ONE_D);
             c->max_imp = std::max(c->max_imp, m.n_imp);
             c->max_oct = std::max(c->max_oct, m.n_oct);
+            c->all_grid = c->all_grid && m.mean_kind == GPIS_MEAN_GRID;
+            c->any_ns = c->any_ns || m.ls_kind != 0u;
         }
         if (rc) break;
         if ((e = cudaMalloc(&c->d_media, host.size() * sizeof(gpis::DevMedium))) != cudaSuccess) { rc = cuda_fail(e, "allocate media"); break; }
@@ -358,7 +384,7 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_res
     if (ctx->any_cond && !in->prev) return fail(GPIS_EINVAL, "conditioning media need the prev stream");
     int rc = ensure_scratch(ctx, n);
     if (rc) return rc;
-    gpis::FlightArgs a;
+    gpis::FlightArgs a = {};
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
     a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
     a.seeds = reinterpret_cast<const uint4 *>(in->seeds);
@@ -379,6 +405,8 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_res
     a.three_d = ctx->all_three_d;
     a.max_imp = ctx->max_imp;
     a.max_oct = ctx->max_oct;
+    a.all_grid = ctx->all_grid;
+    a.any_ns = ctx->any_ns;
     for (const void *p : {(const void *)in->origin_near, (const void *)in->dir_far, (const void *)in->seeds,
                           (const void *)in->prev, (const void *)out->rec})
         if (p && (reinterpret_cast<uintptr_t>(p) & 15u))

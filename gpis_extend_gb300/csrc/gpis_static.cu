@@ -106,7 +106,7 @@ extern "C" int gpis_flights_submit_static(const gpis_medium_desc *medium, const 
     k_store_medium<<<1, 32, 0, s>>>(m, reinterpret_cast<gpis::DevMedium *>(b + kOffMedium));
     if (cudaGetLastError() != cudaSuccess || cudaMemsetAsync(b + kOffCounters, 0, sizeof(gpis_counters), s) != cudaSuccess)
         return fail(GPIS_EIO, "initialising the static working array failed");
-    gpis::FlightArgs a;
+    gpis::FlightArgs a = {};
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
     a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
     a.seeds = reinterpret_cast<const uint4 *>(in->seeds);
@@ -127,6 +127,8 @@ extern "C" int gpis_flights_submit_static(const gpis_medium_desc *medium, const 
     a.three_d = !a.one_d;
     a.max_imp = m.n_imp;
     a.max_oct = m.n_oct;
+    a.all_grid = m.mean_kind == GPIS_MEAN_GRID;
+    a.any_ns = m.ls_kind != 0u;
     if (gpis::launch_flights(a, sms, s) != cudaSuccess) return fail(GPIS_EIO, "launching the flight kernels failed");
     return GPIS_OK;
 }
