@@ -143,6 +143,52 @@ class ResultSoA(ctypes.Structure):
     _fields_ = [("rec", ctypes.c_void_p)]
 
 
+PHASE_LAMBERT = 0
+
+
+class SceneDesc(ctypes.Structure):
+    """gpis_scene_desc: camera, medium cube, quad light and phase of a render."""
+    _fields_ = [
+        ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("spp", ctypes.c_uint32),
+        ("max_bounces", ctypes.c_uint32),
+        ("cam_pos", ctypes.c_float * 3), ("cam_target", ctypes.c_float * 3), ("cam_up", ctypes.c_float * 3),
+        ("tan_half_fov", ctypes.c_float), ("box_half", ctypes.c_float),
+        ("light_center", ctypes.c_float * 3), ("light_u", ctypes.c_float * 3), ("light_v", ctypes.c_float * 3),
+        ("light_emission", ctypes.c_float * 3),
+        ("phase", ctypes.c_uint32), ("albedo", ctypes.c_float * 3),
+        ("scene_seed", ctypes.c_uint32), ("sampler_seed", ctypes.c_uint32), ("medium", ctypes.c_uint32),
+        ("reserved_", ctypes.c_uint32),
+    ]
+
+
+class RenderStats(ctypes.Structure):
+    _fields_ = [("paths", ctypes.c_uint64), ("distance_flights", ctypes.c_uint64),
+                ("shadow_flights", ctypes.c_uint64), ("medium_events", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("ms", ctypes.c_double)]
+
+
+def make_scene(width=64, height=64, spp=4, max_bounces=4, fov_deg=45.0, cam_pos=(0, 0, 4), cam_target=(0, 0, 0),
+               cam_up=(0, 1, 0), box_half=1.5, light_center=(0, 3, 0), light_u=(1, 0, 0), light_v=(0, 0, 1),
+               light_emission=(10, 10, 10), albedo=(0.8, 0.8, 0.8), scene_seed=1, sampler_seed=7, medium=0):
+    """A SceneDesc; the default light is a 1x1 quad at y = 3 facing down."""
+    import math
+    sc = SceneDesc()
+    sc.width, sc.height, sc.spp, sc.max_bounces = width, height, spp, max_bounces
+    sc.cam_pos[:] = cam_pos
+    sc.cam_target[:] = cam_target
+    sc.cam_up[:] = cam_up
+    sc.tan_half_fov = math.tan(math.radians(fov_deg) / 2)
+    sc.box_half = box_half
+    sc.light_center[:] = light_center
+    sc.light_u[:] = light_u
+    sc.light_v[:] = light_v
+    sc.light_emission[:] = light_emission
+    sc.phase = PHASE_LAMBERT
+    sc.albedo[:] = albedo
+    sc.scene_seed, sc.sampler_seed, sc.medium = scene_seed, sampler_seed, medium
+    return sc
+
+
 class NeeSoA(ctypes.Structure):
     """gpis_nee_soa: the realization's flight streams plus point_t and normal (float4 each)."""
     _fields_ = [
@@ -317,6 +363,7 @@ def load_library(path=None):
         "gpis_flights_trace_host": (c_int, [vp, P(FlightSoA), P(ResultSoA), c_u32]),
         "gpis_nee_submit": (c_int, [vp, P(NeeSoA), vp, c_u32, vp]),
         "gpis_nee_host": (c_int, [vp, P(NeeSoA), vp, c_u32]),
+        "gpis_render": (c_int, [vp, P(SceneDesc), vp, P(RenderStats)]),
         "gpis_status": (c_int, [vp, P(Counters), c_int]),
         "gpis_profile_enable": (c_int, [vp, c_int]),
         "gpis_profile_read": (c_int, [vp, P(ctypes.c_double), P(ctypes.c_uint64), c_int]),

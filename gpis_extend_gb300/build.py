@@ -14,7 +14,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgpis_gb300.so")
 ROOT = os.path.dirname(HERE)
 
-SOURCES = ["flights.cu", "gpis_abi.cu", "gpis_static.cu", "medium_json.cpp", "medium_adapter.cpp"]
+SOURCES = ["flights.cu", "gpis_abi.cu", "gpis_static.cu", "render.cu", "medium_json.cpp", "medium_adapter.cpp"]
+# per-file flags: the path tracer rounds every float expression as its CPU restatement
+EXTRA = {"render.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -48,7 +50,8 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc, *ARCH, *common, "-lineinfo", "-Xptxas", "-v", "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc, *ARCH, *common, *EXTRA.get(src, []), "-lineinfo", "-Xptxas", "-v", "-c",
+               os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
             cmd = [nvcc, *common, "-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)

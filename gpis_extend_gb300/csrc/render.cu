@@ -1,0 +1,735 @@
+// render.cu -- gpis_render: a wavefront path tracer around the GPIS medium.
+//
+// The subset of PathTracer::traceSample (PathTracer.cpp:49-292) described in
+// gpis.h: pinhole camera, the medium's bounding cube as a forward boundary, one
+// one-sided quad light outside the cube, GP surface events shaded by
+// BRDFPhaseFunction over LambertBsdf (BRDFPhaseFunction.cpp:29-101) with
+// handleVolume's direct lighting (TraceBase.cpp:993-1014, 798-874).
+//
+// Wavefront form: the paths of a chunk (all pixels x a run of samples) live in a
+// device array.  Each round, k_rt_advance moves every path that is outside the
+// cube to the cube or the light and queues one sampleDistance flight per path
+// inside; the flight kernels trace the queue; k_rt_event applies
+// GaussianProcessMedium::sampleDistance's decisions (GaussianProcessMedium.cpp:
+// 289-381), queues the two direct-lighting transmittance flights of each GP
+// event and samples the continuation; a second flight batch traces those
+// shadow flights and k_rt_shadow adds the light that got through.  Rounds
+// repeat until no path is alive.
+//
+// This file is compiled with -fmad=false: every float expression rounds as the
+// CPU restatement's (built with -ffp-contract=off), and path decisions use no
+// trigonometry, so both make the same decisions from the same counter RNG.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/gpis.h"
+
+extern "C" int gpis_internal_set_error(int code, const char *msg);
+extern "C" const gpis_medium_desc *gpis_internal_ctx_medium(gpis_ctx *ctx, uint32_t index);
+
+namespace {
+
+constexpr float kInvPi = 0.31830988618379067f;
+enum : uint32_t { D_JIT = 0, D_LU = 1, D_LV = 2, D_JS1 = 3, D_PHASE = 4, D_JS2 = 20, D_CONT = 21, D_PIX = 40 };
+constexpr uint32_t kCameraBounce = 0xFFFFu;
+
+enum : uint32_t { PF_ALIVE = 1u, PF_INSIDE = 2u, PF_SPECULAR = 4u, PF_FIRST = 8u };
+
+// one path of the chunk (MediumState fields the medium reads and writes inline)
+struct PathRec {
+    float pos[3], dir[3], T[3], L[3];
+    float last_val, last_aniso[3];
+    uint32_t flags, bounce, pixel, sample;
+    int32_t st_bounce, gp_id;
+    uint32_t pad[2];
+};
+
+// what the medium state machine needs of the medium
+struct RtMedium {
+    float ratio;                // sigma_s / sigma_t
+    int32_t max_bounces;
+    uint32_t seed;
+    uint32_t single_realization;
+    uint32_t global_ctx;
+    uint32_t scene_seed;
+};
+
+struct RtScene {
+    gpis_scene_desc sc;
+    float fwd[3], right[3], up[3];
+    float ln[3];
+    float area;
+    float aspect;
+    uint32_t s0;                // first sample of the chunk
+    uint32_t ns;                // samples in the chunk
+};
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ float rng(uint32_t seed, uint64_t path, uint32_t bounce, uint32_t dim)
+{
+    uint64_t k = mix64(((uint64_t)seed << 32) ^ path);
+    k = mix64(k ^ (((uint64_t)bounce << 32) | dim));
+    return (float)(k >> 40) * (1.0f / 16777216.0f);
+}
+
+__device__ __forceinline__ uint32_t rotl17(uint32_t h) { return (h << 17) | (h >> 15); }
+__device__ __forceinline__ uint32_t xx_fin(uint32_t h)
+{
+    h = 2246822519u * (h ^ (h >> 15));
+    h = 3266489917u * (h ^ (h >> 13));
+    return h ^ (h >> 16);
+}
+// MathUtil::xxhash32(uint) and (Vec4u) (MathUtil.hpp:179-224)
+__device__ __forceinline__ uint32_t xx1(uint32_t p) { return xx_fin(668265263u * rotl17(p + 374761393u)); }
+__device__ __forceinline__ uint32_t xx4(uint32_t x, uint32_t y, uint32_t z, uint32_t w)
+{
+    uint32_t h = w + 374761393u + x * 3266489917u;
+    h = 668265263u * rotl17(h);
+    h += y * 3266489917u;
+    h = 668265263u * rotl17(h);
+    h += z * 3266489917u;
+    h = 668265263u * rotl17(h);
+    return xx_fin(h);
+}
+
+__device__ __forceinline__ float dot3(const float a[3], const float b[3])
+{
+    float s = a[0] * b[0];
+    s = s + a[1] * b[1];
+    s = s + a[2] * b[2];
+    return s;
+}
+
+__device__ __forceinline__ void normalize3(float v[3])
+{
+    const float inv = 1.0f / sqrtf(dot3(v, v));
+    v[0] = v[0] * inv; v[1] = v[1] * inv; v[2] = v[2] * inv;
+}
+
+struct PFrame { float t[3], b[3], n[3]; };
+
+// TangentFrame(n) (TangentFrame.hpp:74-83)
+__device__ void pframe(const float n_in[3], PFrame &f)
+{
+    f.n[0] = n_in[0]; f.n[1] = n_in[1]; f.n[2] = n_in[2];
+    normalize3(f.n);
+    const float *n = f.n;
+    const float sign = copysignf(1.0f, n[2]);
+    const float a = -1.0f / (sign + n[2]);
+    const float b = n[0] * n[1] * a;
+    f.t[0] = 1.0f + sign * n[0] * n[0] * a; f.t[1] = sign * b; f.t[2] = -sign * n[0];
+    f.b[0] = b; f.b[1] = sign + n[1] * n[1] * a; f.b[2] = -n[1];
+    normalize3(f.t);
+    normalize3(f.b);
+}
+
+__device__ __forceinline__ void to_local(const PFrame &f, const float v[3], float o[3])
+{
+    o[0] = dot3(f.t, v); o[1] = dot3(f.b, v); o[2] = dot3(f.n, v);
+}
+
+__device__ __forceinline__ void to_global(const PFrame &f, const float l[3], float o[3])
+{
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float s = f.t[i] * l[0];
+        s = s + f.b[i] * l[1];
+        s = s + f.n[i] * l[2];
+        o[i] = s;
+    }
+}
+
+__device__ void cosine_dir(uint32_t seed, uint64_t path, uint32_t bounce, uint32_t dim0, float w[3])
+{
+    float x = 0.0f, y = 0.0f;
+    for (int k = 0; k < 8; ++k) {
+        const float u = 2.0f * rng(seed, path, bounce, dim0 + 2 * k) - 1.0f;
+        const float v = 2.0f * rng(seed, path, bounce, dim0 + 2 * k + 1) - 1.0f;
+        if (u * u + v * v < 1.0f) { x = u; y = v; break; }
+    }
+    w[0] = x; w[1] = y;
+    const float r2 = x * x + y * y;
+    w[2] = sqrtf(fmaxf(0.0f, 1.0f - r2));
+}
+
+__device__ bool box_hit(const float o[3], const float d[3], float h, float &t0, float &t1)
+{
+    float tmin = -INFINITY, tmax = INFINITY;
+    for (int i = 0; i < 3; ++i) {
+        if (d[i] == 0.0f) {
+            if (o[i] < -h || o[i] > h) return false;
+            continue;
+        }
+        const float inv = 1.0f / d[i];
+        float ta = (-h - o[i]) * inv, tb = (h - o[i]) * inv;
+        if (ta > tb) { const float s = ta; ta = tb; tb = s; }
+        tmin = fmaxf(tmin, ta);
+        tmax = fminf(tmax, tb);
+    }
+    if (tmax < fmaxf(tmin, 0.0f)) return false;
+    t0 = tmin;
+    t1 = tmax;
+    return true;
+}
+
+__device__ float light_hit(const RtScene &S, const float o[3], const float d[3])
+{
+    const gpis_scene_desc &sc = S.sc;
+    const float den = dot3(d, S.ln);
+    if (!(den < 0.0f)) return -1.0f;
+    float co[3];
+    for (int i = 0; i < 3; ++i) co[i] = sc.light_center[i] - o[i];
+    const float t = dot3(co, S.ln) / den;
+    if (!(t > 0.0f)) return -1.0f;
+    float x[3];
+    for (int i = 0; i < 3; ++i) x[i] = (o[i] + t * d[i]) - sc.light_center[i];
+    const float s = dot3(x, sc.light_u) / dot3(sc.light_u, sc.light_u);
+    const float r = dot3(x, sc.light_v) / dot3(sc.light_v, sc.light_v);
+    if (fabsf(s) > 0.5f || fabsf(r) > 0.5f) return -1.0f;
+    return t;
+}
+
+__device__ __forceinline__ float power_heuristic(float a, float b)
+{
+    const float a2 = a * a, b2 = b * b;
+    return a2 / (a2 + b2);
+}
+
+// flight streams of one queue
+struct Queue {
+    float4 *origin_near, *dir_far, *prev;
+    uint4 *seeds;
+    float4 *rec;                // 2 per flight
+    uint32_t *path;             // path index of each flight
+    float4 *payload;            // shadow queues: contribution (rgb) and slot
+    uint32_t *count;
+};
+
+__device__ void push_flight(const Queue &q, uint32_t slot, const float o[3], const float d[3], float far_t,
+                            uint32_t noise_seed, uint32_t normal_seed, uint32_t flags, float jitter, float pv,
+                            const float pg[3])
+{
+    q.origin_near[slot] = make_float4(o[0], o[1], o[2], 0.0f);
+    q.dir_far[slot] = make_float4(d[0], d[1], d[2], far_t);
+    q.seeds[slot] = make_uint4(noise_seed, normal_seed, flags, __float_as_uint(jitter));
+    q.prev[slot] = make_float4(pv, pg[0], pg[1], pg[2]);
+}
+
+// computeSeed and the request's normal seed (SparseConvolutionNoise.cpp:57-66,
+// SparseConvolutionNoiseMedium.cpp:235-238)
+__device__ void flight_seeds(const RtMedium &M, uint32_t px, uint32_t py, uint32_t s, uint32_t w, uint32_t &ns,
+                             uint32_t &nm)
+{
+    const uint32_t sc = xx1(M.scene_seed);
+    ns = M.seed + (M.single_realization ? 0u : xx4(px, py, s, M.global_ctx ? 0u : w) + sc);
+    nm = xx4(px, py, s, w) + sc + 1u;
+}
+
+__global__ void k_rt_camera(RtScene S, PathRec *paths, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const gpis_scene_desc &sc = S.sc;
+    const uint32_t pixel = i / S.ns, s = S.s0 + i % S.ns;
+    const uint32_t px = pixel % sc.width, py = pixel / sc.width;
+    const uint64_t path = ((uint64_t)py * sc.width + px) * sc.spp + s;
+    const float u0 = rng(sc.sampler_seed, path, kCameraBounce, D_PIX);
+    const float u1 = rng(sc.sampler_seed, path, kCameraBounce, D_PIX + 1);
+    const float sx = (2.0f * ((float)px + u0) / (float)sc.width - 1.0f) * sc.tan_half_fov * S.aspect;
+    const float sy = (1.0f - 2.0f * ((float)py + u1) / (float)sc.height) * sc.tan_half_fov;
+    PathRec r;
+    for (int k = 0; k < 3; ++k) {
+        r.pos[k] = sc.cam_pos[k];
+        r.dir[k] = S.fwd[k] + sx * S.right[k] + sy * S.up[k];
+        r.T[k] = 1.0f;
+        r.L[k] = 0.0f;
+        r.last_aniso[k] = 0.0f;
+    }
+    normalize3(r.dir);
+    r.last_val = 0.0f;
+    r.flags = PF_ALIVE | PF_SPECULAR | PF_FIRST;
+    r.bounce = 0;
+    r.pixel = pixel;
+    r.sample = s;
+    r.st_bounce = 0;
+    r.gp_id = 0;
+    r.pad[0] = r.pad[1] = 0u;
+    paths[i] = r;
+}
+
+// Outside the cube: reach the light, the cube or nothing.  Inside: queue the
+// sampleDistance flight to the cube's exit.
+__global__ void k_rt_advance(RtScene S, RtMedium M, PathRec *paths, uint32_t n, Queue q,
+                             unsigned long long *counters)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PathRec r = paths[i];
+    if (!(r.flags & PF_ALIVE)) return;
+    const gpis_scene_desc &sc = S.sc;
+    if (r.bounce >= sc.max_bounces) {
+        r.flags &= ~PF_ALIVE;
+        paths[i] = r;
+        return;
+    }
+    if (!(r.flags & PF_INSIDE)) {
+        float t0, t1;
+        const bool hb = box_hit(r.pos, r.dir, sc.box_half, t0, t1) && t0 > 0.0f;
+        const float tl = light_hit(S, r.pos, r.dir);
+        if (tl > 0.0f && (!hb || tl < t0)) {
+            if (r.flags & PF_SPECULAR)
+                for (int c = 0; c < 3; ++c) r.L[c] = r.L[c] + r.T[c] * sc.light_emission[c];
+            r.flags &= ~PF_ALIVE;
+            paths[i] = r;
+            return;
+        }
+        if (!hb) {
+            r.flags &= ~PF_ALIVE;
+            paths[i] = r;
+            return;
+        }
+        for (int k = 0; k < 3; ++k) {
+            const float e = r.pos[k] + t0 * r.dir[k];
+            r.pos[k] = fminf(fmaxf(e, -sc.box_half), sc.box_half);
+        }
+        r.flags |= PF_INSIDE;
+    }
+    float t0, t1;
+    if (!box_hit(r.pos, r.dir, sc.box_half, t0, t1)) {
+        // numerically outside after all: leaves the cube at once
+        r.flags &= ~PF_INSIDE;
+        paths[i] = r;
+        return;
+    }
+    if (r.st_bounce >= M.max_bounces) {
+        // sampleDistance fails at the medium's bounce limit (GaussianProcessMedium.cpp:222-232)
+        r.flags &= ~PF_ALIVE;
+        atomicAdd(counters + 1, 1ull);
+        paths[i] = r;
+        return;
+    }
+    if (!(t1 > 0.0f)) {
+        // maxT <= nearT: the segment exits at once with weight 1 and no flight
+        r.flags &= ~PF_INSIDE;
+        paths[i] = r;
+        return;
+    }
+    const uint32_t px = r.pixel % sc.width, py = r.pixel / sc.width;
+    const uint64_t path = ((uint64_t)py * sc.width + px) * sc.spp + r.sample;
+    uint32_t ns, nm;
+    flight_seeds(M, px, py, r.sample, r.bounce, ns, nm);
+    const bool first = (r.flags & PF_FIRST) != 0;
+    const float zero[3] = {0.0f, 0.0f, 0.0f};
+    const uint32_t slot = atomicAdd(q.count, 1u);
+    push_flight(q, slot, r.pos, r.dir, t1, ns, nm, first ? GPIS_FLAG_FIRST_SCATTER : 0u,
+                rng(sc.sampler_seed, path, r.bounce, D_JIT), first ? 0.0f : r.last_val, first ? zero : r.last_aniso);
+    q.path[slot] = i;
+    paths[i] = r;
+}
+
+// queue a direct-lighting transmittance flight from p along d (the light lies
+// outside the cube, so the flight ends at the cube's exit)
+__device__ void push_shadow(const RtScene &S, const RtMedium &M, const Queue &q, const PathRec &r, uint32_t pi,
+                            const float p[3], const float d[3], float jitter, const float contrib[3], uint32_t slot_kind,
+                            float *direct)
+{
+    float t0, t1;
+    if (!box_hit(p, d, S.sc.box_half, t0, t1) || !(t1 > 0.0f)) {
+        // no medium in the way: the light arrives (the restatement's shadow() returns 1)
+        for (int c = 0; c < 3; ++c) direct[3 * slot_kind + c] = contrib[c];
+        return;
+    }
+    const uint32_t px = r.pixel % S.sc.width, py = r.pixel / S.sc.width;
+    uint32_t ns, nm;
+    flight_seeds(M, px, py, r.sample, r.bounce + 1, ns, nm);
+    const uint32_t slot = atomicAdd(q.count, 1u);
+    push_flight(q, slot, p, d, t1, ns, nm, GPIS_FLAG_SHADOW, jitter, r.last_val, r.last_aniso);
+    q.path[slot] = pi;
+    q.payload[slot] = make_float4(contrib[0], contrib[1], contrib[2], __uint_as_float(slot_kind));
+}
+
+// GaussianProcessMedium::sampleDistance after the flight (GaussianProcessMedium.cpp:
+// 289-381), then handleVolume (TraceBase.cpp:993-1048) for GP events.
+__global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint32_t nq, Queue sq, float *direct,
+                           unsigned long long *counters)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nq) return;
+    const uint32_t pi = q.path[k];
+    PathRec r = paths[pi];
+    const gpis_scene_desc &sc = S.sc;
+    const float4 r0 = q.rec[2 * k], r1 = q.rec[2 * k + 1];
+    const uint32_t status = __float_as_uint(r1.w);
+    const float far_t = q.dir_far[k].w;
+    float *dslot = direct + 6 * (size_t)pi;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) dslot[c] = 0.0f;
+    if ((status & 0xFFu) != GPIS_FLIGHT_OK) {
+        r.flags &= ~PF_ALIVE;
+        atomicAdd(counters + 1, 1ull);
+        paths[pi] = r;
+        return;
+    }
+    const bool hit = r1.y == 0.0f;
+    const float t = r0.x;
+    float aniso[3] = {r0.z, r0.w, r1.x};
+    const bool first_before = (r.flags & PF_FIRST) != 0;
+    if (hit) {
+        r.gp_id = (int32_t)((status >> 8) & 0xFFu);
+        r.last_val = 0.0f;
+    } else {
+        r.last_val = r0.y;
+    }
+    if (t < far_t) {
+        r.last_aniso[0] = aniso[0]; r.last_aniso[1] = aniso[1]; r.last_aniso[2] = aniso[2];
+        r.flags &= ~PF_FIRST;
+        if (!isfinite((aniso[0] + aniso[1] + aniso[2]) / 3.0f)) {
+            r.flags &= ~PF_ALIVE;
+            atomicAdd(counters + 1, 1ull);
+            paths[pi] = r;
+            return;
+        }
+    }
+    (void)first_before;
+    if (hit) {
+        const double dd = (double)aniso[0] * r.dir[0] + (double)aniso[1] * r.dir[1] + (double)aniso[2] * r.dir[2];
+        const double l2 = (double)aniso[0] * aniso[0] + (double)aniso[1] * aniso[1] + (double)aniso[2] * aniso[2];
+        if (dd > 0 || l2 < 0.0000001f) {
+            r.flags &= ~PF_ALIVE;
+            atomicAdd(counters + 1, 1ull);
+            paths[pi] = r;
+            return;
+        }
+    }
+    const float ts = fminf(t, far_t);
+    float p[3];
+    for (int i = 0; i < 3; ++i) p[i] = r.pos[i] + ts * r.dir[i];
+    r.last_aniso[0] = aniso[0]; r.last_aniso[1] = aniso[1]; r.last_aniso[2] = aniso[2];
+    r.flags &= ~PF_FIRST;
+    r.st_bounce += 1;
+    for (int c = 0; c < 3; ++c) r.T[c] = r.T[c] * M.ratio;
+    if (!hit) {
+        // forward boundary: the path continues outside the cube
+        r.pos[0] = p[0]; r.pos[1] = p[1]; r.pos[2] = p[2];
+        r.flags &= ~PF_INSIDE;
+        paths[pi] = r;
+        return;
+    }
+    atomicAdd(counters + 0, 1ull);
+    PFrame f;
+    pframe(aniso, f);
+    float wi[3];
+    const float nd[3] = {-r.dir[0], -r.dir[1], -r.dir[2]};
+    to_local(f, nd, wi);
+    if (!(wi[2] > 0.0f)) {
+        r.flags &= ~PF_ALIVE;
+        atomicAdd(counters + 1, 1ull);
+        paths[pi] = r;
+        return;
+    }
+    const uint32_t px = r.pixel % sc.width, py = r.pixel / sc.width;
+    const uint64_t path = ((uint64_t)py * sc.width + px) * sc.spp + r.sample;
+    const uint32_t seed = sc.sampler_seed, b = r.bounce;
+    if (b + 1 < sc.max_bounces) {
+        // volumeLightSample
+        const float lu = rng(seed, path, b, D_LU) - 0.5f, lv = rng(seed, path, b, D_LV) - 0.5f;
+        float ld[3];
+        for (int i = 0; i < 3; ++i)
+            ld[i] = ((sc.light_center[i] + lu * sc.light_u[i]) + lv * sc.light_v[i]) - p[i];
+        const float dist2 = dot3(ld, ld), dist = sqrtf(dist2);
+        for (int i = 0; i < 3; ++i) ld[i] = ld[i] / dist;
+        const float cos_l = -dot3(ld, S.ln);
+        if (cos_l > 0.0f) {
+            const float pdf_l = dist2 / (S.area * cos_l);
+            float wo[3];
+            to_local(f, ld, wo);
+            if (wo[2] > 0.0f) {
+                const float pdf_p = wo[2] * kInvPi;
+                const float w = power_heuristic(pdf_l, pdf_p);
+                float contrib[3];
+                for (int c = 0; c < 3; ++c) {
+                    const float fc = sc.albedo[c] * kInvPi * wo[2];
+                    contrib[c] = r.T[c] * (fc * sc.light_emission[c] / pdf_l * w);
+                }
+                push_shadow(S, M, sq, r, pi, p, ld, rng(seed, path, b, D_JS1), contrib, 0u, dslot);
+            }
+        }
+        // volumePhaseSample
+        float wl[3], wg[3];
+        cosine_dir(seed, path, b, D_PHASE, wl);
+        to_global(f, wl, wg);
+        normalize3(wg);
+        const float tlh = light_hit(S, p, wg);
+        if (tlh > 0.0f && wl[2] > 0.0f) {
+            const float pdf_p = wl[2] * kInvPi;
+            const float cl = -dot3(wg, S.ln);
+            const float pdf_l = (tlh * tlh) / (S.area * cl);
+            const float w = power_heuristic(pdf_p, pdf_l);
+            float contrib[3];
+            for (int c = 0; c < 3; ++c) contrib[c] = r.T[c] * (sc.albedo[c] * sc.light_emission[c] * w);
+            push_shadow(S, M, sq, r, pi, p, wg, rng(seed, path, b, D_JS2), contrib, 1u, dslot);
+        }
+    }
+    // the continuation (BRDFPhaseFunction::sample over LambertBsdf)
+    float wl[3], wg[3];
+    cosine_dir(seed, path, b, D_CONT, wl);
+    to_global(f, wl, wg);
+    normalize3(wg);
+    for (int c = 0; c < 3; ++c) r.T[c] = r.T[c] * sc.albedo[c];
+    for (int i = 0; i < 3; ++i) { r.pos[i] = p[i]; r.dir[i] = wg[i]; }
+    r.flags &= ~PF_SPECULAR;
+    r.bounce += 1;
+    paths[pi] = r;
+}
+
+// a transmittance of 1 lets the queued contribution through
+__global__ void k_rt_shadow(Queue sq, uint32_t nq, float *direct)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nq) return;
+    const float4 pl = sq.payload[k];
+    const uint32_t kind = __float_as_uint(pl.w);
+    const float4 r1 = sq.rec[2 * k + 1];
+    // transmittance 1 only for a finished flight that misses (resumeTransmittance)
+    if ((__float_as_uint(r1.w) & 0xFFu) == GPIS_FLIGHT_OK && r1.y > 0.0f) {
+        float *d = direct + 6 * (size_t)sq.path[k] + 3 * kind;
+        d[0] = pl.x; d[1] = pl.y; d[2] = pl.z;
+    }
+}
+
+// L += light sample, then L += phase sample, in the restatement's order
+__global__ void k_rt_collect(PathRec *paths, const uint32_t *qpath, uint32_t nq, float *direct)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nq) return;
+    const uint32_t pi = qpath[k];
+    float *d = direct + 6 * (size_t)pi;
+    PathRec &r = paths[pi];
+    for (int c = 0; c < 3; ++c) r.L[c] = r.L[c] + d[c];
+    for (int c = 0; c < 3; ++c) r.L[c] = r.L[c] + d[3 + c];
+}
+
+__global__ void k_rt_accumulate(const PathRec *paths, uint32_t n_pixels, uint32_t ns, float *acc)
+{
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= n_pixels) return;
+    float a[3] = {acc[3 * px], acc[3 * px + 1], acc[3 * px + 2]};
+    for (uint32_t s = 0; s < ns; ++s) {
+        const PathRec &r = paths[(size_t)px * ns + s];
+        for (int c = 0; c < 3; ++c) a[c] = a[c] + r.L[c];
+    }
+    acc[3 * px] = a[0]; acc[3 * px + 1] = a[1]; acc[3 * px + 2] = a[2];
+}
+
+__global__ void k_rt_finish(float *acc, uint32_t n_pixels, uint32_t spp)
+{
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= n_pixels) return;
+    for (int c = 0; c < 3; ++c) acc[3 * px + c] = acc[3 * px + c] / (float)spp;
+}
+
+inline void hnorm(float v[3])
+{
+    float s = v[0] * v[0];
+    s = s + v[1] * v[1];
+    s = s + v[2] * v[2];
+    const float inv = 1.0f / std::sqrt(s);
+    v[0] = v[0] * inv; v[1] = v[1] * inv; v[2] = v[2] * inv;
+}
+
+inline void hcross(const float a[3], const float b[3], float o[3])
+{
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+struct DevBuf {
+    std::vector<void *> ptrs;
+    ~DevBuf() { for (void *p : ptrs) cudaFree(p); }
+    template <class T>
+    cudaError_t alloc(T *&p, size_t n)
+    {
+        void *v = nullptr;
+        cudaError_t e = cudaMalloc(&v, std::max<size_t>(n, 1) * sizeof(T));
+        if (e == cudaSuccess) ptrs.push_back(v);
+        p = static_cast<T *>(v);
+        return e;
+    }
+};
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    static thread_local char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    return gpis_internal_set_error(GPIS_EIO, buf);
+}
+
+}  // namespace
+
+#define RT_TRY(expr, what)                              \
+    do {                                                \
+        cudaError_t e_ = (expr);                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *image_rgb, gpis_render_stats *stats)
+{
+    if (!ctx || !scene || !image_rgb) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    const gpis_scene_desc &sc = *scene;
+    if (sc.width == 0 || sc.height == 0 || sc.spp == 0 || sc.max_bounces == 0)
+        return gpis_internal_set_error(GPIS_EINVAL, "width, height, spp and max_bounces must be > 0");
+    if (sc.phase != GPIS_PHASE_LAMBERT) return gpis_internal_set_error(GPIS_ENOTSUP, "only the Lambert phase is supported");
+    if (!(sc.box_half > 0.0f) || !(sc.tan_half_fov > 0.0f))
+        return gpis_internal_set_error(GPIS_EINVAL, "box_half and tan_half_fov must be > 0");
+    const gpis_medium_desc *md = gpis_internal_ctx_medium(ctx, sc.medium);
+    if (!md) return gpis_internal_set_error(GPIS_EINVAL, "unknown medium index");
+    const float sa = md->sigma_a * md->density, ss = md->sigma_s * md->density;
+    if (!(ss > 0.0f)) return gpis_internal_set_error(GPIS_ENOTSUP, "the renderer needs a scattering medium (sigma_s > 0)");
+
+    RtMedium M;
+    M.ratio = ss / (sa + ss);
+    M.max_bounces = md->max_bounces;
+    M.seed = md->seed;
+    M.single_realization = md->single_realization;
+    M.global_ctx = md->correlation_context == GPIS_CTX_GLOBAL;
+    M.scene_seed = sc.scene_seed;
+
+    RtScene S;
+    S.sc = sc;
+    for (int i = 0; i < 3; ++i) S.fwd[i] = sc.cam_target[i] - sc.cam_pos[i];
+    hnorm(S.fwd);
+    hcross(S.fwd, sc.cam_up, S.right);
+    hnorm(S.right);
+    hcross(S.right, S.fwd, S.up);
+    hcross(sc.light_u, sc.light_v, S.ln);
+    {
+        float s = S.ln[0] * S.ln[0];
+        s = s + S.ln[1] * S.ln[1];
+        s = s + S.ln[2] * S.ln[2];
+        S.area = std::sqrt(s);
+    }
+    hnorm(S.ln);
+    S.aspect = (float)sc.width / (float)sc.height;
+
+    const uint32_t n_pixels = sc.width * sc.height;
+    const uint32_t target = 1u << 22;
+    const uint32_t ns_chunk = std::max(1u, std::min(sc.spp, target / std::max(1u, n_pixels)));
+    const size_t cap = (size_t)n_pixels * ns_chunk;
+    if (cap > 0xFFFFFFFFull) return gpis_internal_set_error(GPIS_ERANGE, "image too large");
+
+    DevBuf mem;
+    PathRec *paths;
+    float *direct, *acc;
+    Queue q, sq;
+    uint32_t *counts;
+    unsigned long long *dcnt;
+    RT_TRY(mem.alloc(paths, cap), "allocate paths");
+    RT_TRY(mem.alloc(direct, cap * 6), "allocate direct light");
+    RT_TRY(mem.alloc(acc, (size_t)n_pixels * 3), "allocate image");
+    RT_TRY(mem.alloc(counts, 2), "allocate queue counters");
+    RT_TRY(mem.alloc(dcnt, 2), "allocate counters");
+    for (Queue *qq : {&q, &sq}) {
+        const size_t m = qq == &q ? cap : 2 * cap;
+        RT_TRY(mem.alloc(qq->origin_near, m), "allocate queue");
+        RT_TRY(mem.alloc(qq->dir_far, m), "allocate queue");
+        RT_TRY(mem.alloc(qq->prev, m), "allocate queue");
+        RT_TRY(mem.alloc(qq->seeds, m), "allocate queue");
+        RT_TRY(mem.alloc(qq->rec, 2 * m), "allocate queue");
+        RT_TRY(mem.alloc(qq->path, m), "allocate queue");
+        RT_TRY(mem.alloc(qq->payload, m), "allocate queue");
+    }
+    q.count = counts;
+    sq.count = counts + 1;
+    uint32_t *dmedium = nullptr;
+    if (sc.medium != 0) {
+        RT_TRY(mem.alloc(dmedium, 2 * cap), "allocate medium stream");
+        std::vector<uint32_t> h(2 * cap, sc.medium);
+        RT_TRY(cudaMemcpy(dmedium, h.data(), h.size() * 4, cudaMemcpyHostToDevice), "upload medium stream");
+    }
+    cudaStream_t st;
+    RT_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "create stream");
+    struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{st};
+    cudaEvent_t e0, e1;
+    RT_TRY(cudaEventCreate(&e0), "create event");
+    RT_TRY(cudaEventCreate(&e1), "create event");
+    struct EventGuard { cudaEvent_t a, b; ~EventGuard() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{e0, e1};
+    RT_TRY(cudaMemsetAsync(acc, 0, (size_t)n_pixels * 3 * sizeof(float), st), "clear image");
+    RT_TRY(cudaMemsetAsync(dcnt, 0, 2 * sizeof(unsigned long long), st), "clear counters");
+    RT_TRY(cudaEventRecord(e0, st), "record event");
+
+    uint64_t n_dist = 0, n_shadow = 0, n_paths = 0;
+    const unsigned tb = 128;
+    for (uint32_t s0 = 0; s0 < sc.spp; s0 += ns_chunk) {
+        const uint32_t ns = std::min(ns_chunk, sc.spp - s0);
+        const uint32_t n = n_pixels * ns;
+        S.s0 = s0;
+        S.ns = ns;
+        n_paths += n;
+        k_rt_camera<<<(n + tb - 1) / tb, tb, 0, st>>>(S, paths, n);
+        // at most two rounds per bounce (a forward crossing, then an event), plus entry and exit
+        for (uint32_t round = 0; round < 2 * sc.max_bounces + 4; ++round) {
+            RT_TRY(cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), st), "clear queue counters");
+            k_rt_advance<<<(n + tb - 1) / tb, tb, 0, st>>>(S, M, paths, n, q, dcnt);
+            uint32_t nq = 0;
+            RT_TRY(cudaMemcpyAsync(&nq, counts, 4, cudaMemcpyDeviceToHost, st), "read queue");
+            RT_TRY(cudaStreamSynchronize(st), "synchronize");
+            if (nq == 0) {
+                // paths outside the cube were finished by k_rt_advance; none is left inside
+                break;
+            }
+            gpis_flight_soa fin{reinterpret_cast<float *>(q.origin_near), reinterpret_cast<float *>(q.dir_far),
+                                reinterpret_cast<uint32_t *>(q.seeds), reinterpret_cast<float *>(q.prev), dmedium};
+            gpis_result_soa fout{reinterpret_cast<float *>(q.rec)};
+            int rc = gpis_flights_submit(ctx, &fin, &fout, nq, st);
+            if (rc) return rc;
+            n_dist += nq;
+            k_rt_event<<<(nq + tb - 1) / tb, tb, 0, st>>>(S, M, paths, q, nq, sq, direct, dcnt);
+            uint32_t nsq = 0;
+            RT_TRY(cudaMemcpyAsync(&nsq, counts + 1, 4, cudaMemcpyDeviceToHost, st), "read shadow queue");
+            RT_TRY(cudaStreamSynchronize(st), "synchronize");
+            if (nsq) {
+                gpis_flight_soa sin{reinterpret_cast<float *>(sq.origin_near), reinterpret_cast<float *>(sq.dir_far),
+                                    reinterpret_cast<uint32_t *>(sq.seeds), reinterpret_cast<float *>(sq.prev), dmedium};
+                gpis_result_soa sout{reinterpret_cast<float *>(sq.rec)};
+                rc = gpis_flights_submit(ctx, &sin, &sout, nsq, st);
+                if (rc) return rc;
+                n_shadow += nsq;
+                k_rt_shadow<<<(nsq + tb - 1) / tb, tb, 0, st>>>(sq, nsq, direct);
+            }
+            k_rt_collect<<<(nq + tb - 1) / tb, tb, 0, st>>>(paths, q.path, nq, direct);
+        }
+        k_rt_accumulate<<<(n_pixels + tb - 1) / tb, tb, 0, st>>>(paths, n_pixels, ns, acc);
+    }
+    k_rt_finish<<<(n_pixels + tb - 1) / tb, tb, 0, st>>>(acc, n_pixels, sc.spp);
+    RT_TRY(cudaEventRecord(e1, st), "record event");
+    RT_TRY(cudaMemcpyAsync(image_rgb, acc, (size_t)n_pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
+           "read image");
+    unsigned long long hc[2] = {0, 0};
+    RT_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st), "read counters");
+    RT_TRY(cudaStreamSynchronize(st), "synchronize render");
+    RT_TRY(cudaGetLastError(), "render kernels");
+    if (stats) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        stats->paths = n_paths;
+        stats->distance_flights = n_dist;
+        stats->shadow_flights = n_shadow;
+        stats->medium_events = hc[0];
+        stats->failed = hc[1];
+        stats->ms = ms;
+    }
+    return GPIS_OK;
+}

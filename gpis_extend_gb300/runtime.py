@@ -130,6 +130,14 @@ class Context:
         abi.check(self.lib.gpis_nee_host(self.h, ctypes.byref(q), out.ctypes.data, n), "gpis_nee_host")
         return out
 
+    def render(self, scene):
+        """gpis_render: returns (image (h, w, 3) float32, stats dict)."""
+        img = np.zeros((scene.height, scene.width, 3), np.float32)
+        st = abi.RenderStats()
+        abi.check(self.lib.gpis_render(self.h, ctypes.byref(scene), img.ctypes.data, ctypes.byref(st)),
+                  "gpis_render")
+        return img, {k: getattr(st, k) for k, _ in abi.RenderStats._fields_}
+
     def trace_pinned(self, pinned):
         """gpis_flights_trace_host on PinnedFlights (host -> device -> host, synchronous)."""
         soa = pinned.soa()

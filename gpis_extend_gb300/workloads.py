@@ -69,11 +69,12 @@ def sphere_medium(one_d=True, context=abi.CTX_RENEWAL_PLUS, sigma=0.05, length_s
     8 impulses per cell, cell hash seeded 1; 1D sampling with Renewal+ by default
     (the batched-flight microbenchmark), 3D world-space noise with Renewal for the
     image configuration."""
-    return abi.make_medium(sigma=sigma, length_scale=length_scale, kernel_scale=3.0,
-                           impulse_density=impulse_density, seed=seed, one_d_sampling=int(one_d),
-                           correlation_context=context, step_size=step_size, min_step=min_step,
-                           mean_kind=abi.MEAN_SPHERE, mean_params=(0, 0, 0, 1),
-                           sigma_s=0.8, sigma_a=0.2, **kw)
+    params = dict(sigma=sigma, length_scale=length_scale, kernel_scale=3.0,
+                  impulse_density=impulse_density, seed=seed, one_d_sampling=int(one_d),
+                  correlation_context=context, step_size=step_size, min_step=min_step,
+                  mean_kind=abi.MEAN_SPHERE, mean_params=(0, 0, 0, 1), sigma_s=0.8, sigma_a=0.2)
+    params.update(kw)
+    return abi.make_medium(**params)
 
 
 def torus_plane_medium(nonstationary=True, octaves=3, context=abi.CTX_RENEWAL_PLUS, **kw):
@@ -184,3 +185,26 @@ def secondary_flights(primary, rec, desc, seed=7, half=1.5, scene_seed=1):
     b.prev[:, 1:4] = res["grad"][idx]
     b.pss = pss
     return b, idx
+
+
+def render_medium(kind="sphere_3d"):
+    """Media of the image workloads (sigma_a = 0, so sigma_s / sigma_t = 1 and the
+    Lambert albedo carries the surface colour):
+    sphere_3d  the unit-sphere SDF field with 3D world-space noise and Renewal;
+    sphere_1d  the same field with 1D noise and Renewal+;
+    torus      the nonstationary three-octave torus-union-plane field (1D, Renewal+)."""
+    if kind == "sphere_3d":
+        return sphere_medium(one_d=False, context=abi.CTX_RENEWAL, sigma_a=0.0, sigma_s=1.0)
+    if kind == "sphere_1d":
+        return sphere_medium(one_d=True, context=abi.CTX_RENEWAL_PLUS, sigma_a=0.0, sigma_s=1.0)
+    if kind == "torus":
+        return torus_plane_medium(nonstationary=True, octaves=3, sigma_a=0.0, sigma_s=1.0)
+    raise KeyError(kind)
+
+
+def render_scene(width=256, height=256, spp=16, max_bounces=4, box_half=1.5, **kw):
+    """The image workload: pinhole camera at z = 4 looking at the origin (45 degree
+    vertical field of view), a 1 x 1 quad light at y = 3 facing down with radiance
+    20, Lambert albedo 0.8, the medium in the cube [-h, h]^3."""
+    return abi.make_scene(width=width, height=height, spp=spp, max_bounces=max_bounces, box_half=box_half,
+                          light_emission=(20.0, 20.0, 20.0), albedo=(0.8, 0.8, 0.8), **kw)

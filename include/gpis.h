@@ -341,6 +341,57 @@ int gpis_se_splat_1d(const float *queries, const float *centers, float *values,
 int gpis_flights_submit_static(const gpis_medium_desc *medium, const gpis_flight_soa *in,
                                const gpis_result_soa *out, uint32_t n, void *cuda_stream);
 
+/* ---- wavefront path tracer around the medium (images) -------------------
+ * The subset of PathTracer::traceSample (PathTracer.cpp:49-292) that the image
+ * workloads use: a pinhole camera, the medium inside the cube [-h, h]^3 (a
+ * forward-scattering boundary: entering and leaving count no bounce), one
+ * one-sided quad light outside the cube, and the GP surface events of
+ * GaussianProcessMedium::sampleDistance shaded by BRDFPhaseFunction over a
+ * Lambert BSDF (BRDFPhaseFunction.cpp:29-101).  Medium events take volume
+ * direct lighting as TraceBase::handleVolume does (TraceBase.cpp:993-1014,
+ * 798-963): one light sample and one phase sample, each with a transmittance
+ * query through the medium and the power heuristic, with the medium state of
+ * the next bounce.  No Russian roulette; no environment light.
+ *
+ * Path decisions draw from a counter RNG keyed (sampler_seed, path, bounce,
+ * dimension) with path = (y * width + x) * spp + sample; directions are sampled
+ * without trigonometry (rejection in the unit disk), so the CUDA path and the
+ * CPU restatement make the same decisions.  GP seeds follow the reference:
+ * pixelSampleSegment = (x, y, sample, bounce), sceneSeed = scene_seed.       */
+#define GPIS_PHASE_LAMBERT 0u
+
+typedef struct {
+    uint32_t width, height, spp, max_bounces;
+    float cam_pos[3];
+    float cam_target[3];
+    float cam_up[3];
+    float tan_half_fov;         /* tangent of half the vertical field of view    */
+    float box_half;             /* the medium fills the cube [-h, h]^3            */
+    float light_center[3];
+    float light_u[3];           /* the quad is center + s*u + t*v, |s|,|t| <= 1/2 */
+    float light_v[3];
+    float light_emission[3];    /* radiance emitted toward u x v                  */
+    uint32_t phase;             /* GPIS_PHASE_LAMBERT                             */
+    float albedo[3];
+    uint32_t scene_seed;
+    uint32_t sampler_seed;
+    uint32_t medium;            /* medium index in the context                    */
+    uint32_t reserved_;
+} gpis_scene_desc;
+
+typedef struct {
+    uint64_t paths;
+    uint64_t distance_flights;  /* sampleDistance flights                         */
+    uint64_t shadow_flights;    /* transmittance flights of direct lighting       */
+    uint64_t medium_events;
+    uint64_t failed;            /* paths ended by a failed medium or phase sample */
+    double ms;                  /* device time of the render (CUDA events)        */
+} gpis_render_stats;
+
+/* Render into image_rgb (host, height x width x 3 floats, row 0 at the top):
+ * the mean radiance of spp paths per pixel.  Blocking.                       */
+int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *image_rgb, gpis_render_stats *stats);
+
 /* Last error message of the calling thread ("" when none). */
 const char *gpis_last_error(void);
 

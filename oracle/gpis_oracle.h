@@ -90,6 +90,11 @@ int gor_medium_sample_distance(const gpis_medium_desc *desc, const gpis_ray *ray
 int gor_medium_transmittance(const gpis_medium_desc *desc, const gpis_ray *rays, gpis_medium_state *states,
                              const float *jitter, float *transmittance, uint32_t n);
 
+/* Path tracer restatement (gpis_render): rows [row0, row0 + rows) of the image;
+ * counts[4] += {distance flights, shadow flights, medium events, failed paths}. */
+int gor_render(const gpis_medium_desc *md, const gpis_scene_desc *sc, float *image, uint64_t counts[4],
+               uint32_t row0, uint32_t rows);
+
 /* Elementwise SE splat in FP64 (the SeSplat1DTest expectation, SeSplat1DTest.cpp:72-84). */
 void gor_se_splat_1d(const float *q, const float *c, uint32_t n, float scale,
                      double *values, double *derivatives);

@@ -21,7 +21,7 @@ _lib = None
 
 def build(force=False):
     """Compile the oracle with its Makefile (no reference sources needed)."""
-    src = [os.path.join(HERE, "gpis_oracle.c"), os.path.join(HERE, "gpis_oracle.h"),
+    src = [os.path.join(HERE, "gpis_oracle.c"), os.path.join(HERE, "pt_oracle.c"), os.path.join(HERE, "gpis_oracle.h"),
            os.path.join(os.path.dirname(HERE), "include", "gpis.h")]
     stale = not os.path.exists(LIB_PATH) or any(
         os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in src)
@@ -57,6 +57,7 @@ def lib():
                 "gor_se_splat_1d": (None, [vp, vp, u32, ctypes.c_float, vp, vp]),
                 "gor_medium_sample_distance": (c_int, [M, vp, vp, vp, vp, u32]),
                 "gor_medium_transmittance": (c_int, [M, vp, vp, vp, vp, u32]),
+                "gor_render": (c_int, [M, ctypes.POINTER(abi.SceneDesc), vp, vp, u32, u32]),
             }
             for k, (r, a) in sigs.items():
                 f = getattr(L, k)
@@ -200,3 +201,27 @@ def medium_transmittance(desc, rays, states, jitter):
     if rc:
         raise abi.GpisError(f"oracle transmittance failed: {rc}", rc)
     return tr
+
+
+def render(desc, scene, n_threads=0):
+    """The path tracer restatement: returns (image (h, w, 3) float32, counts dict).
+    Rows are split over a thread pool (the C code releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    h, w = scene.height, scene.width
+    img = np.zeros((h, w, 3), np.float32)
+    n_threads = n_threads or os.cpu_count() or 1
+    chunks = [(r, min(h, r + max(1, h // (4 * n_threads)))) for r in range(0, h, max(1, h // (4 * n_threads)))]
+    counts = np.zeros((len(chunks), 4), np.uint64)
+    L = lib()
+
+    def run(k):
+        r0, r1 = chunks[k]
+        rc = L.gor_render(ctypes.byref(desc), ctypes.byref(scene), _p(img), _p(counts[k]), r0, r1 - r0)
+        if rc:
+            raise abi.GpisError(f"oracle render failed: {rc}", rc)
+
+    with ThreadPoolExecutor(n_threads) as ex:
+        list(ex.map(run, range(len(chunks))))
+    c = counts.sum(axis=0)
+    return img, {"distance_flights": int(c[0]), "shadow_flights": int(c[1]), "medium_events": int(c[2]),
+                 "failed": int(c[3])}
