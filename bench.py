@@ -9,6 +9,14 @@ conditioned secondary flights reflected at every primary hit.  Inputs are
 seeded synthetic data generated once; every step re-traces all flights.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py --workload image0|image2 [--size S] [--spp P] [--steps K]
+
+The image workloads render with gpis_render (the wavefront path tracer around
+the medium) and report the flights traced per second of render:
+image0 = 256 x 256, 16 spp, 4 bounces, the sphere field with 3D noise and
+Renewal, Lambert albedo 0.8, a 1 x 1 quad light at y = 3; image2 = 1024 x 1024,
+256 spp, 8 bounces, the nonstationary three-octave torus-union-plane field with
+1D noise and Renewal+ (Lambert; the mirror conductor is not built).
 
 Prints one JSON line (rank 0).  `value` is device-resident throughput (flights/s,
 inputs already in HBM, 512 MiB of flight streams > L2 so no flush is needed);
@@ -192,6 +200,98 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+IMAGE_WORKLOADS = {
+    "image0": dict(medium="sphere_3d", size=256, spp=16, bounces=4,
+                   text="image render: 256x256 pinhole at z=4, 16 spp, 4 bounces, sphere SDF field, 3D SE noise "
+                        "sigma 0.05 l 0.1 N 8, Renewal, Lambert albedo 0.8, 1x1 quad light at y=3"),
+    "image2": dict(medium="torus", size=1024, spp=256, bounces=8,
+                   text="image render: 1024x1024, 256 spp, 8 bounces, torus (R 1, r 0.35) union plane y=-0.5, "
+                        "l(p)=0.11+0.09 sin3x cos2z, 3 octaves sigma 0.04/0.02/0.01, 1D noise, Renewal+, "
+                        "Lambert albedo 0.8 (mirror conductor not built), 1x1 quad light at y=3"),
+}
+
+
+def run_image(args):
+    """An image workload: flights/s during gpis_render, device time (CUDA events in the
+    renderer) and host wall time around the call (e2e)."""
+    import torch
+    from gpis_extend_gb300 import build, roofline, runtime, workloads
+    from oracle import oracle
+    cfg = IMAGE_WORKLOADS[args.workload]
+    size = args.size or cfg["size"]
+    spp = args.spp or cfg["spp"]
+    build.build()
+    desc = workloads.render_medium(cfg["medium"])
+    sc = workloads.render_scene(width=size, height=size, spp=spp, max_bounces=cfg["bounces"])
+    ctx = runtime.Context(desc)
+    for _ in range(args.warmup):
+        ctx.render(workloads.render_scene(width=64, height=64, spp=1, max_bounces=cfg["bounces"]))
+    ctx.counters(reset=True)
+    ctx.profile_read(reset=True)
+    ctx.profile(True)
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    dev_ms, flights, wall, launches = 0.0, 0, 0.0, 0
+    img = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        img, st = ctx.render(sc)
+        wall += time.perf_counter() - t0
+        dev_ms += st["ms"]
+        flights += st["distance_flights"] + st["shadow_flights"]
+        launches += st["launches"]
+    clocks.stop()
+    ctx.profile(False)
+    kms, klaunch = ctx.profile_read(reset=True)
+    cnt = ctx.counters(reset=True)
+    value = flights / (dev_ms * 1e-3)
+    one_d = bool(desc.one_d_sampling)
+    n_imp = int(desc.impulse_density)
+    oct_factor = int(desc.n_octaves) if one_d else 1
+    fpe = (roofline.flops_per_eval_1d(n_imp) * oct_factor) if one_d else roofline.flops_per_eval_3d(n_imp)
+    evals = cnt["steps"] + cnt["refine_evals"] + cnt["flights"] + (cnt["flights"] - cnt["hits"])
+    achieved = evals * fpe / (kms[1] * 1e-3) / 1e12 if kms[1] > 0 else None
+    peak = sgemm_peak_tflops(torch)
+    # CPU baseline: the restatement renders rows through the middle of the same image
+    # on all cores, as many as fit in about 10 s (one row first to size the sample)
+    cores = os.cpu_count() or 1
+    mid = size // 2
+    t0 = time.perf_counter()
+    oracle.render_rows(desc, sc, mid, 1)
+    t1 = time.perf_counter() - t0
+    rows = int(max(1, min(size // 2, cores * max(1, round(args.cpu_seconds / max(t1, 1e-3))))))
+    row0 = max(0, mid - rows // 2)
+    t0 = time.perf_counter()
+    _, cc = oracle.render_rows(desc, sc, row0, rows)
+    cdt = time.perf_counter() - t0
+    cpu_flights = cc["distance_flights"] + cc["shadow_flights"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": cfg["text"], "width": size, "height": size, "spp": spp,
+                   "max_bounces": cfg["bounces"], "arm": "plain", "paths_per_step": size * size * spp,
+                   "flights_per_step": flights // args.steps},
+        "e2e": {"value": flights / wall, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": size * size * 3 * 4},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
+                     "kernel": "k_march (fast + resume passes) inside gpis_render",
+                     "flops_per_eval": fpe, "evals": evals, "march_ms": kms[1],
+                     "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, best of 5, measured in this run"},
+        "image": {"mean": float(img.mean()), "max": float(img.max())},
+        "counters": {k: v for k, v in cnt.items() if k != "reserved"},
+        "clocks": clocks.summary(),
+        "cpu_baseline": {"value": cpu_flights / cdt, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"rows {row0}-{row0 + rows - 1} of the same image and spp (through its "
+                                   f"middle), pt_oracle.c on {cores} threads, {cpu_flights} flights in {cdt:.1f} s"},
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -201,12 +301,19 @@ def main():
     ap.add_argument("--flights", type=int, default=1 << 22)
     ap.add_argument("--ref-sample", type=int, default=1 << 16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="flights", choices=["flights", "image0", "image2"])
+    ap.add_argument("--size", type=int, default=0)
+    ap.add_argument("--spp", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     world, rank, local = dist_env()
 
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload != "flights":
+        run_image(args)
         return
 
     import torch

@@ -164,7 +164,7 @@ class SceneDesc(ctypes.Structure):
 class RenderStats(ctypes.Structure):
     _fields_ = [("paths", ctypes.c_uint64), ("distance_flights", ctypes.c_uint64),
                 ("shadow_flights", ctypes.c_uint64), ("medium_events", ctypes.c_uint64),
-                ("failed", ctypes.c_uint64), ("ms", ctypes.c_double)]
+                ("failed", ctypes.c_uint64), ("ms", ctypes.c_double), ("launches", ctypes.c_uint64)]
 
 
 def make_scene(width=64, height=64, spp=4, max_bounces=4, fov_deg=45.0, cam_pos=(0, 0, 4), cam_target=(0, 0, 0),

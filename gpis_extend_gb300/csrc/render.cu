@@ -670,7 +670,11 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     RT_TRY(cudaMemsetAsync(dcnt, 0, 2 * sizeof(unsigned long long), st), "clear counters");
     RT_TRY(cudaEventRecord(e0, st), "record event");
 
-    uint64_t n_dist = 0, n_shadow = 0, n_paths = 0;
+    uint64_t n_dist = 0, n_shadow = 0, n_paths = 0, n_launch = 0;
+    // a flight batch is 4 kernels (prepare, fast pass, resume pass, finish), 3 without conditioning
+    const bool conditions = !md->single_realization && (md->correlation_context == GPIS_CTX_RENEWAL ||
+                                                         md->correlation_context == GPIS_CTX_RENEWAL_PLUS);
+    const uint64_t per_batch = conditions ? 4 : 3;
     const unsigned tb = 128;
     for (uint32_t s0 = 0; s0 < sc.spp; s0 += ns_chunk) {
         const uint32_t ns = std::min(ns_chunk, sc.spp - s0);
@@ -679,10 +683,12 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
         S.ns = ns;
         n_paths += n;
         k_rt_camera<<<(n + tb - 1) / tb, tb, 0, st>>>(S, paths, n);
+        n_launch += 1;
         // at most two rounds per bounce (a forward crossing, then an event), plus entry and exit
         for (uint32_t round = 0; round < 2 * sc.max_bounces + 4; ++round) {
             RT_TRY(cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), st), "clear queue counters");
             k_rt_advance<<<(n + tb - 1) / tb, tb, 0, st>>>(S, M, paths, n, q, dcnt);
+            n_launch += 1;
             uint32_t nq = 0;
             RT_TRY(cudaMemcpyAsync(&nq, counts, 4, cudaMemcpyDeviceToHost, st), "read queue");
             RT_TRY(cudaStreamSynchronize(st), "synchronize");
@@ -697,6 +703,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
             if (rc) return rc;
             n_dist += nq;
             k_rt_event<<<(nq + tb - 1) / tb, tb, 0, st>>>(S, M, paths, q, nq, sq, direct, dcnt);
+            n_launch += per_batch + 1;
             uint32_t nsq = 0;
             RT_TRY(cudaMemcpyAsync(&nsq, counts + 1, 4, cudaMemcpyDeviceToHost, st), "read shadow queue");
             RT_TRY(cudaStreamSynchronize(st), "synchronize");
@@ -708,12 +715,16 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
                 if (rc) return rc;
                 n_shadow += nsq;
                 k_rt_shadow<<<(nsq + tb - 1) / tb, tb, 0, st>>>(sq, nsq, direct);
+                n_launch += per_batch + 1;
             }
             k_rt_collect<<<(nq + tb - 1) / tb, tb, 0, st>>>(paths, q.path, nq, direct);
+            n_launch += 1;
         }
         k_rt_accumulate<<<(n_pixels + tb - 1) / tb, tb, 0, st>>>(paths, n_pixels, ns, acc);
+        n_launch += 1;
     }
     k_rt_finish<<<(n_pixels + tb - 1) / tb, tb, 0, st>>>(acc, n_pixels, sc.spp);
+    n_launch += 1;
     RT_TRY(cudaEventRecord(e1, st), "record event");
     RT_TRY(cudaMemcpyAsync(image_rgb, acc, (size_t)n_pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
            "read image");
@@ -730,6 +741,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
         stats->medium_events = hc[0];
         stats->failed = hc[1];
         stats->ms = ms;
+        stats->launches = n_launch;
     }
     return GPIS_OK;
 }

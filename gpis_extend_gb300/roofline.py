@@ -25,10 +25,11 @@ def flops_per_eval_1d(impulses_per_cell):
 
 
 def flops_per_eval_3d(impulses_per_cell):
-    # 27 cells x N impulses x (4 pi / 3) / 27 inside; ~20 flops per inside impulse
-    # (3 differences, quadratic form, exp, value + gradient accumulate) + 60 overhead.
-    inside = 27 * impulses_per_cell * 0.155
-    return inside * 20 + 60
+    # every impulse of the 27 cells: 3 differences and the squared length (5 flops);
+    # the (4 pi / 3) / 27 = 0.155 inside: ~20 flops (scaled differences, quadratic
+    # form, exp, weighted accumulate); 60 flops of overhead (evaluateNoise3D).
+    impulses = 27 * impulses_per_cell
+    return impulses * 5 + impulses * 0.155 * 20 + 60
 
 
 # Flight record traffic: 4 input streams of 16 B and 2 result records of 16 B.

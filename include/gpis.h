@@ -386,6 +386,7 @@ typedef struct {
     uint64_t medium_events;
     uint64_t failed;            /* paths ended by a failed medium or phase sample */
     double ms;                  /* device time of the render (CUDA events)        */
+    uint64_t launches;          /* kernels launched by the render                 */
 } gpis_render_stats;
 
 /* Render into image_rgb (host, height x width x 3 floats, row 0 at the top):

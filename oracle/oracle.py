@@ -225,3 +225,25 @@ def render(desc, scene, n_threads=0):
     c = counts.sum(axis=0)
     return img, {"distance_flights": int(c[0]), "shadow_flights": int(c[1]), "medium_events": int(c[2]),
                  "failed": int(c[3])}
+
+
+def render_rows(desc, scene, row0, rows, n_threads=0):
+    """Rows [row0, row0 + rows) of the restatement's image of the full scene (the CPU
+    baseline's bounded sample); returns (rows, counts dict)."""
+    from concurrent.futures import ThreadPoolExecutor
+    h, w = scene.height, scene.width
+    img = np.zeros((h, w, 3), np.float32)
+    n_threads = n_threads or os.cpu_count() or 1
+    counts = np.zeros((rows, 4), np.uint64)
+    L = lib()
+
+    def run(k):
+        rc = L.gor_render(ctypes.byref(desc), ctypes.byref(scene), _p(img), _p(counts[k]), row0 + k, 1)
+        if rc:
+            raise abi.GpisError(f"oracle render failed: {rc}", rc)
+
+    with ThreadPoolExecutor(n_threads) as ex:
+        list(ex.map(run, range(rows)))
+    c = counts.sum(axis=0)
+    return img[row0:row0 + rows], {"distance_flights": int(c[0]), "shadow_flights": int(c[1]),
+                                   "medium_events": int(c[2]), "failed": int(c[3])}
