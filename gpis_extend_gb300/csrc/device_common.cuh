@@ -74,6 +74,8 @@ struct DevMedium {
     float oct_sigma[4];
     float oct_scale[4];
     uint32_t oct_seed[4];
+    float oct_inv[4];       // 1 / oct_scale[k], exact where the scale is a power of two
+    uint32_t oct_pow2;      // bit k: oct_scale[k] is a power of two (x / s == x * oct_inv[k])
 };
 
 struct PcgJump {

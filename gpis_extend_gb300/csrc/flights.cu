@@ -1125,6 +1125,170 @@ struct EvalCoop1D {
     }
 };
 
+// 1D evaluator for media with several octaves (and any length scale): each
+// octave's three-cell impulse window (8 impulses per cell) lives in shared
+// memory, 96 floats per lane, laid out [octave][cell slot][k / 4][lane] in
+// float4 so that a warp's loads are contiguous.  A ring index per octave turns
+// a one-cell move into one refill; refills are warp-cooperative as in
+// EvalCoop1D, with the producing lane writing the impulse straight into the
+// owner's slot.  Every lane of the warp must call value().
+constexpr int kOctMax = 4;
+constexpr int kOctThreads = 256;
+constexpr size_t kSmemOct = (size_t)kOctMax * 3 * 8 * sizeof(float) * kOctThreads;
+
+struct EvalCoopOct {
+    static constexpr bool kCollective = true;
+    static constexpr int kMinBlocks = 2;
+    static constexpr bool kGeneral = true;
+    float *cbase;           // float index ((o * 3 + slot) * 8 + k) maps to cbase[(((o*3+slot)*2 + k/4)*256 + tid)*4 + k%4]
+    int base[kOctMax];
+    int rot[kOctMax];
+    uint32_t valid;         // bit o: octave o's window is filled
+    const PcgJump *sj;
+
+    __device__ __forceinline__ void reset() { valid = 0u; }
+    __device__ __forceinline__ void bind(const PcgJump *t)
+    {
+        extern __shared__ float4 dsm_oct[];
+        cbase = reinterpret_cast<float *>(dsm_oct);
+        sj = t;
+    }
+    __device__ __forceinline__ float *slot_ptr(int tid, int o, int slot, int k) const
+    {
+        return cbase + ((((o * 3 + slot) * 2 + (k >> 2)) * kOctThreads + tid) << 2) + (k & 3);
+    }
+
+    // cooperative generation of one cell per requesting lane into its ring slot
+    __device__ __forceinline__ void fill(bool need, int cell, uint32_t seed, int o, int slot, int lane, uint32_t n_imp)
+    {
+        unsigned mask = __ballot_sync(FULL, need);
+        const int rq = lane >> 3;
+        const int k = lane & 7;
+        const int warp0 = threadIdx.x & ~31;
+        while (mask) {
+            unsigned pass = 0u, mm = mask;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                pass |= mm & (0u - mm);
+                mm &= mm - 1u;
+            }
+            mask = mm;
+            unsigned pm = pass;
+            for (int r = 0; r < rq; ++r) pm &= pm - 1u;
+            const int owner = pm ? __ffs(pm) - 1 : 0;
+            const int ocell = __shfl_sync(FULL, cell, owner);
+            const uint32_t oseed = __shfl_sync(FULL, seed, owner);
+            const int oslot = __shfl_sync(FULL, slot, owner);
+            const uint32_t onimp = __shfl_sync(FULL, n_imp, owner);
+            if (pm != 0u) {
+                float v = __int_as_float(0x7f800000);
+                if ((uint32_t)k < onimp) {
+                    const uint32_t s = xxhash2((uint32_t)ocell, oseed) + 1u;
+                    const uint32_t r1 = pcg_draw(sj[2 + 2 * k], s);
+                    const uint32_t r2 = pcg_draw(sj[3 + 2 * k], s);
+                    v = __uint_as_float(__float_as_uint(unit_float(r1)) | (~r2 & 0x80000000u));
+                }
+                *slot_ptr(warp0 + owner, o, oslot, k) = v;
+            }
+        }
+        __syncwarp();
+    }
+
+    __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
+                                           int &id, uint32_t &refills, bool live)
+    {
+        const int lane = threadIdx.x & 31;
+        const DevMedium &m = *L.m;
+        const int n_oct = live ? (int)m.n_oct : 0;
+        const float ls = live ? ns_scale(m, px, pz) : 1.0f;
+        const float kexp = L.kexp / (ls * ls);
+        const float inv_norm = inv_norm_1d(m, ls);
+        const float ca = splat_cov_1d(ls, L.ls_o);
+        // the isotropic position (divided by the maximum lateral scale) once; each
+        // octave divides it by its length multiplier, a multiply when that is a
+        // power of two (the same rounding as ray_coord_oct's division)
+        float bx = __fmul_rn(m.l_inv[0], px), by = __fmul_rn(m.l_inv[1], py), bz = __fmul_rn(m.l_inv[2], pz);
+        if (m.ls_kind) {
+            bx = __fdiv_rn(bx, m.ls_max);
+            by = __fdiv_rn(by, m.ls_max);
+            bz = __fdiv_rn(bz, m.ls_max);
+        }
+        float total = 0.0f;
+        const int warp_oct = __reduce_max_sync(FULL, (unsigned)n_oct);
+#pragma unroll
+        for (int o = 0; o < kOctMax; ++o) {
+            if (o >= warp_oct) break;
+            const bool act = o < n_oct;
+            const float sc = act ? oct_scale(m, o) : 1.0f;
+            float qx = bx, qy = by, qz = bz;
+            if (sc != 1.0f) {
+                if ((m.oct_pow2 >> o) & 1u) {
+                    const float inv = m.oct_inv[o];
+                    qx = __fmul_rn(qx, inv); qy = __fmul_rn(qy, inv); qz = __fmul_rn(qz, inv);
+                } else {
+                    qx = __fdiv_rn(qx, sc); qy = __fdiv_rn(qy, sc); qz = __fdiv_rn(qz, sc);
+                }
+            }
+            const float z = act ? dot3_rn(L.n[0], L.n[1], L.n[2], qx, qy, qz) : 0.0f;
+            const float tg = __fdiv_rn(z, L.kr);
+            const float fl = floorf(tg);
+            const float frac = __fsub_rn(tg, fl);
+            const int ci = (int)fl;
+            const bool ok = (valid >> o) & 1u;
+            const bool changed = act && (!ok || ci != base[o]);
+            const bool up = changed && ok && ci == base[o] + 1;
+            const bool down = changed && ok && ci == base[o] - 1;
+            const bool full = changed && !up && !down;
+            const uint32_t seed = L.seed + oct_seed(m, o);
+            int r = rot[o];
+            if (up) r = r == 2 ? 0 : r + 1;          // the old middle becomes the low cell
+            if (down) r = r == 0 ? 2 : r - 1;
+            if (full) r = 0;
+            // logical cell j (0: ci - 1, 1: ci, 2: ci + 1) sits in slot (r + j) mod 3
+            const int s0 = r, s1 = r == 2 ? 0 : r + 1, s2 = r == 0 ? 2 : r - 1;
+            fill(full || down, ci - 1, seed, o, s0, lane, L.n_imp);
+            fill(full, ci, seed, o, s1, lane, L.n_imp);
+            fill(full || up, ci + 1, seed, o, s2, lane, L.n_imp);
+            if (changed) {
+                base[o] = ci;
+                rot[o] = r;
+                valid |= 1u << o;
+                refills += full ? 3u : 1u;
+            }
+            if (!act) continue;
+            float acc0 = 0.0f, acc1 = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float tl = __fsub_rn(frac, (float)(c - 1));
+                const int slot = c == 0 ? s0 : (c == 1 ? s1 : s2);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float4 q4 = *reinterpret_cast<const float4 *>(slot_ptr(threadIdx.x, o, slot, 4 * h));
+                    const float qs[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const float sgn = qs[j];
+                        const float tp = __fsub_rn(tl, fabsf(sgn));
+                        const float e = ex2_approx(kexp * (tp * tp));
+                        const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(sgn) & 0x80000000u));
+                        if (j & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
+                        else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
+                    }
+                }
+            }
+            float nk = (acc0 + acc1) * inv_norm;
+            if (L.cond) {
+                float vs, gz, oz;
+                lane_cond_1d(L, o, sc, vs, gz, oz);
+                const Cov1D kc = cov1d(z - oz, ca);
+                nk += vs * kc.k0 + gz * kc.k1;
+            }
+            total += (m.n_oct == 1 ? L.sigma : oct_sigma(m, o)) * nk;
+        }
+        return total + lane_mean(L, px, py, pz, id);
+    }
+};
+
 // Phases of a lane's flight.  The fast evaluator marches; a precise evaluation
 // re-decides every step whose fast value is within the band of zero or changed
 // sign, evaluates the step before a crossing (when that one was fast) and every
@@ -1769,7 +1933,12 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     };
     if (ev) cudaEventRecord(ev[2], stream);
     const bool coop = a.one_d && a.max_imp <= 8 && a.max_oct == 1;
-    if (coop && a.any_ns) {
+    if (a.one_d && a.max_imp <= 8 && a.max_oct > 1) {
+        const void *fn = (const void *)k_march<EvalCoopOct, false>;
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemOct);
+        if (e != cudaSuccess) return e;
+        k_march<EvalCoopOct, false><<<grid(fn, kSmemOct), 256, kSmemOct, stream>>>(a);
+    } else if (coop && a.any_ns) {
         const void *fn = (const void *)k_march<EvalCoop1D<8, false, true>, false>;
         k_march<EvalCoop1D<8, false, true>, false><<<grid(fn), 256, 0, stream>>>(a);
     } else if (coop && a.all_grid) {

@@ -155,6 +155,10 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         m.oct_sigma[k] = on ? d.octave_sigma[k] : 0.0f;
         m.oct_scale[k] = on ? d.octave_scale[k] : 1.0f;
         m.oct_seed[k] = on ? d.octave_seed[k] : 0u;
+        int ex = 0;
+        const bool pow2 = std::frexp(m.oct_scale[k], &ex) == 0.5f;
+        m.oct_inv[k] = 1.0f / m.oct_scale[k];
+        if (pow2) m.oct_pow2 |= 1u << k;
     }
     m.step_size = d.step_size;
     m.min_step = d.min_step;
