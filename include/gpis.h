@@ -341,6 +341,24 @@ int gpis_se_splat_1d(const float *queries, const float *centers, float *values,
 int gpis_flights_submit_static(const gpis_medium_desc *medium, const gpis_flight_soa *in,
                                const gpis_result_soa *out, uint32_t n, void *cuda_stream);
 
+/* ---- asynchronous batch backend -------------------------------------------
+ * The GpRayBatchBackend contract (GpRayBatchBackend.hpp:43-55,
+ * PathTracerSeBatchBackend.cpp:358-397) over flights: gpis_backend_submit
+ * copies the n requests (host streams as gpis_flight_soa) before it returns,
+ * traces them on the backend's own stream and, when the n result records are
+ * in out_rec (host memory the caller keeps until then), calls done(user,
+ * status) once: status GPIS_OK, or an error code with out_rec untouched (the
+ * caller may then trace the requests on the CPU).  done runs on a CUDA
+ * callback thread or the backend's dispatcher thread and must not call CUDA.
+ * Batches complete in submission order.  One dispatcher thread per backend;
+ * submit is thread-safe.  gpis_backend_destroy waits for every batch.      */
+typedef struct gpis_backend gpis_backend;
+typedef void (*gpis_batch_done_fn)(void *user, int status);
+int gpis_backend_create(const gpis_medium_desc *media, int n_media, gpis_backend **out);
+void gpis_backend_destroy(gpis_backend *backend);
+int gpis_backend_submit(gpis_backend *backend, const gpis_flight_soa *in, float *out_rec, uint32_t n,
+                        gpis_batch_done_fn done, void *user);
+
 /* ---- wavefront path tracer around the medium (images) -------------------
  * The subset of PathTracer::traceSample (PathTracer.cpp:49-292) that the image
  * workloads use: a pinhole camera, the medium inside the cube [-h, h]^3 (a
