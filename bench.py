@@ -250,7 +250,7 @@ def run_image(args):
     n_imp = int(desc.impulse_density)
     oct_factor = int(desc.n_octaves) if one_d else 1
     fpe = (roofline.flops_per_eval_1d(n_imp) * oct_factor) if one_d else roofline.flops_per_eval_3d(n_imp)
-    evals = cnt["steps"] + cnt["refine_evals"] + cnt["flights"] + (cnt["flights"] - cnt["hits"])
+    evals = cnt["steps"] - cnt["skipped_steps"] + cnt["refine_evals"] + cnt["flights"] + (cnt["flights"] - cnt["hits"])
     achieved = evals * fpe / (kms[1] * 1e-3) / 1e12 if kms[1] > 0 else None
     peak = sgemm_peak_tflops(torch)
     # CPU baseline: the restatement renders rows through the middle of the same image
@@ -282,7 +282,7 @@ def run_image(args):
                      "flops_per_eval": fpe, "evals": evals, "march_ms": kms[1],
                      "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, best of 5, measured in this run"},
         "image": {"mean": float(img.mean()), "max": float(img.max())},
-        "counters": {k: v for k, v in cnt.items() if k != "reserved"},
+        "counters": cnt,
         "clocks": clocks.summary(),
         "cpu_baseline": {"value": cpu_flights / cdt, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"rows {row0}-{row0 + rows - 1} of the same image and spp (through its "
@@ -405,7 +405,8 @@ def main():
     # ---- roofline of the march kernel ------------------------------------------
     march_launches = max(1, klaunch[1])
     march_ms = kms[1] / march_launches
-    evals_march = cnt["steps"] + cnt["refine_evals"] + cnt["flights"] + (cnt["flights"] - cnt["hits"])
+    evals_march = (cnt["steps"] - cnt["skipped_steps"] + cnt["refine_evals"] + cnt["flights"]
+                   + (cnt["flights"] - cnt["hits"]))
     flops = evals_march * roofline.flops_per_eval_1d(8) / march_launches
     achieved = flops / (march_ms * 1e-3) / 1e12
     peak = sgemm_peak_tflops(torch) if rank == 0 else None
@@ -432,7 +433,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": args.steps * 2 * 3,
         "roofline": roof,
-        "counters": {k: v for k, v in cnt.items() if k != "reserved"},
+        "counters": cnt,
         "clocks": clocks.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

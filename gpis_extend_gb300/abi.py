@@ -201,7 +201,7 @@ class NeeSoA(ctypes.Structure):
 class Counters(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint64) for name in
                 ("flights", "steps", "refine_evals", "hits", "step_limit", "invalid",
-                 "cell_refills", "reserved")]
+                 "cell_refills", "skipped_steps")]
 
 
 def medium_defaults():

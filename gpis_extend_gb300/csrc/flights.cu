@@ -875,6 +875,7 @@ struct EvalGeneric {
     static constexpr bool kCollective = false;
     static constexpr int kMinBlocks = 2;
     static constexpr bool kGeneral = true;
+    static constexpr bool kSkip = false;
     __device__ __forceinline__ void reset() {}
     __device__ __forceinline__ void bind(const PcgJump *) {}
     __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
@@ -1008,6 +1009,7 @@ struct EvalCoop1D {
     static constexpr bool kCollective = true;
     static constexpr int kMinBlocks = 2;
     static constexpr bool kGeneral = NS;   // stationary, single octave, 1D otherwise
+    static constexpr bool kSkip = !GRID && !NS;
     float cache[3][NMAX];
     int base;
     bool valid;
@@ -1140,6 +1142,7 @@ struct EvalCoopOct {
     static constexpr bool kCollective = true;
     static constexpr int kMinBlocks = 2;
     static constexpr bool kGeneral = true;
+    static constexpr bool kSkip = false;
     float *cbase;           // float index ((o * 3 + slot) * 8 + k) maps to cbase[(((o*3+slot)*2 + k/4)*256 + tid)*4 + k%4]
     int base[kOctMax];
     int rot[kOctMax];
@@ -1353,6 +1356,10 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     int sign0 = 1, gpid = 0;
     FF ta = {0, 0}, fac = {0, 0}, tprev = {0, 0}, ttest = {0, 0};
     uint32_t c_flights = 0, c_steps = 0, c_refine = 0, c_hits = 0, c_limit = 0, c_invalid = 0, c_refills = 0;
+    uint32_t c_skipped = 0;
+    // step skipping (fast pass): the field's Lipschitz constant along this ray and
+    // its truncation-jump allowance, fixed and per step
+    float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
 
     for (;;) {
         const bool need = phase == PH_IDLE && !drained;
@@ -1393,6 +1400,21 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                         if (m.step_size < step) step = m.step_size;
                         t0 = __fadd_rn(near_t, __fmul_rn(step, fl.jitter));
                         max_steps = m.max_steps;
+                        skip_lip = -1.0f;
+                        if (Eval::kSkip && !RESUME && m.skip_mean_lip >= 0.0f) {
+                            // |df/dt| <= mean slope + sigma (noise + conditioning slopes) dz/dt with
+                            // dz/dt = |l_inv o d| (iso units per world unit); a truncated splat
+                            // jumps by at most skip_jump where the query crosses its support, and
+                            // an iso interval of D cells holds at most 2 N (D + 1) such crossings
+                            const float lx = m.l_inv[0] * d[0], ly = m.l_inv[1] * d[1], lz = m.l_inv[2] * d[2];
+                            const float dz = sqrtf(lx * lx + ly * ly + lz * lz) * 1.0001f;
+                            const float sg = fabsf(L.sigma);
+                            const float cslope = L.cond ? 0.42888194f * fabsf(L.vs) + 0.5f * fabsf(L.gsz) : 0.0f;
+                            skip_lip = (m.skip_mean_lip + sg * (m.skip_noise_lip + cslope) * dz) * 1.01f;
+                            const float jn = sg * m.skip_jump * 2.0f * (float)m.n_imp * 1.01f;
+                            skip_j0 = jn * 3.0f;
+                            skip_j1 = jn * (step * dz / m.kr_iso);
+                        }
                         th = near_t;
                         tl = 0.0f;
                         steps = 0;
@@ -1496,16 +1518,39 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 pf_precise = phase == PH_MARCH_P;
                 ff_add(th, tl, step);
                 phase = PH_MARCH;
-                if (!t_less(th, tl, far_t)) {
-                    phase = PH_FAR;
-                    th = far_t;
-                    tl = 0.0f;
-                } else if (steps >= max_steps) {
-                    done = true;
-                    status = GPIS_FLIGHT_STEP_LIMIT;
-                    t_out = far_t;
-                    t_end = {far_t, 0.0f};
-                    c_limit++;
+                // Step skipping: over the next k steps |f(t) - f| <= skip_lip |t - t_j| plus
+                // the jump allowance, so while that stays below |f| (less a margin for the
+                // fast value's error and the reference's float evaluation) every skipped
+                // step has the sign of f and the reference would march past it.  Skipped
+                // steps are counted as marched; the resume pass re-evaluates the step before
+                // a crossing, so no skipped value is ever needed.
+                int skip = 0;
+                if (Eval::kSkip && !RESUME && skip_lip >= 0.0f) {
+                    const float af = fabsf(f) * (1.0f - 1e-6f) - 1e-5f - skip_j0;
+                    const float per = skip_lip * step + skip_j1;
+                    if (af > per) skip = (int)fminf(af / per, 1024.0f);
+                }
+                for (;;) {
+                    if (!t_less(th, tl, far_t)) {
+                        phase = PH_FAR;
+                        th = far_t;
+                        tl = 0.0f;
+                        break;
+                    }
+                    if (steps >= max_steps) {
+                        done = true;
+                        status = GPIS_FLIGHT_STEP_LIMIT;
+                        t_out = far_t;
+                        t_end = {far_t, 0.0f};
+                        c_limit++;
+                        break;
+                    }
+                    if (skip == 0) break;
+                    skip--;
+                    steps++;
+                    c_steps++;
+                    c_skipped++;
+                    ff_add(th, tl, step);
                 }
             }
         } else if (phase == PH_PF) {
@@ -1563,7 +1608,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     // counters: one atomic per warp
     const unsigned long long s0 = warp_sum(c_flights), s1 = warp_sum(c_steps), s2 = warp_sum(c_refine),
                              s3 = warp_sum(c_hits), s4 = warp_sum(c_limit), s5 = warp_sum(c_invalid),
-                             s6 = warp_sum(c_refills);
+                             s6 = warp_sum(c_refills), s7 = warp_sum(c_skipped);
     if (lane == 0 && a.counters) {
         atomicAdd(a.counters + 0, s0);
         atomicAdd(a.counters + 1, s1);
@@ -1572,6 +1617,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
         atomicAdd(a.counters + 4, s4);
         atomicAdd(a.counters + 5, s5);
         atomicAdd(a.counters + 6, s6);
+        atomicAdd(a.counters + 7, s7);
     }
 }
 

@@ -160,6 +160,24 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         m.oct_inv[k] = 1.0f / m.oct_scale[k];
         if (pow2) m.oct_pow2 |= 1u << k;
     }
+    // Lipschitz bounds for step skipping: stationary 1D single-octave media with an
+    // analytic mean whose slope is bounded (SDFs are 1-Lipschitz; a linear mean
+    // has the slope of its scaled normal)
+    m.skip_mean_lip = -1.0f;
+    if (d.one_d_sampling && d.n_octaves == 1 && d.ls_kind == GPIS_LS_CONSTANT) {
+        switch (d.mean_kind) {
+        case GPIS_MEAN_SPHERE: case GPIS_MEAN_TORUS: case GPIS_MEAN_TORUS_PLANE: m.skip_mean_lip = 1.0f; break;
+        case GPIS_MEAN_HOMOGENEOUS: m.skip_mean_lip = 0.0f; break;
+        case GPIS_MEAN_PLANE:
+            m.skip_mean_lip = (float)std::sqrt((double)d.mean_params[0] * d.mean_params[0] +
+                                               (double)d.mean_params[1] * d.mean_params[1] +
+                                               (double)d.mean_params[2] * d.mean_params[2]);
+            break;
+        default: break;
+        }
+    }
+    m.skip_noise_lip = (float)(3.0 * m.n_imp * std::exp(-0.5) / (double)m.norm1d);
+    m.skip_jump = (float)(std::exp(-0.5 * (double)m.kr_iso * m.kr_iso) / (double)m.norm1d);
     m.step_size = d.step_size;
     m.min_step = d.min_step;
     m.max_steps = d.max_steps ? d.max_steps : 16384u;

@@ -164,7 +164,7 @@ typedef struct gpis_counters {
     uint64_t step_limit;
     uint64_t invalid;
     uint64_t cell_refills;      /* impulse-cache cell regenerations                */
-    uint64_t reserved;
+    uint64_t skipped_steps;     /* march steps decided by the field bound, unevaluated */
 } gpis_counters;
 
 typedef struct gpis_ctx gpis_ctx;
