@@ -1298,6 +1298,9 @@ struct EvalCoopOct {
 // refinement point.
 enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE, PH_FAR };
 
+// most march steps one evaluation may skip (fast pass)
+constexpr int kMaxSkip = 8;
+
 // Fast values farther than this from zero have the sign of the precise value
 // (the fast evaluator differs from the precise one by a few 1e-8).
 constexpr float kPreciseBand = 1e-6f;
@@ -1528,7 +1531,9 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 if (Eval::kSkip && !RESUME && skip_lip >= 0.0f) {
                     const float af = fabsf(f) * (1.0f - 1e-6f) - 1e-5f - skip_j0;
                     const float per = skip_lip * step + skip_j1;
-                    if (af > per) skip = (int)fminf(af / per, 1024.0f);
+                    // at most kMaxSkip per evaluation: the lanes of a warp skip different
+                    // counts, so the warp runs the longest lane's loop
+                    if (af > per) skip = (int)fminf(af / per, (float)kMaxSkip);
                 }
                 for (;;) {
                     if (!t_less(th, tl, far_t)) {
