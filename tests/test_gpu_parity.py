@@ -173,8 +173,8 @@ def test_gpu_noise_values_vs_fp64(one_d, context):
     print("worst noise error / tolerance:", worst)
 
 
-def flights_vs_oracle(desc, batch, rec_gpu, check_grad=True):
-    rec_cpu = oracle.trace_flights(desc, batch)
+def flights_vs_oracle(desc, batch, rec_gpu, check_grad=True, media=None):
+    rec_cpu = oracle.trace_flights(media if media is not None else desc, batch)
     g, c = abi.unpack_results(rec_gpu), abi.unpack_results(rec_cpu)
     n = batch.n
     assert np.all(g["status"] == c["status"])
