@@ -547,6 +547,34 @@ __device__ __forceinline__ CondRec make_condition(const DevMedium &m, const Flig
 // ---------------------------------------------------------------------------
 // k_prepare: conditioning coefficients at the origin of secondary flights.
 // ---------------------------------------------------------------------------
+// Per-flight set-up of the stationary cooperative fast pass, computed here with
+// every lane busy instead of inside the march, where it runs for the few lanes
+// that start a flight while the rest of the warp waits.  Four float4 per flight:
+// {frame normal, origin coordinate}, {value scale, gradient scale, step, t0},
+// {skip slope, skip jump, skip jump per step, -}, {seed, flags (1 valid, 2
+// conditioned, 4 first scatter), -, -}.
+enum : uint32_t { SF_VALID = 1u, SF_COND = 2u, SF_FIRST = 4u };
+
+__device__ __forceinline__ void skip_params(const DevMedium &m, const float d[3], float sigma, bool cond, float vs,
+                                            float gsz, float step, float &lip, float &j0, float &j1)
+{
+    // |df/dt| <= mean slope + sigma (noise + conditioning slopes) dz/dt with
+    // dz/dt = |l_inv o d| (iso units per world unit); a truncated splat jumps by at
+    // most skip_jump where the query crosses its support, and an iso interval of
+    // D cells holds at most 2 N (D + 1) such crossings
+    lip = -1.0f;
+    j0 = j1 = 0.0f;
+    if (m.skip_mean_lip < 0.0f) return;
+    const float lx = m.l_inv[0] * d[0], ly = m.l_inv[1] * d[1], lz = m.l_inv[2] * d[2];
+    const float dz = sqrtf(lx * lx + ly * ly + lz * lz) * 1.0001f;
+    const float sg = fabsf(sigma);
+    const float cslope = cond ? 0.42888194f * fabsf(vs) + 0.5f * fabsf(gsz) : 0.0f;
+    lip = (m.skip_mean_lip + sg * (m.skip_noise_lip + cslope) * dz) * 1.01f;
+    const float jn = sg * m.skip_jump * 2.0f * (float)m.n_imp * 1.01f;
+    j0 = jn * 3.0f;
+    j1 = jn * (step * dz / m.kr_iso);
+}
+
 __global__ void __launch_bounds__(128) k_prepare(FlightArgs a)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -554,11 +582,31 @@ __global__ void __launch_bounds__(128) k_prepare(FlightArgs a)
     bool mok;
     const DevMedium &m = *medium_of(a, i, mok);
     const FlightIn fl = load_flight(a, i);
-    if (!mok || !conditioned(m, fl) || !flight_valid(fl)) {
-        a.cond[i] = CondRec{};
+    const bool valid = mok && flight_valid(fl);
+    const bool cond = valid && conditioned(m, fl);
+    CondRec c = {};
+    if (cond) c = make_condition(m, fl);
+    if (a.any_cond) a.cond[i] = c;
+    if (!a.setup) return;
+    float4 *s = a.setup + 4 * (size_t)i;
+    if (!valid || !(m.flags & MF_ONE_D)) {
+        s[3] = make_float4(0.0f, __uint_as_float(0u), 0.0f, 0.0f);
         return;
     }
-    a.cond[i] = make_condition(m, fl);
+    Frame f;
+    ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+    const float ozc = cond ? ray_coord_oct(m, f.n, fl.o[0], fl.o[1], fl.o[2], 1.0f) : 0.0f;
+    const float vs = cond ? c.oct[0].vs : 0.0f, gsz = cond ? c.oct[0].gs[2] : 0.0f;
+    float step = __fdiv_rn(__fsub_rn(fl.far_t, fl.near_t), (float)m.min_step);
+    if (m.step_size < step) step = m.step_size;
+    const float t0 = __fadd_rn(fl.near_t, __fmul_rn(step, fl.jitter));
+    float lip, j0, j1;
+    skip_params(m, fl.d, m.sigma, cond, vs, gsz, step, lip, j0, j1);
+    const uint32_t flags = SF_VALID | (cond ? SF_COND : 0u) | ((fl.flags & GPIS_FLAG_FIRST_SCATTER) ? SF_FIRST : 0u);
+    s[0] = make_float4(f.n[0], f.n[1], f.n[2], ozc);
+    s[1] = make_float4(vs, gsz, step, t0);
+    s[2] = make_float4(lip, j0, j1, 0.0f);
+    s[3] = make_float4(__uint_as_float(fl.noise_seed), __uint_as_float(flags), 0.0f, 0.0f);
 }
 
 // ---------------------------------------------------------------------------
@@ -1387,6 +1435,50 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     if (RESUME) rs = a.resume[idx];
                     if (RESUME && (rs.w >> 28) == 0u) {
                         // finished by the fast pass
+                    } else if (Eval::kSkip && !RESUME && a.setup) {
+                        // the set-up k_prepare computed for this flight
+                        const float4 s0 = a.setup[4 * (size_t)idx], s1 = a.setup[4 * (size_t)idx + 1];
+                        const float4 s2 = a.setup[4 * (size_t)idx + 2], s3 = a.setup[4 * (size_t)idx + 3];
+                        const uint32_t flags = __float_as_uint(s3.y);
+                        if (!mok || !(flags & SF_VALID)) {
+                            write_status(a, idx, 0.0f, 0.0f, 1.0f, 0u, GPIS_FLIGHT_INVALID_INPUT);
+                            a.t_end[idx] = 0.0;
+                            a.resume[idx] = make_uint4(0u, 0u, 0u, 0u);
+                            c_invalid++;
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < 3; ++k) { L.o[k] = fl.o[k]; d[k] = fl.d[k]; L.li[k] = m.l_inv[k]; }
+                            near_t = fl.near_t;
+                            far_t = fl.far_t;
+                            first = (flags & SF_FIRST) != 0;
+                            L.seed = __float_as_uint(s3.x);
+                            L.sigma = m.sigma;
+                            L.cond = (flags & SF_COND) != 0;
+                            L.n[0] = s0.x; L.n[1] = s0.y; L.n[2] = s0.z;
+                            L.ozc = s0.w;
+                            L.vs = s1.x;
+                            L.gsz = s1.y;
+                            L.ns = false;
+                            L.ls_o = 1.0f;
+                            L.mean_kind = m.mean_kind;
+#pragma unroll
+                            for (int k = 0; k < 6; ++k) L.mq[k] = m.mean_params[k];
+                            L.n_imp = m.n_imp;
+                            L.kr = m.kr_iso;
+                            L.kexp = m.kexp1d;
+                            L.inv_norm = m.inv_norm1d;
+                            step = s1.z;
+                            t0 = s1.w;
+                            skip_lip = s2.x;
+                            skip_j0 = s2.y;
+                            skip_j1 = s2.z;
+                            max_steps = m.max_steps;
+                            th = near_t;
+                            tl = 0.0f;
+                            steps = 0;
+                            ev.reset();
+                            phase = PH_F0;
+                        }
                     } else if (!mok || !flight_valid(fl)) {
                         write_status(a, idx, 0.0f, 0.0f, 1.0f, 0u, GPIS_FLIGHT_INVALID_INPUT);
                         a.t_end[idx] = 0.0;
@@ -1404,20 +1496,8 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                         t0 = __fadd_rn(near_t, __fmul_rn(step, fl.jitter));
                         max_steps = m.max_steps;
                         skip_lip = -1.0f;
-                        if (Eval::kSkip && !RESUME && m.skip_mean_lip >= 0.0f) {
-                            // |df/dt| <= mean slope + sigma (noise + conditioning slopes) dz/dt with
-                            // dz/dt = |l_inv o d| (iso units per world unit); a truncated splat
-                            // jumps by at most skip_jump where the query crosses its support, and
-                            // an iso interval of D cells holds at most 2 N (D + 1) such crossings
-                            const float lx = m.l_inv[0] * d[0], ly = m.l_inv[1] * d[1], lz = m.l_inv[2] * d[2];
-                            const float dz = sqrtf(lx * lx + ly * ly + lz * lz) * 1.0001f;
-                            const float sg = fabsf(L.sigma);
-                            const float cslope = L.cond ? 0.42888194f * fabsf(L.vs) + 0.5f * fabsf(L.gsz) : 0.0f;
-                            skip_lip = (m.skip_mean_lip + sg * (m.skip_noise_lip + cslope) * dz) * 1.01f;
-                            const float jn = sg * m.skip_jump * 2.0f * (float)m.n_imp * 1.01f;
-                            skip_j0 = jn * 3.0f;
-                            skip_j1 = jn * (step * dz / m.kr_iso);
-                        }
+                        if (Eval::kSkip && !RESUME)
+                            skip_params(m, d, L.sigma, L.cond, L.vs, L.gsz, step, skip_lip, skip_j0, skip_j1);
                         th = near_t;
                         tl = 0.0f;
                         steps = 0;
@@ -1966,7 +2046,11 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     if (a.n == 0) return cudaSuccess;
     const uint32_t blocks = (a.n + 127) / 128;
     if (ev) cudaEventRecord(ev[0], stream);
-    if (a.any_cond) k_prepare<<<blocks, 128, 0, stream>>>(a);
+    // the stationary cooperative fast pass takes its per-flight set-up from k_prepare
+    const bool coop_plain = a.one_d && a.max_imp <= 8 && a.max_oct == 1 && !a.any_ns && !a.all_grid;
+    FlightArgs b = a;
+    if (!coop_plain) b.setup = nullptr;
+    if (b.any_cond || b.setup) k_prepare<<<blocks, 128, 0, stream>>>(b);
     if (ev) cudaEventRecord(ev[1], stream);
     cudaError_t err = cudaMemsetAsync(a.work, 0, 4 * sizeof(uint32_t), stream);
     if (err != cudaSuccess) return err;

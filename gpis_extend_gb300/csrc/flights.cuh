@@ -40,6 +40,8 @@ struct FlightArgs {
                                 // resume-queue length, resume work, unused
     uint32_t *queue;            // scratch, n flight indices handed to the resume pass
     uint4 *resume;              // scratch, n saved march states
+    float4 *setup;              // scratch, 4 per flight: the fast pass's per-flight set-up, written by
+                                // k_prepare when the stationary cooperative evaluator runs (else unused)
     unsigned long long *counters;  // gpis_counters block (8 x u64)
     int any_cond;               // some medium conditions (run the prepare kernel)
     int one_d;                  // all media use 1D noise

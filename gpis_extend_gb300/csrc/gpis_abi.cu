@@ -205,6 +205,7 @@ struct gpis_ctx {
     gpis::CondRec *d_cond = nullptr;
     double *d_tend = nullptr;
     uint4 *d_resume = nullptr;
+    float4 *d_setup = nullptr;
     uint32_t *d_work = nullptr;
     unsigned long long *d_counters = nullptr;
     size_t cap = 0;
@@ -231,6 +232,7 @@ void release(gpis_ctx *c)
     cudaFree(c->d_cond);
     cudaFree(c->d_tend);
     cudaFree(c->d_resume);
+    cudaFree(c->d_setup);
     cudaFree(c->d_work);
     cudaFree(c->d_counters);
     cudaFree(c->d_stage);
@@ -247,13 +249,16 @@ int ensure_scratch(gpis_ctx *c, size_t n)
     cudaFree(c->d_cond);
     cudaFree(c->d_tend);
     cudaFree(c->d_resume);
+    cudaFree(c->d_setup);
     c->d_cond = nullptr;
     c->d_tend = nullptr;
     c->d_resume = nullptr;
+    c->d_setup = nullptr;
     c->cap = 0;
     CUDA_TRY(cudaMalloc(&c->d_cond, cap * sizeof(gpis::CondRec)), "allocate conditioning scratch");
     CUDA_TRY(cudaMalloc(&c->d_tend, cap * sizeof(double)), "allocate end-parameter scratch");
     CUDA_TRY(cudaMalloc(&c->d_resume, cap * sizeof(uint4)), "allocate resume scratch");
+    CUDA_TRY(cudaMalloc(&c->d_setup, cap * 4 * sizeof(float4)), "allocate set-up scratch");
     c->cap = cap;
     return GPIS_OK;
 }
@@ -421,6 +426,7 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_res
     a.work = ctx->d_work;
     a.queue = nullptr;
     a.resume = ctx->d_resume;
+    a.setup = ctx->d_setup;
     a.counters = ctx->d_counters;
     a.any_cond = ctx->any_cond;
     a.one_d = ctx->all_one_d;
