@@ -193,6 +193,8 @@ namespace gpis {
 int derive_medium_host(const gpis_medium_desc &d, DevMedium &m) { return derive_medium(d, m); }
 }  // namespace gpis
 
+constexpr uint32_t kMaxChunks = 64;  // chunks of gpis_flights_trace_host's pipeline
+
 struct gpis_ctx {
     int device = 0;
     int num_sms = 1;
@@ -213,6 +215,9 @@ struct gpis_ctx {
     char *d_stage = nullptr;
     size_t stage_cap = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;  // gpis_flights_trace_host's copies
+    cudaStream_t stream2 = nullptr;                            // its second compute stream
+    std::vector<cudaEvent_t> ev_chunks;
     // per-kernel event timing (gpis_profile_*)
     std::vector<gpis_medium_desc> host_media;  // host copies for the medium queries
     bool profiling = false;
@@ -239,6 +244,10 @@ void release(gpis_ctx *c)
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     for (cudaEvent_t e : c->ev_pending) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
+    if (c->d2h_stream) cudaStreamDestroy(c->d2h_stream);
+    for (cudaEvent_t e : c->ev_chunks) cudaEventDestroy(e);
     delete c;
 }
 
@@ -381,10 +390,13 @@ int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
             rc = cuda_fail(e, "upload media");
             break;
         }
-        if ((e = cudaMalloc(&c->d_work, 4 * sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(e, "allocate work counters"); break; }
+        if ((e = cudaMalloc(&c->d_work, 4 * kMaxChunks * sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(e, "allocate work counters"); break; }
         if ((e = cudaMalloc(&c->d_counters, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "allocate counters"); break; }
         if ((e = cudaMemset(c->d_counters, 0, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "clear counters"); break; }
         if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(e, "create stream"); break; }
+        if ((e = cudaStreamCreateWithFlags(&c->h2d_stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(e, "create stream"); break; }
+        if ((e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(e, "create stream"); break; }
+        if ((e = cudaStreamCreateWithFlags(&c->d2h_stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(e, "create stream"); break; }
     } while (false);
     if (rc) {
         release(c);
@@ -401,16 +413,13 @@ void gpis_ctx_destroy(gpis_ctx *ctx)
     release(ctx);
 }
 
-int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa *out, uint32_t n,
-                        void *cuda_stream)
+namespace {
+
+// gpis_flights_submit on the scratch slice [offset, offset + n) with its own four
+// work counters, so that batches on different streams may run at the same time
+int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa *out, uint32_t n,
+                 cudaStream_t stream, size_t offset, uint32_t *work)
 {
-    if (!ctx || !in || !out) return fail(GPIS_EINVAL, "null argument");
-    if (n == 0) return GPIS_OK;
-    if (!in->origin_near || !in->dir_far || !in->seeds || !out->rec)
-        return fail(GPIS_EINVAL, "flight streams origin_near, dir_far, seeds and rec are required");
-    if (ctx->any_cond && !in->prev) return fail(GPIS_EINVAL, "conditioning media need the prev stream");
-    int rc = ensure_scratch(ctx, n);
-    if (rc) return rc;
     gpis::FlightArgs a = {};
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
     a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
@@ -421,12 +430,12 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_res
     a.media = ctx->d_media;
     a.n_media = ctx->n_media;
     a.n = n;
-    a.cond = ctx->d_cond;
-    a.t_end = ctx->d_tend;
-    a.work = ctx->d_work;
+    a.cond = ctx->d_cond + offset;
+    a.t_end = ctx->d_tend + offset;
+    a.work = work;
     a.queue = nullptr;
-    a.resume = ctx->d_resume;
-    a.setup = ctx->d_setup;
+    a.resume = ctx->d_resume + offset;
+    a.setup = ctx->d_setup + 4 * offset;
     a.counters = ctx->d_counters;
     a.any_cond = ctx->any_cond;
     a.one_d = ctx->all_one_d;
@@ -454,13 +463,28 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_res
         }
         ev = evs;
     }
-    CUDA_TRY(gpis::launch_flights(a, ctx->num_sms, static_cast<cudaStream_t>(cuda_stream), ev), "launch flights");
+    CUDA_TRY(gpis::launch_flights(a, ctx->num_sms, stream, ev), "launch flights");
     if (ctx->profiling) {
         ctx->prof_launches[0] += a.any_cond ? 1 : 0;
         ctx->prof_launches[1] += 1;
         ctx->prof_launches[2] += 1;
     }
     return GPIS_OK;
+}
+
+}  // namespace
+
+int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa *out, uint32_t n,
+                        void *cuda_stream)
+{
+    if (!ctx || !in || !out) return fail(GPIS_EINVAL, "null argument");
+    if (n == 0) return GPIS_OK;
+    if (!in->origin_near || !in->dir_far || !in->seeds || !out->rec)
+        return fail(GPIS_EINVAL, "flight streams origin_near, dir_far, seeds and rec are required");
+    if (ctx->any_cond && !in->prev) return fail(GPIS_EINVAL, "conditioning media need the prev stream");
+    int rc = ensure_scratch(ctx, n);
+    if (rc) return rc;
+    return submit_slice(ctx, in, out, n, static_cast<cudaStream_t>(cuda_stream), 0, ctx->d_work);
 }
 
 int gpis_profile_enable(gpis_ctx *ctx, int on)
@@ -509,30 +533,57 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis
         ctx->stage_cap = need;
     }
     char *base = ctx->d_stage;
-    gpis_flight_soa din;
-    din.origin_near = reinterpret_cast<float *>(base);
-    din.dir_far = reinterpret_cast<float *>(base + rec16);
-    din.seeds = reinterpret_cast<uint32_t *>(base + 2 * rec16);
-    din.prev = reinterpret_cast<float *>(base + 3 * rec16);
-    char *med = base + 4 * rec16;
-    din.medium = in->medium ? reinterpret_cast<uint32_t *>(med) : nullptr;
-    char *outp = base + ((4 * rec16 + (size_t)n * 4 + 63) & ~(size_t)63);
-    gpis_result_soa dout;
-    dout.rec = reinterpret_cast<float *>(outp);
-    cudaStream_t s = ctx->stream;
-    CUDA_TRY(cudaMemcpyAsync((void *)din.origin_near, in->origin_near, rec16, cudaMemcpyHostToDevice, s), "copy origins");
-    CUDA_TRY(cudaMemcpyAsync((void *)din.dir_far, in->dir_far, rec16, cudaMemcpyHostToDevice, s), "copy directions");
-    CUDA_TRY(cudaMemcpyAsync((void *)din.seeds, in->seeds, rec16, cudaMemcpyHostToDevice, s), "copy seeds");
-    if (in->prev)
-        CUDA_TRY(cudaMemcpyAsync((void *)din.prev, in->prev, rec16, cudaMemcpyHostToDevice, s), "copy prev");
-    else
-        CUDA_TRY(cudaMemsetAsync((void *)din.prev, 0, rec16, s), "clear prev");
-    if (in->medium)
-        CUDA_TRY(cudaMemcpyAsync((void *)din.medium, in->medium, (size_t)n * 4, cudaMemcpyHostToDevice, s), "copy media");
-    int rc = gpis_flights_submit(ctx, &din, &dout, n, s);
-    if (rc) return rc;
-    CUDA_TRY(cudaMemcpyAsync(out->rec, dout.rec, rec16 * 2, cudaMemcpyDeviceToHost, s), "copy results");
-    CUDA_TRY(cudaStreamSynchronize(s), "synchronize flights");
+    float *d_on = reinterpret_cast<float *>(base);
+    float *d_df = reinterpret_cast<float *>(base + rec16);
+    uint32_t *d_sd = reinterpret_cast<uint32_t *>(base + 2 * rec16);
+    float *d_pv = reinterpret_cast<float *>(base + 3 * rec16);
+    uint32_t *d_md = reinterpret_cast<uint32_t *>(base + 4 * rec16);
+    float *d_rec = reinterpret_cast<float *>(base + ((4 * rec16 + (size_t)n * 4 + 63) & ~(size_t)63));
+    // Pipelined in chunks: the copies of the next chunk in (one stream) and of the
+    // previous chunk out (another) overlap the flight kernels, and the chunks'
+    // kernels alternate between two compute streams on disjoint slices of the
+    // scratch, so one chunk's tail overlaps the next chunk's start.
+    uint32_t per = n > (3u << 20) ? (1u << 20) : n;
+    if ((n + per - 1) / per > kMaxChunks) per = (n + kMaxChunks - 1) / kMaxChunks;
+    const uint32_t chunks = (n + per - 1) / per;
+    int rc0 = ensure_scratch(ctx, n);
+    if (rc0) return rc0;
+    while (ctx->ev_chunks.size() < 2 * (size_t)chunks) {
+        cudaEvent_t e;
+        CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "create chunk event");
+        ctx->ev_chunks.push_back(e);
+    }
+    cudaStream_t s = ctx->stream, hs = ctx->h2d_stream, ds = ctx->d2h_stream;
+    for (uint32_t k = 0; k < chunks; ++k) {
+        const size_t o = (size_t)k * per, m = std::min<size_t>(per, n - o);
+        const size_t b16 = m * 16;
+        CUDA_TRY(cudaMemcpyAsync(d_on + 4 * o, in->origin_near + 4 * o, b16, cudaMemcpyHostToDevice, hs), "copy origins");
+        CUDA_TRY(cudaMemcpyAsync(d_df + 4 * o, in->dir_far + 4 * o, b16, cudaMemcpyHostToDevice, hs), "copy directions");
+        CUDA_TRY(cudaMemcpyAsync(d_sd + 4 * o, in->seeds + 4 * o, b16, cudaMemcpyHostToDevice, hs), "copy seeds");
+        if (in->prev)
+            CUDA_TRY(cudaMemcpyAsync(d_pv + 4 * o, in->prev + 4 * o, b16, cudaMemcpyHostToDevice, hs), "copy prev");
+        else
+            CUDA_TRY(cudaMemsetAsync(d_pv + 4 * o, 0, b16, hs), "clear prev");
+        if (in->medium)
+            CUDA_TRY(cudaMemcpyAsync(d_md + o, in->medium + o, m * 4, cudaMemcpyHostToDevice, hs), "copy media");
+        CUDA_TRY(cudaEventRecord(ctx->ev_chunks[2 * k], hs), "record copy event");
+        cudaStream_t cs = (k & 1) ? ctx->stream2 : s;
+        CUDA_TRY(cudaStreamWaitEvent(cs, ctx->ev_chunks[2 * k], 0), "wait for copies");
+        gpis_flight_soa din{d_on + 4 * o, d_df + 4 * o, d_sd + 4 * o, d_pv + 4 * o, in->medium ? d_md + o : nullptr};
+        gpis_result_soa dout{d_rec + 8 * o};
+        int rc = submit_slice(ctx, &din, &dout, (uint32_t)m, cs, o, ctx->d_work + 4 * k);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(ctx->ev_chunks[2 * k + 1], cs), "record kernel event");
+    }
+    // results out after every chunk is enqueued: a copy to pageable memory blocks the
+    // calling thread until it is done, which must not hold back the later chunks
+    for (uint32_t k = 0; k < chunks; ++k) {
+        const size_t o = (size_t)k * per, m = std::min<size_t>(per, n - o);
+        CUDA_TRY(cudaStreamWaitEvent(ds, ctx->ev_chunks[2 * k + 1], 0), "wait for kernels");
+        CUDA_TRY(cudaMemcpyAsync(out->rec + 8 * o, d_rec + 8 * o, 2 * m * 16, cudaMemcpyDeviceToHost, ds),
+                 "copy results");
+    }
+    CUDA_TRY(cudaStreamSynchronize(ds), "synchronize flights");
     return GPIS_OK;
 }
 
