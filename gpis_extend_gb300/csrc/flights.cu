@@ -1430,7 +1430,6 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     bool mok;
                     L.m = medium_of(a, idx, mok);
                     const DevMedium &m = *L.m;
-                    const FlightIn fl = load_flight(a, idx);
                     uint4 rs = make_uint4(0u, 0u, 0u, 0u);
                     if (RESUME) rs = a.resume[idx];
                     if (RESUME && (rs.w >> 28) == 0u) {
@@ -1440,6 +1439,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                         const float4 s0 = a.setup[4 * (size_t)idx], s1 = a.setup[4 * (size_t)idx + 1];
                         const float4 s2 = a.setup[4 * (size_t)idx + 2], s3 = a.setup[4 * (size_t)idx + 3];
                         const uint32_t flags = __float_as_uint(s3.y);
+                        const float4 on = a.origin_near[idx], df = a.dir_far[idx];
                         if (!mok || !(flags & SF_VALID)) {
                             write_status(a, idx, 0.0f, 0.0f, 1.0f, 0u, GPIS_FLIGHT_INVALID_INPUT);
                             a.t_end[idx] = 0.0;
@@ -1447,9 +1447,11 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                             c_invalid++;
                         } else {
 #pragma unroll
-                            for (int k = 0; k < 3; ++k) { L.o[k] = fl.o[k]; d[k] = fl.d[k]; L.li[k] = m.l_inv[k]; }
-                            near_t = fl.near_t;
-                            far_t = fl.far_t;
+                            for (int k = 0; k < 3; ++k) L.li[k] = m.l_inv[k];
+                            L.o[0] = on.x; L.o[1] = on.y; L.o[2] = on.z;
+                            d[0] = df.x; d[1] = df.y; d[2] = df.z;
+                            near_t = on.w;
+                            far_t = df.w;
                             first = (flags & SF_FIRST) != 0;
                             L.seed = __float_as_uint(s3.x);
                             L.sigma = m.sigma;
@@ -1479,7 +1481,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                             ev.reset();
                             phase = PH_F0;
                         }
-                    } else if (!mok || !flight_valid(fl)) {
+                    } else if (const FlightIn fl = load_flight(a, idx); !mok || !flight_valid(fl)) {
                         write_status(a, idx, 0.0f, 0.0f, 1.0f, 0u, GPIS_FLIGHT_INVALID_INPUT);
                         a.t_end[idx] = 0.0;
                         a.resume[idx] = make_uint4(0u, 0u, 0u, 0u);
