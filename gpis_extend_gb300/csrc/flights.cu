@@ -1057,7 +1057,7 @@ struct EvalCoop1D {
     static constexpr bool kCollective = true;
     static constexpr int kMinBlocks = 2;
     static constexpr bool kGeneral = NS;   // stationary, single octave, 1D otherwise
-    static constexpr bool kSkip = !GRID && !NS;
+    static constexpr bool kSkip = !NS;
     float cache[3][NMAX];
     int base;
     bool valid;
@@ -2051,10 +2051,10 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     // the stationary cooperative fast pass takes its per-flight set-up from k_prepare
     const bool coop_plain = a.one_d && a.max_imp <= 8 && a.max_oct == 1 && !a.any_ns && !a.all_grid;
     FlightArgs b = a;
-    if (!coop_plain) b.setup = nullptr;
+    if (!coop_plain) b.setup = nullptr;     // the march kernels read set-up records only when written
     if (b.any_cond || b.setup) k_prepare<<<blocks, 128, 0, stream>>>(b);
     if (ev) cudaEventRecord(ev[1], stream);
-    cudaError_t err = cudaMemsetAsync(a.work, 0, 4 * sizeof(uint32_t), stream);
+    cudaError_t err = cudaMemsetAsync(b.work, 0, 4 * sizeof(uint32_t), stream);
     if (err != cudaSuccess) return err;
     // persistent grids: exactly the CTAs that are resident at once, never more
     // warps than flights
@@ -2074,27 +2074,27 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
         const void *fn = (const void *)k_march<EvalCoopOct, false>;
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemOct);
         if (e != cudaSuccess) return e;
-        k_march<EvalCoopOct, false><<<grid(fn, kSmemOct), 256, kSmemOct, stream>>>(a);
+        k_march<EvalCoopOct, false><<<grid(fn, kSmemOct), 256, kSmemOct, stream>>>(b);
     } else if (coop && a.any_ns) {
         const void *fn = (const void *)k_march<EvalCoop1D<8, false, true>, false>;
-        k_march<EvalCoop1D<8, false, true>, false><<<grid(fn), 256, 0, stream>>>(a);
+        k_march<EvalCoop1D<8, false, true>, false><<<grid(fn), 256, 0, stream>>>(b);
     } else if (coop && a.all_grid) {
         const void *fn = (const void *)k_march<EvalCoop1D<8, true>, false>;
-        k_march<EvalCoop1D<8, true>, false><<<grid(fn), 256, 0, stream>>>(a);
+        k_march<EvalCoop1D<8, true>, false><<<grid(fn), 256, 0, stream>>>(b);
     } else if (coop) {
         const void *fn = (const void *)k_march<EvalCoop1D<8>, false>;
-        k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(a);
+        k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(b);
     } else {
         const void *fn = (const void *)k_march<EvalGeneric, false>;
-        k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(a);
+        k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(b);
     }
     {
         const void *fn = (const void *)k_march<EvalGeneric, true>;
-        k_march<EvalGeneric, true><<<grid(fn), 256, 0, stream>>>(a);
+        k_march<EvalGeneric, true><<<grid(fn), 256, 0, stream>>>(b);
     }
     if (ev) cudaEventRecord(ev[3], stream);
     if (ev) cudaEventRecord(ev[4], stream);
-    k_finish<<<blocks, 128, 0, stream>>>(a);
+    k_finish<<<blocks, 128, 0, stream>>>(b);
     if (ev) cudaEventRecord(ev[5], stream);
     return cudaGetLastError();
 }

@@ -173,6 +173,34 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
                                                (double)d.mean_params[1] * d.mean_params[1] +
                                                (double)d.mean_params[2] * d.mean_params[2]);
             break;
+        case GPIS_MEAN_GRID: {
+            // trilinear interpolation of the voxels: |dv/dq_a| <= the largest difference of
+            // neighbours along a, and q = W p + t, so |d mean / dp| <= |scale| |W^T g| with
+            // g_a that largest difference (clamping q only flattens the mean)
+            const gpis_mean_grid *g = d.grid;
+            const int nx = g->dims[0], ny = g->dims[1], nz = g->dims[2];
+            double md[3] = {0.0, 0.0, 0.0};
+            bool finite = true;
+            for (int z = 0; z < nz && finite; ++z)
+                for (int y = 0; y < ny; ++y)
+                    for (int x = 0; x < nx; ++x) {
+                        const size_t i = ((size_t)z * ny + y) * nx + x;
+                        const double v = g->voxels[i];
+                        if (!std::isfinite(v)) { finite = false; break; }
+                        if (x + 1 < nx) md[0] = std::max(md[0], std::fabs((double)g->voxels[i + 1] - v));
+                        if (y + 1 < ny) md[1] = std::max(md[1], std::fabs((double)g->voxels[i + nx] - v));
+                        if (z + 1 < nz) md[2] = std::max(md[2], std::fabs((double)g->voxels[i + (size_t)nx * ny] - v));
+                    }
+            if (!finite) break;
+            double b = 0.0;
+            for (int j = 0; j < 3; ++j) {
+                double c = 0.0;
+                for (int a = 0; a < 3; ++a) c += std::fabs((double)g->world_to_index[4 * a + j]) * md[a];
+                b += c * c;
+            }
+            m.skip_mean_lip = (float)(std::fabs((double)g->scale) * std::sqrt(b) * 1.001);
+            break;
+        }
         default: break;
         }
     }
