@@ -143,7 +143,11 @@ class ResultSoA(ctypes.Structure):
     _fields_ = [("rec", ctypes.c_void_p)]
 
 
-PHASE_LAMBERT = 0
+PHASE_LAMBERT, PHASE_MIRROR, PHASE_CONDUCTOR = 0, 1, 2
+PHASE_NAMES = {"lambert": PHASE_LAMBERT, "mirror": PHASE_MIRROR, "conductor": PHASE_CONDUCTOR}
+# ConductorBsdf's default material, copper (ConductorBsdf.cpp:24-27)
+CU_ETA = (0.200438, 0.924033, 1.10221)
+CU_K = (3.91295, 2.45285, 2.14219)
 
 
 class SceneDesc(ctypes.Structure):
@@ -157,20 +161,23 @@ class SceneDesc(ctypes.Structure):
         ("light_emission", ctypes.c_float * 3),
         ("phase", ctypes.c_uint32), ("albedo", ctypes.c_float * 3),
         ("scene_seed", ctypes.c_uint32), ("sampler_seed", ctypes.c_uint32), ("medium", ctypes.c_uint32),
-        ("reserved_", ctypes.c_uint32),
+        ("eta", ctypes.c_float * 3), ("k", ctypes.c_float * 3), ("reserved_", ctypes.c_uint32),
     ]
 
 
 class RenderStats(ctypes.Structure):
     _fields_ = [("paths", ctypes.c_uint64), ("distance_flights", ctypes.c_uint64),
                 ("shadow_flights", ctypes.c_uint64), ("medium_events", ctypes.c_uint64),
-                ("failed", ctypes.c_uint64), ("ms", ctypes.c_double), ("launches", ctypes.c_uint64)]
+                ("failed", ctypes.c_uint64), ("ms", ctypes.c_double), ("launches", ctypes.c_uint64),
+                ("nee_queries", ctypes.c_uint64)]
 
 
 def make_scene(width=64, height=64, spp=4, max_bounces=4, fov_deg=45.0, cam_pos=(0, 0, 4), cam_target=(0, 0, 0),
                cam_up=(0, 1, 0), box_half=1.5, light_center=(0, 3, 0), light_u=(1, 0, 0), light_v=(0, 0, 1),
-               light_emission=(10, 10, 10), albedo=(0.8, 0.8, 0.8), scene_seed=1, sampler_seed=7, medium=0):
-    """A SceneDesc; the default light is a 1x1 quad at y = 3 facing down."""
+               light_emission=(10, 10, 10), albedo=(0.8, 0.8, 0.8), scene_seed=1, sampler_seed=7, medium=0,
+               phase=PHASE_LAMBERT, eta=CU_ETA, k=CU_K):
+    """A SceneDesc; the default light is a 1x1 quad at y = 3 facing down.  phase is a
+    PHASE_* value or its name; eta and k are the conductor's complex index (copper)."""
     import math
     sc = SceneDesc()
     sc.width, sc.height, sc.spp, sc.max_bounces = width, height, spp, max_bounces
@@ -183,8 +190,10 @@ def make_scene(width=64, height=64, spp=4, max_bounces=4, fov_deg=45.0, cam_pos=
     sc.light_u[:] = light_u
     sc.light_v[:] = light_v
     sc.light_emission[:] = light_emission
-    sc.phase = PHASE_LAMBERT
+    sc.phase = PHASE_NAMES[phase] if isinstance(phase, str) else int(phase)
     sc.albedo[:] = albedo
+    sc.eta[:] = eta
+    sc.k[:] = k
     sc.scene_seed, sc.sampler_seed, sc.medium = scene_seed, sampler_seed, medium
     return sc
 

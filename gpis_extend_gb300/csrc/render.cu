@@ -3,8 +3,9 @@
 // The subset of PathTracer::traceSample (PathTracer.cpp:49-292) described in
 // gpis.h: pinhole camera, the medium's bounding cube as a forward boundary, one
 // one-sided quad light outside the cube, GP surface events shaded by
-// BRDFPhaseFunction over LambertBsdf (BRDFPhaseFunction.cpp:29-101) with
-// handleVolume's direct lighting (TraceBase.cpp:993-1014, 798-874).
+// BRDFPhaseFunction over LambertBsdf, MirrorBsdf or ConductorBsdf
+// (BRDFPhaseFunction.cpp:29-119, MirrorBsdf.cpp:31-109, ConductorBsdf.cpp:58-137)
+// with handleVolume's direct lighting (TraceBase.cpp:993-1014, 798-874).
 //
 // Wavefront form: the paths of a chunk (all pixels x a run of samples) live in a
 // device array.  Each round, k_rt_advance moves every path that is outside the
@@ -13,8 +14,10 @@
 // GaussianProcessMedium::sampleDistance's decisions (GaussianProcessMedium.cpp:
 // 289-381), queues the two direct-lighting transmittance flights of each GP
 // event and samples the continuation; a second flight batch traces those
-// shadow flights and k_rt_shadow adds the light that got through.  Rounds
-// repeat until no path is alive.
+// shadow flights and k_rt_shadow adds the light that got through.  Specular
+// events under the NEE or MIS scheme first queue their neePDF / neeGrad
+// queries (one batch of gpis_nee per round); k_rt_nee turns the answers into
+// shadow flights.  Rounds repeat until no path is alive.
 //
 // This file is compiled with -fmad=false: every float expression rounds as the
 // CPU restatement's (built with -ffp-contract=off), and path decisions use no
@@ -57,6 +60,10 @@ struct RtMedium {
     uint32_t single_realization;
     uint32_t global_ctx;
     uint32_t scene_seed;
+    // samplingScheme (SparseConvolutionNoise.cpp:68-76) of an event
+    uint32_t scheme;            // the medium's 1D sampling scheme
+    uint32_t scheme_uni;        // UNI whatever the event: single realization, 3D noise or sigma < 1e-6
+    uint32_t xy_renewal_plus;   // correlationXY under Renewal+: UNI at t = 0 after a conditioned flight
 };
 
 struct RtScene {
@@ -201,10 +208,40 @@ __device__ float light_hit(const RtScene &S, const float o[3], const float d[3])
     return t;
 }
 
-__device__ __forceinline__ float power_heuristic(float a, float b)
+// SampleWarp::powerHeuristic (SampleWarp.hpp:189-199): the bounded ratio in double
+__device__ __forceinline__ float power_heuristic(double pdf0, double pdf1)
 {
-    const float a2 = a * a, b2 = b * b;
-    return a2 / (a2 + b2);
+    if (pdf0 >= pdf1) {
+        const double ratio = pdf1 / pdf0;
+        return (float)(1.0 / (1.0 + ratio * ratio));
+    }
+    const double ratio = pdf0 / pdf1;
+    return (float)(ratio * ratio / (1.0 + ratio * ratio));
+}
+
+// Fresnel::conductorReflectance (Fresnel.hpp:102-123) of one channel; the
+// mirror phase reflects everything
+__device__ float conductor_reflectance(const gpis_scene_desc &sc, int c, float cos_i)
+{
+    if (sc.phase != GPIS_PHASE_CONDUCTOR) return 1.0f;
+    const float eta = sc.eta[c], k = sc.k[c];
+    if (eta == 0.0f && k == 0.0f) return 1.0f;
+    const float c2 = cos_i * cos_i;
+    const float s2 = fmaxf(1.0f - c2, 0.0f);
+    const float s4 = s2 * s2;
+    const float inner = eta * eta - k * k - s2;
+    const float ab = sqrtf(fmaxf(inner * inner + 4.0f * eta * eta * k * k, 0.0f));
+    const float a = sqrtf(fmaxf((ab + inner) * 0.5f, 0.0f));
+    const float rs = ((ab + c2) - (2.0f * a * cos_i)) / ((ab + c2) + (2.0f * a * cos_i));
+    const float rp = ((c2 * ab + s4) - (2.0f * a * cos_i * s2)) / ((c2 * ab + s4) + (2.0f * a * cos_i * s2));
+    return 0.5f * (rs + rs * rp);
+}
+
+__device__ __forceinline__ uint32_t event_scheme(const RtMedium &M, bool conditioned, float t)
+{
+    if (M.scheme_uni) return GPIS_SCHEME_UNI;
+    if (M.xy_renewal_plus && conditioned && t == 0.0f) return GPIS_SCHEME_UNI;
+    return M.scheme;
 }
 
 // flight streams of one queue
@@ -214,6 +251,19 @@ struct Queue {
     float4 *rec;                // 2 per flight
     uint32_t *path;             // path index of each flight
     float4 *payload;            // shadow queues: contribution (rgb) and slot
+    uint32_t *count;
+};
+
+// NEE queries of specular events (gpis_nee streams) and what shading needs
+// after them: a = (T, light pdf), b = (albedo * F, unused), c = (direction,
+// bounce | kind << 31); kind 0 = the light sample at the half-vector normal,
+// kind 1 = the MIS phase sample at the event's normal
+struct NeeQueue {
+    float4 *origin_near, *dir_far, *prev;
+    uint4 *seeds;
+    float4 *point_t, *normal, *out;
+    float4 *a, *b, *c;
+    uint32_t *path;
     uint32_t *count;
 };
 
@@ -339,11 +389,12 @@ __global__ void k_rt_advance(RtScene S, RtMedium M, PathRec *paths, uint32_t n, 
     paths[i] = r;
 }
 
-// queue a direct-lighting transmittance flight from p along d (the light lies
-// outside the cube, so the flight ends at the cube's exit)
-__device__ void push_shadow(const RtScene &S, const RtMedium &M, const Queue &q, const PathRec &r, uint32_t pi,
-                            const float p[3], const float d[3], float jitter, const float contrib[3], uint32_t slot_kind,
-                            float *direct)
+// queue a direct-lighting transmittance flight from p along d on the medium
+// state of segment `seg` conditioned on (pv, pg) (the light lies outside the
+// cube, so the flight ends at the cube's exit)
+__device__ void push_shadow(const RtScene &S, const RtMedium &M, const Queue &q, const PathRec &r, uint32_t seg,
+                            uint32_t pi, const float p[3], const float d[3], float jitter, const float contrib[3],
+                            uint32_t slot_kind, float *direct, float pv, const float pg[3])
 {
     float t0, t1;
     if (!box_hit(p, d, S.sc.box_half, t0, t1) || !(t1 > 0.0f)) {
@@ -353,17 +404,34 @@ __device__ void push_shadow(const RtScene &S, const RtMedium &M, const Queue &q,
     }
     const uint32_t px = r.pixel % S.sc.width, py = r.pixel / S.sc.width;
     uint32_t ns, nm;
-    flight_seeds(M, px, py, r.sample, r.bounce + 1, ns, nm);
+    flight_seeds(M, px, py, r.sample, seg, ns, nm);
     const uint32_t slot = atomicAdd(q.count, 1u);
-    push_flight(q, slot, p, d, t1, ns, nm, GPIS_FLAG_SHADOW, jitter, r.last_val, r.last_aniso);
+    push_flight(q, slot, p, d, t1, ns, nm, GPIS_FLAG_SHADOW, jitter, pv, pg);
     q.path[slot] = pi;
     q.payload[slot] = make_float4(contrib[0], contrib[1], contrib[2], __uint_as_float(slot_kind));
 }
 
+__device__ void push_nee(const NeeQueue &nq, const Queue &q, uint32_t k, uint32_t pi, const float p[3], float t,
+                         const float nrm[3], const float T[3], float pdf_l, const float fr[3], const float d[3],
+                         uint32_t b, uint32_t kind)
+{
+    const uint32_t slot = atomicAdd(nq.count, 1u);
+    nq.origin_near[slot] = q.origin_near[k];
+    nq.dir_far[slot] = q.dir_far[k];
+    nq.seeds[slot] = q.seeds[k];
+    nq.prev[slot] = q.prev[k];
+    nq.point_t[slot] = make_float4(p[0], p[1], p[2], t);
+    nq.normal[slot] = make_float4(nrm[0], nrm[1], nrm[2], 0.0f);
+    nq.a[slot] = make_float4(T[0], T[1], T[2], pdf_l);
+    nq.b[slot] = make_float4(fr[0], fr[1], fr[2], 0.0f);
+    nq.c[slot] = make_float4(d[0], d[1], d[2], __uint_as_float(b | (kind << 31)));
+    nq.path[slot] = pi;
+}
+
 // GaussianProcessMedium::sampleDistance after the flight (GaussianProcessMedium.cpp:
 // 289-381), then handleVolume (TraceBase.cpp:993-1048) for GP events.
-__global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint32_t nq, Queue sq, float *direct,
-                           unsigned long long *counters)
+__global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint32_t nq, Queue sq, NeeQueue eq,
+                           float *direct, unsigned long long *counters)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nq) return;
@@ -402,7 +470,6 @@ __global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint3
             return;
         }
     }
-    (void)first_before;
     if (hit) {
         const double dd = (double)aniso[0] * r.dir[0] + (double)aniso[1] * r.dir[1] + (double)aniso[2] * r.dir[2];
         const double l2 = (double)aniso[0] * aniso[0] + (double)aniso[1] * aniso[1] + (double)aniso[2] * aniso[2];
@@ -433,6 +500,66 @@ __global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint3
     float wi[3];
     const float nd[3] = {-r.dir[0], -r.dir[1], -r.dir[2]};
     to_local(f, nd, wi);
+    if (sc.phase != GPIS_PHASE_LAMBERT) {
+        // BRDFPhaseFunction over MirrorBsdf / ConductorBsdf: se.wi = frame.toLocal(-w).normalized(),
+        // the reflection (-wi.x, -wi.y, wi.z) with weight albedo * F(wi.z)
+        normalize3(wi);
+        float fr[3], wrg[3];
+        const float wr[3] = {-wi[0], -wi[1], wi[2]};
+        for (int c = 0; c < 3; ++c) fr[c] = sc.albedo[c] * conductor_reflectance(sc, c, wi[2]);
+        to_global(f, wr, wrg);
+        normalize3(wrg);
+        const uint32_t scheme = event_scheme(M, !first_before, t);
+        const uint32_t px = r.pixel % sc.width, py = r.pixel / sc.width;
+        const uint64_t path = ((uint64_t)py * sc.width + px) * sc.spp + r.sample;
+        const uint32_t seed = sc.sampler_seed, b = r.bounce;
+        if (b + 1 < sc.max_bounces) {
+            if (scheme != GPIS_SCHEME_UNI) {
+                // volumeLightSample: neePDF / neeGrad at the half-vector normal, shaded by k_rt_nee
+                const float lu = rng(seed, path, b, D_LU) - 0.5f, lv = rng(seed, path, b, D_LV) - 0.5f;
+                float ld[3];
+                for (int i = 0; i < 3; ++i)
+                    ld[i] = ((sc.light_center[i] + lu * sc.light_u[i]) + lv * sc.light_v[i]) - p[i];
+                const float dist2 = dot3(ld, ld), dist = sqrtf(dist2);
+                for (int i = 0; i < 3; ++i) ld[i] = ld[i] / dist;
+                const float cos_l = -dot3(ld, S.ln);
+                if (cos_l > 0.0f) {
+                    const float pdf_l = dist2 / (S.area * cos_l);
+                    float wo[3], hl[3], hw[3];
+                    to_local(f, ld, wo);
+                    normalize3(wo);
+                    for (int i = 0; i < 3; ++i) hl[i] = (wi[i] + wo[i]) * 0.5f;
+                    to_global(f, hl, hw);
+                    normalize3(hw);
+                    push_nee(eq, q, k, pi, p, ts, hw, r.T, pdf_l, fr, ld, b, 0u);
+                }
+            }
+            if (scheme != GPIS_SCHEME_NEE) {
+                // volumePhaseSample: the reflection, when it reaches the light
+                const float tlh = light_hit(S, p, wrg);
+                if (tlh > 0.0f) {
+                    if (scheme == GPIS_SCHEME_MIS) {
+                        // weighed against neePDF at the event's normal in k_rt_nee
+                        const float cl = -dot3(wrg, S.ln);
+                        const float pdf_l = (tlh * tlh) / (S.area * cl);
+                        push_nee(eq, q, k, pi, p, ts, f.n, r.T, pdf_l, fr, wrg, b, 1u);
+                    } else {
+                        const float w = 1.0f;
+                        float contrib[3];
+                        for (int c = 0; c < 3; ++c) contrib[c] = r.T[c] * (fr[c] * sc.light_emission[c] * w);
+                        push_shadow(S, M, sq, r, b + 1, pi, p, wrg, rng(seed, path, b, D_JS2), contrib, 1u, dslot,
+                                    r.last_val, r.last_aniso);
+                    }
+                }
+            }
+        }
+        for (int c = 0; c < 3; ++c) r.T[c] = r.T[c] * fr[c];
+        for (int i = 0; i < 3; ++i) { r.pos[i] = p[i]; r.dir[i] = wrg[i]; }
+        r.flags &= ~PF_SPECULAR;
+        r.bounce += 1;
+        paths[pi] = r;
+        return;
+    }
     if (!(wi[2] > 0.0f)) {
         r.flags &= ~PF_ALIVE;
         atomicAdd(counters + 1, 1ull);
@@ -463,7 +590,8 @@ __global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint3
                     const float fc = sc.albedo[c] * kInvPi * wo[2];
                     contrib[c] = r.T[c] * (fc * sc.light_emission[c] / pdf_l * w);
                 }
-                push_shadow(S, M, sq, r, pi, p, ld, rng(seed, path, b, D_JS1), contrib, 0u, dslot);
+                push_shadow(S, M, sq, r, b + 1, pi, p, ld, rng(seed, path, b, D_JS1), contrib, 0u, dslot, r.last_val,
+                            r.last_aniso);
             }
         }
         // volumePhaseSample
@@ -479,7 +607,8 @@ __global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint3
             const float w = power_heuristic(pdf_p, pdf_l);
             float contrib[3];
             for (int c = 0; c < 3; ++c) contrib[c] = r.T[c] * (sc.albedo[c] * sc.light_emission[c] * w);
-            push_shadow(S, M, sq, r, pi, p, wg, rng(seed, path, b, D_JS2), contrib, 1u, dslot);
+            push_shadow(S, M, sq, r, b + 1, pi, p, wg, rng(seed, path, b, D_JS2), contrib, 1u, dslot, r.last_val,
+                        r.last_aniso);
         }
     }
     // the continuation (BRDFPhaseFunction::sample over LambertBsdf)
@@ -492,6 +621,45 @@ __global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint3
     r.flags &= ~PF_SPECULAR;
     r.bounce += 1;
     paths[pi] = r;
+}
+
+// after the NEE queries of specular events: the light sample's BSDF value
+// albedo * F * neePDF and its transmittance flight conditioned on neeGrad
+// (volumeLightSample with MirrorBsdf::eval / evalGrad), or the MIS weight of the
+// phase sample against neePDF (MirrorBsdf::sample's pdf)
+__global__ void k_rt_nee(RtScene S, RtMedium M, const PathRec *paths, NeeQueue eq, uint32_t n, Queue sq,
+                         float *direct)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t pi = eq.path[k];
+    const PathRec &r = paths[pi];
+    const gpis_scene_desc &sc = S.sc;
+    const float4 o = eq.out[k], pa = eq.a[k], pb = eq.b[k], pc = eq.c[k], pt = eq.point_t[k];
+    const uint32_t bk = __float_as_uint(pc.w), b = bk & 0x7FFFFFFFu, kind = bk >> 31;
+    const float T[3] = {pa.x, pa.y, pa.z}, fr[3] = {pb.x, pb.y, pb.z};
+    const float p[3] = {pt.x, pt.y, pt.z}, d[3] = {pc.x, pc.y, pc.z};
+    const float pdf_l = pa.w, pdf = o.x;
+    const uint32_t px = r.pixel % sc.width, py = r.pixel / sc.width;
+    const uint64_t path = ((uint64_t)py * sc.width + px) * sc.spp + r.sample;
+    float *dslot = direct + 6 * (size_t)pi;
+    const uint32_t scheme = M.scheme;
+    float contrib[3];
+    if (kind == 0u) {
+        float fl[3];
+        for (int c = 0; c < 3; ++c) fl[c] = fr[c] * pdf;
+        if (!(fl[0] != 0.0f || fl[1] != 0.0f || fl[2] != 0.0f)) return;
+        const float w = scheme == GPIS_SCHEME_MIS ? power_heuristic(pdf_l, pdf) : 1.0f;
+        for (int c = 0; c < 3; ++c) contrib[c] = T[c] * (fl[c] * sc.light_emission[c] / pdf_l * w);
+        const float g[3] = {o.y, o.z, o.w};
+        push_shadow(S, M, sq, r, b + 1, pi, p, d, rng(sc.sampler_seed, path, b, D_JS1), contrib, 0u, dslot,
+                    r.last_val, g);
+    } else {
+        const float w = power_heuristic(pdf, pdf_l);
+        for (int c = 0; c < 3; ++c) contrib[c] = T[c] * (fr[c] * sc.light_emission[c] * w);
+        push_shadow(S, M, sq, r, b + 1, pi, p, d, rng(sc.sampler_seed, path, b, D_JS2), contrib, 1u, dslot,
+                    r.last_val, r.last_aniso);
+    }
 }
 
 // a transmittance of 1 lets the queued contribution through
@@ -591,13 +759,16 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     const gpis_scene_desc &sc = *scene;
     if (sc.width == 0 || sc.height == 0 || sc.spp == 0 || sc.max_bounces == 0)
         return gpis_internal_set_error(GPIS_EINVAL, "width, height, spp and max_bounces must be > 0");
-    if (sc.phase != GPIS_PHASE_LAMBERT) return gpis_internal_set_error(GPIS_ENOTSUP, "only the Lambert phase is supported");
+    if (sc.phase > GPIS_PHASE_CONDUCTOR) return gpis_internal_set_error(GPIS_EINVAL, "unknown phase");
     if (!(sc.box_half > 0.0f) || !(sc.tan_half_fov > 0.0f))
         return gpis_internal_set_error(GPIS_EINVAL, "box_half and tan_half_fov must be > 0");
     const gpis_medium_desc *md = gpis_internal_ctx_medium(ctx, sc.medium);
     if (!md) return gpis_internal_set_error(GPIS_EINVAL, "unknown medium index");
     const float sa = md->sigma_a * md->density, ss = md->sigma_s * md->density;
     if (!(ss > 0.0f)) return gpis_internal_set_error(GPIS_ENOTSUP, "the renderer needs a scattering medium (sigma_s > 0)");
+    if (sc.phase != GPIS_PHASE_LAMBERT && md->sampling_scheme != GPIS_SCHEME_UNI && md->one_d_sampling &&
+        (md->n_octaves > 1 || md->multires))
+        return gpis_internal_set_error(GPIS_ENOTSUP, "1D NEE and MIS need a single-octave medium");
 
     RtMedium M;
     M.ratio = ss / (sa + ss);
@@ -606,6 +777,11 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     M.single_realization = md->single_realization;
     M.global_ctx = md->correlation_context == GPIS_CTX_GLOBAL;
     M.scene_seed = sc.scene_seed;
+    M.scheme = md->sampling_scheme;
+    M.scheme_uni = md->single_realization || !md->one_d_sampling || md->sigma < 1e-6f;
+    M.xy_renewal_plus = md->correlation_xy && !md->single_realization &&
+                        md->correlation_context == GPIS_CTX_RENEWAL_PLUS;
+    const bool specular_nee = sc.phase != GPIS_PHASE_LAMBERT && !M.scheme_uni && M.scheme != GPIS_SCHEME_UNI;
 
     RtScene S;
     S.sc = sc;
@@ -634,12 +810,13 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     PathRec *paths;
     float *direct, *acc;
     Queue q, sq;
+    NeeQueue eq{};
     uint32_t *counts;
     unsigned long long *dcnt;
     RT_TRY(mem.alloc(paths, cap), "allocate paths");
     RT_TRY(mem.alloc(direct, cap * 6), "allocate direct light");
     RT_TRY(mem.alloc(acc, (size_t)n_pixels * 3), "allocate image");
-    RT_TRY(mem.alloc(counts, 2), "allocate queue counters");
+    RT_TRY(mem.alloc(counts, 3), "allocate queue counters");
     RT_TRY(mem.alloc(dcnt, 2), "allocate counters");
     for (Queue *qq : {&q, &sq}) {
         const size_t m = qq == &q ? cap : 2 * cap;
@@ -653,6 +830,22 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     }
     q.count = counts;
     sq.count = counts + 1;
+    eq.count = counts + 2;
+    if (specular_nee) {
+        // at most two queries per event: the light sample and the MIS phase sample
+        const size_t m = 2 * cap;
+        RT_TRY(mem.alloc(eq.origin_near, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.dir_far, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.prev, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.seeds, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.point_t, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.normal, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.out, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.a, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.b, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.c, m), "allocate NEE queue");
+        RT_TRY(mem.alloc(eq.path, m), "allocate NEE queue");
+    }
     uint32_t *dmedium = nullptr;
     if (sc.medium != 0) {
         RT_TRY(mem.alloc(dmedium, 2 * cap), "allocate medium stream");
@@ -670,7 +863,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     RT_TRY(cudaMemsetAsync(dcnt, 0, 2 * sizeof(unsigned long long), st), "clear counters");
     RT_TRY(cudaEventRecord(e0, st), "record event");
 
-    uint64_t n_dist = 0, n_shadow = 0, n_paths = 0, n_launch = 0;
+    uint64_t n_dist = 0, n_shadow = 0, n_paths = 0, n_launch = 0, n_nee = 0;
     // a flight batch is 4 kernels (prepare, fast pass, resume pass, finish), 3 without conditioning
     const bool conditions = !md->single_realization && (md->correlation_context == GPIS_CTX_RENEWAL ||
                                                          md->correlation_context == GPIS_CTX_RENEWAL_PLUS);
@@ -686,7 +879,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
         n_launch += 1;
         // at most two rounds per bounce (a forward crossing, then an event), plus entry and exit
         for (uint32_t round = 0; round < 2 * sc.max_bounces + 4; ++round) {
-            RT_TRY(cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), st), "clear queue counters");
+            RT_TRY(cudaMemsetAsync(counts, 0, 3 * sizeof(uint32_t), st), "clear queue counters");
             k_rt_advance<<<(n + tb - 1) / tb, tb, 0, st>>>(S, M, paths, n, q, dcnt);
             n_launch += 1;
             uint32_t nq = 0;
@@ -702,11 +895,29 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
             int rc = gpis_flights_submit(ctx, &fin, &fout, nq, st);
             if (rc) return rc;
             n_dist += nq;
-            k_rt_event<<<(nq + tb - 1) / tb, tb, 0, st>>>(S, M, paths, q, nq, sq, direct, dcnt);
+            k_rt_event<<<(nq + tb - 1) / tb, tb, 0, st>>>(S, M, paths, q, nq, sq, eq, direct, dcnt);
             n_launch += per_batch + 1;
-            uint32_t nsq = 0;
-            RT_TRY(cudaMemcpyAsync(&nsq, counts + 1, 4, cudaMemcpyDeviceToHost, st), "read shadow queue");
+            uint32_t qc[2] = {0, 0};
+            RT_TRY(cudaMemcpyAsync(qc, counts + 1, 8, cudaMemcpyDeviceToHost, st), "read shadow queue");
             RT_TRY(cudaStreamSynchronize(st), "synchronize");
+            uint32_t nsq = qc[0];
+            if (qc[1]) {
+                // the NEE queries of specular events, then their shadow flights
+                gpis_nee_soa nin;
+                nin.flight = gpis_flight_soa{reinterpret_cast<float *>(eq.origin_near),
+                                             reinterpret_cast<float *>(eq.dir_far),
+                                             reinterpret_cast<uint32_t *>(eq.seeds), reinterpret_cast<float *>(eq.prev),
+                                             dmedium};
+                nin.point_t = reinterpret_cast<const float *>(eq.point_t);
+                nin.normal = reinterpret_cast<const float *>(eq.normal);
+                rc = gpis_nee_submit(ctx, &nin, reinterpret_cast<float *>(eq.out), qc[1], st);
+                if (rc) return rc;
+                n_nee += qc[1];
+                k_rt_nee<<<(qc[1] + tb - 1) / tb, tb, 0, st>>>(S, M, paths, eq, qc[1], sq, direct);
+                n_launch += 2;
+                RT_TRY(cudaMemcpyAsync(&nsq, counts + 1, 4, cudaMemcpyDeviceToHost, st), "read shadow queue");
+                RT_TRY(cudaStreamSynchronize(st), "synchronize");
+            }
             if (nsq) {
                 gpis_flight_soa sin{reinterpret_cast<float *>(sq.origin_near), reinterpret_cast<float *>(sq.dir_far),
                                     reinterpret_cast<uint32_t *>(sq.seeds), reinterpret_cast<float *>(sq.prev), dmedium};
@@ -742,6 +953,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
         stats->failed = hc[1];
         stats->ms = ms;
         stats->launches = n_launch;
+        stats->nee_queries = n_nee;
     }
     return GPIS_OK;
 }

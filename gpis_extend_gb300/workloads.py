@@ -192,7 +192,15 @@ def render_medium(kind="sphere_3d"):
     Lambert albedo carries the surface colour):
     sphere_3d  the unit-sphere SDF field with 3D world-space noise and Renewal;
     sphere_1d  the same field with 1D noise and Renewal+;
-    torus      the nonstationary three-octave torus-union-plane field (1D, Renewal+)."""
+    torus      the nonstationary three-octave torus-union-plane field (1D, Renewal+);
+    sphere_1d_nee, sphere_1d_mis  sphere_1d with the NEE or MIS 1D sampling scheme;
+    torus_nee  the nonstationary single-octave torus-union-plane field with NEE."""
+    if kind in ("sphere_1d_nee", "sphere_1d_mis"):
+        return sphere_medium(one_d=True, context=abi.CTX_RENEWAL_PLUS, sigma_a=0.0, sigma_s=1.0,
+                             sampling_scheme=abi.SCHEME_NEE if kind.endswith("nee") else abi.SCHEME_MIS)
+    if kind == "torus_nee":
+        return torus_plane_medium(nonstationary=True, octaves=1, sigma_a=0.0, sigma_s=1.0,
+                                  sampling_scheme=abi.SCHEME_NEE)
     if kind == "sphere_3d":
         return sphere_medium(one_d=False, context=abi.CTX_RENEWAL, sigma_a=0.0, sigma_s=1.0)
     if kind == "sphere_1d":

@@ -365,18 +365,28 @@ int gpis_backend_submit(gpis_backend *backend, const gpis_flight_soa *in, float 
  * forward-scattering boundary: entering and leaving count no bounce), one
  * one-sided quad light outside the cube, and the GP surface events of
  * GaussianProcessMedium::sampleDistance shaded by BRDFPhaseFunction over a
- * Lambert BSDF (BRDFPhaseFunction.cpp:29-101).  Medium events take volume
- * direct lighting as TraceBase::handleVolume does (TraceBase.cpp:993-1014,
- * 798-963): one light sample and one phase sample, each with a transmittance
- * query through the medium and the power heuristic, with the medium state of
- * the next bounce.  No Russian roulette; no environment light.
+ * Lambert, mirror or conductor BSDF (BRDFPhaseFunction.cpp:29-119,
+ * LambertBsdf, MirrorBsdf.cpp:31-109, ConductorBsdf.cpp:58-137).  Medium events
+ * take volume direct lighting as TraceBase::handleVolume does
+ * (TraceBase.cpp:993-1014, 798-874): one light sample and one phase sample,
+ * each with a transmittance query through the medium, with the medium state of
+ * the next bounce.  Lambert: both, power heuristic.  Mirror and conductor
+ * follow the event's 1D sampling scheme (the medium's sampling_scheme through
+ * samplingScheme): UNI takes the phase sample only, at MIS weight 1; NEE takes
+ * the light sample only, its BSDF value albedo * F * neePDF at the half-vector
+ * normal and its transmittance flight conditioned on neeGrad; MIS takes both
+ * under the power heuristic with neePDF as the phase density.  NEE and MIS
+ * need media that gpis_nee supports (1D, one octave).  No Russian roulette;
+ * no environment light.
  *
  * Path decisions draw from a counter RNG keyed (sampler_seed, path, bounce,
  * dimension) with path = (y * width + x) * spp + sample; directions are sampled
  * without trigonometry (rejection in the unit disk), so the CUDA path and the
  * CPU restatement make the same decisions.  GP seeds follow the reference:
  * pixelSampleSegment = (x, y, sample, bounce), sceneSeed = scene_seed.       */
-#define GPIS_PHASE_LAMBERT 0u
+#define GPIS_PHASE_LAMBERT   0u
+#define GPIS_PHASE_MIRROR    1u
+#define GPIS_PHASE_CONDUCTOR 2u
 
 typedef struct {
     uint32_t width, height, spp, max_bounces;
@@ -389,11 +399,13 @@ typedef struct {
     float light_u[3];           /* the quad is center + s*u + t*v, |s|,|t| <= 1/2 */
     float light_v[3];
     float light_emission[3];    /* radiance emitted toward u x v                  */
-    uint32_t phase;             /* GPIS_PHASE_LAMBERT                             */
+    uint32_t phase;             /* GPIS_PHASE_*                                   */
     float albedo[3];
     uint32_t scene_seed;
     uint32_t sampler_seed;
     uint32_t medium;            /* medium index in the context                    */
+    float eta[3];               /* conductor: complex index of refraction eta + ik; */
+    float k[3];                 /* eta = k = 0 reflects everything (Fresnel.hpp:102-123) */
     uint32_t reserved_;
 } gpis_scene_desc;
 
@@ -405,6 +417,7 @@ typedef struct {
     uint64_t failed;            /* paths ended by a failed medium or phase sample */
     double ms;                  /* device time of the render (CUDA events)        */
     uint64_t launches;          /* kernels launched by the render                 */
+    uint64_t nee_queries;       /* neePDF / neeGrad queries of specular events    */
 } gpis_render_stats;
 
 /* Render into image_rgb (host, height x width x 3 floats, row 0 at the top):

@@ -8,11 +8,14 @@
  * forward boundary (no bounce counted when crossing it), one one-sided quad
  * light outside the cube, GP surface events from
  * GaussianProcessMedium::sampleDistance (gor_medium_sample_distance) shaded by
- * BRDFPhaseFunction over LambertBsdf (BRDFPhaseFunction.cpp:29-101), and
- * handleVolume's direct lighting (TraceBase.cpp:993-1014): volumeLightSample
+ * BRDFPhaseFunction over LambertBsdf, MirrorBsdf or ConductorBsdf
+ * (BRDFPhaseFunction.cpp:29-119, MirrorBsdf.cpp:31-109, ConductorBsdf.cpp:58-137),
+ * and handleVolume's direct lighting (TraceBase.cpp:993-1014): volumeLightSample
  * (:798-839) plus volumePhaseSample (:841-874), each with a transmittance query
- * (gor_medium_transmittance) and the power heuristic, on the medium state of
- * the next bounce (pixelSampleSegment.w + 1).
+ * (gor_medium_transmittance), on the medium state of the next bounce
+ * (pixelSampleSegment.w + 1).  The specular phases follow the event's 1D
+ * sampling scheme: the light sample under NEE and MIS (neePDF / neeGrad, gor_nee),
+ * the phase sample under UNI and MIS, the power heuristic under MIS only.
  *
  * Every float expression is written as the CUDA side writes it and the file is
  * built with -ffp-contract=off, so both make the same decisions: no
@@ -152,10 +155,33 @@ static float light_hit(const gpis_scene_desc *sc, const float ln[3], const float
     return t;
 }
 
-static inline float power_heuristic(float a, float b)
+/* SampleWarp::powerHeuristic (SampleWarp.hpp:189-199): the bounded ratio in double */
+static inline float power_heuristic(double pdf0, double pdf1)
 {
-    const float a2 = a * a, b2 = b * b;
-    return a2 / (a2 + b2);
+    if (pdf0 >= pdf1) {
+        const double ratio = pdf1 / pdf0;
+        return (float)(1.0 / (1.0 + ratio * ratio));
+    }
+    const double ratio = pdf0 / pdf1;
+    return (float)(ratio * ratio / (1.0 + ratio * ratio));
+}
+
+/* Fresnel::conductorReflectance (Fresnel.hpp:102-123) of one channel; the
+ * mirror phase reflects everything */
+static float conductor_reflectance(const gpis_scene_desc *sc, int c, float cos_i)
+{
+    if (sc->phase != GPIS_PHASE_CONDUCTOR) return 1.0f;
+    const float eta = sc->eta[c], k = sc->k[c];
+    if (eta == 0.0f && k == 0.0f) return 1.0f;
+    const float c2 = cos_i * cos_i;
+    const float s2 = fmaxf(1.0f - c2, 0.0f);
+    const float s4 = s2 * s2;
+    const float inner = eta * eta - k * k - s2;
+    const float ab = sqrtf(fmaxf(inner * inner + 4.0f * eta * eta * k * k, 0.0f));
+    const float a = sqrtf(fmaxf((ab + inner) * 0.5f, 0.0f));
+    const float rs = ((ab + c2) - (2.0f * a * cos_i)) / ((ab + c2) + (2.0f * a * cos_i));
+    const float rp = ((c2 * ab + s4) - (2.0f * a * cos_i * s2)) / ((c2 * ab + s4) + (2.0f * a * cos_i * s2));
+    return 0.5f * (rs + rs * rp);
 }
 
 /* transmittance (0/1) through the medium from p along d to the cube's exit */
@@ -241,6 +267,19 @@ static void trace_path(const gpis_medium_desc *md, const gpis_scene_desc *sc, ui
         r.far_t = fmaxf(t1, 0.0f);
         st.pixel_sample_segment[3] = bounce;
         const float jit = rng(seed, path, bounce, D_JIT);
+        /* the distance flight's inputs (gm_flight), for NEE queries on its realization */
+        float fo[3], fd[3], fpv[4];
+        uint32_t fsd[4];
+        {
+            const int first = st.first_scatter != 0;
+            gor_flight_seeds(md, st.pixel_sample_segment, st.scene_seed, &fsd[0], &fsd[1]);
+            fsd[2] = first ? GPIS_FLAG_FIRST_SCATTER : 0u;
+            memcpy(&fsd[3], &jit, 4);
+            memcpy(fo, pos, sizeof(fo));
+            memcpy(fd, dir, sizeof(fd));
+            fpv[0] = first ? 0.0f : st.last_val;
+            for (int i = 0; i < 3; ++i) fpv[1 + i] = first ? 0.0f : st.last_aniso[i];
+        }
         gpis_medium_sample ms;
         gor_medium_sample_distance(md, &r, &st, &jit, &ms, 1);
         cnt->distance++;
@@ -258,6 +297,78 @@ static void trace_path(const gpis_medium_desc *md, const gpis_scene_desc *sc, ui
         pframe(ms.aniso, &f);
         float wi[3], nd[3] = {-dir[0], -dir[1], -dir[2]};
         to_local(&f, nd, wi);
+        if (sc->phase != GPIS_PHASE_LAMBERT) {
+            /* BRDFPhaseFunction over MirrorBsdf / ConductorBsdf: se.wi = frame.toLocal(-w).normalized(),
+               the reflection (-wi.x, -wi.y, wi.z) with weight albedo * F(wi.z) */
+            normalize3(wi);
+            float fr[3], wr[3] = {-wi[0], -wi[1], wi[2]}, wrg[3];
+            for (int c = 0; c < 3; ++c) fr[c] = sc->albedo[c] * conductor_reflectance(sc, c, wi[2]);
+            to_global(&f, wr, wrg);
+            normalize3(wrg);
+            const uint32_t scheme = ms.sampling_scheme;
+            const float *p = ms.p;
+            if (bounce + 1 < sc->max_bounces) {
+                gpis_medium_state s2 = st;
+                s2.pixel_sample_segment[3] = bounce + 1;
+                if (scheme != GPIS_SCHEME_UNI) {
+                    /* volumeLightSample: f = albedo * F * neePDF at the half-vector normal
+                       (MirrorBsdf::eval), the shadow flight conditioned on neeGrad (evalGrad) */
+                    const float lu = rng(seed, path, bounce, D_LU) - 0.5f, lv = rng(seed, path, bounce, D_LV) - 0.5f;
+                    float ld[3];
+                    for (int i = 0; i < 3; ++i)
+                        ld[i] = ((sc->light_center[i] + lu * sc->light_u[i]) + lv * sc->light_v[i]) - p[i];
+                    const float dist2 = dot3(ld, ld), dist = sqrtf(dist2);
+                    for (int i = 0; i < 3; ++i) ld[i] = ld[i] / dist;
+                    const float cos_l = -dot3(ld, ln);
+                    if (cos_l > 0.0f) {
+                        const float pdf_l = dist2 / (area * cos_l);
+                        float wo[3], hl[3], hw[3], grad[3] = {0.0f, 0.0f, 0.0f}, pdf = 0.0f;
+                        to_local(&f, ld, wo);
+                        normalize3(wo);
+                        for (int i = 0; i < 3; ++i) hl[i] = (wi[i] + wo[i]) * 0.5f;
+                        to_global(&f, hl, hw);
+                        normalize3(hw);
+                        gor_nee(md, fo, fd, p, hw, ms.t, fsd, fpv, &pdf, grad);
+                        float fl[3];
+                        for (int c = 0; c < 3; ++c) fl[c] = fr[c] * pdf;
+                        if (fl[0] != 0.0f || fl[1] != 0.0f || fl[2] != 0.0f) {
+                            gpis_medium_state s3 = s2;
+                            memcpy(s3.last_aniso, grad, sizeof(grad));
+                            const float tr = shadow(md, sc, p, ld, &s3, rng(seed, path, bounce, D_JS1), &cnt->shadow);
+                            if (tr > 0.0f) {
+                                const float w = scheme == GPIS_SCHEME_MIS ? power_heuristic(pdf_l, pdf) : 1.0f;
+                                for (int c = 0; c < 3; ++c)
+                                    L[c] = L[c] + T[c] * (fl[c] * sc->light_emission[c] / pdf_l * w);
+                            }
+                        }
+                    }
+                }
+                if (scheme != GPIS_SCHEME_NEE) {
+                    /* volumePhaseSample: the reflection, when it reaches the light; MIS weight 1
+                       under UNI (volumeScatterMisWeight), else against neePDF at the event's normal */
+                    const float tlh = light_hit(sc, ln, p, wrg);
+                    if (tlh > 0.0f) {
+                        float w = 1.0f;
+                        if (scheme == GPIS_SCHEME_MIS) {
+                            float pdf_s = 0.0f, g[3];
+                            gor_nee(md, fo, fd, p, f.n, ms.t, fsd, fpv, &pdf_s, g);
+                            const float cl = -dot3(wrg, ln);
+                            const float pdf_l = (tlh * tlh) / (area * cl);
+                            w = power_heuristic(pdf_s, pdf_l);
+                        }
+                        const float tr = shadow(md, sc, p, wrg, &s2, rng(seed, path, bounce, D_JS2), &cnt->shadow);
+                        if (tr > 0.0f)
+                            for (int c = 0; c < 3; ++c) L[c] = L[c] + T[c] * (fr[c] * sc->light_emission[c] * w);
+                    }
+                }
+            }
+            for (int c = 0; c < 3; ++c) T[c] = T[c] * fr[c];
+            memcpy(pos, p, sizeof(pos));
+            memcpy(dir, wrg, sizeof(dir));
+            was_specular = 0;
+            bounce++;
+            continue;
+        }
         if (!(wi[2] > 0.0f)) { cnt->failed++; break; }      /* LambertBsdf::sample fails */
         const float *p = ms.p;
         if (bounce + 1 < sc->max_bounces) {
@@ -321,6 +432,10 @@ int gor_render(const gpis_medium_desc *md, const gpis_scene_desc *sc, float *ima
                uint32_t row0, uint32_t rows)
 {
     if (!md || !sc || !image || sc->width == 0 || sc->height == 0 || sc->spp == 0) return GPIS_EINVAL;
+    if (sc->phase > GPIS_PHASE_CONDUCTOR) return GPIS_EINVAL;
+    if (sc->phase != GPIS_PHASE_LAMBERT && md->sampling_scheme != GPIS_SCHEME_UNI && md->one_d_sampling &&
+        (md->n_octaves > 1 || md->multires))
+        return GPIS_ENOTSUP;
     pt_counts_t cnt = {0, 0, 0, 0};
     for (uint32_t y = row0; y < row0 + rows && y < sc->height; ++y)
         for (uint32_t x = 0; x < sc->width; ++x) {

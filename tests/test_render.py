@@ -35,21 +35,79 @@ def test_oracle_render_direct_light_visible():
     assert np.allclose(img[3:5, 3:5], 20.0)
 
 
+def test_oracle_specular_nee_is_unbiased():
+    """The 1D NEE estimator of a mirror GP surface (light samples weighted by
+    neePDF) and the plain estimator (the sampled reflection reaching the light)
+    agree in the mean over eight sampler seeds; NEE has far less variance."""
+    means = {}
+    for kind in ("sphere_1d", "sphere_1d_nee"):
+        desc = workloads.render_medium(kind)
+        m = []
+        for seed in range(8):
+            sc = workloads.render_scene(width=16, height=16, spp=128, phase="mirror", max_bounces=2,
+                                        sampler_seed=100 + seed)
+            m.append(oracle.render(desc, sc)[0].mean())
+        means[kind] = np.array(m, np.float64)
+    uni, nee = means["sphere_1d"], means["sphere_1d_nee"]
+    se = np.sqrt(uni.var(ddof=1) / len(uni) + nee.var(ddof=1) / len(nee))
+    assert abs(uni.mean() - nee.mean()) <= 4 * se
+    assert nee.std(ddof=1) < 0.5 * uni.std(ddof=1)
+
+
+def test_oracle_specular_schemes():
+    """UNI takes phase samples only, NEE light samples only, MIS both; a conductor
+    with eta = k = 0 reflects everything (Fresnel.hpp:105-107), as the mirror does."""
+    sc = workloads.render_scene(width=16, height=16, spp=4, phase="mirror")
+    _, uni = oracle.render(workloads.render_medium("sphere_1d"), sc)
+    mir, nee = oracle.render(workloads.render_medium("sphere_1d_nee"), sc)
+    _, mis = oracle.render(workloads.render_medium("sphere_1d_mis"), sc)
+    assert uni["shadow_flights"] < 0.05 * nee["shadow_flights"]
+    assert mis["shadow_flights"] >= nee["shadow_flights"]
+    assert uni["medium_events"] == nee["medium_events"] == mis["medium_events"]
+    cond = workloads.render_scene(width=16, height=16, spp=4, phase="conductor", eta=(0, 0, 0), k=(0, 0, 0))
+    img, _ = oracle.render(workloads.render_medium("sphere_1d_nee"), cond)
+    assert np.array_equal(img, mir)
+    cu = workloads.render_scene(width=16, height=16, spp=4, phase="conductor")
+    img, _ = oracle.render(workloads.render_medium("sphere_1d_nee"), cu)
+    assert 0 < img.mean() < mir.mean()
+
+
+def test_oracle_specular_nee_needs_one_octave():
+    sc = workloads.render_scene(width=4, height=4, spp=1, phase="mirror")
+    desc = workloads.torus_plane_medium(octaves=3, sigma_a=0.0, sigma_s=1.0, sampling_scheme=abi.SCHEME_NEE)
+    with pytest.raises(abi.GpisError):
+        oracle.render(desc, sc)
+
+
+RENDER_CASES = [("sphere_1d", "lambert"), ("sphere_3d", "lambert"), ("torus", "lambert"), ("sphere_1d", "mirror"),
+                ("sphere_1d_nee", "mirror"), ("sphere_1d_mis", "conductor"), ("torus_nee", "conductor")]
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["sphere_1d", "sphere_3d", "torus"])
-def test_gpu_render_matches_restatement(kind):
+@pytest.mark.parametrize("kind,phase", RENDER_CASES)
+def test_gpu_render_matches_restatement(kind, phase):
     from gpis_extend_gb300 import runtime
     desc = workloads.render_medium(kind)
     size = 24 if kind == "sphere_3d" else 32
-    sc = workloads.render_scene(width=size, height=size, spp=4, max_bounces=4)
+    sc = workloads.render_scene(width=size, height=size, spp=4, max_bounces=4, phase=phase)
     with runtime.Context(desc) as ctx:
         g, gs = ctx.render(sc)
     c, cs = oracle.render(desc, sc)
     close = np.all(np.abs(g - c) <= 1e-3 * np.abs(c) + 1e-7, axis=2)
-    print(kind, "pixels within 1e-3", close.mean(), "identical", np.all(g == c, axis=2).mean(),
+    print(kind, phase, "pixels within 1e-3", close.mean(), "identical", np.all(g == c, axis=2).mean(),
           "means", g.mean(), c.mean(), gs, cs)
     assert close.mean() >= 0.99
     assert abs(g.mean() - c.mean()) <= 0.005 * c.mean()
     for k in ("distance_flights", "shadow_flights", "medium_events"):
         assert abs(gs[k] - cs[k]) <= 0.01 * cs[k] + 2, k
     assert gs["paths"] == size * size * 4
+    assert (gs["nee_queries"] > 0) == (desc.sampling_scheme != abi.SCHEME_UNI and phase != "lambert")
+
+
+@pytest.mark.gpu
+def test_gpu_render_nee_needs_one_octave():
+    from gpis_extend_gb300 import runtime
+    desc = workloads.torus_plane_medium(octaves=3, sigma_a=0.0, sigma_s=1.0, sampling_scheme=abi.SCHEME_NEE)
+    with runtime.Context(desc) as ctx:
+        with pytest.raises(abi.GpisError):
+            ctx.render(workloads.render_scene(width=4, height=4, spp=1, phase="mirror"))
