@@ -22,7 +22,11 @@ enum : uint32_t {
     MF_CORR_XY = 1u << 3,        // 1D_gradient_correlationXY
     MF_TRANSVERSE = 1u << 4,     // exact SE transverse law applies
     MF_XYZ_ORDER = 1u << 5,      // next3D drawn x first
+    MF_MULTIRES = 1u << 6,       // 2-level multi-resolution blend of the length scale
 };
+
+// Levels of the multi-resolution grid: scales 2.5^L for L in [-kMrLevels, kMrLevels).
+constexpr int kMrLevels = 16;
 
 // Per-medium constants derived on the host (all float values are rounded as the
 // reference's float expressions round them).
@@ -82,6 +86,14 @@ struct DevMedium {
     float skip_jump;        // e^{-kr^2/2} / norm1d per truncation crossing
     float oct_inv[4];       // 1 / oct_scale[k], exact where the scale is a power of two
     uint32_t oct_pow2;      // bit k: oct_scale[k] is a power of two (x / s == x * oct_inv[k])
+    // multi-resolution grid (MF_MULTIRES; ls_kind is 0 on the device so that the
+    // transforms and splats take the stationary forms, ls_params hold ls(p)):
+    // log(2.5f), the level scales powf(2.5f, L) and the per-level noise-seed
+    // offsets floor(log(scale) / log(2.5f)) at index L + kMrLevels, as the host's
+    // float library rounds them
+    float mr_log_base;
+    float mr_pow[2 * kMrLevels];
+    int32_t mr_seed[2 * kMrLevels];
 };
 
 struct PcgJump {

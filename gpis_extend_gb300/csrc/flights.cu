@@ -93,6 +93,55 @@ __device__ __forceinline__ float ns_scale_precise(const DevMedium &m, float x, f
     return __fdiv_rn(ls, m.ls_max);
 }
 
+// ---- multi-resolution grid ---------------------------------------------------------
+// ls(p) of the procedural length scale (the grid's lateral scale): float, and the
+// double evaluation on Vec3d(p) as ns_scale_precise takes it.
+__device__ __forceinline__ float ls_value(const DevMedium &m, float x, float z)
+{
+    const float *q = m.ls_params;
+    return q[0] + q[1] * sinf(q[2] * x) * cosf(q[3] * z);
+}
+
+__device__ __forceinline__ float ls_value_precise(const DevMedium &m, float x, float z)
+{
+    const float *q = m.ls_params;
+    const double v = __dmul_rn(__dmul_rn((double)q[1], sin(__dmul_rn((double)q[2], (double)x))),
+                               cos(__dmul_rn((double)q[3], (double)z)));
+    return (float)__dadd_rn((double)q[0], v);
+}
+
+// The two levels around ls: scales, weights and noise-seed offsets
+// (kernelScaleLevelRatio, SparseConvolutionNoise.cpp:101-111, and the seed
+// offset of evaluateNoise1DNormalized, :385).
+struct MrLevels {
+    float s[2], w[2];
+    uint32_t seed[2];
+};
+
+__device__ __forceinline__ MrLevels mr_levels(const DevMedium &m, float ls)
+{
+    const float lv = floorf(__fdiv_rn(logf(ls), m.mr_log_base));
+    int li = (int)lv;
+    li = li < -kMrLevels ? -kMrLevels : (li > kMrLevels - 2 ? kMrLevels - 2 : li);
+    MrLevels r;
+    r.s[0] = m.mr_pow[li + kMrLevels];
+    r.s[1] = m.mr_pow[li + kMrLevels + 1];
+    r.seed[0] = (uint32_t)m.mr_seed[li + kMrLevels];
+    r.seed[1] = (uint32_t)m.mr_seed[li + kMrLevels + 1];
+    const float frac = __fdiv_rn(__fsub_rn(ls, r.s[0]), __fsub_rn(r.s[1], r.s[0]));
+    const double f = (double)frac;
+    const double den = __dsqrt_rn(__dadd_rn(__dsub_rn(1.0, __dmul_rn(2.0, f)), __dmul_rn(__dmul_rn(2.0, f), f)));
+    r.w[0] = (float)__ddiv_rn(__dsub_rn(1.0, f), den);
+    r.w[1] = (float)__ddiv_rn(f, den);
+    return r;
+}
+
+// sqr(w_low) + sqr(w_high): the conditioning coefficients' divisor (conditioning1D, :602-633)
+__device__ __forceinline__ float mr_norm(const MrLevels &l)
+{
+    return __fadd_rn(__fmul_rn(l.w[0], l.w[0]), __fmul_rn(l.w[1], l.w[1]));
+}
+
 // getNonstationaryCovSplatCov1D(pq, pc) for the isotropic field.
 __device__ __forceinline__ float splat_cov_1d(float sq, float sc)
 {
@@ -111,6 +160,16 @@ __device__ __forceinline__ void ray_frame(const DevMedium &m, float dx, float dy
         iy = __fdiv_rn(iy, m.ls_max);
         iz = __fdiv_rn(iz, m.ls_max);
     }
+    normalize3_rn(ix, iy, iz);
+    make_frame(ix, iy, iz, f);
+}
+
+// The frame of transformPosDirWorldtoLocal(dir, s).normalized() at a level scale s.
+__device__ __forceinline__ void ray_frame_level(const DevMedium &m, const float d[3], float s, Frame &f)
+{
+    float ix = __fdiv_rn(__fmul_rn(m.l_inv[0], d[0]), s);
+    float iy = __fdiv_rn(__fmul_rn(m.l_inv[1], d[1]), s);
+    float iz = __fdiv_rn(__fmul_rn(m.l_inv[2], d[2]), s);
     normalize3_rn(ix, iy, iz);
     make_frame(ix, iy, iz, f);
 }
@@ -355,6 +414,86 @@ __device__ void transverse_moments(const DevMedium &m, const CondRec &c, const f
     }
 }
 
+// One level of the multi-resolution 1D noise at p (evaluateNoise1DNormalized at
+// kernelSpatialScale s): value, derivative along the ray and the transverse
+// conditioning splats; ow is the origin's weight of the level.
+__device__ __forceinline__ void noise1d_level(const DevMedium &m, const FlightIn &fl, const CondOct &co, bool cond,
+                                              const Frame &f, const float p[3], float s, uint32_t seed_off, float ow,
+                                              float &v, float &dv, float &gcx, float &gcy)
+{
+    const float z = ray_coord_oct(m, f.n, p[0], p[1], p[2], s);
+    noise1d_generic<true>(m, z, fl.noise_seed + seed_off, v, dv, 1.0f);
+    v *= m.inv_norm1d;
+    dv *= m.inv_norm1d;
+    gcx = gcy = 0.0f;
+    if (cond) {
+        const float oz = ray_coord_oct(m, f.n, fl.o[0], fl.o[1], fl.o[2], s);
+        const Cov1D k = cov1d(z - oz);
+        const float gzs = s * co.gs[2];
+        v += ow * (co.vs * k.k0 + gzs * k.k1);
+        dv += ow * (co.vs * k.k1 + gzs * k.k2);
+        if (m.flags & MF_CORR_XY) {
+            gcx = ow * s * co.gs[0] * k.k3;
+            gcy = ow * s * co.gs[1] * k.k3;
+        }
+    }
+}
+
+// evaluateGradientNoise1D on the multi-resolution grid (SparseConvolutionNoise.cpp:
+// 244-295): both levels' base gradients, a normal pair per level at the start of
+// the ray (pairs 0, 1) and at its end (pairs 2, 3), each level's gradient taken
+// to world space through its own frame and scale, blended by the level weights.
+__device__ void noise_gradient_mr(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
+                                  const float p[3], float t_segment, float &value, float g[3])
+{
+    const MrLevels lv = mr_levels(m, ls_value_precise(m, p[0], p[2]));
+    float ow[2] = {1.0f, 1.0f};
+    if (cond) {
+        const MrLevels lo = mr_levels(m, ls_value_precise(m, fl.o[0], fl.o[2]));
+        ow[0] = lo.w[0];
+        ow[1] = lo.w[1];
+    }
+    Frame f;
+    ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+    const float inv_s2 = 1.0f / 1.41421354f;
+    value = 0.0f;
+    g[0] = g[1] = g[2] = 0.0f;
+#pragma unroll 1
+    for (int j = 0; j < 2; ++j) {
+        float v, dv, gcx, gcy;
+        noise1d_level(m, fl, c.oct[0], cond, f, p, lv.s[j], lv.seed[j], ow[j], v, dv, gcx, gcy);
+        value += lv.w[j] * v;
+        float z0, z1;
+        normal_draws(fl.normal_seed, j, z0, z1);
+        const float x1 = z0 * inv_s2, y1 = z1 * inv_s2;
+        float gl[3];
+        if (t_segment == 0.0f) {
+            gl[0] = x1 + gcx;
+            gl[1] = y1 + gcy;
+        } else if (!((m.flags & MF_RENEWAL_PLUS) && (m.flags & MF_CORR_XY))) {
+            float z2, z3;
+            normal_draws(fl.normal_seed, 2 + j, z2, z3);
+            gl[0] = z2 * inv_s2 + gcx;
+            gl[1] = z3 * inv_s2 + gcy;
+        } else {
+            float fac, cv, z2, z3;
+            corr_moments(t_segment, fac, cv);
+            normal_draws(fl.normal_seed, 2 + j, z2, z3);
+            const float sq = sqrtf(cv);
+            gl[0] = (z2 * sq + fac * 2.0f * x1) + gcx;
+            gl[1] = (z3 * sq + fac * 2.0f * y1) + gcy;
+        }
+        gl[2] = dv;
+        Frame fj;
+        ray_frame_level(m, fl.d, lv.s[j], fj);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float gi = fj.t[i] * gl[0] + fj.b[i] * gl[1] + fj.n[i] * gl[2];
+            g[i] += lv.w[j] * (m.l_inv[i] * gi / lv.s[j]);
+        }
+    }
+}
+
 // Noise of octave k at p with its world gradient (evaluateGradientNoise1D /
 // evaluateNoise3D gradient).  cond: the octave's conditioning splats are active.
 __device__ __forceinline__ void noise_gradient_oct(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
@@ -373,6 +512,10 @@ __device__ __forceinline__ void noise_gradient_oct(const DevMedium &m, const Fli
 #pragma unroll
             for (int i = 0; i < 3; ++i) g[i] += cg[i];
         }
+        return;
+    }
+    if (m.flags & MF_MULTIRES) {
+        noise_gradient_mr(m, fl, c, cond, p, t_segment, value, g);
         return;
     }
     const CondOct &co = c.oct[oc];
@@ -465,6 +608,9 @@ __device__ __forceinline__ void condition_octave(const DevMedium &m, const Fligh
     if (amp == 0.0f) return;
     CondOct &co = c.oct[k];
     co.vs = (tv - mean) / amp - v;
+    // the multi-resolution splats carry both levels' weights (conditioning1D, :602-633)
+    const float mrn = (m.flags & MF_MULTIRES) ? mr_norm(mr_levels(m, ls_value_precise(m, fl.o[0], fl.o[2]))) : 1.0f;
+    if (m.flags & MF_MULTIRES) co.vs = __fdiv_rn(co.vs, mrn);
     if (!(m.flags & MF_RENEWAL_PLUS)) return;
     float delta[3];
 #pragma unroll
@@ -487,6 +633,10 @@ __device__ __forceinline__ void condition_octave(const DevMedium &m, const Fligh
         co.gs[0] = xy ? -2.0f * gx * s2 : 0.0f;
         co.gs[1] = xy ? -2.0f * gy * s2 : 0.0f;
         co.gs[2] = -2.0f * gz * s2;
+        if (m.flags & MF_MULTIRES) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) co.gs[i] = __fdiv_rn(co.gs[i], mrn);
+        }
         if (k == 0) {
 #pragma unroll
             for (int i = 0; i < 3; ++i) c.tgn[i] = (tg[i] - mg[i]) / amp;
@@ -628,6 +778,7 @@ struct LaneField {
     uint32_t n_imp;         // impulses per cell
     bool ns;                // nonstationary length scale
     float ls_o;             // kernel scale at the origin (conditioning)
+    float mr_ow[2];         // multi-resolution: the origin's weights of the low and high level
 };
 
 // Safe contents for a lane without a flight (collective evaluators run every lane).
@@ -648,6 +799,7 @@ __device__ __forceinline__ void lane_field_idle(LaneField &L, const DevMedium *m
     L.n_imp = 0u;
     L.ns = false;
     L.ls_o = 1.0f;
+    L.mr_ow[0] = L.mr_ow[1] = 1.0f;
 }
 
 // A lane's registers for flight fl of medium m; cond points at its conditioning record.
@@ -665,6 +817,12 @@ __device__ __forceinline__ void lane_field_setup(LaneField &L, const DevMedium &
     L.vs = L.gsz = L.ozc = 0.0f;
     L.ns = m.ls_kind != 0u;
     L.ls_o = 1.0f;
+    L.mr_ow[0] = L.mr_ow[1] = 1.0f;
+    if (GENERAL && (m.flags & MF_MULTIRES) && L.cond) {
+        const MrLevels lo = mr_levels(m, ls_value_precise(m, fl.o[0], fl.o[2]));
+        L.mr_ow[0] = lo.w[0];
+        L.mr_ow[1] = lo.w[1];
+    }
     L.mean_kind = m.mean_kind;
 #pragma unroll
     for (int k = 0; k < 6; ++k) L.mq[k] = m.mean_params[k];
@@ -881,6 +1039,33 @@ __device__ float field_precise(const LaneField &L, float px, float py, float pz,
         }
         return mean_plus_precise(m, __fmul_rn(L.sigma, noise), px, py, pz, id);
     }
+    if (m.flags & MF_MULTIRES) {
+        // evaluateValueNoise1D on the multi-resolution grid (SparseConvolutionNoise.cpp:156-165)
+        const MrLevels lv = mr_levels(m, ls_value_precise(m, px, pz));
+        float nl[2];
+#pragma unroll 1
+        for (int j = 0; j < 2; ++j) {
+            const float z = ray_coord_oct(m, L.n, px, py, pz, lv.s[j]);
+            float noise = noise1d_precise(m, z, L.seed + lv.seed[j], 1.0f);
+            if (L.cond) {
+                const float oz = ray_coord_oct(m, L.n, L.o[0], L.o[1], L.o[2], lv.s[j]);
+                const float d = __fsub_rn(z, oz);
+                const float den2 = m.cov_den2;
+                const float k0 = expf(-__fdiv_rn(__fmul_rn(d, d), den2));
+                const float r = -2.0f * d;
+                const float qh = __fdiv_rn(r, den2);
+                const float ql = __fdiv_rn(__fmaf_rn(-qh, den2, r), den2);
+                const float ph = __fmul_rn(qh, k0);
+                const float k1 = __fadd_rn(ph, __fmaf_rn(ql, k0, __fmaf_rn(qh, k0, -ph)));
+                const float vs0 = __fmul_rn(L.vs, k0);
+                const float gz0 = __fmul_rn(__fmul_rn(lv.s[j], L.gsz), k1);
+                noise = __fadd_rn(noise, __fmul_rn(L.mr_ow[j], __fadd_rn(vs0, gz0)));
+            }
+            nl[j] = noise;
+        }
+        const float nb = __fadd_rn(__fmul_rn(lv.w[0], nl[0]), __fmul_rn(lv.w[1], nl[1]));
+        return mean_plus_precise(m, __fmul_rn(L.sigma, nb), px, py, pz, id);
+    }
     const float ls = ns_scale_precise(m, px, pz);
     float an = 0.0f;
     for (int k = 0; k < (int)m.n_oct; ++k) {
@@ -931,6 +1116,25 @@ struct EvalGeneric {
     {
         const DevMedium &m = *L.m;
         float noise;
+        if (m.flags & MF_MULTIRES) {
+            const MrLevels lv = mr_levels(m, ls_value(m, px, pz));
+            noise = 0.0f;
+#pragma unroll 1
+            for (int j = 0; j < 2; ++j) {
+                const float z = ray_coord_oct(m, L.n, px, py, pz, lv.s[j]);
+                float v, dv;
+                noise1d_generic<false>(m, z, L.seed + lv.seed[j], v, dv, 1.0f);
+                float nk = v * m.inv_norm1d;
+                if (L.cond) {
+                    const float oz = ray_coord_oct(m, L.n, L.o[0], L.o[1], L.o[2], lv.s[j]);
+                    const Cov1D c = cov1d(z - oz);
+                    nk += L.mr_ow[j] * (L.vs * c.k0 + (lv.s[j] * L.gsz) * c.k1);
+                }
+                noise += lv.w[j] * nk;
+                refills += 3;
+            }
+            return L.sigma * noise + lane_mean(L, px, py, pz, id);
+        }
         if (m.flags & MF_ONE_D) {
             const float ls = ns_scale(m, px, pz);
             noise = 0.0f;
@@ -1819,7 +2023,26 @@ __global__ void k_debug_field(const DevMedium *mp, const float4 *origins, const 
     float v = 0.0f, g[3] = {0.0f, 0.0f, 0.0f}, fv_noise;
     // value and derivative parts of the noise (the 1D xy entries are the
     // conditioning splats); several octaves report amplitude-weighted sums
-    if (m.flags & MF_ONE_D) {
+    if (m.flags & MF_MULTIRES) {
+        Frame f;
+        ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+        const MrLevels lv = mr_levels(m, ls_value_precise(m, p[0], p[2]));
+        float ow[2] = {1.0f, 1.0f};
+        if (cond) {
+            const MrLevels lo = mr_levels(m, ls_value_precise(m, fl.o[0], fl.o[2]));
+            ow[0] = lo.w[0];
+            ow[1] = lo.w[1];
+        }
+        for (int j = 0; j < 2; ++j) {
+            float vk, dv, gx, gy;
+            noise1d_level(m, fl, c.oct[0], cond, f, p, lv.s[j], lv.seed[j], ow[j], vk, dv, gx, gy);
+            v += lv.w[j] * vk;
+            g[0] += lv.w[j] * gx;
+            g[1] += lv.w[j] * gy;
+            g[2] += lv.w[j] * dv;
+        }
+        fv_noise = m.sigma * v;
+    } else if (m.flags & MF_ONE_D) {
         Frame f;
         ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
         const float ls = ns_scale(m, p[0], p[2]);
@@ -1931,10 +2154,29 @@ __global__ void __launch_bounds__(128) k_nee(FlightArgs a, const float4 *point_t
     const float ls = ns_scale_precise(m, p[0], p[2]);
     const float z = ray_coord_oct(m, f.n, p[0], p[1], p[2], 1.0f);
     float v, dv;
+    float gc[3] = {0.0f, 0.0f, 0.0f};
+    const bool mr = (m.flags & MF_MULTIRES) != 0;
+    MrLevels lv = {};
+    if (mr) {
+        // the levels' parts, each weighted by w / s (SparseConvolutionNoise.cpp:687-692)
+        lv = mr_levels(m, ls_value_precise(m, p[0], p[2]));
+        float ow[2] = {1.0f, 1.0f};
+        if (cond) {
+            const MrLevels lo = mr_levels(m, ls_value_precise(m, fl.o[0], fl.o[2]));
+            ow[0] = lo.w[0];
+            ow[1] = lo.w[1];
+        }
+        for (int j = 0; j < 2; ++j) {
+            float gx, gy;
+            noise1d_level(m, fl, c.oct[0], cond, f, p, lv.s[j], lv.seed[j], ow[j], v, dv, gx, gy);
+            gc[0] += gx * lv.w[j] / lv.s[j];
+            gc[1] += gy * lv.w[j] / lv.s[j];
+            gc[2] += dv * lv.w[j] / lv.s[j];
+        }
+    } else {
     noise1d_generic<true>(m, z, fl.noise_seed, v, dv, ls);
     const float inrm = inv_norm_1d(m, ls);
     dv *= inrm;
-    float gc[3] = {0.0f, 0.0f, 0.0f};
     if (cond) {
         const CondOct &co = c.oct[0];
         const float oz = ray_coord_oct(m, f.n, fl.o[0], fl.o[1], fl.o[2], 1.0f);
@@ -1946,6 +2188,7 @@ __global__ void __launch_bounds__(128) k_nee(FlightArgs a, const float4 *point_t
         }
     }
     gc[2] = dv;
+    }
     // the gradient plane and the gradient that points along the normal
     float ppt[3], px[3], py[3], cr[3];
 #pragma unroll
@@ -1982,6 +2225,28 @@ __global__ void __launch_bounds__(128) k_nee(FlightArgs a, const float4 *point_t
             } else {
                 const double dx = (double)g3[0] - m0, dy = (double)g3[1] - m1;
                 pdf_area = exp(-0.5 * (dx * dx + dy * dy) / var) / (two_pi * var);
+            }
+        } else if (mr) {
+            // the multi-resolution law (SparseConvolutionNoise.cpp:776-808): transverse
+            // scales times 1 / sqrt((w_low / s_low)^2 + (w_high / s_high)^2)
+            const float a0 = lv.w[0] / lv.s[0], a1 = lv.w[1] / lv.s[1];
+            const float nss = (float)(1.0 / (double)sqrtf(a0 * a0 + a1 * a1));
+            if (!((m.flags & MF_RENEWAL_PLUS) && (m.flags & MF_CORR_XY)) || t_seg == 0.0f) {
+                const float sx = (float)((double)(g3[0] - gc[0]) * 1.4142135623730951 * nss);
+                const float sy = (float)((double)(g3[1] - gc[1]) * 1.4142135623730951 * nss);
+                pdf_area = exp(-(double)(sx * sx) / 2.0) * exp(-(double)(sy * sy) / 2.0) / two_pi * 2.0 * nss * nss;
+            } else {
+                float z0, z1, z2, z3, fac, cv;
+                normal_draws(nseed, 0, z0, z1);
+                normal_draws(nseed, 1, z2, z3);
+                corr_moments(t_seg, fac, cv);
+                const double s2 = 1.41421354;
+                const double mx = fac * 2.0 * ((double)z0 / s2 * lv.w[0] / lv.s[0] + (double)z2 / s2 * lv.w[1] / lv.s[1]);
+                const double my = fac * 2.0 * ((double)z1 / s2 * lv.w[0] / lv.s[0] + (double)z3 / s2 * lv.w[1] / lv.s[1]);
+                const double sq = sqrt((double)cv);
+                const float sx = (float)(((double)(g3[0] - gc[0]) - mx) / sq * nss);
+                const float sy = (float)(((double)(g3[1] - gc[1]) - my) / sq * nss);
+                pdf_area = exp(-(double)(sx * sx) / 2.0) * exp(-(double)(sy * sy) / 2.0) / (two_pi * cv) * (double)(nss * nss);
             }
         } else if (!((m.flags & MF_RENEWAL_PLUS) && (m.flags & MF_CORR_XY)) || t_seg == 0.0f) {
             const float sc = splat_cov_1d(ls, ls);
@@ -2049,7 +2314,7 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     const uint32_t blocks = (a.n + 127) / 128;
     if (ev) cudaEventRecord(ev[0], stream);
     // the stationary cooperative fast pass takes its per-flight set-up from k_prepare
-    const bool coop_plain = a.one_d && a.max_imp <= 8 && a.max_oct == 1 && !a.any_ns && !a.all_grid;
+    const bool coop_plain = a.one_d && a.max_imp <= 8 && a.max_oct == 1 && !a.any_ns && !a.all_grid && !a.any_mr;
     FlightArgs b = a;
     if (!coop_plain) b.setup = nullptr;     // the march kernels read set-up records only when written
     if (b.any_cond || b.setup) k_prepare<<<blocks, 128, 0, stream>>>(b);
@@ -2069,8 +2334,12 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
         return c == 0 ? 1u : c;
     };
     if (ev) cudaEventRecord(ev[2], stream);
-    const bool coop = a.one_d && a.max_imp <= 8 && a.max_oct == 1;
-    if (a.one_d && a.max_imp <= 8 && a.max_oct > 1) {
+    // multi-resolution media take the generic evaluator (two levels per evaluation)
+    const bool coop = a.one_d && a.max_imp <= 8 && a.max_oct == 1 && !a.any_mr;
+    if (a.any_mr) {
+        const void *fn = (const void *)k_march<EvalGeneric, false>;
+        k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(b);
+    } else if (a.one_d && a.max_imp <= 8 && a.max_oct > 1) {
         const void *fn = (const void *)k_march<EvalCoopOct, false>;
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemOct);
         if (e != cudaSuccess) return e;

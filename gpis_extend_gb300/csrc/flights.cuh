@@ -50,6 +50,7 @@ struct FlightArgs {
     uint32_t max_oct;           // max octaves over the media
     int all_grid;               // all media have a grid mean
     int any_ns;                 // some medium has a nonstationary length scale
+    int any_mr;                 // some medium blends multi-resolution levels
 };
 
 // Upload the jump-ahead PCG table to the current device (once per device).

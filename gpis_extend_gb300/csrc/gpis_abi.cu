@@ -62,7 +62,6 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
     if (d.sampling_scheme > GPIS_SCHEME_MIS) return fail(GPIS_EINVAL, "unknown 1D_sampling_scheme");
     for (int i = 0; i < 8; ++i)
         if (!std::isfinite(d.mean_params[i])) return fail(GPIS_EINVAL, "mean parameters must be finite");
-    if (d.multires) return fail(GPIS_ENOTSUP, "multi-resolution fields are not supported");
     if (d.n_octaves < 1 || d.n_octaves > 4) return fail(GPIS_EINVAL, "n_octaves must be in 1..4");
     if (d.ls_kind > GPIS_LS_SINCOS) return fail(GPIS_EINVAL, "unknown ls_kind");
     if ((d.ls_kind != GPIS_LS_CONSTANT || d.n_octaves != 1) && !d.one_d_sampling)
@@ -71,6 +70,17 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         if (!(std::isfinite(d.ls_max) && d.ls_max > 0.0f)) return fail(GPIS_EINVAL, "ls_max must be finite and > 0");
         for (int i = 0; i < 4; ++i)
             if (!std::isfinite(d.ls_params[i])) return fail(GPIS_EINVAL, "ls parameters must be finite");
+    }
+    // _multiResolutionGrid = !isStationaryKernel() && useMultiResolutionGrid() (SparseConvolutionNoise.cpp:47)
+    const bool multires = d.multires && d.ls_kind != GPIS_LS_CONSTANT;
+    if (multires) {
+        if (d.n_octaves != 1) return fail(GPIS_ENOTSUP, "multi-resolution fields take one octave");
+        const float lo = d.ls_params[0] - std::fabs(d.ls_params[1]), hi = d.ls_params[0] + std::fabs(d.ls_params[1]);
+        if (!(lo > 0.0f) || !std::isfinite(hi))
+            return fail(GPIS_EINVAL, "multi-resolution fields need ls(p) > 0 everywhere");
+        const float lb = std::log(2.5f);
+        if (std::floor(std::log(lo) / lb) < -gpis::kMrLevels || std::floor(std::log(hi) / lb) >= gpis::kMrLevels - 1)
+            return fail(GPIS_ERANGE, "multi-resolution length scales outside 2.5^[-16, 15)");
     }
     if (d.n_octaves > 1)
         for (uint32_t k = 0; k < d.n_octaves; ++k)
@@ -133,6 +143,7 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         d.ls_kind == GPIS_LS_CONSTANT && d.n_octaves == 1)
         flags |= gpis::MF_TRANSVERSE;
     if (d.impulse_xyz_order) flags |= gpis::MF_XYZ_ORDER;
+    if (multires) flags |= gpis::MF_MULTIRES;
     m.flags = flags;
     m.mean_kind = d.mean_kind;
     std::memcpy(m.mean_params, d.mean_params, sizeof(m.mean_params));
@@ -146,9 +157,19 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         m.grid_offset = g->offset;
         m.grid_scale = g->scale;
     }
-    m.ls_kind = d.ls_kind;
+    m.ls_kind = multires ? 0u : d.ls_kind;
     for (int i = 0; i < 4; ++i) m.ls_params[i] = d.ls_params[i];
-    m.ls_max = d.ls_kind != GPIS_LS_CONSTANT ? d.ls_max : 1.0f;
+    m.ls_max = d.ls_kind != GPIS_LS_CONSTANT && !multires ? d.ls_max : 1.0f;
+    // kernelScaleLevelRatio's float log / pow (SparseConvolutionNoise.cpp:101-111, 385),
+    // evaluated by the float library at run time (no compile-time folding), as the
+    // CPU restatement evaluates them
+    volatile float base = 2.5f;
+    m.mr_log_base = std::log((float)base);
+    for (int l = -gpis::kMrLevels; l < gpis::kMrLevels; ++l) {
+        const float sc = std::pow((float)base, (float)l);
+        m.mr_pow[l + gpis::kMrLevels] = sc;
+        m.mr_seed[l + gpis::kMrLevels] = (int32_t)std::floor(std::log(sc) / m.mr_log_base);
+    }
     m.n_oct = d.n_octaves;
     for (int k = 0; k < 4; ++k) {
         const bool on = (uint32_t)k < d.n_octaves && d.n_octaves > 1;
@@ -229,7 +250,7 @@ struct gpis_ctx {
     int n_media = 0;
     gpis::DevMedium *d_media = nullptr;
     std::vector<float *> d_grids;
-    bool any_cond = false, all_one_d = true, all_three_d = true, all_grid = true, any_ns = false;
+    bool any_cond = false, all_one_d = true, all_three_d = true, all_grid = true, any_ns = false, any_mr = false;
     uint32_t max_imp = 0, max_oct = 1;
     // scratch of the flight kernels
     gpis::CondRec *d_cond = nullptr;
@@ -411,6 +432,7 @@ int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
             c->max_oct = std::max(c->max_oct, m.n_oct);
             c->all_grid = c->all_grid && m.mean_kind == GPIS_MEAN_GRID;
             c->any_ns = c->any_ns || m.ls_kind != 0u;
+            c->any_mr = c->any_mr || (m.flags & gpis::MF_MULTIRES) != 0u;
         }
         if (rc) break;
         if ((e = cudaMalloc(&c->d_media, host.size() * sizeof(gpis::DevMedium))) != cudaSuccess) { rc = cuda_fail(e, "allocate media"); break; }
@@ -472,6 +494,7 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.max_oct = ctx->max_oct;
     a.all_grid = ctx->all_grid;
     a.any_ns = ctx->any_ns;
+    a.any_mr = ctx->any_mr;
     for (const void *p : {(const void *)in->origin_near, (const void *)in->dir_far, (const void *)in->seeds,
                           (const void *)in->prev, (const void *)out->rec})
         if (p && (reinterpret_cast<uintptr_t>(p) & 15u))

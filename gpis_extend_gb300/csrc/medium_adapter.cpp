@@ -79,12 +79,14 @@ struct Flights {
     }
 };
 
-// samplingScheme at the end point (SparseConvolutionNoise.cpp:68-76).
+// samplingScheme at the end point (SparseConvolutionNoise.cpp:68-76); the
+// observed-origin case needs the stationary SE covariance.
 uint32_t scheme_at(const gpis_medium_desc &d, bool conditioned_rp, float t)
 {
     if (d.single_realization || !d.one_d_sampling) return GPIS_SCHEME_UNI;
     if (d.sigma < 1e-6f) return GPIS_SCHEME_UNI;
-    if (d.correlation_xy && conditioned_rp && t == 0.0f) return GPIS_SCHEME_UNI;  // p == ray origin
+    if (d.correlation_xy && conditioned_rp && t == 0.0f && d.ls_kind == GPIS_LS_CONSTANT)
+        return GPIS_SCHEME_UNI;  // p == ray origin
     return d.sampling_scheme;
 }
 

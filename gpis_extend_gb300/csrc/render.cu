@@ -63,7 +63,7 @@ struct RtMedium {
     // samplingScheme (SparseConvolutionNoise.cpp:68-76) of an event
     uint32_t scheme;            // the medium's 1D sampling scheme
     uint32_t scheme_uni;        // UNI whatever the event: single realization, 3D noise or sigma < 1e-6
-    uint32_t xy_renewal_plus;   // correlationXY under Renewal+: UNI at t = 0 after a conditioned flight
+    uint32_t xy_renewal_plus;   // correlationXY under Renewal+ (SE covariance): UNI at t = 0 after a conditioned flight
 };
 
 struct RtScene {
@@ -767,7 +767,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     const float sa = md->sigma_a * md->density, ss = md->sigma_s * md->density;
     if (!(ss > 0.0f)) return gpis_internal_set_error(GPIS_ENOTSUP, "the renderer needs a scattering medium (sigma_s > 0)");
     if (sc.phase != GPIS_PHASE_LAMBERT && md->sampling_scheme != GPIS_SCHEME_UNI && md->one_d_sampling &&
-        (md->n_octaves > 1 || md->multires))
+        md->n_octaves > 1)
         return gpis_internal_set_error(GPIS_ENOTSUP, "1D NEE and MIS need a single-octave medium");
 
     RtMedium M;
@@ -780,7 +780,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     M.scheme = md->sampling_scheme;
     M.scheme_uni = md->single_realization || !md->one_d_sampling || md->sigma < 1e-6f;
     M.xy_renewal_plus = md->correlation_xy && !md->single_realization &&
-                        md->correlation_context == GPIS_CTX_RENEWAL_PLUS;
+                        md->correlation_context == GPIS_CTX_RENEWAL_PLUS && md->ls_kind == GPIS_LS_CONSTANT;
     const bool specular_nee = sc.phase != GPIS_PHASE_LAMBERT && !M.scheme_uni && M.scheme != GPIS_SCHEME_UNI;
 
     RtScene S;

@@ -194,13 +194,15 @@ def render_medium(kind="sphere_3d"):
     sphere_1d  the same field with 1D noise and Renewal+;
     torus      the nonstationary three-octave torus-union-plane field (1D, Renewal+);
     sphere_1d_nee, sphere_1d_mis  sphere_1d with the NEE or MIS 1D sampling scheme;
-    torus_nee  the nonstationary single-octave torus-union-plane field with NEE."""
+    torus_nee  the nonstationary single-octave torus-union-plane field with NEE;
+    torus_mr_nee  the same length scale on the multi-resolution grid with NEE."""
     if kind in ("sphere_1d_nee", "sphere_1d_mis"):
         return sphere_medium(one_d=True, context=abi.CTX_RENEWAL_PLUS, sigma_a=0.0, sigma_s=1.0,
                              sampling_scheme=abi.SCHEME_NEE if kind.endswith("nee") else abi.SCHEME_MIS)
-    if kind == "torus_nee":
+    if kind in ("torus_nee", "torus_mr_nee", "torus_mr"):
         return torus_plane_medium(nonstationary=True, octaves=1, sigma_a=0.0, sigma_s=1.0,
-                                  sampling_scheme=abi.SCHEME_NEE)
+                                  multires=int(kind.startswith("torus_mr")),
+                                  sampling_scheme=abi.SCHEME_UNI if kind == "torus_mr" else abi.SCHEME_NEE)
     if kind == "sphere_3d":
         return sphere_medium(one_d=False, context=abi.CTX_RENEWAL, sigma_a=0.0, sigma_s=1.0)
     if kind == "sphere_1d":

@@ -20,6 +20,13 @@
 #define _GNU_SOURCE
 #include "gpis_oracle.h"
 
+/* multi-resolution grid: _base (SparseConvolutionNoise.cpp:49), read at run time so
+ * that logf / powf of it are the float library's, and the range of levels a
+ * medium may use */
+static volatile float mr_base_v = 2.5f;
+#define MR_BASE ((float)mr_base_v)
+#define MR_LEVEL_MAX 16
+
 #include <math.h>
 #include <pthread.h>
 #include <stdatomic.h>
@@ -206,6 +213,7 @@ typedef struct {
     float kr_iso;            /* splattingKernelRadius(true, 1), GPFunctions.cpp:706-709 */
     float kr_world;          /* splattingKernelRadius(false, 1), GPFunctions.cpp:711-718 */
     float ls_max;            /* sparseConvNoiseMaxLateralScale */
+    int multires;            /* 2-level multi-resolution blend (SparseConvolutionNoise.cpp:47-49) */
     /* grid mean copy */
     const float *grid_vox;
 } om_t;
@@ -218,9 +226,19 @@ static int om_init(om_t *m, const gpis_medium_desc *d)
         return GPIS_EINVAL;
     if (d->n_octaves < 1 || d->n_octaves > 4) return GPIS_EINVAL;
     if (d->mean_kind == GPIS_MEAN_GRID && (!d->grid || !d->grid->voxels)) return GPIS_EINVAL;
-    if (d->multires) return GPIS_ENOTSUP;
     if ((d->ls_kind != GPIS_LS_CONSTANT || d->n_octaves != 1) && !d->one_d_sampling) return GPIS_ENOTSUP;
     if (d->ls_kind != GPIS_LS_CONSTANT && !(d->ls_max > 0.0f)) return GPIS_EINVAL;
+    /* _multiResolutionGrid = !isStationaryKernel() && useMultiResolutionGrid() */
+    m->multires = d->multires && d->ls_kind != GPIS_LS_CONSTANT;
+    if (m->multires) {
+        if (d->n_octaves != 1) return GPIS_ENOTSUP;
+        /* the levels need ls(p) > 0 everywhere: a - |b| > 0 for the sin-cos field, and
+           levels inside [-MR_LEVEL_MAX, MR_LEVEL_MAX) */
+        const float lo = d->ls_params[0] - fabsf(d->ls_params[1]), hi = d->ls_params[0] + fabsf(d->ls_params[1]);
+        if (!(lo > 0.0f) || !isfinite(hi)) return GPIS_EINVAL;
+        if (floorf(logf(lo) / logf(MR_BASE)) < -MR_LEVEL_MAX || floorf(logf(hi) / logf(MR_BASE)) >= MR_LEVEL_MAX - 1)
+            return GPIS_ERANGE;
+    }
     m->n_imp = (uint32_t)d->impulse_density;
     m->activate_cond = !d->single_realization &&
         (d->correlation_context == GPIS_CTX_RENEWAL || d->correlation_context == GPIS_CTX_RENEWAL_PLUS);
@@ -235,7 +253,8 @@ static int om_init(om_t *m, const gpis_medium_desc *d)
         m->l_inv[i] = inv;
     }
     m->nonstationary = d->ls_kind != GPIS_LS_CONSTANT;
-    m->ls_max = m->nonstationary ? d->ls_max : 1.0f;
+    /* the maximum lateral scale enters the brute-force transforms only */
+    m->ls_max = m->nonstationary && !m->multires ? d->ls_max : 1.0f;
     float mtx = fmaxf(fmaxf(m->l_aniso[0], m->l_aniso[1]), m->l_aniso[2]);
     /* NonstationaryCovariance::splattingKernelRadius (GPFunctions.cpp:1250-1254) scales
        localScale by the maximum lateral scale in brute-force mode. */
@@ -256,32 +275,64 @@ static inline float ls_field(const om_t *m, const float p[3])
     return (float)((double)q[0] + (double)q[1] * sin((double)q[2] * p[0]) * cos((double)q[3] * p[2]));
 }
 
-/* nonStationarySplattingKernelScale, GPFunctions.cpp:1229-1235 (brute force) */
+/* nonStationarySplattingKernelScale, GPFunctions.cpp:1229-1235: ls(p) / ls_max by
+ * brute force, 1 on the multi-resolution grid */
 static inline float ns_scale(const om_t *m, const float p[3])
 {
-    if (!m->nonstationary) return 1.0f;
+    if (!m->nonstationary || m->multires) return 1.0f;
     return ls_field(m, p) / m->ls_max;
 }
 
-/* transformPosDirWorldtoLocal (GPFunctions.cpp:634-636; nonstationary 1268-1271) */
+/* transformPosDirWorldtoLocal (GPFunctions.cpp:634-636; nonstationary 1270-1273:
+ * the maximum lateral scale by brute force, the level scale on the
+ * multi-resolution grid) */
+static inline float ns_transform_scale(const om_t *m, float scale)
+{
+    return m->nonstationary && !m->multires ? m->ls_max : scale;
+}
+
 static inline void w2l_pos(const om_t *m, const float v[3], float scale, float o[3])
 {
-    float s = m->nonstationary ? m->ls_max : scale;
+    float s = ns_transform_scale(m, scale);
     for (int i = 0; i < 3; ++i) o[i] = (m->l_inv[i] * v[i]) / s;
 }
 
-/* transformGradLocaltoWorld (GPFunctions.cpp:644) */
+/* transformGradLocaltoWorld (GPFunctions.cpp:644; nonstationary 1285-1288) */
 static inline void l2w_grad(const om_t *m, const float v[3], float scale, float o[3])
 {
-    float s = m->nonstationary ? m->ls_max : scale;
+    float s = ns_transform_scale(m, scale);
     for (int i = 0; i < 3; ++i) o[i] = (m->l_inv[i] * v[i]) / s;
 }
 
-/* transformGradWorldtoLocal (GPFunctions.cpp:642) */
+/* transformGradWorldtoLocal (GPFunctions.cpp:642; nonstationary 1280-1283) */
 static inline void w2l_grad(const om_t *m, const float v[3], float scale, float o[3])
 {
-    float s = m->nonstationary ? m->ls_max : scale;
+    float s = ns_transform_scale(m, scale);
     for (int i = 0; i < 3; ++i) o[i] = (m->l_aniso[i] * v[i]) * s;
+}
+
+/* kernelScaleLevelRatio (SparseConvolutionNoise.cpp:101-111), float overloads of
+ * log / floor / pow: (scale of the low level, of the high level, weight of the
+ * low level, weight of the high level), the weights of unit total variance. */
+static void level_ratio(const om_t *m, const float p[3], float info[4])
+{
+    const float ls = ls_field(m, p);
+    const float level_low = floorf(logf(ls) / logf(MR_BASE));
+    const float level_high = level_low + 1;
+    const float sl = powf(MR_BASE, level_low), sh = powf(MR_BASE, level_high);
+    const float frac = (ls - sl) / (sh - sl);
+    const double den = sqrt(1.0 - 2.0 * frac + 2.0 * frac * frac);
+    info[0] = sl;
+    info[1] = sh;
+    info[2] = (float)((1.0 - frac) / den);
+    info[3] = (float)(frac / den);
+}
+
+/* the per-level seed offset floor(log(scale) / log(base)) of evaluateNoise1DNormalized
+ * (SparseConvolutionNoise.cpp:385) */
+static inline uint32_t level_seed(float scale)
+{
+    return (uint32_t)(int)floorf(logf(scale) / logf(MR_BASE));
 }
 
 /* ------------------------------------------------------------------------ */
@@ -456,7 +507,7 @@ static inline float amplitude(const real_t *r)
 
 /* 1D query coordinate p_iso_ray.z (evaluateNoise1DNormalized, SparseConvolutionNoise.cpp:381-384),
  * with the octave's length-scale multiplier folded into the iso transform. */
-static float coord_1d(const real_t *r, const float p[3], const float dir[3], frame_t *f)
+static float coord_1d(const real_t *r, const float p[3], const float dir[3], float ks, frame_t *f)
 {
     const om_t *m = r->m;
     float sc = oct_scale(m, r->octave);
@@ -464,7 +515,7 @@ static float coord_1d(const real_t *r, const float p[3], const float dir[3], fra
     w2l_pos(m, dir, 1.0f, diso);
     normalize3f(diso, diso_n);
     frame_make(diso_n, f);
-    w2l_pos(m, p, 1.0f, piso);
+    w2l_pos(m, p, ks, piso);
     if (sc != 1.0f)
         for (int i = 0; i < 3; ++i) piso[i] = piso[i] / sc;
     return dot3f(f->n, piso);
@@ -571,15 +622,17 @@ static inline float splat_cov_1d(const om_t *m, const float pq[3], const float p
     return sqrtf(s);
 }
 
-/* evaluateNoise1DNormalized (SparseConvolutionNoise.cpp:379-417).
+/* evaluateNoise1DNormalized (SparseConvolutionNoise.cpp:379-417) at kernel spatial
+ * scale ks (1, or a level scale of the multi-resolution grid; low selects the
+ * origin's level weight of the conditioning splats).
  * out = (value, cond x splat, cond y splat, dvalue/dz); float mode or FP64. */
-static void noise1d_norm(const real_t *r, const float p[3], const float dir[3], int cond,
-                         int dbl, double out[4])
+static void noise1d_level(const real_t *r, const float p[3], const float dir[3], int cond,
+                          int dbl, float ks, int low, double out[4])
 {
     const om_t *m = r->m;
     frame_t f;
-    float z = coord_1d(r, p, dir, &f);
-    uint32_t seed = r->noise_seed + oct_seed(m, r->octave);
+    float z = coord_1d(r, p, dir, ks, &f);
+    uint32_t seed = r->noise_seed + oct_seed(m, r->octave) + (m->multires ? level_seed(ks) : 0u);
     float ls = ns_scale(m, p);
     /* sparseConvNoiseVariance1D: impulseDensity/kernelRadius (float) * sqrt(pi) * localScale */
     float var = (float)((double)(m->d.impulse_density / m->kr_iso) * (sqrt(M_PI) * (double)ls));
@@ -602,7 +655,16 @@ static void noise1d_norm(const real_t *r, const float p[3], const float dir[3], 
         const coef_t *c = &r->c1;
         float oiso[3], oray[3];
         float sc = oct_scale(m, r->octave);
-        w2l_pos(m, c->origin, 1.0f, oiso);
+        /* kernelSpatialScale: the level scale, or the octave's length multiplier */
+        const float kss = m->multires ? ks : sc;
+        /* origin_scale_factor: the origin's weight of this level (multi-resolution) */
+        float osf = 1.0f;
+        if (m->multires) {
+            float oinfo[4];
+            level_ratio(m, c->origin, oinfo);
+            osf = low ? oinfo[2] : oinfo[3];
+        }
+        w2l_pos(m, c->origin, ks, oiso);
         if (sc != 1.0f)
             for (int i = 0; i < 3; ++i) oiso[i] = oiso[i] / sc;
         frame_to_local(&f, oiso, oray);
@@ -612,30 +674,51 @@ static void noise1d_norm(const real_t *r, const float p[3], const float dir[3], 
             float k[4];
             cov1d_f(d, a, k);
             float vs0 = c->value_scale * k[0], vs1 = c->value_scale * k[1];
-            float gz0 = sc * c->gs[2] * k[1], gz1 = sc * c->gs[2] * k[2];
-            float nv = (float)v[0] + 1.0f * (vs0 + gz0);
-            float ng = (float)v[1] + 1.0f * (vs1 + gz1);
+            float gz0 = kss * c->gs[2] * k[1], gz1 = kss * c->gs[2] * k[2];
+            float nv = (float)v[0] + osf * (vs0 + gz0);
+            float ng = (float)v[1] + osf * (vs1 + gz1);
             v[0] = nv; v[1] = ng;
             if (m->d.correlation_xy) {
                 float kt[4], kb[4];
                 cov1d_f(d, a, kt);   /* the tangent/bitangent directions only enter through a */
                 cov1d_f(d, a, kb);
-                gx = 1.0f * sc * c->gs[0] * kt[3];
-                gy = 1.0f * sc * c->gs[1] * kb[3];
+                gx = osf * kss * c->gs[0] * kt[3];
+                gy = osf * kss * c->gs[1] * kb[3];
             }
         } else {
             double d = (double)z - (double)oray[2];
             double k[4];
             cov1d_d(d, (double)a, k);
-            v[0] += c->value_scale * k[0] + (double)sc * c->gs[2] * k[1];
-            v[1] += c->value_scale * k[1] + (double)sc * c->gs[2] * k[2];
+            v[0] += (double)osf * (c->value_scale * k[0] + (double)kss * c->gs[2] * k[1]);
+            v[1] += (double)osf * (c->value_scale * k[1] + (double)kss * c->gs[2] * k[2]);
             if (m->d.correlation_xy) {
-                gx = (double)sc * c->gs[0] * k[3];
-                gy = (double)sc * c->gs[1] * k[3];
+                gx = (double)osf * kss * c->gs[0] * k[3];
+                gy = (double)osf * kss * c->gs[1] * k[3];
             }
         }
     }
     out[0] = v[0]; out[1] = gx; out[2] = gy; out[3] = v[1];
+}
+
+/* evaluateValueNoise1D (SparseConvolutionNoise.cpp:156-165): one level, or the
+ * blend w_low * noise_low + w_high * noise_high of the two levels around ls(p)
+ * on the multi-resolution grid (every component blended the same way). */
+static void noise1d_norm(const real_t *r, const float p[3], const float dir[3], int cond,
+                         int dbl, double out[4])
+{
+    const om_t *m = r->m;
+    if (!m->multires) {
+        noise1d_level(r, p, dir, cond, dbl, 1.0f, 1, out);
+        return;
+    }
+    float info[4];
+    level_ratio(m, p, info);
+    double lo[4], hi[4];
+    noise1d_level(r, p, dir, cond, dbl, info[0], 1, lo);
+    noise1d_level(r, p, dir, cond, dbl, info[1], 0, hi);
+    for (int k = 0; k < 4; ++k)
+        out[k] = dbl ? (double)info[2] * lo[k] + (double)info[3] * hi[k]
+                     : (double)(info[2] * (float)lo[k] + info[3] * (float)hi[k]);
 }
 
 /* --- 3D noise (world space) -------------------------------------------- */
@@ -810,7 +893,7 @@ static inline int transverse_law(const om_t *m)
     /* seTransverseGradientMoments needs a SquaredExponentialCovariance (a
        nonstationary wrapper fails the dynamic_cast) and one realization */
     return m->d.one_d_sampling && m->d.correlation_xy &&
-           m->d.correlation_context == GPIS_CTX_RENEWAL_PLUS && !m->d.multires &&
+           m->d.correlation_context == GPIS_CTX_RENEWAL_PLUS && !m->multires &&
            !m->nonstationary && m->d.n_octaves == 1;
 }
 
@@ -843,6 +926,74 @@ static int transverse_moments(const real_t *r, const float p[3], const float dir
     return 1;
 }
 
+/* evaluateGradientNoise1D on the multi-resolution grid (SparseConvolutionNoise.cpp:
+ * 244-295): the two levels' base gradients, two normal pairs (low, high) at the
+ * start of the ray and two more at its end, each level's gradient taken to world
+ * space through its own frame and scale, blended by the level weights. */
+static void grad_noise_1d_levels(const real_t *r, const float p[3], float t_segment, const float dir[3],
+                                 int cond, double xs0, double xs1, float out[3])
+{
+    const om_t *m = r->m;
+    float info[4];
+    level_ratio(m, p, info);
+    double lo4[4], hi4[4];
+    noise1d_level(r, p, dir, cond, 0, info[0], 1, lo4);
+    noise1d_level(r, p, dir, cond, 0, info[1], 0, hi4);
+    const float blo[3] = {(float)lo4[1], (float)lo4[2], (float)lo4[3]};
+    const float bhi[3] = {(float)hi4[1], (float)hi4[2], (float)hi4[3]};
+    pcg_t g;
+    pcg_set_state(&g, (uint64_t)r->normal_seed);
+    double x1l[2], x1h[2];
+    rand_normal_2(&g, x1l);
+    rand_normal_2(&g, x1h);
+    const double s2 = (double)sqrtf(2.f);
+    for (int i = 0; i < 2; ++i) {
+        x1l[i] /= s2;
+        x1h[i] /= s2;
+    }
+    float gl[3], gh[3];
+    if (t_segment == 0) {
+        x1l[0] *= xs0; x1l[1] *= xs1;
+        x1h[0] *= xs0; x1h[1] *= xs1;
+        gl[0] = (float)x1l[0] + blo[0]; gl[1] = (float)x1l[1] + blo[1];
+        gh[0] = (float)x1h[0] + bhi[0]; gh[1] = (float)x1h[1] + bhi[1];
+    } else if (!(m->d.correlation_context == GPIS_CTX_RENEWAL_PLUS && m->d.correlation_xy)) {
+        double x2l[2], x2h[2];
+        rand_normal_2(&g, x2l);
+        rand_normal_2(&g, x2h);
+        x2l[0] = x2l[0] / s2 * xs0; x2l[1] = x2l[1] / s2 * xs1;
+        x2h[0] = x2h[0] / s2 * xs0; x2h[1] = x2h[1] / s2 * xs1;
+        gl[0] = (float)x2l[0] + blo[0]; gl[1] = (float)x2l[1] + blo[1];
+        gh[0] = (float)x2h[0] + bhi[0]; gh[1] = (float)x2h[1] + bhi[1];
+    } else {
+        double fac, cov;
+        corr_moments(t_segment, &fac, &cov);
+        double x2l[2], x2h[2];
+        rand_normal_2(&g, x2l);
+        rand_normal_2(&g, x2h);
+        const double sc = sqrt(cov);
+        gl[0] = (float)(x2l[0] * sc + fac * 2.0 * x1l[0]) + blo[0];
+        gl[1] = (float)(x2l[1] * sc + fac * 2.0 * x1l[1]) + blo[1];
+        gh[0] = (float)(x2h[0] * sc + fac * 2.0 * x1h[0]) + bhi[0];
+        gh[1] = (float)(x2h[1] * sc + fac * 2.0 * x1h[1]) + bhi[1];
+    }
+    gl[2] = 0.f + blo[2];
+    gh[2] = 0.f + bhi[2];
+    float dl[3], dh[3], dln[3], dhn[3], gil[3], gih[3], gwl[3], gwh[3];
+    frame_t fl, fh;
+    w2l_pos(m, dir, info[0], dl);
+    normalize3f(dl, dln);
+    frame_make(dln, &fl);
+    w2l_pos(m, dir, info[1], dh);
+    normalize3f(dh, dhn);
+    frame_make(dhn, &fh);
+    frame_to_global(&fl, gl, gil);
+    frame_to_global(&fh, gh, gih);
+    l2w_grad(m, gil, info[0], gwl);
+    l2w_grad(m, gih, info[1], gwh);
+    for (int i = 0; i < 3; ++i) out[i] = info[2] * gwl[i] + info[3] * gwh[i];
+}
+
 /* evaluateGradientNoise1D (SparseConvolutionNoise.cpp:178-243), stationary branch. */
 static void grad_noise_1d(const real_t *r, const float p[3], float t_segment, const float dir[3],
                           int cond, float out[3])
@@ -870,6 +1021,10 @@ static void grad_noise_1d(const real_t *r, const float p[3], float t_segment, co
     }
     float scx = splat_cov_1d(m, p, p), scy = scx;
     double xs0 = 1.0 / scx, xs1 = 1.0 / scy;
+    if (m->multires) {
+        grad_noise_1d_levels(r, p, t_segment, dir, cond, xs0, xs1, out);
+        return;
+    }
     double b4[4];
     noise1d_norm(r, p, dir, cond, 0, b4);
     float base[3] = {(float)b4[1], (float)b4[2], (float)b4[3]};
@@ -941,6 +1096,15 @@ static void conditioning_1d(real_t *r, const float p[3], const float dir[3], flo
     noise1d_norm(r, p, dir, 0, 0, v4);
     float cur = (float)v4[0];
     c->value_scale = (target_val - mean) / amp - cur;
+    /* the multi-resolution splats carry both levels' weights (conditioning1D,
+       SparseConvolutionNoise.cpp:602-604, 631-633) */
+    float mr_norm = 1.0f;
+    if (m->multires) {
+        float info[4];
+        level_ratio(m, p, info);
+        mr_norm = info[2] * info[2] + info[3] * info[3];
+        c->value_scale /= mr_norm;
+    }
     if (m->d.correlation_context == GPIS_CTX_RENEWAL_PLUS) {
         float cg[3];
         grad_noise_1d(r, p, 0.0f, dir, 0, cg);
@@ -959,6 +1123,8 @@ static void conditioning_1d(real_t *r, const float p[3], const float dir[3], flo
         float s = splat_cov_1d(m, p, p);
         float s2 = s * s;
         for (int i = 0; i < 3; ++i) c->gs[i] = -2.f * gl[i] * s2;
+        if (m->multires)
+            for (int i = 0; i < 3; ++i) c->gs[i] /= mr_norm;
         if (!m->d.correlation_xy) c->gs[0] = c->gs[1] = 0;
         for (int i = 0; i < 3; ++i) c->tgn[i] = (target_grad[i] - mgrad[i]) / amp;
         c->has_grad_obs = 1;
@@ -1397,6 +1563,18 @@ int gor_field(const gpis_medium_desc *desc, const float origin[3], const float d
     return GPIS_OK;
 }
 
+int gor_level_ratio(const gpis_medium_desc *desc, const float p[3], float info[4], uint32_t level_seeds[2])
+{
+    om_t m;
+    int rc = om_init(&m, desc);
+    if (rc) return rc;
+    if (!m.multires) return GPIS_EINVAL;
+    level_ratio(&m, p, info);
+    level_seeds[0] = level_seed(info[0]);
+    level_seeds[1] = level_seed(info[1]);
+    return GPIS_OK;
+}
+
 int gor_gradient(const gpis_medium_desc *desc, const float origin[3], const float dir[3],
                  const float p[3], float t_segment, const uint32_t seeds[4],
                  const float prev[4], float out[3])
@@ -1487,9 +1665,19 @@ int gor_nee(const gpis_medium_desc *desc, const float origin[3], const float dir
     }
     float Ai[9];
     inv3(A, Ai);
-    double gc4[4];
-    noise1d_norm(r, p, dir, 1, 0, gc4);
-    float gc[3] = {(float)gc4[1], (float)gc4[2], (float)gc4[3]};
+    float gc[3], info[4] = {1.0f, 1.0f, 1.0f, 0.0f};
+    if (m.multires) {
+        /* grad_constraint_3d on the multi-resolution grid (SparseConvolutionNoise.cpp:687-692) */
+        level_ratio(&m, p, info);
+        double lo[4], hi[4];
+        noise1d_level(r, p, dir, 1, 0, info[0], 1, lo);
+        noise1d_level(r, p, dir, 1, 0, info[1], 0, hi);
+        for (int i = 0; i < 3; ++i) gc[i] = (float)lo[1 + i] * info[2] / info[0] + (float)hi[1 + i] * info[3] / info[1];
+    } else {
+        double gc4[4];
+        noise1d_norm(r, p, dir, 1, 0, gc4);
+        gc[0] = (float)gc4[1]; gc[1] = (float)gc4[2]; gc[2] = (float)gc4[3];
+    }
     float ppt[3], px[3], py[3], cr[3];
     for (int i = 0; i < 3; ++i) {
         ppt[i] = A[3 * i + 2] * gc[2] + mg[i];
@@ -1514,6 +1702,34 @@ int gor_nee(const gpis_medium_desc *desc, const float origin[3], const float dir
         if (!(tv > 0.)) { *pdf = 0.0f; return GPIS_OK; }
         const double dx = g3[0] - tm[0], dy = g3[1] - tm[1];
         pdf_area = (float)(exp(-0.5 * (dx * dx + dy * dy) / tv) / (2.0 * M_PI * tv));
+    } else if (m.multires) {
+        /* the multi-resolution law (SparseConvolutionNoise.cpp:776-808): the transverse
+           scales shrink by 1 / sqrt((w_low / s_low)^2 + (w_high / s_high)^2) */
+        const float a = info[2] / info[0], b = info[3] / info[1];
+        const float nss = (float)(1.0 / (double)sqrtf(a * a + b * b));
+        const float scx = splat_cov_1d(&m, p, p) * nss, scy = scx;
+        if (!(m.d.correlation_context == GPIS_CTX_RENEWAL_PLUS && m.d.correlation_xy) || t_segment == 0.0f) {
+            float sx = (float)((double)(g3[0] - gc[0]) * sqrt(2.0) * scx);
+            float sy = (float)((double)(g3[1] - gc[1]) * sqrt(2.0) * scy);
+            pdf_area = (float)(exp(-sx * sx / 2.0) * exp(-sy * sy / 2.0) / (2.0 * M_PI) * 2.0 * scx * scy);
+        } else {
+            pcg_t g;
+            pcg_set_state(&g, (uint64_t)r->normal_seed);
+            double xy1[2], xy2[2];
+            rand_normal_2(&g, xy1);
+            rand_normal_2(&g, xy2);
+            const double s2 = (double)sqrtf(2.f);
+            double fac, cov, mu[2];
+            corr_moments(t_segment, &fac, &cov);
+            for (int i = 0; i < 2; ++i) {
+                xy1[i] /= s2;
+                xy2[i] /= s2;
+                mu[i] = fac * 2.0 * (xy1[i] * info[2] / info[0] + xy2[i] * info[3] / info[1]);
+            }
+            float sx = (float)((g3[0] - gc[0] - mu[0]) / sqrt(cov) * nss);
+            float sy = (float)((g3[1] - gc[1] - mu[1]) / sqrt(cov) * nss);
+            pdf_area = (float)(exp(-sx * sx / 2.0) * exp(-sy * sy / 2.0) / (2.0 * M_PI * cov) * (nss * nss));
+        }
     } else if (!(m.d.correlation_context == GPIS_CTX_RENEWAL_PLUS && m.d.correlation_xy) || t_segment == 0.0f) {
         float scx = splat_cov_1d(&m, p, p), scy = scx;
         float sx = (float)((double)(g3[0] - gc[0]) * sqrt(2.0) * scx);
@@ -1573,11 +1789,14 @@ static void gm_flight(const gpis_medium_desc *d, const gpis_ray *r, float far_t,
     gor_trace_flights(d, 1, &in, &out, 1, 1);
 }
 
+/* samplingScheme (SparseConvolutionNoise.cpp:68-76) at a hit t along the flight: UNI
+ * for a vanishing amplitude, and at the observed origin (t = 0 after a Renewal+
+ * conditioning) under correlationXY for the stationary SE covariance */
 static uint32_t gm_scheme(const gpis_medium_desc *d, int conditioned_rp, float t)
 {
     if (d->single_realization || !d->one_d_sampling) return GPIS_SCHEME_UNI;
     if (d->sigma < 1e-6f) return GPIS_SCHEME_UNI;
-    if (d->correlation_xy && conditioned_rp && t == 0.0f) return GPIS_SCHEME_UNI;
+    if (d->correlation_xy && conditioned_rp && t == 0.0f && d->ls_kind == GPIS_LS_CONSTANT) return GPIS_SCHEME_UNI;
     return d->sampling_scheme;
 }
 

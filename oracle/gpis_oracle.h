@@ -74,6 +74,11 @@ int gor_transverse_moments(const gpis_medium_desc *desc, const float origin[3],
                            const float dir[3], const float p[3], const uint32_t seeds[4],
                            const float prev[4], int conditioning, double mean[2], double *var);
 
+/* Multi-resolution levels at p (kernelScaleLevelRatio, SparseConvolutionNoise.cpp:101-111):
+ * info = (low scale, high scale, low weight, high weight) and the two levels'
+ * noise-seed offsets.  EINVAL for a medium without the multi-resolution grid. */
+int gor_level_ratio(const gpis_medium_desc *desc, const float p[3], float info[4], uint32_t level_seeds[2]);
+
 /* 1D NEE PDF and gradient (neePDF / neeGrad, SparseConvolutionNoise.cpp:662-821). */
 int gor_nee(const gpis_medium_desc *desc, const float origin[3], const float dir[3],
             const float p[3], const float normal[3], float t_segment, const uint32_t seeds[4],

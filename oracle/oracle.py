@@ -53,6 +53,7 @@ def lib():
                 "gor_flight_seeds": (None, [M, vp, u32, vp, vp]),
                 "gor_transverse_moments": (c_int, [M, vp, vp, vp, vp, vp, c_int, vp, vp]),
                 "gor_nee": (c_int, [M, vp, vp, vp, vp, ctypes.c_float, vp, vp, vp, vp]),
+                "gor_level_ratio": (c_int, [M, vp, vp, vp]),
                 "gor_sampling_scheme": (c_int, [M, vp, vp, vp]),
                 "gor_se_splat_1d": (None, [vp, vp, u32, ctypes.c_float, vp, vp]),
                 "gor_medium_sample_distance": (c_int, [M, vp, vp, vp, vp, u32]),
@@ -132,6 +133,18 @@ def nee(desc, origin, direction, p, normal, t_segment, seeds, prev):
     if rc:
         raise abi.GpisError(f"oracle nee failed: {rc}", rc)
     return float(pdf[0]), g
+
+
+def level_ratio(desc, p):
+    """Multi-resolution levels at p: ((low scale, high scale, low weight, high weight),
+    (low seed offset, high seed offset))."""
+    q = _f3(p)
+    info = np.zeros(4, np.float32)
+    seeds = np.zeros(2, np.uint32)
+    rc = lib().gor_level_ratio(ctypes.byref(desc), _p(q), _p(info), _p(seeds))
+    if rc:
+        raise abi.GpisError(f"oracle level_ratio failed: {rc}", rc)
+    return info, seeds
 
 
 def sampling_scheme(desc, origin, p, seeds):

@@ -1,5 +1,6 @@
 """Nonstationary length scale and octaves (the torus-union-plane field with
-ls(p) = 0.11 + 0.09 sin(3x) cos(2z) and three octaves).
+ls(p) = 0.11 + 0.09 sin(3x) cos(2z) and three octaves), by brute force and on
+the multi-resolution grid.
 
 CPU: the oracle's conditioning meets the birth value and the along-ray birth
 gradient of the summed field exactly (up to float rounding), for one octave and
@@ -13,7 +14,8 @@ import pytest
 from gpis_extend_gb300 import abi, workloads
 from oracle import oracle
 
-CASES = [(True, 1), (False, 3), (True, 3)]
+# (nonstationary, octaves, multi-resolution grid)
+CASES = [(True, 1, 0), (False, 3, 0), (True, 3, 0), (True, 1, 1)]
 
 
 def birth_points(n, rng):
@@ -30,9 +32,9 @@ def birth_points(n, rng):
     return o, d, seeds, prev
 
 
-@pytest.mark.parametrize("ns,octaves", CASES)
-def test_oracle_conditioning_meets_birth_state(ns, octaves):
-    desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves)
+@pytest.mark.parametrize("ns,octaves,mr", CASES)
+def test_oracle_conditioning_meets_birth_state(ns, octaves, mr):
+    desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves, multires=mr)
     rng = np.random.default_rng(5 + octaves + 2 * ns)
     o, d, seeds, prev = birth_points(200, rng)
     for i in range(len(o)):
@@ -78,10 +80,10 @@ def test_oracle_rejects_unsupported_combinations():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ns,octaves", CASES)
-def test_gpu_nonstationary_noise_vs_fp64(ns, octaves):
+@pytest.mark.parametrize("ns,octaves,mr", CASES)
+def test_gpu_nonstationary_noise_vs_fp64(ns, octaves, mr):
     from gpis_extend_gb300 import runtime
-    desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves)
+    desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves, multires=mr)
     rng = np.random.default_rng(17 + octaves + 2 * ns)
     n = 1500
     o, d, seeds, prev = birth_points(n, rng)
@@ -99,11 +101,11 @@ def test_gpu_nonstationary_noise_vs_fp64(ns, octaves):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ns,octaves", CASES)
-def test_gpu_nonstationary_flights_vs_oracle(ns, octaves):
+@pytest.mark.parametrize("ns,octaves,mr", CASES)
+def test_gpu_nonstationary_flights_vs_oracle(ns, octaves, mr):
     from gpis_extend_gb300 import runtime
     from test_gpu_parity import flights_vs_oracle
-    desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves)
+    desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves, multires=mr)
     prim = workloads.sphere_flights(1 << 14, desc)
     with runtime.Context(desc) as ctx:
         rec = ctx.trace_host(prim)
@@ -120,6 +122,7 @@ PRECISE_MEDIA = {
     "torus_ns": lambda: workloads.torus_plane_medium(nonstationary=True, octaves=1),
     "torus_oct": lambda: workloads.torus_plane_medium(nonstationary=False, octaves=3),
     "torus_ns_oct": lambda: workloads.torus_plane_medium(nonstationary=True, octaves=3),
+    "torus_mr": lambda: workloads.torus_plane_medium(nonstationary=True, octaves=1, multires=1),
 }
 
 
