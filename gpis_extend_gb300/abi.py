@@ -384,6 +384,17 @@ def load_library(path=None):
         "gpis_flights_submit_static": (c_int, [P(MediumDesc), P(FlightSoA), P(ResultSoA), c_u32, vp]),
         "gpis_medium_sample_distance": (c_int, [vp, c_u32, vp, vp, vp, vp, c_u32]),
         "gpis_medium_transmittance": (c_int, [vp, c_u32, vp, vp, vp, vp, c_u32]),
+        "gpis_proposal_n_params": (c_u32, []),
+        "gpis_proposal_create": (c_int, [vp, P(vp)]),
+        "gpis_proposal_destroy": (None, [vp]),
+        "gpis_proposal_set_params": (c_int, [vp, vp]),
+        "gpis_proposal_get_params": (c_int, [vp, vp]),
+        "gpis_proposal_features": (c_int, [vp, P(FlightSoA), vp, c_u32, vp]),
+        "gpis_proposal_train_step": (c_int, [vp, vp, vp, c_u32, ctypes.c_float, P(ctypes.c_float)]),
+        "gpis_proposal_gradient": (c_int, [vp, vp, vp, c_u32, vp, P(ctypes.c_float)]),
+        "gpis_proposal_forward": (c_int, [vp, vp, c_u32, vp]),
+        "gpis_proposal_infer": (c_int, [vp, P(FlightSoA), vp, vp, c_u32, vp]),
+        "gpis_flights_submit_proposed": (c_int, [vp, P(FlightSoA), vp, P(ResultSoA), c_u32, vp]),
         "gpis_last_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

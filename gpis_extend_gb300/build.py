@@ -14,8 +14,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgpis_gb300.so")
 ROOT = os.path.dirname(HERE)
 
-SOURCES = ["flights.cu", "gpis_abi.cu", "gpis_static.cu", "render.cu", "backend.cu", "medium_json.cpp",
-           "medium_adapter.cpp"]
+SOURCES = ["flights.cu", "gpis_abi.cu", "gpis_static.cu", "render.cu", "backend.cu", "proposal.cu",
+           "medium_json.cpp", "medium_adapter.cpp"]
 # per-file flags: the path tracer rounds every float expression as its CPU restatement
 EXTRA = {"render.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

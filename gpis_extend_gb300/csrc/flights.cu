@@ -1552,6 +1552,8 @@ enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE
 
 // most march steps one evaluation may skip (fast pass)
 constexpr int kMaxSkip = 8;
+// before a proposed crossing interval the cap is this (every skipped step is still certified)
+constexpr int kMaxSkipProposed = 64;
 
 // Fast values farther than this from zero have the sign of the precise value
 // (the fast evaluator differs from the precise one by a few 1e-8).
@@ -1615,6 +1617,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     // step skipping (fast pass): the field's Lipschitz constant along this ray and
     // its truncation-jump allowance, fixed and per step
     float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
+    float prop_a = -INFINITY;   // start of the proposed crossing interval (learned proposal)
 
     for (;;) {
         const bool need = phase == PH_IDLE && !drained;
@@ -1631,6 +1634,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 } else {
                     fid = idx;
                     if (!RESUME) c_flights++;
+                    prop_a = (!RESUME && a.proposal) ? a.proposal[idx].x : -INFINITY;
                     bool mok;
                     L.m = medium_of(a, idx, mok);
                     const DevMedium &m = *L.m;
@@ -1819,7 +1823,8 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     const float per = skip_lip * step + skip_j1;
                     // at most kMaxSkip per evaluation: the lanes of a warp skip different
                     // counts, so the warp runs the longest lane's loop
-                    if (af > per) skip = (int)fminf(af / per, (float)kMaxSkip);
+                    const float cap = th < prop_a ? (float)kMaxSkipProposed : (float)kMaxSkip;
+                    if (af > per) skip = (int)fminf(af / per, cap);
                 }
                 for (;;) {
                     if (!t_less(th, tl, far_t)) {

@@ -51,7 +51,14 @@ struct FlightArgs {
     int all_grid;               // all media have a grid mean
     int any_ns;                 // some medium has a nonstationary length scale
     int any_mr;                 // some medium blends multi-resolution levels
+    const float4 *proposal;     // may be null: per flight the proposed crossing interval
+                                // (t_a, t_b, miss probability, -); the fast pass may skip
+                                // further than its usual cap before t_a
 };
+
+// Per-flight features of the learned proposal (proposal.cu).
+cudaError_t launch_features(const DevMedium *media, int n_media, const gpis_flight_soa &in, uint32_t n, float *feat,
+                            cudaStream_t s);
 
 // Upload the jump-ahead PCG table to the current device (once per device).
 cudaError_t upload_pcg_table();

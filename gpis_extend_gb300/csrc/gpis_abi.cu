@@ -468,9 +468,10 @@ namespace {
 // gpis_flights_submit on the scratch slice [offset, offset + n) with its own four
 // work counters, so that batches on different streams may run at the same time
 int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa *out, uint32_t n,
-                 cudaStream_t stream, size_t offset, uint32_t *work)
+                 cudaStream_t stream, size_t offset, uint32_t *work, const float *proposal = nullptr)
 {
     gpis::FlightArgs a = {};
+    a.proposal = reinterpret_cast<const float4 *>(proposal);
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
     a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
     a.seeds = reinterpret_cast<const uint4 *>(in->seeds);
@@ -536,6 +537,32 @@ int gpis_flights_submit(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_res
     int rc = ensure_scratch(ctx, n);
     if (rc) return rc;
     return submit_slice(ctx, in, out, n, static_cast<cudaStream_t>(cuda_stream), 0, ctx->d_work);
+}
+
+int gpis_flights_submit_proposed(gpis_ctx *ctx, const gpis_flight_soa *in, const float *intervals,
+                                 const gpis_result_soa *out, uint32_t n, void *cuda_stream)
+{
+    if (!ctx || !in || !out || (n && !intervals)) return fail(GPIS_EINVAL, "null argument");
+    if (n == 0) return GPIS_OK;
+    if (!in->origin_near || !in->dir_far || !in->seeds || !out->rec)
+        return fail(GPIS_EINVAL, "flight streams origin_near, dir_far and seeds and rec are required");
+    if (ctx->any_cond && !in->prev) return fail(GPIS_EINVAL, "conditioning media need the prev stream");
+    if (reinterpret_cast<uintptr_t>(intervals) & 15u) return fail(GPIS_EINVAL, "intervals must be 16-byte aligned");
+    int rc = ensure_scratch(ctx, n);
+    if (rc) return rc;
+    return submit_slice(ctx, in, out, n, static_cast<cudaStream_t>(cuda_stream), 0, ctx->d_work, intervals);
+}
+
+int gpis_proposal_features(gpis_ctx *ctx, const gpis_flight_soa *in, float *features, uint32_t n, void *cuda_stream)
+{
+    if (!ctx || !in || (n && !features)) return fail(GPIS_EINVAL, "null argument");
+    if (n == 0) return GPIS_OK;
+    if (!in->origin_near || !in->dir_far || !in->seeds)
+        return fail(GPIS_EINVAL, "flight streams origin_near, dir_far and seeds are required");
+    CUDA_TRY(gpis::launch_features(ctx->d_media, ctx->n_media, *in, n, features,
+                                   static_cast<cudaStream_t>(cuda_stream)),
+             "proposal features");
+    return GPIS_OK;
 }
 
 int gpis_profile_enable(gpis_ctx *ctx, int on)

@@ -1,0 +1,874 @@
+// proposal.cu -- the learned crossing proposal of the flight path.
+//
+// A small network predicts, per flight, where along [near, far] the first
+// downcrossing lies: a GRU (hidden 32) over eight samples of the mean SDF and its
+// slope along the ray, then a 3 x 64 GELU MLP over the GRU state and eight
+// per-flight features, emitting an 8-component logistic mixture over
+// u = (t - near) / (far - near) and a miss logit.  Every contraction runs on the
+// tensor cores as BF16 x BF16 -> FP32 (mma.sync m16n8k16); the elementwise parts,
+// the loss and Adam are FP32.  Training uses an unfused layer-by-layer forward
+// that keeps its activations and a hand-written backward; inference is one fused
+// kernel per 16 flights a warp with the weights in shared memory.
+//
+// The proposal never changes a flight's result: gpis_flights_submit_proposed lets
+// the march take longer certified skips before the proposed interval, and every
+// skipped step is still proven free of a sign change by the same bound as the
+// plain march's step skipping.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/gpis.h"
+#include "device_common.cuh"
+#include "flights.cuh"
+
+extern "C" int gpis_internal_set_error(int code, const char *msg);
+
+namespace gpis {
+namespace prop {
+
+constexpr int HID = 32, NIN = 16, MLPIN = 48, WID = 64, NOUT = 32, NHIST = 8, NFEAT = 24, NCOMP = 8;
+// offsets into the flat parameter vector (weights row-major [out][in])
+constexpr int O_WIH = 0, O_BIH = O_WIH + 3 * HID * NIN, O_WHH = O_BIH + 3 * HID, O_BHH = O_WHH + 3 * HID * HID,
+              O_W1 = O_BHH + 3 * HID, O_B1 = O_W1 + WID * MLPIN, O_W2 = O_B1 + WID, O_B2 = O_W2 + WID * WID,
+              O_W3 = O_B2 + WID, O_B3 = O_W3 + WID * WID, O_W4 = O_B3 + WID, O_B4 = O_W4 + NOUT * WID,
+              N_PARAMS = O_B4 + NOUT;
+static_assert(N_PARAMS == 18336, "parameter layout");
+
+typedef __nv_bfloat16 bf;
+
+__device__ __forceinline__ uint32_t bf_bits(bf x) { return (uint32_t)__bfloat16_as_ushort(x); }
+__device__ __forceinline__ uint32_t pack2(bf lo, bf hi) { return bf_bits(lo) | (bf_bits(hi) << 16); }
+__device__ __forceinline__ uint32_t pack2f(float lo, float hi)
+{
+    return pack2(__float2bfloat16_rn(lo), __float2bfloat16_rn(hi));
+}
+
+// D = A(16x16, row) * B(16x8, col) + D, BF16 inputs, FP32 accumulators.
+// Fragments (g = lane / 4, t = lane % 4): a0 (g, 2t..2t+1), a1 (g+8, 2t..), a2 (g, 2t+8..),
+// a3 (g+8, 2t+8..); b0 (k 2t..2t+1, n g), b1 (k 2t+8.., n g); d0,d1 (g, 2t..2t+1),
+// d2,d3 (g+8, 2t..2t+1).  The lower half of each register holds the lower index.
+__device__ __forceinline__ void mma_bf16(float d[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float sigm(float x) { return 1.0f / (1.0f + expf(-x)); }
+__device__ __forceinline__ float softplus(float x) { return x > 20.0f ? x : log1pf(expf(x)); }
+constexpr float kGeluC = 0.7978845608028654f;
+__device__ __forceinline__ float gelu(float x)
+{
+    return 0.5f * x * (1.0f + tanhf(kGeluC * (x + 0.044715f * x * x * x)));
+}
+__device__ __forceinline__ float gelu_grad(float x)
+{
+    const float t = tanhf(kGeluC * (x + 0.044715f * x * x * x));
+    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * kGeluC * (1.0f + 3.0f * 0.044715f * x * x);
+}
+
+// ---- generic strided GEMM: C(m, n) (+)= sum_k A(m, k) B(k, n) --------------------------
+// A(m, k) = A[m * lam + k * lak], B(k, n) = B[k * lbk + n * lbn]; one warp per 16 x 8 tile
+// of C and K chunk; M % 16 == 0, N % 8 == 0, K % 16 == 0.  ksplit > 1 adds into C
+// with atomics (C zeroed or holding the sum to add to).
+struct Gemm {
+    const bf *A;
+    long lam, lak;
+    const bf *B;
+    long lbk, lbn;
+    float *C;
+    long ldc;
+    int M, N, K, accumulate, ksplit;
+};
+
+__global__ void __launch_bounds__(128) k_gemm(Gemm g)
+{
+    const long warp = (long)blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int tn_count = g.N / 8;
+    const long total = (long)(g.M / 16) * tn_count * g.ksplit;
+    if (warp >= total) return;
+    const int lane = threadIdx.x & 31, gi = lane >> 2, ti = lane & 3;
+    const int kc = (int)(warp % g.ksplit);
+    const long tile = warp / g.ksplit;
+    const int m0 = (int)(tile / tn_count) * 16, n0 = (int)(tile % tn_count) * 8;
+    const int ktiles = g.K / 16;
+    const int per = (ktiles + g.ksplit - 1) / g.ksplit;
+    const int kt0 = kc * per, kt1 = min(ktiles, kt0 + per);
+    float d[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const bf *A = g.A, *B = g.B;
+    for (int kt = kt0; kt < kt1; ++kt) {
+        const long k = (long)kt * 16 + 2 * ti;
+        const long r0 = (long)(m0 + gi) * g.lam, r1 = (long)(m0 + gi + 8) * g.lam;
+        const uint32_t a0 = pack2(A[r0 + k * g.lak], A[r0 + (k + 1) * g.lak]);
+        const uint32_t a1 = pack2(A[r1 + k * g.lak], A[r1 + (k + 1) * g.lak]);
+        const uint32_t a2 = pack2(A[r0 + (k + 8) * g.lak], A[r0 + (k + 9) * g.lak]);
+        const uint32_t a3 = pack2(A[r1 + (k + 8) * g.lak], A[r1 + (k + 9) * g.lak]);
+        const long c = (long)(n0 + gi) * g.lbn;
+        const uint32_t b0 = pack2(B[k * g.lbk + c], B[(k + 1) * g.lbk + c]);
+        const uint32_t b1 = pack2(B[(k + 8) * g.lbk + c], B[(k + 9) * g.lbk + c]);
+        mma_bf16(d, a0, a1, a2, a3, b0, b1);
+    }
+    float *c0 = g.C + (long)(m0 + gi) * g.ldc + n0 + 2 * ti;
+    float *c1 = g.C + (long)(m0 + gi + 8) * g.ldc + n0 + 2 * ti;
+    if (g.ksplit > 1) {
+        atomicAdd(c0, d[0]);
+        atomicAdd(c0 + 1, d[1]);
+        atomicAdd(c1, d[2]);
+        atomicAdd(c1 + 1, d[3]);
+    } else if (g.accumulate) {
+        c0[0] += d[0]; c0[1] += d[1]; c1[0] += d[2]; c1[1] += d[3];
+    } else {
+        c0[0] = d[0]; c0[1] = d[1]; c1[0] = d[2]; c1[1] = d[3];
+    }
+}
+
+// ---- elementwise kernels ---------------------------------------------------------------
+// GRU inputs of every step, the globals part of the MLP input, h_0 = 0.
+__global__ void k_prep(const float *feat, uint32_t n, bf *xb, bf *ub, float *h0, bf *h0b)
+{
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    const float *f = feat + (size_t)m * NFEAT;
+    for (int j = 0; j < NHIST; ++j) {
+        bf *x = xb + ((size_t)j * n + m) * NIN;
+        x[0] = __float2bfloat16_rn(f[2 * j]);
+        x[1] = __float2bfloat16_rn(f[2 * j + 1]);
+        for (int c = 2; c < NIN; ++c) x[c] = __float2bfloat16_rn(0.0f);
+    }
+    bf *u = ub + (size_t)m * MLPIN;
+    for (int c = 0; c < 8; ++c) u[HID + c] = __float2bfloat16_rn(f[16 + c]);
+    for (int c = HID + 8; c < MLPIN; ++c) u[c] = __float2bfloat16_rn(0.0f);
+    for (int c = 0; c < HID; ++c) {
+        h0[(size_t)m * HID + c] = 0.0f;
+        h0b[(size_t)m * HID + c] = __float2bfloat16_rn(0.0f);
+    }
+}
+
+// GRU cell (PyTorch gate order r, z, n) from the raw products gi = x W_ih^T, gh = h W_hh^T.
+__global__ void k_gru_cell(const float *gi, const float *gh, const float *P, const float *hprev, uint32_t n,
+                           float *r_o, float *z_o, float *n_o, float *ghn_o, float *hnew, bf *hnewb, bf *ub)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * HID) return;
+    const uint32_t m = i / HID, c = i % HID;
+    const float *bih = P + O_BIH, *bhh = P + O_BHH;
+    const float *a = gi + (size_t)m * 3 * HID, *b = gh + (size_t)m * 3 * HID;
+    const float r = sigm(a[c] + bih[c] + b[c] + bhh[c]);
+    const float z = sigm(a[HID + c] + bih[HID + c] + b[HID + c] + bhh[HID + c]);
+    const float ghn = b[2 * HID + c] + bhh[2 * HID + c];
+    const float nn = tanhf(a[2 * HID + c] + bih[2 * HID + c] + r * ghn);
+    const float h = (1.0f - z) * nn + z * hprev[i];
+    r_o[i] = r; z_o[i] = z; n_o[i] = nn; ghn_o[i] = ghn;
+    hnew[i] = h;
+    hnewb[i] = __float2bfloat16_rn(h);
+    if (ub) ub[(size_t)m * MLPIN + c] = __float2bfloat16_rn(h);
+}
+
+// a += bias in place, y = bf16(gelu(a))
+__global__ void k_bias_gelu(float *a, const float *bias, uint32_t n, int width, bf *y)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * (uint32_t)width) return;
+    const float v = a[i] + bias[i % width];
+    a[i] = v;
+    y[i] = __float2bfloat16_rn(gelu(v));
+}
+
+// the mixture's negative log-likelihood and its gradient w.r.t. the 32 outputs, / n
+__global__ void k_loss(float *o, const float *bias, const float2 *tgt, uint32_t n, float inv_n, float *dof, bf *dob,
+                       float *loss)
+{
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    float nll = 0.0f;
+    if (m < n) {
+        float *x = o + (size_t)m * NOUT;
+        for (int c = 0; c < NOUT; ++c) x[c] += bias[c];
+        const float us = tgt[m].x;
+        const bool hit = tgt[m].y != 0.0f;
+        float g[NOUT];
+        for (int c = 0; c < NOUT; ++c) g[c] = 0.0f;
+        const float ql = x[24];
+        if (hit) {
+            float lmax = x[0];
+            for (int k = 1; k < NCOMP; ++k) lmax = fmaxf(lmax, x[k]);
+            float se = 0.0f;
+            for (int k = 0; k < NCOMP; ++k) se += expf(x[k] - lmax);
+            const float lse_pi = lmax + logf(se);
+            float comp[NCOMP], y[NCOMP], s[NCOMP], mu[NCOMP];
+            float cmax = -INFINITY;
+            for (int k = 0; k < NCOMP; ++k) {
+                mu[k] = sigm(x[8 + k]);
+                s[k] = softplus(x[16 + k]) + 1e-3f;
+                y[k] = (us - mu[k]) / s[k];
+                const float logf_k = -softplus(-y[k]) - softplus(y[k]) - logf(s[k]);
+                comp[k] = x[k] - lse_pi + logf_k;
+                cmax = fmaxf(cmax, comp[k]);
+            }
+            float cs = 0.0f;
+            for (int k = 0; k < NCOMP; ++k) cs += expf(comp[k] - cmax);
+            const float lse = cmax + logf(cs);
+            nll = softplus(ql) - lse;
+            for (int k = 0; k < NCOMP; ++k) {
+                const float w = expf(comp[k] - lse);
+                const float pk = expf(x[k] - lse_pi);
+                g[k] = pk - w;
+                const float dldy = tanhf(0.5f * y[k]);
+                const float dm = w * dldy * (-1.0f / s[k]);
+                const float ds = w * (dldy * (-y[k] / s[k]) + 1.0f / s[k]);
+                g[8 + k] = dm * mu[k] * (1.0f - mu[k]);
+                g[16 + k] = ds * sigm(x[16 + k]);
+            }
+            g[24] = sigm(ql);
+        } else {
+            nll = softplus(-ql);
+            g[24] = -sigm(-ql);
+        }
+        for (int c = 0; c < NOUT; ++c) {
+            const float v = g[c] * inv_n;
+            dof[(size_t)m * NOUT + c] = v;
+            dob[(size_t)m * NOUT + c] = __float2bfloat16_rn(v);
+        }
+    }
+    // one atomic per warp
+    for (int off = 16; off > 0; off >>= 1) nll += __shfl_xor_sync(0xffffffffu, nll, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, nll);
+}
+
+// out[c] += sum over rows of x[m * ld + c], c < width
+__global__ void k_colsum(const float *x, uint32_t n, int width, long ld, float *out)
+{
+    const int c = threadIdx.x % width;
+    const int rows_per = blockDim.x / width;
+    float s = 0.0f;
+    for (uint32_t m = blockIdx.x * rows_per + threadIdx.x / width; m < n; m += gridDim.x * rows_per)
+        s += x[(size_t)m * ld + c];
+    if ((int)threadIdx.x < rows_per * width) atomicAdd(out + c, s);
+}
+
+// da = dy * gelu'(a) (fp32 and bf16)
+__global__ void k_gelu_back(const float *dy, const float *a, uint32_t n, int width, float *daf, bf *dab)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * (uint32_t)width) return;
+    const float v = dy[i] * gelu_grad(a[i]);
+    daf[i] = v;
+    dab[i] = __float2bfloat16_rn(v);
+}
+
+// one GRU step backward: gate gradients and dh * z
+__global__ void k_gru_back(const float *dh, long ldh, const float *r_, const float *z_, const float *n_,
+                           const float *ghn_, const float *hprev, uint32_t n, float *dgif, bf *dgib, float *dghf,
+                           bf *dghb, float *dhpart)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * HID) return;
+    const uint32_t m = i / HID, c = i % HID;
+    const float d = dh[(size_t)m * ldh + c];
+    const float r = r_[i], z = z_[i], nn = n_[i], ghn = ghn_[i];
+    const float dz = d * (hprev[i] - nn) * z * (1.0f - z);
+    const float dn = d * (1.0f - z) * (1.0f - nn * nn);
+    const float dr = dn * ghn * r * (1.0f - r);
+    float *gi = dgif + (size_t)m * 3 * HID, *gh = dghf + (size_t)m * 3 * HID;
+    bf *gib = dgib + (size_t)m * 3 * HID, *ghb = dghb + (size_t)m * 3 * HID;
+    gi[c] = dr; gi[HID + c] = dz; gi[2 * HID + c] = dn;
+    gh[c] = dr; gh[HID + c] = dz; gh[2 * HID + c] = dn * r;
+    gib[c] = __float2bfloat16_rn(dr); gib[HID + c] = __float2bfloat16_rn(dz); gib[2 * HID + c] = __float2bfloat16_rn(dn);
+    ghb[c] = __float2bfloat16_rn(dr); ghb[HID + c] = __float2bfloat16_rn(dz);
+    ghb[2 * HID + c] = __float2bfloat16_rn(dn * r);
+    dhpart[i] = d * z;
+}
+
+// Adam on the FP32 master parameters, then their BF16 copies
+__global__ void k_adam(float *p, const float *g, float *m1, float *m2, int n, float lr, float b1, float b2, float eps,
+                       float c1, float c2, bf *pb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float a = b1 * m1[i] + (1.0f - b1) * gi;
+    const float b = b2 * m2[i] + (1.0f - b2) * gi * gi;
+    m1[i] = a;
+    m2[i] = b;
+    const float v = p[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+    p[i] = v;
+    pb[i] = __float2bfloat16_rn(v);
+}
+
+__global__ void k_to_bf16(const float *p, int n, bf *pb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pb[i] = __float2bfloat16_rn(p[i]);
+}
+
+// ---- features --------------------------------------------------------------------------
+// 24 per flight: the mean SDF and its slope along the ray at the centres of eight
+// equal parts of [near, far] (clamped to +-4), then t_max / 4, 10 x the local length
+// scale at near, the conditioned value and derivative along the ray (clamped to +-4),
+// the first-scatter flag, 10 x the amplitude, step / t_max and the mean at near.
+__global__ void k_features(const DevMedium *media, int n_media, const float4 *on, const float4 *df, const uint4 *sd,
+                           const float4 *pv, const uint32_t *mid, uint32_t n, float *feat)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t mi = mid ? mid[i] : 0u;
+    const DevMedium &m = media[mi < (uint32_t)n_media ? mi : 0u];
+    const float4 o = on[i], d = df[i];
+    const float near_t = o.w, far_t = d.w, tm = fmaxf(far_t - near_t, 0.0f);
+    float *f = feat + (size_t)i * NFEAT;
+    for (int j = 0; j < NHIST; ++j) {
+        const float t = near_t + ((float)j + 0.5f) * 0.125f * tm;
+        const float x = o.x + t * d.x, y = o.y + t * d.y, z = o.z + t * d.z;
+        int id;
+        const float mv = mean_value(m, x, y, z, id);
+        float g[3];
+        mean_grad(m, x, y, z, g);
+        const float sl = g[0] * d.x + g[1] * d.y + g[2] * d.z;
+        f[2 * j] = fminf(fmaxf(mv, -4.0f), 4.0f);
+        f[2 * j + 1] = fminf(fmaxf(sl, -4.0f), 4.0f);
+    }
+    const float *q = m.ls_params;
+    const bool varying = m.ls_kind != 0u || (m.flags & MF_MULTIRES);
+    const float ls_here = varying ? q[0] + q[1] * sinf(q[2] * o.x) * cosf(q[3] * o.z) : 1.0f;
+    const float ell = ls_here * m.l_aniso[0] * 1.41421356f;
+    const bool first = (sd[i].z & GPIS_FLAG_FIRST_SCATTER) != 0u;
+    const float4 p = pv ? pv[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float amp = m.sigma;
+    if (m.n_oct > 1) {
+        amp = 0.0f;
+        for (int k = 0; k < (int)m.n_oct; ++k) amp += m.oct_sigma[k];
+    }
+    float step = tm / (float)m.min_step;
+    if (m.step_size < step) step = m.step_size;
+    int id;
+    f[16] = tm * 0.25f;
+    f[17] = 10.0f * ell;
+    f[18] = first ? 0.0f : fminf(fmaxf(p.x, -4.0f), 4.0f);
+    f[19] = first ? 0.0f : fminf(fmaxf(p.y * d.x + p.z * d.y + p.w * d.z, -4.0f), 4.0f);
+    f[20] = first ? 1.0f : 0.0f;
+    f[21] = 10.0f * amp;
+    f[22] = tm > 0.0f ? fminf(step / tm, 1.0f) : 1.0f;
+    f[23] = fminf(fmaxf(mean_value(m, o.x + near_t * d.x, o.y + near_t * d.y, o.z + near_t * d.z, id), -4.0f), 4.0f);
+}
+
+// ---- fused inference -------------------------------------------------------------------
+// 4 warps x 16 flights per block; BF16 weights and FP32 biases in shared memory.
+constexpr int kWeights = 3 * HID * NIN + 3 * HID * HID + WID * MLPIN + 2 * WID * WID + NOUT * WID;
+constexpr int S_WIH = 0, S_WHH = S_WIH + 3 * HID * NIN, S_W1 = S_WHH + 3 * HID * HID, S_W2 = S_W1 + WID * MLPIN,
+              S_W3 = S_W2 + WID * WID, S_W4 = S_W3 + WID * WID;
+constexpr int kBiases = 6 * HID + 3 * WID + NOUT;
+
+// b0, b1 of output tile nt and K tile kt of a [out][in] weight in shared memory
+__device__ __forceinline__ void bfrag(const bf *w, int in, int nt, int kt, int gi, int ti, uint32_t &b0, uint32_t &b1)
+{
+    const uint32_t *row = reinterpret_cast<const uint32_t *>(w + (nt * 8 + gi) * in + kt * 16);
+    b0 = row[ti];
+    b1 = row[ti + 4];
+}
+
+// one dense layer: acc[NT][4] = A (KT K-tiles of fragments) * W^T
+template <int NT, int KT>
+__device__ __forceinline__ void dense(const uint32_t (&a)[KT][4], const bf *w, int in, int gi, int ti,
+                                      float (&acc)[NT][4])
+{
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+        for (int kt = 0; kt < KT; ++kt) {
+            uint32_t b0, b1;
+            bfrag(w, in, nt, kt, gi, ti, b0, b1);
+            mma_bf16(acc[nt], a[kt][0], a[kt][1], a[kt][2], a[kt][3], b0, b1);
+        }
+    }
+}
+
+// bias, GELU and the C -> A fragment reuse of a 64-wide layer
+__device__ __forceinline__ void gelu_frag(float (&acc)[8][4], const float *bias, int ti, uint32_t (&a)[4][4])
+{
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int nt = 2 * kt + h;
+            const int c = nt * 8 + 2 * ti;
+            const float v0 = gelu(acc[nt][0] + bias[c]), v1 = gelu(acc[nt][1] + bias[c + 1]);
+            const float v2 = gelu(acc[nt][2] + bias[c]), v3 = gelu(acc[nt][3] + bias[c + 1]);
+            a[kt][2 * h] = pack2f(v0, v1);
+            a[kt][2 * h + 1] = pack2f(v2, v3);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *params, const float *feat,
+                                                 const float4 *on, const float4 *df, uint32_t n, float4 *out)
+{
+    __shared__ __align__(16) bf sw[kWeights];
+    __shared__ float sb[kBiases];
+    const int tid = threadIdx.x;
+    // weights: w_ih, w_hh, w1, w2, w3, w4 (each contiguous in the flat vector)
+    const int src[6] = {O_WIH, O_WHH, O_W1, O_W2, O_W3, O_W4};
+    const int dst[6] = {S_WIH, S_WHH, S_W1, S_W2, S_W3, S_W4};
+    const int len[6] = {3 * HID * NIN, 3 * HID * HID, WID * MLPIN, WID * WID, WID * WID, NOUT * WID};
+    for (int s = 0; s < 6; ++s)
+        for (int k = tid; k < len[s]; k += blockDim.x) sw[dst[s] + k] = wb[src[s] + k];
+    for (int k = tid; k < 3 * HID; k += blockDim.x) {
+        sb[k] = params[O_BIH + k];
+        sb[3 * HID + k] = params[O_BHH + k];
+    }
+    for (int k = tid; k < WID; k += blockDim.x) {
+        sb[6 * HID + k] = params[O_B1 + k];
+        sb[6 * HID + WID + k] = params[O_B2 + k];
+        sb[6 * HID + 2 * WID + k] = params[O_B3 + k];
+    }
+    for (int k = tid; k < NOUT; k += blockDim.x) sb[6 * HID + 3 * WID + k] = params[O_B4 + k];
+    __syncthreads();
+    const int lane = tid & 31, gi = lane >> 2, ti = lane & 3;
+    const long row0 = ((long)blockIdx.x * 4 + (tid >> 5)) * 16;
+    if (row0 >= (long)n) return;
+    const long ra = min(row0 + gi, (long)n - 1), rb = min(row0 + gi + 8, (long)n - 1);
+    const float *fa = feat + ra * NFEAT, *fb = feat + rb * NFEAT;
+    const float *bih = sb, *bhh = sb + 3 * HID, *b1 = sb + 6 * HID, *b2 = b1 + WID, *b3 = b2 + WID, *b4 = b3 + WID;
+    // GRU
+    float h[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) h[nt][0] = h[nt][1] = h[nt][2] = h[nt][3] = 0.0f;
+    for (int j = 0; j < NHIST; ++j) {
+        uint32_t ha[2][4];
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt) {
+            ha[kt][0] = pack2f(h[2 * kt][0], h[2 * kt][1]);
+            ha[kt][1] = pack2f(h[2 * kt][2], h[2 * kt][3]);
+            ha[kt][2] = pack2f(h[2 * kt + 1][0], h[2 * kt + 1][1]);
+            ha[kt][3] = pack2f(h[2 * kt + 1][2], h[2 * kt + 1][3]);
+        }
+        const uint32_t xa0 = ti == 0 ? pack2f(fa[2 * j], fa[2 * j + 1]) : 0u;
+        const uint32_t xa1 = ti == 0 ? pack2f(fb[2 * j], fb[2 * j + 1]) : 0u;
+        float hn[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            float gr[4] = {0, 0, 0, 0}, gz[4] = {0, 0, 0, 0}, gin[4] = {0, 0, 0, 0}, ghn[4] = {0, 0, 0, 0};
+            uint32_t b0, b1;
+            bfrag(sw + S_WIH, NIN, nt, 0, gi, ti, b0, b1);
+            mma_bf16(gr, xa0, xa1, 0u, 0u, b0, b1);
+            bfrag(sw + S_WIH, NIN, 4 + nt, 0, gi, ti, b0, b1);
+            mma_bf16(gz, xa0, xa1, 0u, 0u, b0, b1);
+            bfrag(sw + S_WIH, NIN, 8 + nt, 0, gi, ti, b0, b1);
+            mma_bf16(gin, xa0, xa1, 0u, 0u, b0, b1);
+#pragma unroll
+            for (int kt = 0; kt < 2; ++kt) {
+                bfrag(sw + S_WHH, HID, nt, kt, gi, ti, b0, b1);
+                mma_bf16(gr, ha[kt][0], ha[kt][1], ha[kt][2], ha[kt][3], b0, b1);
+                bfrag(sw + S_WHH, HID, 4 + nt, kt, gi, ti, b0, b1);
+                mma_bf16(gz, ha[kt][0], ha[kt][1], ha[kt][2], ha[kt][3], b0, b1);
+                bfrag(sw + S_WHH, HID, 8 + nt, kt, gi, ti, b0, b1);
+                mma_bf16(ghn, ha[kt][0], ha[kt][1], ha[kt][2], ha[kt][3], b0, b1);
+            }
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = nt * 8 + 2 * ti + (e & 1);
+                const float r = sigm(gr[e] + bih[c] + bhh[c]);
+                const float z = sigm(gz[e] + bih[HID + c] + bhh[HID + c]);
+                const float nn = tanhf(gin[e] + bih[2 * HID + c] + r * (ghn[e] + bhh[2 * HID + c]));
+                hn[nt][e] = (1.0f - z) * nn + z * h[nt][e];
+            }
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) h[nt][e] = hn[nt][e];
+    }
+    // MLP input: [h (2 K tiles), globals (K tile 2: columns 32..39, zeros 40..47)]
+    uint32_t u[3][4];
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt) {
+        u[kt][0] = pack2f(h[2 * kt][0], h[2 * kt][1]);
+        u[kt][1] = pack2f(h[2 * kt][2], h[2 * kt][3]);
+        u[kt][2] = pack2f(h[2 * kt + 1][0], h[2 * kt + 1][1]);
+        u[kt][3] = pack2f(h[2 * kt + 1][2], h[2 * kt + 1][3]);
+    }
+    u[2][0] = pack2f(fa[16 + 2 * ti], fa[17 + 2 * ti]);
+    u[2][1] = pack2f(fb[16 + 2 * ti], fb[17 + 2 * ti]);
+    u[2][2] = 0u;
+    u[2][3] = 0u;
+    float acc[8][4];
+    uint32_t y[4][4];
+    dense<8, 3>(u, sw + S_W1, MLPIN, gi, ti, acc);
+    gelu_frag(acc, b1, ti, y);
+    dense<8, 4>(y, sw + S_W2, WID, gi, ti, acc);
+    gelu_frag(acc, b2, ti, y);
+    dense<8, 4>(y, sw + S_W3, WID, gi, ti, acc);
+    gelu_frag(acc, b3, ti, y);
+    float o[4][4];
+    dense<4, 4>(y, sw + S_W4, WID, gi, ti, o);
+    // per row (g: e = 0, 1; g + 8: e = 2, 3): the dominant component over the 4 lanes of the group
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        float best = -INFINITY, bm = 0.0f, bs = 1.0f;
+        int bk = 0;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int k = 2 * ti + e;
+            const float lg = o[0][2 * half + e] + b4[k];
+            if (lg > best) {
+                best = lg;
+                bk = k;
+                bm = sigm(o[1][2 * half + e] + b4[8 + k]);
+                bs = softplus(o[2][2 * half + e] + b4[16 + k]) + 1e-3f;
+            }
+        }
+#pragma unroll
+        for (int off = 1; off < 4; off <<= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const int ok = __shfl_xor_sync(0xffffffffu, bk, off);
+            const float om = __shfl_xor_sync(0xffffffffu, bm, off);
+            const float os = __shfl_xor_sync(0xffffffffu, bs, off);
+            if (ob > best || (ob == best && ok < bk)) {
+                best = ob;
+                bk = ok;
+                bm = om;
+                bs = os;
+            }
+        }
+        const float q = sigm(o[3][2 * half] + b4[24]);   // column 24 sits at lane t = 0
+        const long r = row0 + gi + 8 * half;
+        if (ti == 0 && r < (long)n) {
+            const float4 a = on[r], b = df[r];
+            const float tm = b.w - a.w;
+            const float ua = fminf(fmaxf(bm - 3.0f * bs, 0.0f), 1.0f);
+            const float ub = fminf(fmaxf(bm + 3.0f * bs, 0.0f), 1.0f);
+            out[r] = make_float4(a.w + ua * tm, a.w + ub * tm, q, bm);
+        }
+    }
+}
+
+}  // namespace prop
+}  // namespace gpis
+
+using namespace gpis::prop;
+
+// ---- host objects ----------------------------------------------------------------------
+struct gpis_proposal {
+    float *p = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;
+    bf *pb = nullptr;
+    uint32_t step = 0;
+    cudaStream_t stream = nullptr;
+    // activations of the unfused pass for a batch of `cap` flights
+    uint32_t cap = 0;
+    std::vector<void *> act;
+    bf *xb = nullptr, *ub = nullptr, *hb = nullptr, *y1 = nullptr, *y2 = nullptr, *y3 = nullptr, *dob = nullptr,
+       *dab = nullptr, *dgib = nullptr, *dghb = nullptr;
+    float *h = nullptr, *gi = nullptr, *gh = nullptr, *r = nullptr, *z = nullptr, *nn = nullptr, *ghn = nullptr,
+          *a1 = nullptr, *a2 = nullptr, *a3 = nullptr, *o = nullptr, *dof = nullptr, *dy = nullptr, *daf = nullptr,
+          *du = nullptr, *dgif = nullptr, *dghf = nullptr, *dh = nullptr, *loss = nullptr;
+};
+
+namespace {
+
+int cfail(cudaError_t e, const char *what)
+{
+    static thread_local char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    return gpis_internal_set_error(GPIS_EIO, buf);
+}
+
+#define PTRY(expr, what)                                    \
+    do {                                                    \
+        cudaError_t e_ = (expr);                            \
+        if (e_ != cudaSuccess) return cfail(e_, what);      \
+    } while (0)
+
+template <class T>
+cudaError_t palloc(gpis_proposal *p, T *&ptr, size_t count)
+{
+    void *v = nullptr;
+    cudaError_t e = cudaMalloc(&v, count * sizeof(T));
+    if (e == cudaSuccess) p->act.push_back(v);
+    ptr = static_cast<T *>(v);
+    return e;
+}
+
+int ensure_batch(gpis_proposal *p, uint32_t n)
+{
+    if (n <= p->cap) return GPIS_OK;
+    for (void *v : p->act) cudaFree(v);
+    p->act.clear();
+    p->cap = 0;
+    const size_t N = n;
+    PTRY(palloc(p, p->xb, N * NHIST * NIN), "allocate proposal activations");
+    PTRY(palloc(p, p->ub, N * MLPIN), "allocate proposal activations");
+    PTRY(palloc(p, p->hb, N * (NHIST + 1) * HID), "allocate proposal activations");
+    PTRY(palloc(p, p->h, N * (NHIST + 1) * HID), "allocate proposal activations");
+    PTRY(palloc(p, p->gi, N * 3 * HID), "allocate proposal activations");
+    PTRY(palloc(p, p->gh, N * 3 * HID), "allocate proposal activations");
+    for (float **q : {&p->r, &p->z, &p->nn, &p->ghn}) PTRY(palloc(p, *q, N * NHIST * HID), "allocate proposal activations");
+    for (float **q : {&p->a1, &p->a2, &p->a3, &p->dy, &p->daf}) PTRY(palloc(p, *q, N * WID), "allocate proposal activations");
+    for (bf **q : {&p->y1, &p->y2, &p->y3, &p->dab}) PTRY(palloc(p, *q, N * WID), "allocate proposal activations");
+    PTRY(palloc(p, p->o, N * NOUT), "allocate proposal activations");
+    PTRY(palloc(p, p->dof, N * NOUT), "allocate proposal activations");
+    PTRY(palloc(p, p->dob, N * NOUT), "allocate proposal activations");
+    PTRY(palloc(p, p->du, N * MLPIN), "allocate proposal activations");
+    PTRY(palloc(p, p->dgif, N * 3 * HID), "allocate proposal activations");
+    PTRY(palloc(p, p->dghf, N * 3 * HID), "allocate proposal activations");
+    PTRY(palloc(p, p->dgib, N * 3 * HID), "allocate proposal activations");
+    PTRY(palloc(p, p->dghb, N * 3 * HID), "allocate proposal activations");
+    PTRY(palloc(p, p->dh, N * HID), "allocate proposal activations");
+    PTRY(palloc(p, p->loss, 1), "allocate proposal activations");
+    p->cap = n;
+    return GPIS_OK;
+}
+
+void gemm(cudaStream_t s, const bf *A, long lam, long lak, const bf *B, long lbk, long lbn, float *C, long ldc, int M,
+          int N, int K, int accumulate, int ksplit = 1)
+{
+    Gemm g{A, lam, lak, B, lbk, lbn, C, ldc, M, N, K, accumulate, ksplit};
+    const long warps = (long)(M / 16) * (N / 8) * ksplit;
+    k_gemm<<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(g);
+}
+
+inline unsigned nb(size_t n, unsigned t = 256) { return (unsigned)((n + t - 1) / t); }
+
+// the unfused forward over the batch: activations kept for backward; outputs o (+ b4 in k_loss)
+void forward(gpis_proposal *p, const float *feat, uint32_t n, cudaStream_t s)
+{
+    const bf *wb = p->pb;
+    k_prep<<<nb(n), 256, 0, s>>>(feat, n, p->xb, p->ub, p->h, p->hb);
+    for (int j = 0; j < NHIST; ++j) {
+        const bf *x = p->xb + (size_t)j * n * NIN;
+        const bf *hb = p->hb + (size_t)j * n * HID;
+        gemm(s, x, NIN, 1, wb + O_WIH, 1, NIN, p->gi, 3 * HID, n, 3 * HID, NIN, 0);
+        gemm(s, hb, HID, 1, wb + O_WHH, 1, HID, p->gh, 3 * HID, n, 3 * HID, HID, 0);
+        const size_t o = (size_t)j * n * HID;
+        k_gru_cell<<<nb((size_t)n * HID), 256, 0, s>>>(p->gi, p->gh, p->p, p->h + o, n, p->r + o, p->z + o, p->nn + o,
+                                                        p->ghn + o, p->h + o + (size_t)n * HID, p->hb + o + (size_t)n * HID,
+                                                        j == NHIST - 1 ? p->ub : nullptr);
+    }
+    gemm(s, p->ub, MLPIN, 1, wb + O_W1, 1, MLPIN, p->a1, WID, n, WID, MLPIN, 0);
+    k_bias_gelu<<<nb((size_t)n * WID), 256, 0, s>>>(p->a1, p->p + O_B1, n, WID, p->y1);
+    gemm(s, p->y1, WID, 1, wb + O_W2, 1, WID, p->a2, WID, n, WID, WID, 0);
+    k_bias_gelu<<<nb((size_t)n * WID), 256, 0, s>>>(p->a2, p->p + O_B2, n, WID, p->y2);
+    gemm(s, p->y2, WID, 1, wb + O_W3, 1, WID, p->a3, WID, n, WID, WID, 0);
+    k_bias_gelu<<<nb((size_t)n * WID), 256, 0, s>>>(p->a3, p->p + O_B3, n, WID, p->y3);
+    gemm(s, p->y3, WID, 1, wb + O_W4, 1, WID, p->o, NOUT, n, NOUT, WID, 0);
+}
+
+int ksplit_for(uint32_t n) { return (int)std::max(1u, std::min(64u, n / 256)); }
+
+// loss and gradient of the mean loss into p->g (zeroed here)
+void backward(gpis_proposal *p, const float2 *tgt, uint32_t n, cudaStream_t s)
+{
+    const bf *wb = p->pb;
+    float *G = p->g;
+    const int ks = ksplit_for(n);
+    cudaMemsetAsync(G, 0, N_PARAMS * sizeof(float), s);
+    cudaMemsetAsync(p->loss, 0, sizeof(float), s);
+    k_loss<<<nb(n), 256, 0, s>>>(p->o, p->p + O_B4, tgt, n, 1.0f / (float)n, p->dof, p->dob, p->loss);
+    // output layer
+    gemm(s, p->dob, 1, NOUT, p->y3, WID, 1, G + O_W4, WID, NOUT, WID, n, 1, ks);
+    k_colsum<<<64, 256, 0, s>>>(p->dof, n, NOUT, NOUT, G + O_B4);
+    gemm(s, p->dob, NOUT, 1, wb + O_W4, WID, 1, p->dy, WID, n, WID, NOUT, 0);
+    // hidden layers 3, 2, 1
+    const float *acts[3] = {p->a3, p->a2, p->a1};
+    const bf *ins[3] = {p->y2, p->y1, p->ub};
+    const int ow[3] = {O_W3, O_W2, O_W1}, ob[3] = {O_B3, O_B2, O_B1}, inw[3] = {WID, WID, MLPIN};
+    for (int l = 0; l < 3; ++l) {
+        k_gelu_back<<<nb((size_t)n * WID), 256, 0, s>>>(p->dy, acts[l], n, WID, p->daf, p->dab);
+        gemm(s, p->dab, 1, WID, ins[l], inw[l], 1, G + ow[l], inw[l], WID, inw[l], n, 1, ks);
+        k_colsum<<<64, 256, 0, s>>>(p->daf, n, WID, WID, G + ob[l]);
+        if (l < 2) gemm(s, p->dab, WID, 1, wb + ow[l], WID, 1, p->dy, WID, n, WID, WID, 0);
+        else gemm(s, p->dab, WID, 1, wb + ow[l], MLPIN, 1, p->du, MLPIN, n, MLPIN, WID, 0);
+    }
+    // GRU, through time
+    const float *dh = p->du;
+    long ldh = MLPIN;
+    for (int j = NHIST - 1; j >= 0; --j) {
+        const size_t o = (size_t)j * n * HID;
+        k_gru_back<<<nb((size_t)n * HID), 256, 0, s>>>(dh, ldh, p->r + o, p->z + o, p->nn + o, p->ghn + o, p->h + o,
+                                                        n, p->dgif, p->dgib, p->dghf, p->dghb, p->dh);
+        const bf *x = p->xb + (size_t)j * n * NIN;
+        const bf *hb = p->hb + o;
+        gemm(s, p->dgib, 1, 3 * HID, x, NIN, 1, G + O_WIH, NIN, 3 * HID, NIN, n, 1, ks);
+        gemm(s, p->dghb, 1, 3 * HID, hb, HID, 1, G + O_WHH, HID, 3 * HID, HID, n, 1, ks);
+        k_colsum<<<64, 192, 0, s>>>(p->dgif, n, 3 * HID, 3 * HID, G + O_BIH);
+        k_colsum<<<64, 192, 0, s>>>(p->dghf, n, 3 * HID, 3 * HID, G + O_BHH);
+        gemm(s, p->dghb, 3 * HID, 1, wb + O_WHH, HID, 1, p->dh, HID, n, HID, 3 * HID, 1);
+        dh = p->dh;
+        ldh = HID;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t gpis_proposal_n_params(void) { return (uint32_t)N_PARAMS; }
+
+void gpis_proposal_destroy(gpis_proposal *p)
+{
+    if (!p) return;
+    for (void *v : p->act) cudaFree(v);
+    cudaFree(p->p);
+    cudaFree(p->g);
+    cudaFree(p->m1);
+    cudaFree(p->m2);
+    cudaFree(p->pb);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+int gpis_proposal_set_params(gpis_proposal *p, const float *params)
+{
+    if (!p || !params) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    PTRY(cudaMemcpy(p->p, params, N_PARAMS * sizeof(float), cudaMemcpyHostToDevice), "upload proposal parameters");
+    k_to_bf16<<<nb(N_PARAMS), 256, 0, p->stream>>>(p->p, N_PARAMS, p->pb);
+    PTRY(cudaMemsetAsync(p->m1, 0, N_PARAMS * sizeof(float), p->stream), "reset Adam state");
+    PTRY(cudaMemsetAsync(p->m2, 0, N_PARAMS * sizeof(float), p->stream), "reset Adam state");
+    p->step = 0;
+    PTRY(cudaStreamSynchronize(p->stream), "set proposal parameters");
+    return GPIS_OK;
+}
+
+int gpis_proposal_create(const float *params, gpis_proposal **out)
+{
+    if (!out) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    *out = nullptr;
+    gpis_proposal *p = new gpis_proposal;
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&p->p, N_PARAMS * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&p->g, N_PARAMS * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&p->m1, N_PARAMS * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&p->m2, N_PARAMS * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&p->pb, N_PARAMS * sizeof(bf)) != cudaSuccess) {
+        gpis_proposal_destroy(p);
+        return gpis_internal_set_error(GPIS_ENOMEM, "allocate proposal parameters");
+    }
+    std::vector<float> zero;
+    if (!params) {
+        zero.assign(N_PARAMS, 0.0f);
+        params = zero.data();
+    }
+    const int rc = gpis_proposal_set_params(p, params);
+    if (rc) {
+        gpis_proposal_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return GPIS_OK;
+}
+
+int gpis_proposal_get_params(gpis_proposal *p, float *params)
+{
+    if (!p || !params) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    PTRY(cudaStreamSynchronize(p->stream), "synchronize proposal");
+    PTRY(cudaMemcpy(params, p->p, N_PARAMS * sizeof(float), cudaMemcpyDeviceToHost), "read proposal parameters");
+    return GPIS_OK;
+}
+
+static int check_batch(gpis_proposal *p, const float *feat, uint32_t n)
+{
+    if (!p || !feat) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    if (n == 0 || n % 16) return gpis_internal_set_error(GPIS_EINVAL, "the batch must be a positive multiple of 16");
+    return ensure_batch(p, n);
+}
+
+int gpis_proposal_forward(gpis_proposal *p, const float *features, uint32_t n, float *outputs)
+{
+    int rc = check_batch(p, features, n);
+    if (rc) return rc;
+    if (!outputs) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    forward(p, features, n, p->stream);
+    // add the output bias the loss kernel adds in place
+    std::vector<float> b(NOUT);
+    PTRY(cudaMemcpyAsync(b.data(), p->p + O_B4, NOUT * sizeof(float), cudaMemcpyDeviceToHost, p->stream), "read bias");
+    PTRY(cudaMemcpyAsync(outputs, p->o, (size_t)n * NOUT * sizeof(float), cudaMemcpyDeviceToDevice, p->stream),
+         "copy outputs");
+    PTRY(cudaStreamSynchronize(p->stream), "proposal forward");
+    std::vector<float> h((size_t)n * NOUT);
+    PTRY(cudaMemcpy(h.data(), outputs, h.size() * sizeof(float), cudaMemcpyDeviceToHost), "read outputs");
+    for (size_t i = 0; i < h.size(); ++i) h[i] += b[i % NOUT];
+    PTRY(cudaMemcpy(outputs, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice), "write outputs");
+    PTRY(cudaGetLastError(), "proposal forward kernels");
+    return GPIS_OK;
+}
+
+int gpis_proposal_gradient(gpis_proposal *p, const float *features, const float *targets, uint32_t n, float *grad,
+                           float *loss)
+{
+    int rc = check_batch(p, features, n);
+    if (rc) return rc;
+    if (!targets || !grad) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    forward(p, features, n, p->stream);
+    backward(p, reinterpret_cast<const float2 *>(targets), n, p->stream);
+    PTRY(cudaStreamSynchronize(p->stream), "proposal gradient");
+    PTRY(cudaGetLastError(), "proposal gradient kernels");
+    PTRY(cudaMemcpy(grad, p->g, N_PARAMS * sizeof(float), cudaMemcpyDeviceToHost), "read gradient");
+    float l = 0.0f;
+    PTRY(cudaMemcpy(&l, p->loss, sizeof(float), cudaMemcpyDeviceToHost), "read loss");
+    if (loss) *loss = l / (float)n;
+    return GPIS_OK;
+}
+
+int gpis_proposal_train_step(gpis_proposal *p, const float *features, const float *targets, uint32_t n, float lr,
+                             float *loss)
+{
+    int rc = check_batch(p, features, n);
+    if (rc) return rc;
+    if (!targets) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    cudaStream_t s = p->stream;
+    forward(p, features, n, s);
+    backward(p, reinterpret_cast<const float2 *>(targets), n, s);
+    p->step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f - std::pow(b1, (float)p->step), c2 = 1.0f - std::pow(b2, (float)p->step);
+    k_adam<<<nb(N_PARAMS), 256, 0, s>>>(p->p, p->g, p->m1, p->m2, N_PARAMS, lr, b1, b2, 1e-8f, c1, c2, p->pb);
+    PTRY(cudaGetLastError(), "proposal training kernels");
+    if (loss) {
+        float l = 0.0f;
+        PTRY(cudaMemcpyAsync(&l, p->loss, sizeof(float), cudaMemcpyDeviceToHost, s), "read loss");
+        PTRY(cudaStreamSynchronize(s), "proposal training step");
+        *loss = l / (float)n;
+    }
+    return GPIS_OK;
+}
+
+int gpis_proposal_infer(gpis_proposal *p, const gpis_flight_soa *in, const float *features, float *intervals,
+                        uint32_t n, void *cuda_stream)
+{
+    if (!p || !in || !features || !intervals) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    if (n == 0) return GPIS_OK;
+    if (!in->origin_near || !in->dir_far) return gpis_internal_set_error(GPIS_EINVAL, "origin_near and dir_far are required");
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    // the parameters are written on the proposal's own stream
+    cudaEvent_t ev;
+    PTRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "create event");
+    cudaEventRecord(ev, p->stream);
+    cudaStreamWaitEvent(s, ev, 0);
+    cudaEventDestroy(ev);
+    const unsigned blocks = (unsigned)((n + 63) / 64);
+    k_propose<<<blocks, 128, 0, s>>>(p->pb, p->p, features, reinterpret_cast<const float4 *>(in->origin_near),
+                                     reinterpret_cast<const float4 *>(in->dir_far), n,
+                                     reinterpret_cast<float4 *>(intervals));
+    PTRY(cudaGetLastError(), "proposal inference kernel");
+    return GPIS_OK;
+}
+
+}  // extern "C"
+
+namespace gpis {
+cudaError_t launch_features(const DevMedium *media, int n_media, const gpis_flight_soa &in, uint32_t n, float *feat,
+                            cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_features<<<(n + 127) / 128, 128, 0, s>>>(media, n_media, reinterpret_cast<const float4 *>(in.origin_near),
+                                               reinterpret_cast<const float4 *>(in.dir_far),
+                                               reinterpret_cast<const uint4 *>(in.seeds),
+                                               reinterpret_cast<const float4 *>(in.prev), in.medium, n, feat);
+    return cudaGetLastError();
+}
+}  // namespace gpis

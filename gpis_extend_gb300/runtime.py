@@ -245,3 +245,94 @@ def se_splat_1d(q, c, scale):
                                    float(scale), None), "gpis_se_splat_1d")
     torch.cuda.synchronize()
     return v.cpu().numpy(), dv.cpu().numpy()
+
+
+class Proposal:
+    """The learned crossing proposal (gpis_proposal_*) on the current CUDA device.
+
+    Device batches are torch tensors: features (n, 24) float32, targets (n, 2)
+    float32 (u*, hit), intervals (n, 4) float32 (t_a, t_b, miss probability, m)."""
+
+    def __init__(self, params=None):
+        self.lib = abi.load_library()
+        self.n_params = int(self.lib.gpis_proposal_n_params())
+        h = ctypes.c_void_p()
+        ptr = None
+        if params is not None:
+            params = np.ascontiguousarray(params, np.float32)
+            assert params.size == self.n_params
+            ptr = params.ctypes.data
+        abi.check(self.lib.gpis_proposal_create(ptr, ctypes.byref(h)), "gpis_proposal_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.gpis_proposal_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_params(self, params):
+        params = np.ascontiguousarray(params, np.float32)
+        abi.check(self.lib.gpis_proposal_set_params(self.h, params.ctypes.data), "gpis_proposal_set_params")
+
+    def get_params(self):
+        out = np.zeros(self.n_params, np.float32)
+        abi.check(self.lib.gpis_proposal_get_params(self.h, out.ctypes.data), "gpis_proposal_get_params")
+        return out
+
+    def train_step(self, feats, targets, lr, want_loss=True):
+        loss = ctypes.c_float()
+        abi.check(self.lib.gpis_proposal_train_step(self.h, feats.data_ptr(), targets.data_ptr(), feats.shape[0],
+                                                    float(lr), ctypes.byref(loss) if want_loss else None),
+                  "gpis_proposal_train_step")
+        return loss.value if want_loss else None
+
+    def gradient(self, feats, targets):
+        g = np.zeros(self.n_params, np.float32)
+        loss = ctypes.c_float()
+        abi.check(self.lib.gpis_proposal_gradient(self.h, feats.data_ptr(), targets.data_ptr(), feats.shape[0],
+                                                  g.ctypes.data, ctypes.byref(loss)), "gpis_proposal_gradient")
+        return g, loss.value
+
+    def forward(self, feats):
+        torch = _torch()
+        out = torch.zeros((feats.shape[0], 32), dtype=torch.float32, device=feats.device)
+        abi.check(self.lib.gpis_proposal_forward(self.h, feats.data_ptr(), feats.shape[0], out.data_ptr()),
+                  "gpis_proposal_forward")
+        return out
+
+    def infer(self, dev, feats, stream=None):
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        out = torch.zeros((dev.n, 4), dtype=torch.float32, device=feats.device)
+        soa = dev.soa()
+        abi.check(self.lib.gpis_proposal_infer(self.h, ctypes.byref(soa), feats.data_ptr(), out.data_ptr(), dev.n,
+                                               ctypes.c_void_p(s.cuda_stream)), "gpis_proposal_infer")
+        return out
+
+
+def proposal_features(ctx, dev, stream=None):
+    """gpis_proposal_features of a DeviceFlights batch: (n, 24) float32 on the device."""
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    out = torch.zeros((dev.n, 24), dtype=torch.float32, device="cuda")
+    soa = dev.soa()
+    abi.check(ctx.lib.gpis_proposal_features(ctx.h, ctypes.byref(soa), out.data_ptr(), dev.n,
+                                             ctypes.c_void_p(s.cuda_stream)), "gpis_proposal_features")
+    return out
+
+
+def submit_proposed(ctx, dev, intervals, stream=None):
+    """gpis_flights_submit_proposed: the flights of dev with proposals (results in dev.rec)."""
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    soa = dev.soa()
+    res = dev.result_soa()
+    abi.check(ctx.lib.gpis_flights_submit_proposed(ctx.h, ctypes.byref(soa), intervals.data_ptr(), ctypes.byref(res),
+                                                   dev.n, ctypes.c_void_p(s.cuda_stream)),
+              "gpis_flights_submit_proposed")

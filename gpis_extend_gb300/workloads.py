@@ -148,6 +148,36 @@ def sphere_flights(n, desc, seed=7, half=1.5, bounce=0, scene_seed=1, index_offs
     return b
 
 
+def torus_flights(n, desc, seed=11, half=2.0, bounce=0, scene_seed=1, index_offset=0):
+    """Primary flights through the torus-union-plane field (bounded by the cube +-2):
+    origins uniform on a radius-4 sphere, directions toward uniform points of the box
+    [-1.4, 1.4] x [-0.6, 0.4] x [-1.4, 1.4] around the torus and the plane; the rest
+    as sphere_flights."""
+    i = np.arange(n, dtype=np.uint64) + np.uint64(index_offset)
+    o = 4.0 * _unit_sphere(counter_uniform(seed, i, 0), counter_uniform(seed, i, 1))
+    tgt = np.stack([2.8 * counter_uniform(seed, i, 2) - 1.4, counter_uniform(seed, i, 3) - 0.6,
+                    2.8 * counter_uniform(seed, i, 4) - 1.4], axis=1)
+    d = tgt - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tmin, tmax = clip_to_cube(o, d, half)
+    entry = np.clip((o + d * tmin[:, None]).astype(np.float32), -half, half).astype(np.float32)
+    b = abi.FlightBatch(n)
+    b.origin_near[:, :3] = entry
+    b.origin_near[:, 3] = 0.0
+    b.dir_far[:, :3] = d.astype(np.float32)
+    b.dir_far[:, 3] = (tmax - tmin).astype(np.float32)
+    pss = np.stack([(i % 2048).astype(np.uint32), (i // 2048).astype(np.uint32),
+                    np.zeros(n, np.uint32), np.full(n, bounce, np.uint32)], axis=1)
+    ns, nm = pss_seeds(desc, pss, scene_seed)
+    b.seeds[:, 0] = ns
+    b.seeds[:, 1] = nm
+    b.seeds[:, 2] = abi.FLAG_FIRST_SCATTER
+    b.set_jitter(counter_float32_unit(seed, i, 5))
+    b.pss = pss
+    b.index_offset = int(index_offset)
+    return b
+
+
 def secondary_flights(primary, rec, desc, seed=7, half=1.5, scene_seed=1):
     """Conditioned secondary flights from the hits of a primary pass: origin = hit
     point, direction = mirror reflection about the sampled normal, prevValue = 0,

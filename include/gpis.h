@@ -424,6 +424,53 @@ typedef struct {
  * the mean radiance of spp paths per pixel.  Blocking.                       */
 int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *image_rgb, gpis_render_stats *stats);
 
+/* ---- learned crossing proposal -------------------------------------------
+ * A GRU (hidden 32) over eight samples of the mean SDF and its slope along the
+ * flight, then a 3 x 64 GELU MLP over its state and eight per-flight features,
+ * emitting an 8-component logistic mixture over u = (t - near) / (far - near)
+ * of the first downcrossing and a miss logit.  BF16 tensor-core contractions,
+ * FP32 accumulation, elementwise parts, loss and Adam.  The parameters are one
+ * float vector of gpis_proposal_n_params() values: w_ih (96 x 16), b_ih (96),
+ * w_hh (96 x 32), b_hh (96), w1 (64 x 48), b1, w2 (64 x 64), b2, w3 (64 x 64),
+ * b3, w4 (32 x 64), b4 (32), weights row-major [out][in]; the padded input
+ * columns (w_ih 2..15, w1 40..47) and output rows (w4, b4 25..31) are unused.
+ * Outputs: 0..7 mixture logits, 8..15 locations (through a sigmoid), 16..23
+ * scales (softplus + 1e-3), 24 the miss logit.
+ * The proposal never changes a flight's result: gpis_flights_submit_proposed
+ * lets the march take longer certified skips before the proposed interval.   */
+typedef struct gpis_proposal gpis_proposal;
+uint32_t gpis_proposal_n_params(void);
+/* params: host vector, NULL for zeros.  One CUDA stream per proposal. */
+int gpis_proposal_create(const float *params, gpis_proposal **out);
+void gpis_proposal_destroy(gpis_proposal *prop);
+int gpis_proposal_set_params(gpis_proposal *prop, const float *params);    /* resets Adam */
+int gpis_proposal_get_params(gpis_proposal *prop, float *params);
+/* 24 features per flight (device pointers, asynchronous): the mean SDF and its
+ * slope along the ray at the centres of eight equal parts of [near, far], then
+ * t_max / 4, 10 x the local length scale, the conditioned value and derivative,
+ * the first-scatter flag, 10 x the amplitude, step / t_max, the mean at near. */
+int gpis_proposal_features(gpis_ctx *ctx, const gpis_flight_soa *in, float *features, uint32_t n,
+                           void *cuda_stream);
+/* Training on device batches: features (24 per flight), targets (u*, hit) per
+ * flight; n a positive multiple of 16.  train_step: one Adam step (lr), loss =
+ * mean negative log-likelihood before the step (NULL: no synchronization).
+ * gradient: the gradient of the mean loss (host vector) without a step.
+ * forward: the 32 raw outputs per flight (device).  Blocking.               */
+int gpis_proposal_train_step(gpis_proposal *prop, const float *features, const float *targets, uint32_t n,
+                             float lr, float *loss);
+int gpis_proposal_gradient(gpis_proposal *prop, const float *features, const float *targets, uint32_t n,
+                           float *grad, float *loss);
+int gpis_proposal_forward(gpis_proposal *prop, const float *features, uint32_t n, float *outputs);
+/* Fused inference (asynchronous, device pointers): per flight the dominant
+ * component's interval [m - 3s, m + 3s] in t, the miss probability and m:
+ * intervals[4 i .. 4 i + 3] = (t_a, t_b, q, m).                             */
+int gpis_proposal_infer(gpis_proposal *prop, const gpis_flight_soa *in, const float *features, float *intervals,
+                        uint32_t n, void *cuda_stream);
+/* gpis_flights_submit with proposals: identical results; intervals from
+ * gpis_proposal_infer (16-byte aligned).                                    */
+int gpis_flights_submit_proposed(gpis_ctx *ctx, const gpis_flight_soa *in, const float *intervals,
+                                 const gpis_result_soa *out, uint32_t n, void *cuda_stream);
+
 /* Last error message of the calling thread ("" when none). */
 const char *gpis_last_error(void);
 

@@ -1,0 +1,217 @@
+"""The learned crossing proposal (csrc/proposal.cu) against its NumPy restatement
+(oracle/proposal_ref.py): features, the BF16 forward, the backward (every
+parameter's gradient), Adam, the fused inference kernel, training on plain
+flights, and flights with proposals identical to plain flights.
+
+Tolerances: the kernels and the restatement round the same GEMM operands to
+BF16; the kernels accumulate in FP32 and the restatement in FP64, so an
+activation can round to the neighbouring BF16 value now and then (2^-8
+relative): outputs within 1e-2 absolute, gradients within 3e-2 relative L2 per
+tensor."""
+import numpy as np
+import pytest
+
+from gpis_extend_gb300 import abi, proposal, workloads
+from oracle import proposal_ref as R
+
+
+def random_features(n, rng):
+    f = rng.normal(size=(n, 24)).astype(np.float32)
+    f[:, 20] = (rng.random(n) < 0.5).astype(np.float32)
+    return f
+
+
+def random_targets(n, rng):
+    return np.stack([rng.uniform(0.02, 0.98, n), (rng.random(n) < 0.7).astype(np.float64)], axis=1).astype(np.float32)
+
+
+def test_reference_backward_matches_finite_differences(monkeypatch):
+    monkeypatch.setattr(R, "bf16", lambda x: np.asarray(x, np.float64))
+    rng = np.random.default_rng(0)
+    p = R.unflatten(proposal.init_params(1).astype(np.float64))
+    f = rng.normal(size=(16, 24))
+    tg = random_targets(16, rng)
+    o, c = R.forward(p, f)
+    _, g = R.loss_and_grad_out(o, tg[:, 0].astype(np.float64), tg[:, 1] > 0)
+    gflat = R.flatten(R.backward(p, c, g))
+    flat = R.flatten(p)
+    for i in rng.choice(len(flat), 30, replace=False):
+        e = 1e-6
+        fp, fm = flat.copy(), flat.copy()
+        fp[i] += e
+        fm[i] -= e
+        lp = R.loss_and_grad_out(R.forward(R.unflatten(fp), f)[0], tg[:, 0], tg[:, 1] > 0)[0]
+        lm = R.loss_and_grad_out(R.forward(R.unflatten(fm), f)[0], tg[:, 0], tg[:, 1] > 0)[0]
+        fd = (lp - lm) / (2 * e)
+        assert abs(fd - gflat[i]) <= 1e-4 * (abs(fd) + 1e-3), (i, fd, gflat[i])
+
+
+def test_init_params_layout():
+    p = proposal.init_params(3)
+    assert p.size == R.n_params() == 18336
+    d = R.unflatten(p)
+    assert np.all(d["w_ih"][:, 2:] == 0) and np.all(d["w1"][:, 40:] == 0)
+    assert np.all(d["w4"][25:] == 0) and np.all(d["b4"][25:] == 0)
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    torch = pytest.importorskip("torch")
+    from gpis_extend_gb300 import runtime
+    return torch, runtime
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["sphere", "torus"])
+def test_gpu_features_match_restatement(gpu, kind):
+    torch, runtime = gpu
+    if kind == "sphere":
+        desc = workloads.sphere_medium()
+        prim = workloads.sphere_flights(4096, desc)
+        half = 1.5
+    else:
+        desc = proposal.config2_medium()
+        prim = workloads.torus_flights(4096, desc)
+        half = 2.0
+    with runtime.Context(desc) as ctx:
+        rec = ctx.trace_host(prim)
+        sec, _ = workloads.secondary_flights(prim, rec, desc, half=half)
+        for b in (prim, sec):
+            dev = runtime.DeviceFlights(b)
+            f = runtime.proposal_features(ctx, dev).cpu().numpy()
+            ref = R.features(desc, b.origin_near, b.dir_far, b.seeds, b.prev)
+            err = np.abs(f - ref)
+            assert np.all(err <= 1e-4 * (1 + np.abs(ref))), (np.unravel_index(np.argmax(err), err.shape), err.max())
+
+
+@pytest.mark.gpu
+def test_gpu_forward_and_gradient_match_reference(gpu):
+    torch, runtime = gpu
+    rng = np.random.default_rng(4)
+    n = 512
+    f = random_features(n, rng)
+    tg = random_targets(n, rng)
+    params = proposal.init_params(5)
+    with runtime.Proposal(params) as prop:
+        fd = torch.from_numpy(f).cuda()
+        td = torch.from_numpy(tg).cuda()
+        out = prop.forward(fd).cpu().numpy()
+        grad, loss = prop.gradient(fd, td)
+    p = R.unflatten(params.astype(np.float64))
+    o, cache = R.forward(p, f)
+    assert np.max(np.abs(out[:, :25] - o[:, :25])) <= 1e-2
+    assert np.median(np.abs(out[:, :25] - o[:, :25])) <= 1e-4
+    lref, g = R.loss_and_grad_out(o, tg[:, 0].astype(np.float64), tg[:, 1] > 0)
+    assert abs(loss - lref) <= 1e-3 * (1 + abs(lref))
+    gref = R.backward(p, cache, g)
+    gd = R.unflatten(grad.astype(np.float64))
+    for name, _ in R.PARAMS:
+        a, b = gd[name], gref[name]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+        print(name, "relative L2", rel)
+        assert rel <= 3e-2, (name, rel)
+
+
+@pytest.mark.gpu
+def test_gpu_adam_step_matches_reference(gpu):
+    torch, runtime = gpu
+    rng = np.random.default_rng(6)
+    n = 256
+    f = torch.from_numpy(random_features(n, rng)).cuda()
+    t = torch.from_numpy(random_targets(n, rng)).cuda()
+    params = proposal.init_params(7)
+    with runtime.Proposal(params) as prop:
+        g0, _ = prop.gradient(f, t)
+        prop.train_step(f, t, 1e-2)
+        p1 = prop.get_params()
+        g1, _ = prop.gradient(f, t)
+        prop.train_step(f, t, 1e-2)
+        p2 = prop.get_params()
+    flat, m, v = params.astype(np.float64), np.zeros(params.size), np.zeros(params.size)
+    flat, m, v = R.adam(flat, g0.astype(np.float64), m, v, 1, 1e-2)
+    assert np.max(np.abs(p1 - flat)) <= 1e-5
+    flat, m, v = R.adam(p1.astype(np.float64), g1.astype(np.float64), m, v, 2, 1e-2)
+    assert np.max(np.abs(p2 - flat)) <= 1e-5
+
+
+@pytest.mark.gpu
+def test_gpu_fused_inference_matches_unfused(gpu):
+    torch, runtime = gpu
+    desc = proposal.config2_medium()
+    b = workloads.torus_flights(2048, desc)
+    params = proposal.init_params(9)
+    with runtime.Context(desc) as ctx, runtime.Proposal(params) as prop:
+        dev = runtime.DeviceFlights(b)
+        f = runtime.proposal_features(ctx, dev)
+        iv = prop.infer(dev, f).cpu().numpy()
+        out = prop.forward(f).cpu().numpy()
+    logits = out[:, :8]
+    top2 = np.sort(logits, axis=1)[:, -2:]
+    clear = (top2[:, 1] - top2[:, 0]) > 1e-2
+    ua, ub, q = R.interval(out.astype(np.float64))
+    near, far = b.origin_near[:, 3], b.dir_far[:, 3]
+    tm = far - near
+    # an untrained network's logits are close together: compare the rows whose
+    # leading component is clear of the second by more than the two paths differ
+    assert clear.sum() >= 200
+    assert np.all(np.abs((iv[clear, 0] - near[clear]) / tm[clear] - ua[clear]) <= 2e-2)
+    assert np.all(np.abs((iv[clear, 1] - near[clear]) / tm[clear] - ub[clear]) <= 2e-2)
+    assert np.all(np.abs(iv[:, 2] - q) <= 1e-2)
+
+
+@pytest.mark.gpu
+def test_gpu_training_learns_and_proposals_keep_flights(gpu):
+    """Training on plain config-2 flights lowers the loss and puts more crossings
+    inside the proposed intervals; proposed flights equal plain flights bit for bit."""
+    torch, runtime = gpu
+    desc = proposal.config2_medium()
+    batches = proposal.flight_set(desc, 1 << 15)
+    with runtime.Context(desc) as ctx, runtime.Proposal(proposal.init_params(0)) as prop:
+        f, t = proposal.dataset(ctx, batches)
+        hist, secs = proposal.train(prop, f, t, steps=300, batch=4096, lr=3e-3, log_every=50)
+        print("loss", hist, "seconds", secs)
+        assert hist[-1][1] < hist[0][1] - 0.2
+        test = workloads.torus_flights(1 << 14, desc, seed=23)
+        dev = runtime.DeviceFlights(test)
+        ctx.submit(dev)
+        torch.cuda.synchronize()
+        plain = dev.rec.cpu().numpy().copy()
+        feats = runtime.proposal_features(ctx, dev)
+        iv = prop.infer(dev, feats)
+        dev.rec.zero_()
+        runtime.submit_proposed(ctx, dev, iv)
+        torch.cuda.synchronize()
+        prop_rec = dev.rec.cpu().numpy()
+        inside, hits = proposal.interval_hits(iv.cpu().numpy(), test, plain)
+        print("crossings inside the proposed interval", inside, "of", hits)
+        assert inside > 0.5
+    assert np.array_equal(plain.view(np.uint32), prop_rec.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_gpu_proposed_sphere_flights_identical_with_any_proposal(gpu):
+    """Soundness: whatever the intervals, every flight's record is unchanged (the
+    stationary sphere field, where the proposal lifts the skip cap)."""
+    torch, runtime = gpu
+    desc = workloads.sphere_medium()
+    prim = workloads.sphere_flights(1 << 15, desc)
+    rng = np.random.default_rng(1)
+    with runtime.Context(desc) as ctx:
+        dev = runtime.DeviceFlights(prim)
+        ctx.submit(dev)
+        torch.cuda.synchronize()
+        plain = dev.rec.cpu().numpy().copy()
+        far = prim.dir_far[:, 3]
+        for mode in ("far", "random", "zero"):
+            iv = np.zeros((prim.n, 4), np.float32)
+            if mode == "far":
+                iv[:, 0] = far
+            elif mode == "random":
+                iv[:, 0] = rng.uniform(0, 1, prim.n) * far
+            iv[:, 1] = far
+            ivd = torch.from_numpy(iv).cuda()
+            dev.rec.zero_()
+            runtime.submit_proposed(ctx, dev, ivd)
+            torch.cuda.synchronize()
+            got = dev.rec.cpu().numpy()
+            assert np.array_equal(plain.view(np.uint32), got.view(np.uint32)), mode
