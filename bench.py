@@ -10,13 +10,22 @@ seeded synthetic data generated once; every step re-traces all flights.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
     python bench.py --workload image0|image2 [--size S] [--spp P] [--steps K]
+    python bench.py --workload learned [--flights N] [--train-flights N] [--train-steps K]
 
 The image workloads render with gpis_render (the wavefront path tracer around
 the medium) and report the flights traced per second of render:
 image0 = 256 x 256, 16 spp, 4 bounces, the sphere field with 3D noise and
 Renewal, Lambert albedo 0.8, a 1 x 1 quad light at y = 3; image2 = 1024 x 1024,
 256 spp, 8 bounces, the nonstationary three-octave torus-union-plane field with
-1D noise and Renewal+ (Lambert; the mirror conductor is not built).
+1D noise and Renewal+, a copper conductor phase (plain reflection sampling: the
+1D NEE law is defined for one realization, not for an octave sum).
+
+The learned arm: a proposal network (GRU 32 + 3 x 64 GELU MLP -> 8-component
+logistic mixture over the crossing interval, BF16 tensor-core kernels) trained
+on flights the plain kernels traced, then features + inference + the march with
+proposals on the same flights.  The default line carries it as `learned` (a
+network trained on 2^20 disjoint sphere flights); `--workload learned` runs it on
+the three-octave torus-plane field with 2^22 + secondary training flights.
 
 Prints one JSON line (rank 0).  `value` is device-resident throughput (flights/s,
 inputs already in HBM, 512 MiB of flight streams > L2 so no flush is needed);
@@ -204,11 +213,135 @@ IMAGE_WORKLOADS = {
     "image0": dict(medium="sphere_3d", size=256, spp=16, bounces=4,
                    text="image render: 256x256 pinhole at z=4, 16 spp, 4 bounces, sphere SDF field, 3D SE noise "
                         "sigma 0.05 l 0.1 N 8, Renewal, Lambert albedo 0.8, 1x1 quad light at y=3"),
-    "image2": dict(medium="torus", size=1024, spp=256, bounces=8,
+    "image2": dict(medium="torus", size=1024, spp=256, bounces=8, phase="conductor", box=2.0,
                    text="image render: 1024x1024, 256 spp, 8 bounces, torus (R 1, r 0.35) union plane y=-0.5, "
                         "l(p)=0.11+0.09 sin3x cos2z, 3 octaves sigma 0.04/0.02/0.01, 1D noise, Renewal+, "
-                        "Lambert albedo 0.8 (mirror conductor not built), 1x1 quad light at y=3"),
+                        "copper conductor phase with plain reflection sampling (1D NEE needs one octave), "
+                        "cube 2, 1x1 quad light at y=3"),
 }
+
+
+def train_proposal(ctx, desc, make_flights, n_train, steps, batch, half, seed=101):
+    """The learned proposal trained on flights the plain kernels traced (primaries of
+    make_flights and the conditioned secondaries at their hits)."""
+    from gpis_extend_gb300 import proposal, runtime, workloads
+    prim = make_flights(n_train, desc, seed=seed, half=half)
+    rec = ctx.trace_host(prim)
+    sec, _ = workloads.secondary_flights(prim, rec, desc, seed=seed, half=half)
+    f, t = proposal.dataset(ctx, [prim, sec])
+    prop = runtime.Proposal(proposal.init_params(0))
+    hist, secs = proposal.train(prop, f, t, steps=steps, batch=batch, lr=3e-3, log_every=max(1, steps // 4))
+    info = {"flights": int(f.shape[0]), "steps": steps, "batch": batch, "seconds": secs,
+            "loss": [[k, round(v, 4)] for k, v in hist]}
+    return prop, info
+
+
+def learned_arm(ctx, prop, batches, devs, steps, stream, plain_ms):
+    """Per step and batch: features, fused inference, the march with proposals.  Returns
+    the arm's summary (flights/s, ratio to the plain arm, interval statistics, identity
+    of every record with the plain records)."""
+    import torch
+    from gpis_extend_gb300 import proposal, runtime
+    plain = [d.rec.clone() for d in devs]
+    feats = [torch.empty((d.n, 24), dtype=torch.float32, device="cuda") for d in devs]
+    ivs = [torch.empty((d.n, 4), dtype=torch.float32, device="cuda") for d in devs]
+
+    def step():
+        for d, f, iv in zip(devs, feats, ivs):
+            runtime.proposal_features(ctx, d, stream, out=f)
+            prop.infer(d, f, stream, out=iv)
+            runtime.submit_proposed(ctx, d, iv, stream)
+
+    step()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        step()
+    end.record(stream)
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    # the parts of one step, timed alone
+    part = {}
+    for name, fn in (("features", lambda d, f, iv: runtime.proposal_features(ctx, d, stream, out=f)),
+                     ("inference", lambda d, f, iv: prop.infer(d, f, stream, out=iv)),
+                     ("march", lambda d, f, iv: runtime.submit_proposed(ctx, d, iv, stream))):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for d, f, iv in zip(devs, feats, ivs):
+            fn(d, f, iv)
+        b.record(stream)
+        torch.cuda.synchronize()
+        part[name] = a.elapsed_time(b)
+    identical = all(torch.equal(p.view(torch.int32), d.rec.view(torch.int32)) for p, d in zip(plain, devs))
+    inside, hits = 0.0, 0
+    for b_, d, iv in zip(batches, devs, ivs):
+        fr, h = proposal.interval_hits(iv.cpu().numpy(), b_, d.rec.cpu().numpy())
+        inside += fr * h
+        hits += h
+    n = sum(d.n for d in devs)
+    value = n * steps / (ms * 1e-3)
+    plain_value = n * steps / (plain_ms * 1e-3)
+    return {"value": value, "unit": UNIT, "ms_per_step": ms / steps, "plain_value": plain_value,
+            "ratio_vs_plain": value / plain_value, "ms_per_part": part,
+            "inside_interval": inside / max(1, hits), "miss_fallback_rate": 1.0 - inside / max(1, hits),
+            "identical_to_plain": bool(identical),
+            "equal_image_rmse": "every flight record equals the plain arm's bit for bit, so images and their "
+                                "RMSE are equal at equal spp"}
+
+
+def run_learned(args):
+    """The learned-proposal workload on the three-octave torus-plane field: 10^7
+    training flights from the plain kernels, then plain vs learned on a fresh set."""
+    import torch
+    from gpis_extend_gb300 import build, proposal, runtime, workloads
+    build.build()
+    desc = proposal.config2_medium()
+    ctx = runtime.Context(desc)
+    prop, info = train_proposal(ctx, desc, workloads.torus_flights, args.train_flights, args.train_steps, 8192, 2.0)
+    n = args.flights
+    prim = workloads.torus_flights(n, desc, seed=23)
+    rec = ctx.trace_host(prim)
+    sec, _ = workloads.secondary_flights(prim, rec, desc, seed=23, half=2.0)
+    devs = [runtime.DeviceFlights(prim), runtime.DeviceFlights(sec)]
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        for d in devs:
+            ctx.submit(d, stream)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        for d in devs:
+            ctx.submit(d, stream)
+    end.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = start.elapsed_time(end)
+    learned = learned_arm(ctx, prop, [prim, sec], devs, args.steps, stream, plain_ms)
+    clocks.stop()
+    flights = prim.n + sec.n
+    line = {
+        "metric": METRIC, "value": learned["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": learned["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 field, bf16 network", "data": "synthetic",
+        "config": {"workload": "learned proposal on the three-octave torus-plane field: GRU 32 + 3x64 GELU MLP "
+                               "-> 8-component logistic mixture, BF16 weights, FP32 accumulation; primary flights "
+                               "(radius-4 origins, seed 23, cube 2) + conditioned secondaries",
+                   "arm": "learned", "flights_per_step": flights, "train": info},
+        "plain": {"value": flights * args.steps / (plain_ms * 1e-3), "ms_per_step": plain_ms / args.steps},
+        "learned": learned,
+        "gpu_launches": args.steps * 2 * 6,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    prop.close()
+    ctx.close()
 
 
 def run_image(args):
@@ -222,7 +355,8 @@ def run_image(args):
     spp = args.spp or cfg["spp"]
     build.build()
     desc = workloads.render_medium(cfg["medium"])
-    sc = workloads.render_scene(width=size, height=size, spp=spp, max_bounces=cfg["bounces"])
+    sc = workloads.render_scene(width=size, height=size, spp=spp, max_bounces=cfg["bounces"],
+                                phase=cfg.get("phase", "lambert"), box_half=cfg.get("box", 1.5))
     ctx = runtime.Context(desc)
     for _ in range(args.warmup):
         ctx.render(workloads.render_scene(width=64, height=64, spp=1, max_bounces=cfg["bounces"]))
@@ -301,7 +435,10 @@ def main():
     ap.add_argument("--flights", type=int, default=1 << 22)
     ap.add_argument("--ref-sample", type=int, default=1 << 16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="flights", choices=["flights", "image0", "image2"])
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--workload", default="flights", choices=["flights", "image0", "image2", "learned"])
+    ap.add_argument("--train-flights", type=int, default=1 << 22)
+    ap.add_argument("--train-steps", type=int, default=1200)
     ap.add_argument("--size", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -311,6 +448,9 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "learned":
+        run_learned(args)
         return
     if args.workload != "flights":
         run_image(args)
@@ -436,6 +576,17 @@ def main():
         "counters": cnt,
         "clocks": clocks.summary(),
     }
+    if rank == 0 and world == 1 and not args.no_learned:
+        # the learned-proposal arm on the same flights (config-1 network trained on a
+        # disjoint flight set); a failure is reported, not raised
+        try:
+            prop, info = train_proposal(ctx, desc, workloads.sphere_flights, 1 << 20, 400, 8192, 1.5)
+            learned = learned_arm(ctx, prop, [prim, sec], [dev_p, dev_s], args.steps, stream, ms)
+            learned["train"] = info
+            prop.close()
+        except Exception as e:  # noqa: BLE001
+            learned = {"error": f"{type(e).__name__}: {e}"}
+        line["learned"] = learned
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(desc, prim, sec)
     if rank == 0:

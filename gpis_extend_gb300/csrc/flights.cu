@@ -1553,7 +1553,7 @@ enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE
 // most march steps one evaluation may skip (fast pass)
 constexpr int kMaxSkip = 8;
 // before a proposed crossing interval the cap is this (every skipped step is still certified)
-constexpr int kMaxSkipProposed = 64;
+constexpr int kMaxSkipProposed = 16;
 
 // Fast values farther than this from zero have the sign of the precise value
 // (the fast evaluator differs from the precise one by a few 1e-8).

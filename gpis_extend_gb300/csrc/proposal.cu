@@ -19,6 +19,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -328,7 +329,15 @@ __global__ void k_features(const DevMedium *media, int n_media, const float4 *on
         int id;
         const float mv = mean_value(m, x, y, z, id);
         float g[3];
-        mean_grad(m, x, y, z, g);
+        if (m.mean_kind == GPIS_MEAN_SPHERE) {
+            // float form of the sphere's gradient (mean_grad takes the reference's double path)
+            const float *c = m.mean_params;
+            const float dx = x - c[0], dy = y - c[1], dz = z - c[2];
+            const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+            g[0] = dx * inv; g[1] = dy * inv; g[2] = dz * inv;
+        } else {
+            mean_grad(m, x, y, z, g);
+        }
         const float sl = g[0] * d.x + g[1] * d.y + g[2] * d.z;
         f[2 * j] = fminf(fmaxf(mv, -4.0f), 4.0f);
         f[2 * j + 1] = fminf(fmaxf(sl, -4.0f), 4.0f);
@@ -406,6 +415,7 @@ __device__ __forceinline__ void gelu_frag(float (&acc)[8][4], const float *bias,
     }
 }
 
+// Persistent: each block loads the weights once and its warps walk 16-flight tiles.
 __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *params, const float *feat,
                                                  const float4 *on, const float4 *df, uint32_t n, float4 *out)
 {
@@ -430,8 +440,9 @@ __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *para
     for (int k = tid; k < NOUT; k += blockDim.x) sb[6 * HID + 3 * WID + k] = params[O_B4 + k];
     __syncthreads();
     const int lane = tid & 31, gi = lane >> 2, ti = lane & 3;
-    const long row0 = ((long)blockIdx.x * 4 + (tid >> 5)) * 16;
-    if (row0 >= (long)n) return;
+    const long tiles = ((long)n + 15) / 16;
+    for (long tile = (long)blockIdx.x * 4 + (tid >> 5); tile < tiles; tile += (long)gridDim.x * 4) {
+    const long row0 = tile * 16;
     const long ra = min(row0 + gi, (long)n - 1), rb = min(row0 + gi + 8, (long)n - 1);
     const float *fa = feat + ra * NFEAT, *fb = feat + rb * NFEAT;
     const float *bih = sb, *bhh = sb + 3 * HID, *b1 = sb + 6 * HID, *b2 = b1 + WID, *b3 = b2 + WID, *b4 = b3 + WID;
@@ -545,6 +556,7 @@ __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *para
             const float ub = fminf(fmaxf(bm + 3.0f * bs, 0.0f), 1.0f);
             out[r] = make_float4(a.w + ua * tm, a.w + ub * tm, q, bm);
         }
+    }
     }
 }
 
@@ -850,7 +862,12 @@ int gpis_proposal_infer(gpis_proposal *p, const gpis_flight_soa *in, const float
     cudaEventRecord(ev, p->stream);
     cudaStreamWaitEvent(s, ev, 0);
     cudaEventDestroy(ev);
-    const unsigned blocks = (unsigned)((n + 63) / 64);
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_propose, 128, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const unsigned blocks = (unsigned)std::min<long>(((long)n + 63) / 64, (long)sms * per_sm);
     k_propose<<<blocks, 128, 0, s>>>(p->pb, p->p, features, reinterpret_cast<const float4 *>(in->origin_near),
                                      reinterpret_cast<const float4 *>(in->dir_far), n,
                                      reinterpret_cast<float4 *>(intervals));

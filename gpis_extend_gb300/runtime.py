@@ -306,21 +306,23 @@ class Proposal:
                   "gpis_proposal_forward")
         return out
 
-    def infer(self, dev, feats, stream=None):
+    def infer(self, dev, feats, stream=None, out=None):
         torch = _torch()
         s = stream if stream is not None else torch.cuda.current_stream()
-        out = torch.zeros((dev.n, 4), dtype=torch.float32, device=feats.device)
+        if out is None:
+            out = torch.zeros((dev.n, 4), dtype=torch.float32, device=feats.device)
         soa = dev.soa()
         abi.check(self.lib.gpis_proposal_infer(self.h, ctypes.byref(soa), feats.data_ptr(), out.data_ptr(), dev.n,
                                                ctypes.c_void_p(s.cuda_stream)), "gpis_proposal_infer")
         return out
 
 
-def proposal_features(ctx, dev, stream=None):
+def proposal_features(ctx, dev, stream=None, out=None):
     """gpis_proposal_features of a DeviceFlights batch: (n, 24) float32 on the device."""
     torch = _torch()
     s = stream if stream is not None else torch.cuda.current_stream()
-    out = torch.zeros((dev.n, 24), dtype=torch.float32, device="cuda")
+    if out is None:
+        out = torch.zeros((dev.n, 24), dtype=torch.float32, device="cuda")
     soa = dev.soa()
     abi.check(ctx.lib.gpis_proposal_features(ctx.h, ctypes.byref(soa), out.data_ptr(), dev.n,
                                              ctypes.c_void_p(s.cuda_stream)), "gpis_proposal_features")
