@@ -169,7 +169,7 @@ class RenderStats(ctypes.Structure):
     _fields_ = [("paths", ctypes.c_uint64), ("distance_flights", ctypes.c_uint64),
                 ("shadow_flights", ctypes.c_uint64), ("medium_events", ctypes.c_uint64),
                 ("failed", ctypes.c_uint64), ("ms", ctypes.c_double), ("launches", ctypes.c_uint64),
-                ("nee_queries", ctypes.c_uint64)]
+                ("nee_queries", ctypes.c_uint64), ("graphed", ctypes.c_uint32), ("passes", ctypes.c_uint32)]
 
 
 def make_scene(width=64, height=64, spp=4, max_bounces=4, fov_deg=45.0, cam_pos=(0, 0, 4), cam_target=(0, 0, 0),
@@ -373,6 +373,7 @@ def load_library(path=None):
         "gpis_nee_submit": (c_int, [vp, P(NeeSoA), vp, c_u32, vp]),
         "gpis_nee_host": (c_int, [vp, P(NeeSoA), vp, c_u32]),
         "gpis_render": (c_int, [vp, P(SceneDesc), vp, P(RenderStats)]),
+        "gpis_render_batch": (c_int, [vp, vp, c_u32, vp, P(RenderStats)]),
         "gpis_status": (c_int, [vp, P(Counters), c_int]),
         "gpis_profile_enable": (c_int, [vp, c_int]),
         "gpis_profile_read": (c_int, [vp, P(ctypes.c_double), P(ctypes.c_uint64), c_int]),

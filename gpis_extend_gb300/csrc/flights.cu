@@ -20,6 +20,7 @@
 // are evaluated op-for-op in IEEE float without contraction, so the set of
 // impulses inside the truncated kernel is the reference's.  The splat values
 // use ex2.approx and agree with an FP64 evaluation to ~1e-6 relative.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -386,6 +387,12 @@ __device__ __forceinline__ const DevMedium *medium_of(const FlightArgs &a, uint3
     return a.media + (ok ? mi : 0u);
 }
 
+// flights of the launch: the capacity n, or the live count in device memory
+__device__ __forceinline__ uint32_t live_n(const FlightArgs &a)
+{
+    return a.n_dev ? min(*a.n_dev, a.n) : a.n;
+}
+
 __device__ __forceinline__ bool conditioned(const DevMedium &m, const FlightIn &f)
 {
     return (m.flags & MF_COND) && !(f.flags & GPIS_FLAG_FIRST_SCATTER);
@@ -725,10 +732,8 @@ __device__ __forceinline__ void skip_params(const DevMedium &m, const float d[3]
     j1 = jn * (step * dz / m.kr_iso);
 }
 
-__global__ void __launch_bounds__(128) k_prepare(FlightArgs a)
+__device__ __forceinline__ void prepare_one(const FlightArgs &a, uint32_t i)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
     bool mok;
     const DevMedium &m = *medium_of(a, i, mok);
     const FlightIn fl = load_flight(a, i);
@@ -757,6 +762,12 @@ __global__ void __launch_bounds__(128) k_prepare(FlightArgs a)
     s[1] = make_float4(vs, gsz, step, t0);
     s[2] = make_float4(lip, j0, j1, 0.0f);
     s[3] = make_float4(__uint_as_float(fl.noise_seed), __uint_as_float(flags), 0.0f, 0.0f);
+}
+
+__global__ void __launch_bounds__(128) k_prepare(FlightArgs a)
+{
+    const uint32_t n = live_n(a);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) prepare_one(a, i);
 }
 
 // ---------------------------------------------------------------------------
@@ -1618,6 +1629,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     // its truncation-jump allowance, fixed and per step
     float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
     float prop_a = -INFINITY;   // start of the proposed crossing interval (learned proposal)
+    const uint32_t n_live = live_n(a);
 
     for (;;) {
         const bool need = phase == PH_IDLE && !drained;
@@ -1629,7 +1641,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
             base = __shfl_sync(FULL, base, leader);
             if (need) {
                 const uint32_t idx = base + (uint32_t)__popc(need_mask & lt_mask);
-                if (idx >= a.n) {
+                if (idx >= n_live) {
                     drained = true;
                 } else {
                     fid = idx;
@@ -1920,10 +1932,8 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
 // ---------------------------------------------------------------------------
 // k_finish: gradient sample at the end point.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_finish(FlightArgs a)
+__device__ __forceinline__ void finish_one(const FlightArgs &a, uint32_t i)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
     float4 r0 = a.out[2 * i];
     float4 r1 = a.out[2 * i + 1];
     const uint32_t status = __float_as_uint(r1.w) & 0xFFu;
@@ -1969,6 +1979,12 @@ __global__ void __launch_bounds__(128) k_finish(FlightArgs a)
     r1.x = __fadd_rn(gs[2], mg[2]);
     a.out[2 * i] = r0;
     a.out[2 * i + 1] = r1;
+}
+
+__global__ void __launch_bounds__(128) k_finish(FlightArgs a)
+{
+    const uint32_t n = live_n(a);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) finish_one(a, i);
 }
 
 // ---------------------------------------------------------------------------
@@ -2118,10 +2134,9 @@ __device__ __forceinline__ void inv3(const float A[9], float R[9])
     R[8] = (A[0] * A[4] - A[1] * A[3]) * id;
 }
 
-__global__ void __launch_bounds__(128) k_nee(FlightArgs a, const float4 *point_t, const float4 *normal, float4 *out)
+__device__ __forceinline__ void nee_one(const FlightArgs &a, const float4 *point_t, const float4 *normal, float4 *out,
+                                        uint32_t i)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
     bool mok;
     const DevMedium &m = *medium_of(a, i, mok);
     FlightIn fl = load_flight(a, i);
@@ -2279,6 +2294,13 @@ __global__ void __launch_bounds__(128) k_nee(FlightArgs a, const float4 *point_t
     out[i] = make_float4(pdf, g[0], g[1], g[2]);
 }
 
+__global__ void __launch_bounds__(128) k_nee(FlightArgs a, const float4 *point_t, const float4 *normal, float4 *out)
+{
+    const uint32_t n = live_n(a);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        nee_one(a, point_t, normal, out, i);
+}
+
 // Corner table of a grid mean: cell c holds the 8 clamped corner voxels that
 // grid_fetch would load for any point whose trilinear cell is c.
 __global__ void k_pack_grid(DevMedium m, float4 *cells, size_t n)
@@ -2316,7 +2338,10 @@ __global__ void k_se_splat_1d(const float *q, const float *c, float *v, float *d
 cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream, cudaEvent_t *ev)
 {
     if (a.n == 0) return cudaSuccess;
-    const uint32_t blocks = (a.n + 127) / 128;
+    // one thread per flight; with a live count in device memory, grid-stride over a
+    // grid of at most 16 blocks per SM
+    uint32_t blocks = (a.n + 127) / 128;
+    if (a.n_dev) blocks = std::min<uint32_t>(blocks, (uint32_t)num_sms * 16u);
     if (ev) cudaEventRecord(ev[0], stream);
     // the stationary cooperative fast pass takes its per-flight set-up from k_prepare
     const bool coop_plain = a.one_d && a.max_imp <= 8 && a.max_oct == 1 && !a.any_ns && !a.all_grid && !a.any_mr;
@@ -2403,7 +2428,9 @@ cudaError_t launch_nee(const FlightArgs &a, const float4 *point_t, const float4 
                        cudaStream_t stream)
 {
     if (a.n == 0) return cudaSuccess;
-    k_nee<<<(a.n + 127) / 128, 128, 0, stream>>>(a, point_t, normal, out);
+    uint32_t blocks = (a.n + 127) / 128;
+    if (a.n_dev) blocks = std::min<uint32_t>(blocks, 2048u);
+    k_nee<<<blocks, 128, 0, stream>>>(a, point_t, normal, out);
     return cudaGetLastError();
 }
 

@@ -51,6 +51,8 @@ struct FlightArgs {
     int all_grid;               // all media have a grid mean
     int any_ns;                 // some medium has a nonstationary length scale
     int any_mr;                 // some medium blends multi-resolution levels
+    const uint32_t *n_dev;      // may be null: the live flight count in device memory (<= n,
+                                // which is then the capacity the grids are sized for)
     const float4 *proposal;     // may be null: per flight the proposed crossing interval
                                 // (t_a, t_b, miss probability, -); the fast pass may skip
                                 // further than its usual cap before t_a

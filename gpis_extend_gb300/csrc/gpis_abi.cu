@@ -468,10 +468,12 @@ namespace {
 // gpis_flights_submit on the scratch slice [offset, offset + n) with its own four
 // work counters, so that batches on different streams may run at the same time
 int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa *out, uint32_t n,
-                 cudaStream_t stream, size_t offset, uint32_t *work, const float *proposal = nullptr)
+                 cudaStream_t stream, size_t offset, uint32_t *work, const float *proposal = nullptr,
+                 const uint32_t *n_dev = nullptr)
 {
     gpis::FlightArgs a = {};
     a.proposal = reinterpret_cast<const float4 *>(proposal);
+    a.n_dev = n_dev;
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
     a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
     a.seeds = reinterpret_cast<const uint4 *>(in->seeds);
@@ -551,6 +553,59 @@ int gpis_flights_submit_proposed(gpis_ctx *ctx, const gpis_flight_soa *in, const
     int rc = ensure_scratch(ctx, n);
     if (rc) return rc;
     return submit_slice(ctx, in, out, n, static_cast<cudaStream_t>(cuda_stream), 0, ctx->d_work, intervals);
+}
+
+// Flight and NEE batches whose live count sits in device memory (n_dev <= cap), for
+// callers that capture whole rounds in a CUDA graph (the path tracer).
+__attribute__((visibility("hidden"))) int gpis_internal_submit_live(gpis_ctx *ctx, const gpis_flight_soa *in,
+                                                                    const gpis_result_soa *out, uint32_t cap,
+                                                                    const uint32_t *n_dev, void *cuda_stream)
+{
+    if (!ctx || !in || !out || !n_dev) return fail(GPIS_EINVAL, "null argument");
+    if (cap == 0) return GPIS_OK;
+    int rc = ensure_scratch(ctx, cap);
+    if (rc) return rc;
+    return submit_slice(ctx, in, out, cap, static_cast<cudaStream_t>(cuda_stream), 0, ctx->d_work, nullptr, n_dev);
+}
+
+__attribute__((visibility("hidden"))) int gpis_internal_nee_live(gpis_ctx *ctx, const gpis_nee_soa *in, float *out,
+                                                                 uint32_t cap, const uint32_t *n_dev,
+                                                                 void *cuda_stream)
+{
+    if (!ctx || !in || !out || !n_dev) return fail(GPIS_EINVAL, "null argument");
+    if (cap == 0) return GPIS_OK;
+    const gpis_flight_soa &f = in->flight;
+    gpis::FlightArgs a = {};
+    a.origin_near = reinterpret_cast<const float4 *>(f.origin_near);
+    a.dir_far = reinterpret_cast<const float4 *>(f.dir_far);
+    a.seeds = reinterpret_cast<const uint4 *>(f.seeds);
+    a.prev = reinterpret_cast<const float4 *>(f.prev);
+    a.medium = f.medium;
+    a.media = ctx->d_media;
+    a.n_media = ctx->n_media;
+    a.n = cap;
+    a.n_dev = n_dev;
+    CUDA_TRY(gpis::launch_nee(a, reinterpret_cast<const float4 *>(in->point_t),
+                              reinterpret_cast<const float4 *>(in->normal), reinterpret_cast<float4 *>(out),
+                              static_cast<cudaStream_t>(cuda_stream)),
+             "launch NEE");
+    return GPIS_OK;
+}
+
+// SM count, whether per-kernel profiling is on, and whether a flight batch runs the
+// prepare kernel (conditioning media, or the stationary cooperative fast pass's set-up)
+__attribute__((visibility("hidden"))) int gpis_internal_ctx_info(gpis_ctx *ctx, int *num_sms, int *profiling,
+                                                                 int *prepare_runs)
+{
+    if (!ctx) return GPIS_EINVAL;
+    if (num_sms) *num_sms = ctx->num_sms;
+    if (profiling) *profiling = ctx->profiling ? 1 : 0;
+    if (prepare_runs) {
+        const bool coop_plain = ctx->all_one_d && ctx->max_imp <= 8 && ctx->max_oct == 1 && !ctx->any_ns &&
+                                !ctx->all_grid && !ctx->any_mr;
+        *prepare_runs = (ctx->any_cond || coop_plain) ? 1 : 0;
+    }
+    return GPIS_OK;
 }
 
 int gpis_proposal_features(gpis_ctx *ctx, const gpis_flight_soa *in, float *features, uint32_t n, void *cuda_stream)

@@ -72,8 +72,18 @@ struct RtScene {
     float ln[3];
     float area;
     float aspect;
-    uint32_t s0;                // first sample of the chunk
-    uint32_t ns;                // samples in the chunk
+    RtMedium M;                 // the scene's medium
+    uint32_t medium;            // its index in the context
+    uint32_t acc_off;           // first pixel of the scene in the image accumulator
+    uint32_t n_pixels;
+    uint32_t pad_;
+};
+
+// a run of samples of one scene inside a pass: paths [start, start + n_pixels * ns)
+// hold samples s0 .. s0 + ns - 1 of every pixel (pixel-major); pixels
+// [pix_start, pix_start + n_pixels) of the pass's pixel range
+struct Seg {
+    uint32_t start, scene, s0, ns, pix_start, pad_[3];
 };
 
 __device__ __forceinline__ uint64_t mix64(uint64_t z)
@@ -251,6 +261,7 @@ struct Queue {
     float4 *rec;                // 2 per flight
     uint32_t *path;             // path index of each flight
     float4 *payload;            // shadow queues: contribution (rgb) and slot
+    uint32_t *medium;           // medium index of each flight
     uint32_t *count;
 };
 
@@ -264,13 +275,15 @@ struct NeeQueue {
     float4 *point_t, *normal, *out;
     float4 *a, *b, *c;
     uint32_t *path;
+    uint32_t *medium;
     uint32_t *count;
 };
 
 __device__ void push_flight(const Queue &q, uint32_t slot, const float o[3], const float d[3], float far_t,
                             uint32_t noise_seed, uint32_t normal_seed, uint32_t flags, float jitter, float pv,
-                            const float pg[3])
+                            const float pg[3], uint32_t medium)
 {
+    q.medium[slot] = medium;
     q.origin_near[slot] = make_float4(o[0], o[1], o[2], 0.0f);
     q.dir_far[slot] = make_float4(d[0], d[1], d[2], far_t);
     q.seeds[slot] = make_uint4(noise_seed, normal_seed, flags, __float_as_uint(jitter));
@@ -287,12 +300,28 @@ __device__ void flight_seeds(const RtMedium &M, uint32_t px, uint32_t py, uint32
     nm = xx4(px, py, s, w) + sc + 1u;
 }
 
-__global__ void k_rt_camera(RtScene S, PathRec *paths, uint32_t n)
+// the segment holding path i: the last one starting at or before i
+__device__ __forceinline__ int find_seg(const Seg *segs, int n_segs, uint32_t i, bool by_pixel)
+{
+    int lo = 0, hi = n_segs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const uint32_t st = by_pixel ? segs[mid].pix_start : segs[mid].start;
+        if (st <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_rt_camera(const RtScene *scenes, const Seg *segs, int n_segs, PathRec *paths, uint32_t n)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const Seg &g = segs[find_seg(segs, n_segs, i, false)];
+    const RtScene &S = scenes[g.scene];
     const gpis_scene_desc &sc = S.sc;
-    const uint32_t pixel = i / S.ns, s = S.s0 + i % S.ns;
+    const uint32_t j = i - g.start;
+    const uint32_t pixel = j / g.ns, s = g.s0 + j % g.ns;
     const uint32_t px = pixel % sc.width, py = pixel / sc.width;
     const uint64_t path = ((uint64_t)py * sc.width + px) * sc.spp + s;
     const float u0 = rng(sc.sampler_seed, path, kCameraBounce, D_PIX);
@@ -315,19 +344,19 @@ __global__ void k_rt_camera(RtScene S, PathRec *paths, uint32_t n)
     r.sample = s;
     r.st_bounce = 0;
     r.gp_id = 0;
-    r.pad[0] = r.pad[1] = 0u;
+    r.pad[0] = g.scene;
+    r.pad[1] = 0u;
     paths[i] = r;
 }
 
 // Outside the cube: reach the light, the cube or nothing.  Inside: queue the
 // sampleDistance flight to the cube's exit.
-__global__ void k_rt_advance(RtScene S, RtMedium M, PathRec *paths, uint32_t n, Queue q,
-                             unsigned long long *counters)
+__device__ void advance_one(const RtScene *scenes, PathRec *paths, uint32_t i, Queue q, unsigned long long *counters)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     PathRec r = paths[i];
     if (!(r.flags & PF_ALIVE)) return;
+    const RtScene &S = scenes[r.pad[0]];
+    const RtMedium &M = S.M;
     const gpis_scene_desc &sc = S.sc;
     if (r.bounce >= sc.max_bounces) {
         r.flags &= ~PF_ALIVE;
@@ -384,9 +413,18 @@ __global__ void k_rt_advance(RtScene S, RtMedium M, PathRec *paths, uint32_t n, 
     const float zero[3] = {0.0f, 0.0f, 0.0f};
     const uint32_t slot = atomicAdd(q.count, 1u);
     push_flight(q, slot, r.pos, r.dir, t1, ns, nm, first ? GPIS_FLAG_FIRST_SCATTER : 0u,
-                rng(sc.sampler_seed, path, r.bounce, D_JIT), first ? 0.0f : r.last_val, first ? zero : r.last_aniso);
+                rng(sc.sampler_seed, path, r.bounce, D_JIT), first ? 0.0f : r.last_val, first ? zero : r.last_aniso,
+                S.medium);
     q.path[slot] = i;
     paths[i] = r;
+}
+
+__global__ void k_rt_advance(const RtScene *scenes, PathRec *paths, const uint32_t *n_paths, Queue q,
+                             unsigned long long *counters)
+{
+    const uint32_t n = *n_paths;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        advance_one(scenes, paths, i, q, counters);
 }
 
 // queue a direct-lighting transmittance flight from p along d on the medium
@@ -406,7 +444,7 @@ __device__ void push_shadow(const RtScene &S, const RtMedium &M, const Queue &q,
     uint32_t ns, nm;
     flight_seeds(M, px, py, r.sample, seg, ns, nm);
     const uint32_t slot = atomicAdd(q.count, 1u);
-    push_flight(q, slot, p, d, t1, ns, nm, GPIS_FLAG_SHADOW, jitter, pv, pg);
+    push_flight(q, slot, p, d, t1, ns, nm, GPIS_FLAG_SHADOW, jitter, pv, pg, S.medium);
     q.path[slot] = pi;
     q.payload[slot] = make_float4(contrib[0], contrib[1], contrib[2], __uint_as_float(slot_kind));
 }
@@ -420,6 +458,7 @@ __device__ void push_nee(const NeeQueue &nq, const Queue &q, uint32_t k, uint32_
     nq.dir_far[slot] = q.dir_far[k];
     nq.seeds[slot] = q.seeds[k];
     nq.prev[slot] = q.prev[k];
+    nq.medium[slot] = q.medium[k];
     nq.point_t[slot] = make_float4(p[0], p[1], p[2], t);
     nq.normal[slot] = make_float4(nrm[0], nrm[1], nrm[2], 0.0f);
     nq.a[slot] = make_float4(T[0], T[1], T[2], pdf_l);
@@ -430,13 +469,13 @@ __device__ void push_nee(const NeeQueue &nq, const Queue &q, uint32_t k, uint32_
 
 // GaussianProcessMedium::sampleDistance after the flight (GaussianProcessMedium.cpp:
 // 289-381), then handleVolume (TraceBase.cpp:993-1048) for GP events.
-__global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint32_t nq, Queue sq, NeeQueue eq,
-                           float *direct, unsigned long long *counters)
+__device__ void event_one(const RtScene *scenes, PathRec *paths, Queue q, uint32_t k, Queue sq, NeeQueue eq,
+                          float *direct, unsigned long long *counters)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nq) return;
     const uint32_t pi = q.path[k];
     PathRec r = paths[pi];
+    const RtScene &S = scenes[r.pad[0]];
+    const RtMedium &M = S.M;
     const gpis_scene_desc &sc = S.sc;
     const float4 r0 = q.rec[2 * k], r1 = q.rec[2 * k + 1];
     const uint32_t status = __float_as_uint(r1.w);
@@ -623,17 +662,25 @@ __global__ void k_rt_event(RtScene S, RtMedium M, PathRec *paths, Queue q, uint3
     paths[pi] = r;
 }
 
+__global__ void k_rt_event(const RtScene *scenes, PathRec *paths, Queue q, const uint32_t *counts, Queue sq,
+                           NeeQueue eq, float *direct, unsigned long long *counters)
+{
+    const uint32_t n = counts[0];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        event_one(scenes, paths, q, k, sq, eq, direct, counters);
+}
+
 // after the NEE queries of specular events: the light sample's BSDF value
 // albedo * F * neePDF and its transmittance flight conditioned on neeGrad
 // (volumeLightSample with MirrorBsdf::eval / evalGrad), or the MIS weight of the
 // phase sample against neePDF (MirrorBsdf::sample's pdf)
-__global__ void k_rt_nee(RtScene S, RtMedium M, const PathRec *paths, NeeQueue eq, uint32_t n, Queue sq,
-                         float *direct)
+__device__ void nee_shade_one(const RtScene *scenes, const PathRec *paths, NeeQueue eq, uint32_t k, Queue sq,
+                              float *direct)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
     const uint32_t pi = eq.path[k];
     const PathRec &r = paths[pi];
+    const RtScene &S = scenes[r.pad[0]];
+    const RtMedium &M = S.M;
     const gpis_scene_desc &sc = S.sc;
     const float4 o = eq.out[k], pa = eq.a[k], pb = eq.b[k], pc = eq.c[k], pt = eq.point_t[k];
     const uint32_t bk = __float_as_uint(pc.w), b = bk & 0x7FFFFFFFu, kind = bk >> 31;
@@ -662,11 +709,17 @@ __global__ void k_rt_nee(RtScene S, RtMedium M, const PathRec *paths, NeeQueue e
     }
 }
 
-// a transmittance of 1 lets the queued contribution through
-__global__ void k_rt_shadow(Queue sq, uint32_t nq, float *direct)
+__global__ void k_rt_nee(const RtScene *scenes, const PathRec *paths, NeeQueue eq, const uint32_t *counts, Queue sq,
+                         float *direct)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nq) return;
+    const uint32_t n = counts[2];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        nee_shade_one(scenes, paths, eq, k, sq, direct);
+}
+
+// a transmittance of 1 lets the queued contribution through
+__device__ void shadow_one(Queue sq, uint32_t k, float *direct)
+{
     const float4 pl = sq.payload[k];
     const uint32_t kind = __float_as_uint(pl.w);
     const float4 r1 = sq.rec[2 * k + 1];
@@ -677,35 +730,66 @@ __global__ void k_rt_shadow(Queue sq, uint32_t nq, float *direct)
     }
 }
 
+__global__ void k_rt_shadow(Queue sq, const uint32_t *counts, float *direct)
+{
+    const uint32_t n = counts[1];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        shadow_one(sq, k, direct);
+}
+
 // L += light sample, then L += phase sample, in the restatement's order
-__global__ void k_rt_collect(PathRec *paths, const uint32_t *qpath, uint32_t nq, float *direct)
+__global__ void k_rt_collect(PathRec *paths, const uint32_t *qpath, const uint32_t *counts, float *direct)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nq) return;
-    const uint32_t pi = qpath[k];
-    float *d = direct + 6 * (size_t)pi;
-    PathRec &r = paths[pi];
-    for (int c = 0; c < 3; ++c) r.L[c] = r.L[c] + d[c];
-    for (int c = 0; c < 3; ++c) r.L[c] = r.L[c] + d[3 + c];
-}
-
-__global__ void k_rt_accumulate(const PathRec *paths, uint32_t n_pixels, uint32_t ns, float *acc)
-{
-    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
-    if (px >= n_pixels) return;
-    float a[3] = {acc[3 * px], acc[3 * px + 1], acc[3 * px + 2]};
-    for (uint32_t s = 0; s < ns; ++s) {
-        const PathRec &r = paths[(size_t)px * ns + s];
-        for (int c = 0; c < 3; ++c) a[c] = a[c] + r.L[c];
+    const uint32_t n = counts[0];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t pi = qpath[k];
+        float *d = direct + 6 * (size_t)pi;
+        PathRec &r = paths[pi];
+        for (int c = 0; c < 3; ++c) r.L[c] = r.L[c] + d[c];
+        for (int c = 0; c < 3; ++c) r.L[c] = r.L[c] + d[3 + c];
     }
-    acc[3 * px] = a[0]; acc[3 * px + 1] = a[1]; acc[3 * px + 2] = a[2];
 }
 
-__global__ void k_rt_finish(float *acc, uint32_t n_pixels, uint32_t spp)
+// the round's queue lengths into the render's flight counters
+__global__ void k_rt_tally(const uint32_t *counts, unsigned long long *counters)
 {
-    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
-    if (px >= n_pixels) return;
-    for (int c = 0; c < 3; ++c) acc[3 * px + c] = acc[3 * px + c] / (float)spp;
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        counters[2] += counts[0];
+        counters[3] += counts[1];
+        counters[4] += counts[2];
+    }
+}
+
+// pixel t of the pass: add its ns samples (in sample order) to the scene's accumulator
+__global__ void k_rt_accumulate(const RtScene *scenes, const Seg *segs, int n_segs, const PathRec *paths,
+                                uint32_t n_pix, float *acc)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_pix) return;
+    const Seg &g = segs[find_seg(segs, n_segs, t, true)];
+    const uint32_t px = t - g.pix_start;
+    float *a = acc + 3 * ((size_t)scenes[g.scene].acc_off + px);
+    float v[3] = {a[0], a[1], a[2]};
+    for (uint32_t s = 0; s < g.ns; ++s) {
+        const PathRec &r = paths[g.start + (size_t)px * g.ns + s];
+        for (int c = 0; c < 3; ++c) v[c] = v[c] + r.L[c];
+    }
+    a[0] = v[0]; a[1] = v[1]; a[2] = v[2];
+}
+
+// the mean over each scene's spp
+__global__ void k_rt_finish(const RtScene *scenes, int n_scenes, float *acc, uint32_t total_pixels)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total_pixels) return;
+    int lo = 0, hi = n_scenes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (scenes[mid].acc_off <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const float spp = (float)scenes[lo].sc.spp;
+    for (int c = 0; c < 3; ++c) acc[3 * (size_t)t + c] = acc[3 * (size_t)t + c] / spp;
 }
 
 inline void hnorm(float v[3])
@@ -753,15 +837,24 @@ int cuda_fail(cudaError_t e, const char *what)
         if (e_ != cudaSuccess) return cuda_fail(e_, what); \
     } while (0)
 
-extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *image_rgb, gpis_render_stats *stats)
+extern "C" int gpis_internal_submit_live(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa *out,
+                                         uint32_t cap, const uint32_t *n_dev, void *cuda_stream);
+extern "C" int gpis_internal_nee_live(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t cap,
+                                      const uint32_t *n_dev, void *cuda_stream);
+extern "C" int gpis_internal_ctx_info(gpis_ctx *ctx, int *num_sms, int *profiling, int *prepare_runs);
+
+namespace {
+
+// scene and medium constants of one scene (host)
+int make_scene(gpis_ctx *ctx, const gpis_scene_desc &sc, RtScene &S, bool &specular_nee)
 {
-    if (!ctx || !scene || !image_rgb) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
-    const gpis_scene_desc &sc = *scene;
     if (sc.width == 0 || sc.height == 0 || sc.spp == 0 || sc.max_bounces == 0)
         return gpis_internal_set_error(GPIS_EINVAL, "width, height, spp and max_bounces must be > 0");
     if (sc.phase > GPIS_PHASE_CONDUCTOR) return gpis_internal_set_error(GPIS_EINVAL, "unknown phase");
     if (!(sc.box_half > 0.0f) || !(sc.tan_half_fov > 0.0f))
         return gpis_internal_set_error(GPIS_EINVAL, "box_half and tan_half_fov must be > 0");
+    if ((uint64_t)sc.width * sc.height > (1ull << 28))
+        return gpis_internal_set_error(GPIS_ERANGE, "image too large");
     const gpis_medium_desc *md = gpis_internal_ctx_medium(ctx, sc.medium);
     if (!md) return gpis_internal_set_error(GPIS_EINVAL, "unknown medium index");
     const float sa = md->sigma_a * md->density, ss = md->sigma_s * md->density;
@@ -769,8 +862,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     if (sc.phase != GPIS_PHASE_LAMBERT && md->sampling_scheme != GPIS_SCHEME_UNI && md->one_d_sampling &&
         md->n_octaves > 1)
         return gpis_internal_set_error(GPIS_ENOTSUP, "1D NEE and MIS need a single-octave medium");
-
-    RtMedium M;
+    RtMedium &M = S.M;
     M.ratio = ss / (sa + ss);
     M.max_bounces = md->max_bounces;
     M.seed = md->seed;
@@ -781,9 +873,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     M.scheme_uni = md->single_realization || !md->one_d_sampling || md->sigma < 1e-6f;
     M.xy_renewal_plus = md->correlation_xy && !md->single_realization &&
                         md->correlation_context == GPIS_CTX_RENEWAL_PLUS && md->ls_kind == GPIS_LS_CONSTANT;
-    const bool specular_nee = sc.phase != GPIS_PHASE_LAMBERT && !M.scheme_uni && M.scheme != GPIS_SCHEME_UNI;
-
-    RtScene S;
+    specular_nee = sc.phase != GPIS_PHASE_LAMBERT && !M.scheme_uni && M.scheme != GPIS_SCHEME_UNI;
     S.sc = sc;
     for (int i = 0; i < 3; ++i) S.fwd[i] = sc.cam_target[i] - sc.cam_pos[i];
     hnorm(S.fwd);
@@ -792,34 +882,106 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     hcross(S.right, S.fwd, S.up);
     hcross(sc.light_u, sc.light_v, S.ln);
     {
-        float s = S.ln[0] * S.ln[0];
-        s = s + S.ln[1] * S.ln[1];
-        s = s + S.ln[2] * S.ln[2];
-        S.area = std::sqrt(s);
+        float v = S.ln[0] * S.ln[0];
+        v = v + S.ln[1] * S.ln[1];
+        v = v + S.ln[2] * S.ln[2];
+        S.area = std::sqrt(v);
     }
     hnorm(S.ln);
     S.aspect = (float)sc.width / (float)sc.height;
+    S.medium = sc.medium;
+    S.n_pixels = sc.width * sc.height;
+    S.pad_ = 0;
+    return GPIS_OK;
+}
 
-    const uint32_t n_pixels = sc.width * sc.height;
+}  // namespace
+
+// Render a batch of scenes in one wavefront: the paths of all scenes share the
+// flight batches of every round (the flight kernels take each flight's medium),
+// so many small images fill the GPU together.  A pass holds up to 2^22 paths
+// (runs of samples of one or several scenes); each pass runs rounds of the
+// bounce loop until every path has ended, with the queue lengths in device
+// memory, so a round needs no host synchronization and is replayed from one
+// captured CUDA graph (launched directly while the context profiles its kernels).
+extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, uint32_t n_scenes, float *const *images,
+                                 gpis_render_stats *stats)
+{
+    if (!ctx || !scenes || !images || n_scenes == 0) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    std::vector<RtScene> hs(n_scenes);
+    bool any_nee = false;
+    uint32_t max_bounces = 0;
+    uint64_t total_pixels = 0, total_paths = 0;
+    for (uint32_t k = 0; k < n_scenes; ++k) {
+        if (!images[k]) return gpis_internal_set_error(GPIS_EINVAL, "null image");
+        bool nee = false;
+        int rc = make_scene(ctx, scenes[k], hs[k], nee);
+        if (rc) return rc;
+        any_nee = any_nee || nee;
+        max_bounces = std::max(max_bounces, scenes[k].max_bounces);
+        hs[k].acc_off = (uint32_t)total_pixels;
+        total_pixels += hs[k].n_pixels;
+        total_paths += (uint64_t)hs[k].n_pixels * scenes[k].spp;
+        if (total_pixels > 0xFFFFFFFFull) return gpis_internal_set_error(GPIS_ERANGE, "images too large");
+    }
+    // passes: runs of samples, up to `target` paths each (one sample of an image
+    // larger than that makes a pass of its own)
     const uint32_t target = 1u << 22;
-    const uint32_t ns_chunk = std::max(1u, std::min(sc.spp, target / std::max(1u, n_pixels)));
-    const size_t cap = (size_t)n_pixels * ns_chunk;
-    if (cap > 0xFFFFFFFFull) return gpis_internal_set_error(GPIS_ERANGE, "image too large");
+    std::vector<std::vector<Seg>> passes(1);
+    std::vector<uint32_t> pass_n(1, 0), pass_pix(1, 0);
+    for (uint32_t k = 0; k < n_scenes; ++k) {
+        const uint32_t np = hs[k].n_pixels;
+        uint32_t left = scenes[k].spp, s0 = 0;
+        while (left > 0) {
+            uint32_t room = target > pass_n.back() ? target - pass_n.back() : 0;
+            if (room < np && pass_n.back() > 0) {
+                passes.emplace_back();
+                pass_n.push_back(0);
+                pass_pix.push_back(0);
+                room = target;
+            }
+            const uint32_t ns = std::max(1u, std::min(left, room / std::max(1u, np)));
+            Seg g;
+            g.start = pass_n.back();
+            g.scene = k;
+            g.s0 = s0;
+            g.ns = ns;
+            g.pix_start = pass_pix.back();
+            g.pad_[0] = g.pad_[1] = g.pad_[2] = 0;
+            passes.back().push_back(g);
+            pass_n.back() += np * ns;
+            pass_pix.back() += np;
+            s0 += ns;
+            left -= ns;
+        }
+    }
+    uint32_t cap = 0, max_segs = 0;
+    for (size_t p = 0; p < passes.size(); ++p) {
+        cap = std::max(cap, pass_n[p]);
+        max_segs = std::max<uint32_t>(max_segs, (uint32_t)passes[p].size());
+    }
+    int num_sms = 1, profiling = 0, prepare_runs = 1;
+    gpis_internal_ctx_info(ctx, &num_sms, &profiling, &prepare_runs);
 
     DevBuf mem;
+    RtScene *d_scenes;
+    Seg *d_segs;
     PathRec *paths;
     float *direct, *acc;
-    Queue q, sq;
+    Queue q{}, sq{};
     NeeQueue eq{};
-    uint32_t *counts;
+    uint32_t *counts, *n_paths;
     unsigned long long *dcnt;
+    RT_TRY(mem.alloc(d_scenes, n_scenes), "allocate scenes");
+    RT_TRY(mem.alloc(d_segs, max_segs), "allocate segments");
     RT_TRY(mem.alloc(paths, cap), "allocate paths");
-    RT_TRY(mem.alloc(direct, cap * 6), "allocate direct light");
-    RT_TRY(mem.alloc(acc, (size_t)n_pixels * 3), "allocate image");
+    RT_TRY(mem.alloc(direct, (size_t)cap * 6), "allocate direct light");
+    RT_TRY(mem.alloc(acc, (size_t)total_pixels * 3), "allocate images");
     RT_TRY(mem.alloc(counts, 3), "allocate queue counters");
-    RT_TRY(mem.alloc(dcnt, 2), "allocate counters");
+    RT_TRY(mem.alloc(n_paths, 1), "allocate path count");
+    RT_TRY(mem.alloc(dcnt, 5), "allocate counters");
     for (Queue *qq : {&q, &sq}) {
-        const size_t m = qq == &q ? cap : 2 * cap;
+        const size_t m = qq == &q ? cap : 2 * (size_t)cap;
         RT_TRY(mem.alloc(qq->origin_near, m), "allocate queue");
         RT_TRY(mem.alloc(qq->dir_far, m), "allocate queue");
         RT_TRY(mem.alloc(qq->prev, m), "allocate queue");
@@ -827,13 +989,14 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
         RT_TRY(mem.alloc(qq->rec, 2 * m), "allocate queue");
         RT_TRY(mem.alloc(qq->path, m), "allocate queue");
         RT_TRY(mem.alloc(qq->payload, m), "allocate queue");
+        RT_TRY(mem.alloc(qq->medium, m), "allocate queue");
     }
     q.count = counts;
     sq.count = counts + 1;
     eq.count = counts + 2;
-    if (specular_nee) {
+    if (any_nee) {
         // at most two queries per event: the light sample and the MIS phase sample
-        const size_t m = 2 * cap;
+        const size_t m = 2 * (size_t)cap;
         RT_TRY(mem.alloc(eq.origin_near, m), "allocate NEE queue");
         RT_TRY(mem.alloc(eq.dir_far, m), "allocate NEE queue");
         RT_TRY(mem.alloc(eq.prev, m), "allocate NEE queue");
@@ -845,12 +1008,7 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
         RT_TRY(mem.alloc(eq.b, m), "allocate NEE queue");
         RT_TRY(mem.alloc(eq.c, m), "allocate NEE queue");
         RT_TRY(mem.alloc(eq.path, m), "allocate NEE queue");
-    }
-    uint32_t *dmedium = nullptr;
-    if (sc.medium != 0) {
-        RT_TRY(mem.alloc(dmedium, 2 * cap), "allocate medium stream");
-        std::vector<uint32_t> h(2 * cap, sc.medium);
-        RT_TRY(cudaMemcpy(dmedium, h.data(), h.size() * 4, cudaMemcpyHostToDevice), "upload medium stream");
+        RT_TRY(mem.alloc(eq.medium, m), "allocate NEE queue");
     }
     cudaStream_t st;
     RT_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "create stream");
@@ -859,101 +1017,137 @@ extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *i
     RT_TRY(cudaEventCreate(&e0), "create event");
     RT_TRY(cudaEventCreate(&e1), "create event");
     struct EventGuard { cudaEvent_t a, b; ~EventGuard() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{e0, e1};
-    RT_TRY(cudaMemsetAsync(acc, 0, (size_t)n_pixels * 3 * sizeof(float), st), "clear image");
-    RT_TRY(cudaMemsetAsync(dcnt, 0, 2 * sizeof(unsigned long long), st), "clear counters");
-    RT_TRY(cudaEventRecord(e0, st), "record event");
+    RT_TRY(cudaMemcpyAsync(d_scenes, hs.data(), hs.size() * sizeof(RtScene), cudaMemcpyHostToDevice, st),
+           "upload scenes");
+    RT_TRY(cudaMemsetAsync(acc, 0, (size_t)total_pixels * 3 * sizeof(float), st), "clear images");
+    RT_TRY(cudaMemsetAsync(dcnt, 0, 5 * sizeof(unsigned long long), st), "clear counters");
+    RT_TRY(cudaMemsetAsync(counts, 0, 3 * sizeof(uint32_t), st), "clear queue counters");
 
-    uint64_t n_dist = 0, n_shadow = 0, n_paths = 0, n_launch = 0, n_nee = 0;
-    // a flight batch is 4 kernels (prepare, fast pass, resume pass, finish), 3 without conditioning
-    const bool conditions = !md->single_realization && (md->correlation_context == GPIS_CTX_RENEWAL ||
-                                                         md->correlation_context == GPIS_CTX_RENEWAL_PLUS);
-    const uint64_t per_batch = conditions ? 4 : 3;
-    const unsigned tb = 128;
-    for (uint32_t s0 = 0; s0 < sc.spp; s0 += ns_chunk) {
-        const uint32_t ns = std::min(ns_chunk, sc.spp - s0);
-        const uint32_t n = n_pixels * ns;
-        S.s0 = s0;
-        S.ns = ns;
-        n_paths += n;
-        k_rt_camera<<<(n + tb - 1) / tb, tb, 0, st>>>(S, paths, n);
-        n_launch += 1;
-        // at most two rounds per bounce (a forward crossing, then an event), plus entry and exit
-        for (uint32_t round = 0; round < 2 * sc.max_bounces + 4; ++round) {
-            RT_TRY(cudaMemsetAsync(counts, 0, 3 * sizeof(uint32_t), st), "clear queue counters");
-            k_rt_advance<<<(n + tb - 1) / tb, tb, 0, st>>>(S, M, paths, n, q, dcnt);
-            n_launch += 1;
-            uint32_t nq = 0;
-            RT_TRY(cudaMemcpyAsync(&nq, counts, 4, cudaMemcpyDeviceToHost, st), "read queue");
-            RT_TRY(cudaStreamSynchronize(st), "synchronize");
-            if (nq == 0) {
-                // paths outside the cube were finished by k_rt_advance; none is left inside
-                break;
-            }
-            gpis_flight_soa fin{reinterpret_cast<float *>(q.origin_near), reinterpret_cast<float *>(q.dir_far),
-                                reinterpret_cast<uint32_t *>(q.seeds), reinterpret_cast<float *>(q.prev), dmedium};
-            gpis_result_soa fout{reinterpret_cast<float *>(q.rec)};
-            int rc = gpis_flights_submit(ctx, &fin, &fout, nq, st);
-            if (rc) return rc;
-            n_dist += nq;
-            k_rt_event<<<(nq + tb - 1) / tb, tb, 0, st>>>(S, M, paths, q, nq, sq, eq, direct, dcnt);
-            n_launch += per_batch + 1;
-            uint32_t qc[2] = {0, 0};
-            RT_TRY(cudaMemcpyAsync(qc, counts + 1, 8, cudaMemcpyDeviceToHost, st), "read shadow queue");
-            RT_TRY(cudaStreamSynchronize(st), "synchronize");
-            uint32_t nsq = qc[0];
-            if (qc[1]) {
-                // the NEE queries of specular events, then their shadow flights
-                gpis_nee_soa nin;
-                nin.flight = gpis_flight_soa{reinterpret_cast<float *>(eq.origin_near),
-                                             reinterpret_cast<float *>(eq.dir_far),
-                                             reinterpret_cast<uint32_t *>(eq.seeds), reinterpret_cast<float *>(eq.prev),
-                                             dmedium};
-                nin.point_t = reinterpret_cast<const float *>(eq.point_t);
-                nin.normal = reinterpret_cast<const float *>(eq.normal);
-                rc = gpis_nee_submit(ctx, &nin, reinterpret_cast<float *>(eq.out), qc[1], st);
-                if (rc) return rc;
-                n_nee += qc[1];
-                k_rt_nee<<<(qc[1] + tb - 1) / tb, tb, 0, st>>>(S, M, paths, eq, qc[1], sq, direct);
-                n_launch += 2;
-                RT_TRY(cudaMemcpyAsync(&nsq, counts + 1, 4, cudaMemcpyDeviceToHost, st), "read shadow queue");
-                RT_TRY(cudaStreamSynchronize(st), "synchronize");
-            }
-            if (nsq) {
-                gpis_flight_soa sin{reinterpret_cast<float *>(sq.origin_near), reinterpret_cast<float *>(sq.dir_far),
-                                    reinterpret_cast<uint32_t *>(sq.seeds), reinterpret_cast<float *>(sq.prev), dmedium};
-                gpis_result_soa sout{reinterpret_cast<float *>(sq.rec)};
-                rc = gpis_flights_submit(ctx, &sin, &sout, nsq, st);
-                if (rc) return rc;
-                n_shadow += nsq;
-                k_rt_shadow<<<(nsq + tb - 1) / tb, tb, 0, st>>>(sq, nsq, direct);
-                n_launch += per_batch + 1;
-            }
-            k_rt_collect<<<(nq + tb - 1) / tb, tb, 0, st>>>(paths, q.path, nq, direct);
-            n_launch += 1;
-        }
-        k_rt_accumulate<<<(n_pixels + tb - 1) / tb, tb, 0, st>>>(paths, n_pixels, ns, acc);
-        n_launch += 1;
+    gpis_flight_soa fin{reinterpret_cast<float *>(q.origin_near), reinterpret_cast<float *>(q.dir_far),
+                        reinterpret_cast<uint32_t *>(q.seeds), reinterpret_cast<float *>(q.prev), q.medium};
+    gpis_result_soa fout{reinterpret_cast<float *>(q.rec)};
+    gpis_flight_soa sin{reinterpret_cast<float *>(sq.origin_near), reinterpret_cast<float *>(sq.dir_far),
+                        reinterpret_cast<uint32_t *>(sq.seeds), reinterpret_cast<float *>(sq.prev), sq.medium};
+    gpis_result_soa sout{reinterpret_cast<float *>(sq.rec)};
+    gpis_nee_soa nin{};
+    if (any_nee) {
+        nin.flight = gpis_flight_soa{reinterpret_cast<float *>(eq.origin_near), reinterpret_cast<float *>(eq.dir_far),
+                                     reinterpret_cast<uint32_t *>(eq.seeds), reinterpret_cast<float *>(eq.prev),
+                                     eq.medium};
+        nin.point_t = reinterpret_cast<const float *>(eq.point_t);
+        nin.normal = reinterpret_cast<const float *>(eq.normal);
     }
-    k_rt_finish<<<(n_pixels + tb - 1) / tb, tb, 0, st>>>(acc, n_pixels, sc.spp);
+    // the flight scratch for the largest batch, allocated before any capture (the
+    // queue counters are zero here, so these launches trace nothing)
+    int rc = gpis_internal_submit_live(ctx, &sin, &sout, 2 * cap, counts + 1, st);
+    if (rc) return rc;
+    if (any_nee) {
+        rc = gpis_internal_nee_live(ctx, &nin, reinterpret_cast<float *>(eq.out), 2 * cap, counts + 2, st);
+        if (rc) return rc;
+    }
+    const unsigned tb = 128;
+    const unsigned gs = (unsigned)std::max(1, num_sms * 8);   // grid of the grid-stride kernels
+    // one round of the bounce loop; every length it needs is in device memory
+    auto round = [&]() -> int {
+        cudaError_t e = cudaMemsetAsync(counts, 0, 3 * sizeof(uint32_t), st);
+        if (e != cudaSuccess) return cuda_fail(e, "clear queue counters");
+        k_rt_advance<<<gs, tb, 0, st>>>(d_scenes, paths, n_paths, q, dcnt);
+        int r = gpis_internal_submit_live(ctx, &fin, &fout, cap, counts, st);
+        if (r) return r;
+        k_rt_event<<<gs, tb, 0, st>>>(d_scenes, paths, q, counts, sq, eq, direct, dcnt);
+        if (any_nee) {
+            r = gpis_internal_nee_live(ctx, &nin, reinterpret_cast<float *>(eq.out), 2 * cap, counts + 2, st);
+            if (r) return r;
+            k_rt_nee<<<gs, tb, 0, st>>>(d_scenes, paths, eq, counts, sq, direct);
+        }
+        r = gpis_internal_submit_live(ctx, &sin, &sout, 2 * cap, counts + 1, st);
+        if (r) return r;
+        k_rt_shadow<<<gs, tb, 0, st>>>(sq, counts, direct);
+        k_rt_collect<<<gs, tb, 0, st>>>(paths, q.path, counts, direct);
+        k_rt_tally<<<1, 32, 0, st>>>(counts, dcnt);
+        return GPIS_OK;
+    };
+    // kernels of one round: advance, event, shadow, collect, tally, and per flight batch
+    // prepare (when it runs), march, resume and finish; NEE adds its kernel and the shading
+    const uint64_t per_batch = 3 + (prepare_runs ? 1 : 0);
+    const uint64_t per_round = 5 + 2 * per_batch + (any_nee ? 2 : 0);
+    const uint32_t rounds = 2 * max_bounces + 4;
+    cudaGraphExec_t gexec = nullptr;
+    struct GraphGuard { cudaGraphExec_t g; ~GraphGuard() { if (g) cudaGraphExecDestroy(g); } } gg{nullptr};
+    bool graphed = false;
+    if (!profiling) {
+        // a capture that fails leaves the rounds to direct launches
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            rc = round();
+            const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+            if (rc == GPIS_OK && ce == cudaSuccess && graph &&
+                cudaGraphInstantiate(&gexec, graph, 0) == cudaSuccess) {
+                gg.g = gexec;
+                graphed = true;
+            } else {
+                gexec = nullptr;
+            }
+            if (graph) cudaGraphDestroy(graph);
+        }
+        (void)cudaGetLastError();
+    }
+    if (stats) stats->graphed = graphed ? 1u : 0u;
+    RT_TRY(cudaEventRecord(e0, st), "record event");
+    uint64_t n_launch = 0;
+    for (size_t p = 0; p < passes.size(); ++p) {
+        const std::vector<Seg> &segs = passes[p];
+        RT_TRY(cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(Seg), cudaMemcpyHostToDevice, st),
+               "upload segments");
+        RT_TRY(cudaMemcpyAsync(n_paths, &pass_n[p], sizeof(uint32_t), cudaMemcpyHostToDevice, st), "upload pass size");
+        k_rt_camera<<<(pass_n[p] + tb - 1) / tb, tb, 0, st>>>(d_scenes, d_segs, (int)segs.size(), paths, pass_n[p]);
+        n_launch += 1;
+        for (uint32_t k = 0; k < rounds; ++k) {
+            if (gexec) {
+                RT_TRY(cudaGraphLaunch(gexec, st), "launch the round graph");
+            } else {
+                rc = round();
+                if (rc) return rc;
+            }
+            n_launch += per_round;
+        }
+        k_rt_accumulate<<<(pass_pix[p] + tb - 1) / tb, tb, 0, st>>>(d_scenes, d_segs, (int)segs.size(), paths,
+                                                                    pass_pix[p], acc);
+        n_launch += 1;
+        // the host's segment table and pass size must outlive their asynchronous copies
+        RT_TRY(cudaStreamSynchronize(st), "synchronize pass");
+    }
+    k_rt_finish<<<(unsigned)((total_pixels + tb - 1) / tb), tb, 0, st>>>(d_scenes, (int)n_scenes, acc,
+                                                                         (uint32_t)total_pixels);
     n_launch += 1;
     RT_TRY(cudaEventRecord(e1, st), "record event");
-    RT_TRY(cudaMemcpyAsync(image_rgb, acc, (size_t)n_pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
-           "read image");
-    unsigned long long hc[2] = {0, 0};
+    for (uint32_t k = 0; k < n_scenes; ++k)
+        RT_TRY(cudaMemcpyAsync(images[k], acc + 3 * (size_t)hs[k].acc_off, (size_t)hs[k].n_pixels * 3 * sizeof(float),
+                               cudaMemcpyDeviceToHost, st),
+               "read image");
+    unsigned long long hc[5] = {0, 0, 0, 0, 0};
     RT_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st), "read counters");
     RT_TRY(cudaStreamSynchronize(st), "synchronize render");
     RT_TRY(cudaGetLastError(), "render kernels");
     if (stats) {
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
-        stats->paths = n_paths;
-        stats->distance_flights = n_dist;
-        stats->shadow_flights = n_shadow;
+        stats->paths = total_paths;
+        stats->distance_flights = hc[2];
+        stats->shadow_flights = hc[3];
         stats->medium_events = hc[0];
         stats->failed = hc[1];
         stats->ms = ms;
         stats->launches = n_launch;
-        stats->nee_queries = n_nee;
+        stats->nee_queries = hc[4];
+        stats->passes = (uint32_t)passes.size();
     }
     return GPIS_OK;
+}
+
+extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *image_rgb, gpis_render_stats *stats)
+{
+    if (!ctx || !scene || !image_rgb) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    float *const images[1] = {image_rgb};
+    return gpis_render_batch(ctx, scene, 1, images, stats);
 }

@@ -138,6 +138,15 @@ class Context:
                   "gpis_render")
         return img, {k: getattr(st, k) for k, _ in abi.RenderStats._fields_}
 
+    def render_batch(self, scenes):
+        """gpis_render_batch: returns (list of images (h, w, 3) float32, stats dict)."""
+        imgs = [np.zeros((sc.height, sc.width, 3), np.float32) for sc in scenes]
+        arr = (abi.SceneDesc * len(scenes))(*scenes)
+        ptrs = (ctypes.c_void_p * len(scenes))(*[im.ctypes.data for im in imgs])
+        st = abi.RenderStats()
+        abi.check(self.lib.gpis_render_batch(self.h, arr, len(scenes), ptrs, ctypes.byref(st)), "gpis_render_batch")
+        return imgs, {k: getattr(st, k) for k, _ in abi.RenderStats._fields_}
+
     def trace_pinned(self, pinned):
         """gpis_flights_trace_host on PinnedFlights (host -> device -> host, synchronous)."""
         soa = pinned.soa()

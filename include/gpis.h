@@ -418,11 +418,20 @@ typedef struct {
     double ms;                  /* device time of the render (CUDA events)        */
     uint64_t launches;          /* kernels launched by the render                 */
     uint64_t nee_queries;       /* neePDF / neeGrad queries of specular events    */
+    uint32_t graphed;           /* 1: the bounce loop ran as a captured CUDA graph */
+    uint32_t passes;            /* passes of up to 2^22 paths                     */
 } gpis_render_stats;
 
 /* Render into image_rgb (host, height x width x 3 floats, row 0 at the top):
  * the mean radiance of spp paths per pixel.  Blocking.                       */
 int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *image_rgb, gpis_render_stats *stats);
+/* Render n_scenes scenes (each with its own medium of the context, image size,
+ * spp and bounces) in one wavefront: their paths share every flight batch.
+ * images[k] as image_rgb of scene k; each image equals its own gpis_render.
+ * The bounce loop keeps its queue lengths on the device and runs as one
+ * captured CUDA graph per round (direct launches while the context profiles). */
+int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, uint32_t n_scenes, float *const *images,
+                      gpis_render_stats *stats);
 
 /* ---- learned crossing proposal -------------------------------------------
  * A GRU (hidden 32) over eight samples of the mean SDF and its slope along the

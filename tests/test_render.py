@@ -111,3 +111,56 @@ def test_gpu_render_nee_needs_one_octave():
     with runtime.Context(desc) as ctx:
         with pytest.raises(abi.GpisError):
             ctx.render(workloads.render_scene(width=4, height=4, spp=1, phase="mirror"))
+
+
+def batch_scenes():
+    """Three scenes over two media of one context: different sizes, spp, bounces and phases."""
+    media = [workloads.render_medium("sphere_1d_nee"), workloads.render_medium("torus")]
+    scenes = [workloads.render_scene(width=24, height=16, spp=3, max_bounces=3, phase="mirror", medium=0),
+              workloads.render_scene(width=16, height=16, spp=5, max_bounces=4, medium=1, box_half=2.0),
+              workloads.render_scene(width=8, height=12, spp=2, max_bounces=2, phase="conductor", medium=0,
+                                     sampler_seed=99)]
+    return media, scenes
+
+
+@pytest.mark.gpu
+def test_gpu_render_batch_equals_single_renders():
+    """One wavefront over several scenes gives each scene's own image bit for bit
+    (flights are independent), with the flight counts summed."""
+    from gpis_extend_gb300 import runtime
+    media, scenes = batch_scenes()
+    with runtime.Context(media) as ctx:
+        imgs, st = ctx.render_batch(scenes)
+        singles = [ctx.render(sc) for sc in scenes]
+    for img, (one, _) in zip(imgs, singles):
+        assert np.array_equal(img, one)
+    for k in ("paths", "distance_flights", "shadow_flights", "medium_events", "failed", "nee_queries"):
+        assert st[k] == sum(s[k] for _, s in singles), k
+    assert st["graphed"] == 1
+
+
+@pytest.mark.gpu
+def test_gpu_render_graph_equals_direct_rounds():
+    """The bounce loop as a captured graph and as direct launches (profiling on)."""
+    from gpis_extend_gb300 import runtime
+    media, scenes = batch_scenes()
+    with runtime.Context(media) as ctx:
+        g, gs = ctx.render_batch(scenes)
+        ctx.profile(True)
+        d, ds = ctx.render_batch(scenes)
+        ctx.profile(False)
+    assert gs["graphed"] == 1 and ds["graphed"] == 0
+    for a, b in zip(g, d):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_gpu_render_batch_matches_restatement_per_scene():
+    from gpis_extend_gb300 import runtime
+    media, scenes = batch_scenes()
+    with runtime.Context(media) as ctx:
+        imgs, _ = ctx.render_batch(scenes)
+    for img, sc in zip(imgs, scenes):
+        c, _ = oracle.render(media[sc.medium], sc)
+        close = np.all(np.abs(img - c) <= 1e-3 * np.abs(c) + 1e-7, axis=2)
+        assert close.mean() >= 0.98, close.mean()
