@@ -344,6 +344,50 @@ def run_learned(args):
     ctx.close()
 
 
+def run_batch(args):
+    """The uneven image batch in one wavefront (gpis_render_batch): 64 media and images
+    from seed 11, the render pass size from the autotuner, the bounce loop as a graph."""
+    import torch
+    from gpis_extend_gb300 import autotune, build, runtime, workloads
+    build.build()
+    media, scenes = workloads.config4_batch(spp_scale=args.spp_scale)
+    ctx = runtime.Context(media)
+    sched = autotune.tune_render(ctx, scenes)
+    ctx.render_batch([workloads.render_scene(width=32, height=32, spp=1, max_bounces=4, medium=k)
+                      for k in range(len(media))])
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    dev_ms, flights, wall, launches = 0.0, 0, 0.0, 0
+    st = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        imgs, st = ctx.render_batch(scenes)
+        wall += time.perf_counter() - t0
+        dev_ms += st["ms"]
+        flights += st["distance_flights"] + st["shadow_flights"]
+        launches += st["launches"]
+    clocks.stop()
+    pixels = sum(sc.width * sc.height for sc in scenes)
+    line = {
+        "metric": METRIC, "value": flights / (dev_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": 1, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "uneven image batch in one wavefront: 64 media from seed 11 (sphere/torus/plane/"
+                               "torus-union-plane means, l 0.02-0.3, 1-3 octaves, Renewal or Renewal+), images "
+                               "64^2-1024^2, 1-64 spp, 4 bounces, Lambert 0.8; bounce loop as a CUDA graph",
+                   "arm": "plain", "scenes": len(scenes), "pixels": pixels, "paths_per_step": st["paths"],
+                   "flights_per_step": flights // args.steps, "passes": st["passes"], "graphed": st["graphed"],
+                   "spp_scale": args.spp_scale, "schedule": sched,
+                   "sizes": sorted(int(sc.width) for sc in scenes), "spp": [int(sc.spp) for sc in scenes]},
+        "e2e": {"value": flights / wall, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": pixels * 12},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_image(args):
     """An image workload: flights/s during gpis_render, device time (CUDA events in the
     renderer) and host wall time around the call (e2e)."""
@@ -436,7 +480,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=1 << 16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
-    ap.add_argument("--workload", default="flights", choices=["flights", "image0", "image2", "learned"])
+    ap.add_argument("--workload", default="flights", choices=["flights", "image0", "image2", "learned", "batch"])
+    ap.add_argument("--spp-scale", type=float, default=1.0)
     ap.add_argument("--train-flights", type=int, default=1 << 22)
     ap.add_argument("--train-steps", type=int, default=1200)
     ap.add_argument("--size", type=int, default=0)
@@ -451,6 +496,9 @@ def main():
         return
     if args.workload == "learned":
         run_learned(args)
+        return
+    if args.workload == "batch":
+        run_batch(args)
         return
     if args.workload != "flights":
         run_image(args)
@@ -494,6 +542,9 @@ def main():
     dev_s = runtime.DeviceFlights(sec)
     flights_per_step = prim.n + sec.n
     stream = torch.cuda.current_stream()
+    # the schedule: the fast pass's persistent grid from the autotuner, on these flights
+    from gpis_extend_gb300 import autotune
+    schedule = [autotune.tune_march(ctx, [dev_p, dev_s])]
 
     # ---- device-resident throughput --------------------------------------------
     for _ in range(args.warmup):
@@ -528,6 +579,7 @@ def main():
     # ---- end to end through the host entry point -------------------------------
     pin_p = runtime.PinnedFlights(prim)
     pin_s = runtime.PinnedFlights(sec)
+    schedule.append(autotune.tune_host_chunk(ctx, [pin_p, pin_s]))
     ctx.trace_pinned(pin_p)
     ctx.trace_pinned(pin_s)
     barrier()
@@ -569,7 +621,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "arm": "plain", "flights_per_step_per_gpu": flights_per_step,
                    "primary": prim.n, "secondary": sec.n, "l2": "inputs 512 MiB > L2 (no flush)",
-                   "parallelism": f"replicas x{world} (disjoint flight ranges)"},
+                   "parallelism": f"replicas x{world} (disjoint flight ranges)", "schedule": schedule},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": args.steps * 2 * 3,
         "roofline": roof,

@@ -144,6 +144,7 @@ class ResultSoA(ctypes.Structure):
 
 
 PHASE_LAMBERT, PHASE_MIRROR, PHASE_CONDUCTOR = 0, 1, 2
+TUNE_MARCH_CTAS_PER_SM, TUNE_RENDER_PASS_PATHS, TUNE_HOST_CHUNK = 0, 1, 2
 PHASE_NAMES = {"lambert": PHASE_LAMBERT, "mirror": PHASE_MIRROR, "conductor": PHASE_CONDUCTOR}
 # ConductorBsdf's default material, copper (ConductorBsdf.cpp:24-27)
 CU_ETA = (0.200438, 0.924033, 1.10221)
@@ -374,6 +375,8 @@ def load_library(path=None):
         "gpis_nee_host": (c_int, [vp, P(NeeSoA), vp, c_u32]),
         "gpis_render": (c_int, [vp, P(SceneDesc), vp, P(RenderStats)]),
         "gpis_render_batch": (c_int, [vp, vp, c_u32, vp, P(RenderStats)]),
+        "gpis_tune_set": (c_int, [vp, c_u32, ctypes.c_uint64]),
+        "gpis_tune_get": (c_int, [vp, c_u32, P(ctypes.c_uint64)]),
         "gpis_status": (c_int, [vp, P(Counters), c_int]),
         "gpis_profile_enable": (c_int, [vp, c_int]),
         "gpis_profile_read": (c_int, [vp, P(ctypes.c_double), P(ctypes.c_uint64), c_int]),

@@ -2355,10 +2355,12 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     // warps than flights
     const uint32_t warps_needed = (a.n + 31) / 32;
     const uint32_t ctas_needed = (warps_needed + 7) / 8;
-    auto grid = [&](const void *fn, size_t smem = 0) {
+    auto grid = [&](const void *fn, size_t smem = 0, bool tuned = true) {
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem) != cudaSuccess || per_sm < 1)
             per_sm = 1;
+        // the schedule's CTAs per SM (never more than are resident at once)
+        if (tuned && a.ctas_per_sm > 0 && (int)a.ctas_per_sm < per_sm) per_sm = (int)a.ctas_per_sm;
         uint32_t c = (uint32_t)num_sms * (uint32_t)per_sm;
         if (c > ctas_needed) c = ctas_needed;
         return c == 0 ? 1u : c;
@@ -2389,7 +2391,7 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     }
     {
         const void *fn = (const void *)k_march<EvalGeneric, true>;
-        k_march<EvalGeneric, true><<<grid(fn), 256, 0, stream>>>(b);
+        k_march<EvalGeneric, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
     }
     if (ev) cudaEventRecord(ev[3], stream);
     if (ev) cudaEventRecord(ev[4], stream);

@@ -51,6 +51,7 @@ struct FlightArgs {
     int all_grid;               // all media have a grid mean
     int any_ns;                 // some medium has a nonstationary length scale
     int any_mr;                 // some medium blends multi-resolution levels
+    uint32_t ctas_per_sm;       // fast-pass persistent grid: CTAs per SM (0: every resident CTA)
     const uint32_t *n_dev;      // may be null: the live flight count in device memory (<= n,
                                 // which is then the capacity the grids are sized for)
     const float4 *proposal;     // may be null: per flight the proposed crossing interval

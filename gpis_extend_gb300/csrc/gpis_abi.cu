@@ -274,6 +274,8 @@ struct gpis_ctx {
     std::vector<cudaEvent_t> ev_pending;   // groups of 6 recorded events
     double prof_ms[3] = {0, 0, 0};
     uint64_t prof_launches[3] = {0, 0, 0};
+    // schedule knobs (gpis_tune_set; 0 = default)
+    uint64_t tune[3] = {0, 0, 0};
 };
 
 namespace {
@@ -474,6 +476,7 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     gpis::FlightArgs a = {};
     a.proposal = reinterpret_cast<const float4 *>(proposal);
     a.n_dev = n_dev;
+    a.ctas_per_sm = (uint32_t)ctx->tune[GPIS_TUNE_MARCH_CTAS_PER_SM];
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
     a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
     a.seeds = reinterpret_cast<const uint4 *>(in->seeds);
@@ -594,6 +597,33 @@ __attribute__((visibility("hidden"))) int gpis_internal_nee_live(gpis_ctx *ctx, 
 
 // SM count, whether per-kernel profiling is on, and whether a flight batch runs the
 // prepare kernel (conditioning media, or the stationary cooperative fast pass's set-up)
+int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value)
+{
+    if (!ctx) return fail(GPIS_EINVAL, "null context");
+    if (key > GPIS_TUNE_HOST_CHUNK) return fail(GPIS_EINVAL, "unknown schedule knob");
+    if (key == GPIS_TUNE_MARCH_CTAS_PER_SM && value > 64) return fail(GPIS_ERANGE, "CTAs per SM must be <= 64");
+    if (key == GPIS_TUNE_RENDER_PASS_PATHS && value && (value < 4096 || value > (1ull << 26)))
+        return fail(GPIS_ERANGE, "render pass size must be in [4096, 2^26]");
+    if (key == GPIS_TUNE_HOST_CHUNK && value && (value < 4096 || value > (1ull << 26)))
+        return fail(GPIS_ERANGE, "host chunk must be in [4096, 2^26]");
+    ctx->tune[key] = value;
+    return GPIS_OK;
+}
+
+int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value)
+{
+    if (!ctx || !value) return fail(GPIS_EINVAL, "null argument");
+    if (key > GPIS_TUNE_HOST_CHUNK) return fail(GPIS_EINVAL, "unknown schedule knob");
+    *value = ctx->tune[key];
+    return GPIS_OK;
+}
+
+__attribute__((visibility("hidden"))) uint32_t gpis_internal_render_pass(gpis_ctx *ctx)
+{
+    return ctx && ctx->tune[GPIS_TUNE_RENDER_PASS_PATHS] ? (uint32_t)ctx->tune[GPIS_TUNE_RENDER_PASS_PATHS]
+                                                         : (1u << 22);
+}
+
 __attribute__((visibility("hidden"))) int gpis_internal_ctx_info(gpis_ctx *ctx, int *num_sms, int *profiling,
                                                                  int *prepare_runs)
 {
@@ -676,7 +706,8 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis
     // previous chunk out (another) overlap the flight kernels, and the chunks'
     // kernels alternate between two compute streams on disjoint slices of the
     // scratch, so one chunk's tail overlaps the next chunk's start.
-    uint32_t per = n > (3u << 20) ? (1u << 20) : n;
+    const uint32_t chunk = ctx->tune[GPIS_TUNE_HOST_CHUNK] ? (uint32_t)ctx->tune[GPIS_TUNE_HOST_CHUNK] : (1u << 20);
+    uint32_t per = n > 3 * (uint64_t)chunk ? chunk : n;
     if ((n + per - 1) / per > kMaxChunks) per = (n + kMaxChunks - 1) / kMaxChunks;
     const uint32_t chunks = (n + per - 1) / per;
     int rc0 = ensure_scratch(ctx, n);

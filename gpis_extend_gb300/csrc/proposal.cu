@@ -63,6 +63,19 @@ __device__ __forceinline__ void mma_bf16(float d[4], uint32_t a0, uint32_t a1, u
 }
 
 __device__ __forceinline__ float sigm(float x) { return 1.0f / (1.0f + expf(-x)); }
+// inference forms: the proposal only steers the march, so the fused kernel takes the
+// hardware approximations (tanh.approx, ex2.approx, approximate division)
+__device__ __forceinline__ float tanh_fast(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sigm_fast(float x) { return 0.5f + 0.5f * tanh_fast(0.5f * x); }
+__device__ __forceinline__ float gelu_fast(float x)
+{
+    return 0.5f * x * (1.0f + tanh_fast(0.7978845608028654f * (x + 0.044715f * x * x * x)));
+}
 __device__ __forceinline__ float softplus(float x) { return x > 20.0f ? x : log1pf(expf(x)); }
 constexpr float kGeluC = 0.7978845608028654f;
 __device__ __forceinline__ float gelu(float x)
@@ -407,8 +420,8 @@ __device__ __forceinline__ void gelu_frag(float (&acc)[8][4], const float *bias,
         for (int h = 0; h < 2; ++h) {
             const int nt = 2 * kt + h;
             const int c = nt * 8 + 2 * ti;
-            const float v0 = gelu(acc[nt][0] + bias[c]), v1 = gelu(acc[nt][1] + bias[c + 1]);
-            const float v2 = gelu(acc[nt][2] + bias[c]), v3 = gelu(acc[nt][3] + bias[c + 1]);
+            const float v0 = gelu_fast(acc[nt][0] + bias[c]), v1 = gelu_fast(acc[nt][1] + bias[c + 1]);
+            const float v2 = gelu_fast(acc[nt][2] + bias[c]), v3 = gelu_fast(acc[nt][3] + bias[c + 1]);
             a[kt][2 * h] = pack2f(v0, v1);
             a[kt][2 * h + 1] = pack2f(v2, v3);
         }
@@ -484,9 +497,9 @@ __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *para
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const int c = nt * 8 + 2 * ti + (e & 1);
-                const float r = sigm(gr[e] + bih[c] + bhh[c]);
-                const float z = sigm(gz[e] + bih[HID + c] + bhh[HID + c]);
-                const float nn = tanhf(gin[e] + bih[2 * HID + c] + r * (ghn[e] + bhh[2 * HID + c]));
+                const float r = sigm_fast(gr[e] + bih[c] + bhh[c]);
+                const float z = sigm_fast(gz[e] + bih[HID + c] + bhh[HID + c]);
+                const float nn = tanh_fast(gin[e] + bih[2 * HID + c] + r * (ghn[e] + bhh[2 * HID + c]));
                 hn[nt][e] = (1.0f - z) * nn + z * h[nt][e];
             }
         }

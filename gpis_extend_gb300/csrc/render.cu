@@ -842,6 +842,7 @@ extern "C" int gpis_internal_submit_live(gpis_ctx *ctx, const gpis_flight_soa *i
 extern "C" int gpis_internal_nee_live(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t cap,
                                       const uint32_t *n_dev, void *cuda_stream);
 extern "C" int gpis_internal_ctx_info(gpis_ctx *ctx, int *num_sms, int *profiling, int *prepare_runs);
+extern "C" uint32_t gpis_internal_render_pass(gpis_ctx *ctx);
 
 namespace {
 
@@ -900,6 +901,7 @@ int make_scene(gpis_ctx *ctx, const gpis_scene_desc &sc, RtScene &S, bool &specu
 // Render a batch of scenes in one wavefront: the paths of all scenes share the
 // flight batches of every round (the flight kernels take each flight's medium),
 // so many small images fill the GPU together.  A pass holds up to 2^22 paths
+// (GPIS_TUNE_RENDER_PASS_PATHS)
 // (runs of samples of one or several scenes); each pass runs rounds of the
 // bounce loop until every path has ended, with the queue lengths in device
 // memory, so a round needs no host synchronization and is replayed from one
@@ -926,7 +928,7 @@ extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, u
     }
     // passes: runs of samples, up to `target` paths each (one sample of an image
     // larger than that makes a pass of its own)
-    const uint32_t target = 1u << 22;
+    const uint32_t target = gpis_internal_render_pass(ctx);
     std::vector<std::vector<Seg>> passes(1);
     std::vector<uint32_t> pass_n(1, 0), pass_pix(1, 0);
     for (uint32_t k = 0; k < n_scenes; ++k) {

@@ -138,6 +138,14 @@ class Context:
                   "gpis_render")
         return img, {k: getattr(st, k) for k, _ in abi.RenderStats._fields_}
 
+    def tune(self, key, value=None):
+        """Set (value given) and return a schedule knob (abi.TUNE_*)."""
+        if value is not None:
+            abi.check(self.lib.gpis_tune_set(self.h, key, int(value)), "gpis_tune_set")
+        v = ctypes.c_uint64()
+        abi.check(self.lib.gpis_tune_get(self.h, key, ctypes.byref(v)), "gpis_tune_get")
+        return v.value
+
     def render_batch(self, scenes):
         """gpis_render_batch: returns (list of images (h, w, 3) float32, stats dict)."""
         imgs = [np.zeros((sc.height, sc.width, 3), np.float32) for sc in scenes]

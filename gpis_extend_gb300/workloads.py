@@ -248,3 +248,41 @@ def render_scene(width=256, height=256, spp=16, max_bounces=4, box_half=1.5, **k
     20, Lambert albedo 0.8, the medium in the cube [-h, h]^3."""
     return abi.make_scene(width=width, height=height, spp=spp, max_bounces=max_bounces, box_half=box_half,
                           light_emission=(20.0, 20.0, 20.0), albedo=(0.8, 0.8, 0.8), **kw)
+
+
+def config4_batch(n=64, seed=11, sizes=(64, 128, 256, 512, 1024), size_p=(0.35, 0.3, 0.2, 0.1, 0.05),
+                  spps=(1, 2, 4, 8, 16, 32, 64), max_bounces=4, spp_scale=1.0):
+    """The uneven image batch: n media drawn from `seed` -- sphere, torus, plane or
+    torus-union-plane mean SDFs, length scales 0.02-0.3, one to three octaves (1D
+    noise), Renewal or Renewal+, std 0.02-0.06 -- each with its own image (size from
+    `sizes` with probabilities `size_p`, spp from `spps` times spp_scale), Lambert
+    albedo 0.8, 4 bounces.  Returns (media, scenes); scene k renders medium k."""
+    rng = np.random.default_rng(seed)
+    media, scenes = [], []
+    for i in range(n):
+        kind = int(rng.integers(0, 4))
+        octaves = int(rng.integers(1, 4))
+        ctx = abi.CTX_RENEWAL_PLUS if rng.random() < 0.5 else abi.CTX_RENEWAL
+        ell = float(rng.uniform(0.02, 0.3))
+        sigma = float(rng.uniform(0.02, 0.06))
+        params = dict(sigma=sigma, length_scale=ell, kernel_scale=3.0, impulse_density=8.0,
+                      seed=int(rng.integers(1, 1000)), one_d_sampling=1, correlation_context=ctx,
+                      step_size=float(max(0.004, ell / 10)), min_step=8, sigma_s=1.0, sigma_a=0.0)
+        if kind == 0:
+            params.update(mean_kind=abi.MEAN_SPHERE, mean_params=(0, 0, 0, 1))
+        elif kind == 1:
+            params.update(mean_kind=abi.MEAN_TORUS, mean_params=(0, 0, 0, 1.0, 0.35))
+        elif kind == 2:
+            params.update(mean_kind=abi.MEAN_PLANE, mean_params=(0, 1, 0, -0.5))
+        else:
+            params.update(mean_kind=abi.MEAN_TORUS_PLANE, mean_params=(0, 0, 0, 1.0, 0.35, -0.5))
+        if octaves > 1:
+            params.update(n_octaves=octaves, octave_sigma=[sigma / 2 ** k for k in range(octaves)],
+                          octave_scale=[0.5 ** k for k in range(octaves)],
+                          octave_seed=[0x1F123BB5 * k for k in range(octaves)])
+        media.append(abi.make_medium(**params))
+        size = int(rng.choice(sizes, p=size_p))
+        spp = max(1, int(round(int(rng.choice(spps)) * spp_scale)))
+        scenes.append(render_scene(width=size, height=size, spp=spp, max_bounces=max_bounces, medium=i,
+                                   box_half=1.5 if kind == 0 else 2.0, sampler_seed=7 + i))
+    return media, scenes

@@ -276,6 +276,16 @@ int gpis_nee_submit(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t 
 /* Blocking, host pointers. */
 int gpis_nee_host(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n);
 
+/* ---- schedule knobs (the autotuner's outputs) ------------------------------
+ * 0 restores a knob's default.                                               */
+#define GPIS_TUNE_MARCH_CTAS_PER_SM 0u   /* fast-pass persistent grid: CTAs per SM
+                                            (default: every CTA that is resident)   */
+#define GPIS_TUNE_RENDER_PASS_PATHS 1u   /* paths per render pass (default 2^22)     */
+#define GPIS_TUNE_HOST_CHUNK        2u   /* flights per chunk of the host pipeline
+                                            (default 2^20)                          */
+int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value);
+int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value);
+
 /* Read (and optionally reset) the device counter block. */
 int gpis_status(gpis_ctx *ctx, gpis_counters *out, int reset);
 
