@@ -17,8 +17,8 @@ the medium) and report the flights traced per second of render:
 image0 = 256 x 256, 16 spp, 4 bounces, the sphere field with 3D noise and
 Renewal, Lambert albedo 0.8, a 1 x 1 quad light at y = 3; image2 = 1024 x 1024,
 256 spp, 8 bounces, the nonstationary three-octave torus-union-plane field with
-1D noise and Renewal+, a copper conductor phase (plain reflection sampling: the
-1D NEE law is defined for one realization, not for an octave sum).
+1D noise and Renewal+, a copper conductor phase with 1D NEE (for the octave sum
+the NEE law is that of the summed transverse gradient).
 
 The learned arm: a proposal network (GRU 32 + 3 x 64 GELU MLP -> 8-component
 logistic mixture over the crossing interval, BF16 tensor-core kernels) trained
@@ -213,11 +213,10 @@ IMAGE_WORKLOADS = {
     "image0": dict(medium="sphere_3d", size=256, spp=16, bounces=4,
                    text="image render: 256x256 pinhole at z=4, 16 spp, 4 bounces, sphere SDF field, 3D SE noise "
                         "sigma 0.05 l 0.1 N 8, Renewal, Lambert albedo 0.8, 1x1 quad light at y=3"),
-    "image2": dict(medium="torus", size=1024, spp=256, bounces=8, phase="conductor", box=2.0,
+    "image2": dict(medium="torus_oct_nee", size=1024, spp=256, bounces=8, phase="conductor", box=2.0,
                    text="image render: 1024x1024, 256 spp, 8 bounces, torus (R 1, r 0.35) union plane y=-0.5, "
                         "l(p)=0.11+0.09 sin3x cos2z, 3 octaves sigma 0.04/0.02/0.01, 1D noise, Renewal+, "
-                        "copper conductor phase with plain reflection sampling (1D NEE needs one octave), "
-                        "cube 2, 1x1 quad light at y=3"),
+                        "copper conductor phase with 1D NEE (the octave sum's law), cube 2, 1x1 quad light at y=3"),
 }
 
 

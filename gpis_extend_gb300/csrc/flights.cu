@@ -2134,6 +2134,90 @@ __device__ __forceinline__ void inv3(const float A[9], float R[9])
     R[8] = (A[0] * A[4] - A[1] * A[3]) * id;
 }
 
+// NEE for a field of several octaves (no reference form: the reference's NEE is for
+// one realization).  Octave k contributes c_k (x_k, y_k, dv_k) in the common iso-ray
+// frame, c_k = amplitude / length multiplier, with independent transverse draws of the
+// law its gradient sample uses (noise_gradient_oct): N(base_k, 1 / (2 scx^2)) per
+// component, or under Renewal+ with correlationXY away from the origin
+// N(base_k + 2 fac x1_k, cov).  The summed transverse gradient is Gaussian with mean
+// sum c_k m_k and variance v sum c_k^2; the along-ray component is Z = sum c_k dv_k.
+// In double; returns {pdf, gradient}.
+__device__ float4 nee_octaves(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond, const Frame &f,
+                              const float p[3], const float nw[3], float t_seg, const float mg[3])
+{
+    double A[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const double li = m.ls_kind ? (double)m.l_inv[r] / m.ls_max : (double)m.l_inv[r];
+        A[3 * r + 0] = li * f.t[r];
+        A[3 * r + 1] = li * f.b[r];
+        A[3 * r + 2] = li * f.n[r];
+    }
+    const bool corr = (m.flags & MF_RENEWAL_PLUS) && (m.flags & MF_CORR_XY) && t_seg != 0.0f;
+    float facf = 0.0f, covf = 0.0f;
+    if (corr) corr_moments(t_seg, facf, covf);
+    const float ls = ns_scale_precise(m, p[0], p[2]);
+    const double scx = splat_cov_1d(ls, ls);
+    const double v1 = corr ? (double)covf : 1.0 / (2.0 * scx * scx);
+    double Z = 0.0, MX = 0.0, MY = 0.0, S2 = 0.0;
+    const float ls_o = cond ? ns_scale_precise(m, fl.o[0], fl.o[2]) : 1.0f;
+    for (int k = 0; k < (int)m.n_oct; ++k) {
+        const float sc = oct_scale(m, k);
+        const float z = ray_coord_oct(m, f.n, p[0], p[1], p[2], sc);
+        float v, dv;
+        noise1d_generic<true>(m, z, fl.noise_seed + oct_seed(m, k), v, dv, ls);
+        dv *= inv_norm_1d(m, ls);
+        double bx = 0.0, by = 0.0;
+        if (cond) {
+            const CondOct &co = c.oct[k];
+            const float oz = ray_coord_oct(m, f.n, fl.o[0], fl.o[1], fl.o[2], sc);
+            const Cov1D kk = cov1d(z - oz, splat_cov_1d(ls, ls_o));
+            dv += co.vs * kk.k1 + (sc * co.gs[2]) * kk.k2;
+            if (m.flags & MF_CORR_XY) {
+                bx = (sc * co.gs[0]) * kk.k3;
+                by = (sc * co.gs[1]) * kk.k3;
+            }
+        }
+        if (corr) {
+            float z0, z1;
+            normal_draws(oct_normal_seed(m, fl.normal_seed, k), 0, z0, z1);
+            bx += (double)facf * 2.0 * ((double)z0 / 1.41421354);
+            by += (double)facf * 2.0 * ((double)z1 / 1.41421354);
+        }
+        const double ck = (double)oct_sigma(m, k) / sc;
+        Z += ck * dv;
+        MX += ck * bx;
+        MY += ck * by;
+        S2 += ck * ck;
+    }
+    const double V = v1 * S2;
+    const double ax[3] = {A[0], A[3], A[6]}, ay[3] = {A[1], A[4], A[7]};
+    double ppt[3], cr[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) ppt[r] = A[3 * r + 2] * Z + mg[r];
+    cr[0] = ax[1] * ay[2] - ax[2] * ay[1];
+    cr[1] = ax[2] * ay[0] - ax[0] * ay[2];
+    cr[2] = ax[0] * ay[1] - ax[1] * ay[0];
+    const double jac = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    const double pn[3] = {cr[0] / jac, cr[1] / jac, cr[2] / jac};
+    const double npn = nw[0] * pn[0] + nw[1] * pn[1] + nw[2] * pn[2];
+    const double isect = (ppt[0] * pn[0] + ppt[1] * pn[1] + ppt[2] * pn[2]) / npn;
+    const float g0 = (float)(isect * nw[0]), g1 = (float)(isect * nw[1]), g2 = (float)(isect * nw[2]);
+    if (!(isect >= 0.0) || !(V > 0.0)) return make_float4(0.0f, g0, g1, g2);
+    const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
+    const double id = 1.0 / (A[0] * c00 + A[1] * c01 + A[2] * c02);
+    const double i0 = c00 * id, i1 = (A[2] * A[7] - A[1] * A[8]) * id, i2 = (A[1] * A[5] - A[2] * A[4]) * id;
+    const double i3 = c01 * id, i4 = (A[0] * A[8] - A[2] * A[6]) * id, i5 = (A[2] * A[3] - A[0] * A[5]) * id;
+    const double gw0 = isect * nw[0] - mg[0], gw1 = isect * nw[1] - mg[1], gw2 = isect * nw[2] - mg[2];
+    const double X = i0 * gw0 + i1 * gw1 + i2 * gw2;
+    const double Y = i3 * gw0 + i4 * gw1 + i5 * gw2;
+    const double dx = X - MX, dy = Y - MY;
+    const double pdf_area = exp(-0.5 * (dx * dx + dy * dy) / V) / (6.283185307179586 * V);
+    const double pdf_n = pdf_area * isect * isect / fabs(npn) / jac;
+    const double ndr = -((double)nw[0] * fl.d[0] + (double)nw[1] * fl.d[1] + (double)nw[2] * fl.d[2]);
+    return make_float4((float)(pdf_n / (4.0 * ndr)), g0, g1, g2);
+}
+
 __device__ __forceinline__ void nee_one(const FlightArgs &a, const float4 *point_t, const float4 *normal, float4 *out,
                                         uint32_t i)
 {
@@ -2143,7 +2227,7 @@ __device__ __forceinline__ void nee_one(const FlightArgs &a, const float4 *point
     const float4 q = point_t[i], nv = normal[i];
     const float p[3] = {q.x, q.y, q.z}, nw[3] = {nv.x, nv.y, nv.z};
     const float t_seg = q.w;
-    bool ok = mok && (m.flags & MF_ONE_D) && m.n_oct == 1 && isfinite(t_seg);
+    bool ok = mok && (m.flags & MF_ONE_D) && isfinite(t_seg);
 #pragma unroll
     for (int k = 0; k < 3; ++k)
         ok = ok && isfinite(fl.o[k]) && isfinite(fl.d[k]) && isfinite(p[k]) && isfinite(nw[k]);
@@ -2159,6 +2243,10 @@ __device__ __forceinline__ void nee_one(const FlightArgs &a, const float4 *point
     mean_grad(m, p[0], p[1], p[2], mg);
     Frame f;
     ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+    if (m.n_oct > 1) {
+        out[i] = nee_octaves(m, fl, c, cond, f, p, nw, t_seg, mg);
+        return;
+    }
     // mtx_pt = amplitude * localToWorldInvTransposeMatrix(p) * [t b n]
     float A[9], Ai[9];
 #pragma unroll

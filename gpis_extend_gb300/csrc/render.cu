@@ -860,9 +860,6 @@ int make_scene(gpis_ctx *ctx, const gpis_scene_desc &sc, RtScene &S, bool &specu
     if (!md) return gpis_internal_set_error(GPIS_EINVAL, "unknown medium index");
     const float sa = md->sigma_a * md->density, ss = md->sigma_s * md->density;
     if (!(ss > 0.0f)) return gpis_internal_set_error(GPIS_ENOTSUP, "the renderer needs a scattering medium (sigma_s > 0)");
-    if (sc.phase != GPIS_PHASE_LAMBERT && md->sampling_scheme != GPIS_SCHEME_UNI && md->one_d_sampling &&
-        md->n_octaves > 1)
-        return gpis_internal_set_error(GPIS_ENOTSUP, "1D NEE and MIS need a single-octave medium");
     RtMedium &M = S.M;
     M.ratio = ss / (sa + ss);
     M.max_bounces = md->max_bounces;

@@ -225,7 +225,11 @@ def render_medium(kind="sphere_3d"):
     torus      the nonstationary three-octave torus-union-plane field (1D, Renewal+);
     sphere_1d_nee, sphere_1d_mis  sphere_1d with the NEE or MIS 1D sampling scheme;
     torus_nee  the nonstationary single-octave torus-union-plane field with NEE;
-    torus_mr_nee  the same length scale on the multi-resolution grid with NEE."""
+    torus_mr_nee  the same length scale on the multi-resolution grid with NEE;
+    torus_oct_nee  the three-octave field of `torus` with NEE (the octave sum's law)."""
+    if kind == "torus_oct_nee":
+        return torus_plane_medium(nonstationary=True, octaves=3, sigma_a=0.0, sigma_s=1.0,
+                                  sampling_scheme=abi.SCHEME_NEE)
     if kind in ("sphere_1d_nee", "sphere_1d_mis"):
         return sphere_medium(one_d=True, context=abi.CTX_RENEWAL_PLUS, sigma_a=0.0, sigma_s=1.0,
                              sampling_scheme=abi.SCHEME_NEE if kind.endswith("nee") else abi.SCHEME_MIS)

@@ -263,7 +263,9 @@ int gpis_medium_transmittance(gpis_ctx *ctx, uint32_t medium, const gpis_ray *ra
  * far and jitter are not read), the point and segment parameter
  * point_t[i] = {p, info->t} and the world normal normal[i] = {n, unused}.
  * out[i] = {pdf (neePDF), gradient (neeGrad, 3 floats)}.  Media must use 1D
- * sampling with one octave; a query on another medium or with non-finite
+ * sampling; with several octaves the law is the octave sum's (the transverse
+ * gradient is the sum of the octaves' independent Gaussian draws, weighted by
+ * amplitude / length multiplier).  A query on a 3D medium or with non-finite
  * inputs gets a NaN pdf.  All streams 16-byte aligned.                      */
 typedef struct {
     gpis_flight_soa flight;
@@ -385,9 +387,8 @@ int gpis_backend_submit(gpis_backend *backend, const gpis_flight_soa *in, float 
  * samplingScheme): UNI takes the phase sample only, at MIS weight 1; NEE takes
  * the light sample only, its BSDF value albedo * F * neePDF at the half-vector
  * normal and its transmittance flight conditioned on neeGrad; MIS takes both
- * under the power heuristic with neePDF as the phase density.  NEE and MIS
- * need media that gpis_nee supports (1D, one octave).  No Russian roulette;
- * no environment light.
+ * under the power heuristic with neePDF as the phase density (1D media).  No
+ * Russian roulette; no environment light.
  *
  * Path decisions draw from a counter RNG keyed (sampler_seed, path, bounce,
  * dimension) with path = (y * width + x) * spp + sample; directions are sampled

@@ -1635,6 +1635,94 @@ static void inv3(const float A[9], float R[9])
 
 /* neeShared / neeGrad / neePDF (SparseConvolutionNoise.cpp:662-821), single-resolution
  * branch, one octave (stationary or nonstationary length scale). */
+/* neeShared / neePDF for a field of several octaves (no reference form: the
+ * reference NEE is defined for one realization).  Octave k contributes
+ * c_k (x_k, y_k, dv_k) in the common iso-ray frame, c_k = amplitude / length
+ * multiplier, with independent transverse draws of the law its gradient sample
+ * uses (grad_noise_1d): N(base_k, 1 / (2 scx^2)) per component, or under
+ * Renewal+ with correlationXY away from the origin N(base_k + 2 fac x1_k, cov).
+ * So the summed transverse gradient (X, Y) is Gaussian with mean sum c_k m_k and
+ * variance v sum c_k^2, the along-ray component is Z = sum c_k dv_k, and the
+ * gradient plane, its intersection with the normal and the solid-angle Jacobian
+ * are those of the one-realization case with the matrix l2w * [t b n]. */
+static int nee_octaves(const om_t *m, const field_t *F, const float dir[3], const float p[3],
+                       const float normal[3], float t_segment, float *pdf, float grad[3])
+{
+    float mg[3];
+    mean_grad_f(m, p, mg);
+    float diso[3], dn[3];
+    w2l_pos(m, dir, 1.0f, diso);
+    normalize3f(diso, dn);
+    frame_t f;
+    frame_make(dn, &f);
+    double A[9];
+    for (int i = 0; i < 3; ++i) {
+        const double li = m->nonstationary ? (double)m->l_inv[i] / m->ls_max : (double)m->l_inv[i];
+        A[3 * i + 0] = li * f.t[i];
+        A[3 * i + 1] = li * f.b[i];
+        A[3 * i + 2] = li * f.n[i];
+    }
+    const int corr = m->d.correlation_context == GPIS_CTX_RENEWAL_PLUS && m->d.correlation_xy && t_segment != 0.0f;
+    double fac = 0.0, cov = 0.0;
+    if (corr) corr_moments(t_segment, &fac, &cov);
+    const double scx = splat_cov_1d(m, p, p);
+    const double v1 = corr ? cov : 1.0 / (2.0 * scx * scx);
+    double Z = 0.0, MX = 0.0, MY = 0.0, S2 = 0.0;
+    for (int k = 0; k < F->n; ++k) {
+        const real_t *r = &F->oct[k];
+        const double c = (double)amplitude(r) / oct_scale(m, k);
+        double o4[4];
+        noise1d_norm(r, p, dir, 1, 0, o4);
+        Z += c * o4[3];
+        double bx = o4[1], by = o4[2];
+        if (corr) {
+            pcg_t g;
+            pcg_set_state(&g, (uint64_t)r->normal_seed);
+            double xy1[2];
+            rand_normal_2(&g, xy1);
+            const double s2 = (double)sqrtf(2.f);
+            bx += fac * 2.0 * (xy1[0] / s2);
+            by += fac * 2.0 * (xy1[1] / s2);
+        }
+        MX += c * bx;
+        MY += c * by;
+        S2 += c * c;
+    }
+    const double V = v1 * S2;
+    /* the gradient plane {A (X, Y, Z) + mg}, its normal and the stretch of its axes */
+    double ppt[3], cr[3], ax[3] = {A[0], A[3], A[6]}, ay[3] = {A[1], A[4], A[7]};
+    for (int i = 0; i < 3; ++i) ppt[i] = A[3 * i + 2] * Z + mg[i];
+    cr[0] = ax[1] * ay[2] - ax[2] * ay[1];
+    cr[1] = ax[2] * ay[0] - ax[0] * ay[2];
+    cr[2] = ax[0] * ay[1] - ax[1] * ay[0];
+    const double jac = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    double pn[3] = {cr[0] / jac, cr[1] / jac, cr[2] / jac};
+    const double npn = normal[0] * pn[0] + normal[1] * pn[1] + normal[2] * pn[2];
+    const double isect = (ppt[0] * pn[0] + ppt[1] * pn[1] + ppt[2] * pn[2]) / npn;
+    for (int i = 0; i < 3; ++i) grad[i] = (float)(isect * normal[i]);
+    if (!(isect >= 0.0) || !(V > 0.0)) {
+        *pdf = 0.0f;
+        return GPIS_OK;
+    }
+    /* (X, Y) of the gradient isect * normal: solve A (X, Y, Z') = g - mg */
+    double Af[9], Ai[9];
+    for (int i = 0; i < 9; ++i) Af[i] = A[i];
+    const double c00 = Af[4] * Af[8] - Af[5] * Af[7], c01 = Af[5] * Af[6] - Af[3] * Af[8], c02 = Af[3] * Af[7] - Af[4] * Af[6];
+    const double id = 1.0 / (Af[0] * c00 + Af[1] * c01 + Af[2] * c02);
+    Ai[0] = c00 * id; Ai[1] = (Af[2] * Af[7] - Af[1] * Af[8]) * id; Ai[2] = (Af[1] * Af[5] - Af[2] * Af[4]) * id;
+    Ai[3] = c01 * id; Ai[4] = (Af[0] * Af[8] - Af[2] * Af[6]) * id; Ai[5] = (Af[2] * Af[3] - Af[0] * Af[5]) * id;
+    double gw[3];
+    for (int i = 0; i < 3; ++i) gw[i] = isect * normal[i] - mg[i];
+    const double X = Ai[0] * gw[0] + Ai[1] * gw[1] + Ai[2] * gw[2];
+    const double Y = Ai[3] * gw[0] + Ai[4] * gw[1] + Ai[5] * gw[2];
+    const double dx = X - MX, dy = Y - MY;
+    const double pdf_area = exp(-0.5 * (dx * dx + dy * dy) / V) / (2.0 * M_PI * V);
+    const double pdf_n = pdf_area * isect * isect / fabs(npn) / jac;
+    const double ndr = -(normal[0] * dir[0] + normal[1] * dir[1] + normal[2] * dir[2]);
+    *pdf = (float)(pdf_n / (4.0 * ndr));
+    return GPIS_OK;
+}
+
 int gor_nee(const gpis_medium_desc *desc, const float origin[3], const float dir[3],
             const float p[3], const float normal[3], float t_segment, const uint32_t seeds[4],
             const float prev[4], float *pdf, float grad[3])
@@ -1643,7 +1731,8 @@ int gor_nee(const gpis_medium_desc *desc, const float origin[3], const float dir
     field_t F;
     int rc = field_setup(desc, &m, &F, origin, dir, seeds, prev);
     if (rc) return rc;
-    if (F.n != 1 || !m.d.one_d_sampling) return GPIS_ENOTSUP;
+    if (!m.d.one_d_sampling) return GPIS_ENOTSUP;
+    if (F.n > 1) return nee_octaves(&m, &F, dir, p, normal, t_segment, pdf, grad);
     const real_t *r = &F.oct[0];
     float amp = amplitude(r);
     float mg[3];

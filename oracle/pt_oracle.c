@@ -433,9 +433,6 @@ int gor_render(const gpis_medium_desc *md, const gpis_scene_desc *sc, float *ima
 {
     if (!md || !sc || !image || sc->width == 0 || sc->height == 0 || sc->spp == 0) return GPIS_EINVAL;
     if (sc->phase > GPIS_PHASE_CONDUCTOR) return GPIS_EINVAL;
-    if (sc->phase != GPIS_PHASE_LAMBERT && md->sampling_scheme != GPIS_SCHEME_UNI && md->one_d_sampling &&
-        md->n_octaves > 1)
-        return GPIS_ENOTSUP;
     pt_counts_t cnt = {0, 0, 0, 0};
     for (uint32_t y = row0; y < row0 + rows && y < sc->height; ++y)
         for (uint32_t x = 0; x < sc->width; ++x) {

@@ -115,14 +115,15 @@ def compare_nee(desc, sub, p, t, nrm, out):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["sphere_xy", "sphere", "torus_ns", "torus_ns_xy", "torus_mr", "torus_mr_xy"])
+@pytest.mark.parametrize("case", ["sphere_xy", "sphere", "torus_ns", "torus_ns_xy", "torus_mr", "torus_mr_xy",
+                                  "torus_oct", "torus_oct_xy"])
 def test_gpu_nee_vs_oracle(case):
     from gpis_extend_gb300 import runtime
     if case.startswith("sphere"):
         desc = workloads.sphere_medium(sampling_scheme=abi.SCHEME_MIS, correlation_xy=int(case.endswith("xy")))
     else:
-        desc = workloads.torus_plane_medium(nonstationary=True, octaves=1, sampling_scheme=abi.SCHEME_MIS,
-                                            correlation_xy=int(case.endswith("xy")),
+        desc = workloads.torus_plane_medium(nonstationary=True, octaves=3 if case.startswith("torus_oct") else 1,
+                                            sampling_scheme=abi.SCHEME_MIS, correlation_xy=int(case.endswith("xy")),
                                             multires=int(case.startswith("torus_mr")))
     prim = workloads.sphere_flights(1 << 11, desc)
     with runtime.Context(desc) as ctx:
