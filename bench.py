@@ -368,6 +368,29 @@ def run_batch(args):
         launches += st["launches"]
     clocks.stop()
     pixels = sum(sc.width * sc.height for sc in scenes)
+    learned = None
+    if not args.no_learned:
+        # the learned arm side by side: a proposal trained on 2^15 flights through each
+        # medium of the batch, then the same render with features, inference and the
+        # proposed march in every round
+        try:
+            from gpis_extend_gb300 import proposal
+            tf = workloads.batch_flights(media, 1 << 15)
+            f, t = proposal.dataset(ctx, [tf])
+            prop = runtime.Proposal(proposal.init_params(0))
+            hist, secs = proposal.train(prop, f, t, steps=400, batch=8192, lr=3e-3, log_every=100)
+            l_ms, l_imgs, ok = 0.0, None, True
+            for _ in range(args.steps):
+                l_imgs, lst = ctx.render_batch(scenes, proposal=prop)
+                l_ms += lst["ms"]
+            ok = all(np.array_equal(a, b) for a, b in zip(imgs, l_imgs))
+            learned = {"value": flights / (l_ms * 1e-3), "unit": UNIT, "ms_per_step": l_ms / args.steps,
+                       "ratio_vs_plain": dev_ms / l_ms, "identical_to_plain": bool(ok),
+                       "train": {"flights": int(f.shape[0]), "steps": 400, "seconds": secs,
+                                 "loss": [[k, round(v, 4)] for k, v in hist]}}
+            prop.close()
+        except Exception as e:  # noqa: BLE001
+            learned = {"error": f"{type(e).__name__}: {e}"}
     line = {
         "metric": METRIC, "value": flights / (dev_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": 1, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -382,6 +405,7 @@ def run_batch(args):
         "e2e": {"value": flights / wall, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": pixels * 12},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "learned": learned,
     }
     print(json.dumps(line), flush=True)
     ctx.close()

@@ -375,6 +375,7 @@ def load_library(path=None):
         "gpis_nee_host": (c_int, [vp, P(NeeSoA), vp, c_u32]),
         "gpis_render": (c_int, [vp, P(SceneDesc), vp, P(RenderStats)]),
         "gpis_render_batch": (c_int, [vp, vp, c_u32, vp, P(RenderStats)]),
+        "gpis_render_batch_proposed": (c_int, [vp, vp, vp, c_u32, vp, P(RenderStats)]),
         "gpis_tune_set": (c_int, [vp, c_u32, ctypes.c_uint64]),
         "gpis_tune_get": (c_int, [vp, c_u32, P(ctypes.c_uint64)]),
         "gpis_status": (c_int, [vp, P(Counters), c_int]),

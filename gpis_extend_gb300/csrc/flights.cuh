@@ -61,7 +61,7 @@ struct FlightArgs {
 
 // Per-flight features of the learned proposal (proposal.cu).
 cudaError_t launch_features(const DevMedium *media, int n_media, const gpis_flight_soa &in, uint32_t n, float *feat,
-                            cudaStream_t s);
+                            cudaStream_t s, const uint32_t *n_dev = nullptr);
 
 // Upload the jump-ahead PCG table to the current device (once per device).
 cudaError_t upload_pcg_table();

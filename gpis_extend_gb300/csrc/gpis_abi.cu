@@ -562,13 +562,25 @@ int gpis_flights_submit_proposed(gpis_ctx *ctx, const gpis_flight_soa *in, const
 // callers that capture whole rounds in a CUDA graph (the path tracer).
 __attribute__((visibility("hidden"))) int gpis_internal_submit_live(gpis_ctx *ctx, const gpis_flight_soa *in,
                                                                     const gpis_result_soa *out, uint32_t cap,
-                                                                    const uint32_t *n_dev, void *cuda_stream)
+                                                                    const uint32_t *n_dev, void *cuda_stream,
+                                                                    const float *intervals)
 {
     if (!ctx || !in || !out || !n_dev) return fail(GPIS_EINVAL, "null argument");
     if (cap == 0) return GPIS_OK;
     int rc = ensure_scratch(ctx, cap);
     if (rc) return rc;
-    return submit_slice(ctx, in, out, cap, static_cast<cudaStream_t>(cuda_stream), 0, ctx->d_work, nullptr, n_dev);
+    return submit_slice(ctx, in, out, cap, static_cast<cudaStream_t>(cuda_stream), 0, ctx->d_work, intervals, n_dev);
+}
+
+__attribute__((visibility("hidden"))) int gpis_internal_features_live(gpis_ctx *ctx, const gpis_flight_soa *in,
+                                                                      float *features, uint32_t cap,
+                                                                      const uint32_t *n_dev, void *cuda_stream)
+{
+    if (!ctx || !in || !features || !n_dev) return fail(GPIS_EINVAL, "null argument");
+    CUDA_TRY(gpis::launch_features(ctx->d_media, ctx->n_media, *in, cap, features,
+                                   static_cast<cudaStream_t>(cuda_stream), n_dev),
+             "proposal features");
+    return GPIS_OK;
 }
 
 __attribute__((visibility("hidden"))) int gpis_internal_nee_live(gpis_ctx *ctx, const gpis_nee_soa *in, float *out,

@@ -326,11 +326,10 @@ __global__ void k_to_bf16(const float *p, int n, bf *pb)
 // equal parts of [near, far] (clamped to +-4), then t_max / 4, 10 x the local length
 // scale at near, the conditioned value and derivative along the ray (clamped to +-4),
 // the first-scatter flag, 10 x the amplitude, step / t_max and the mean at near.
-__global__ void k_features(const DevMedium *media, int n_media, const float4 *on, const float4 *df, const uint4 *sd,
-                           const float4 *pv, const uint32_t *mid, uint32_t n, float *feat)
+__device__ __forceinline__ void features_one(const DevMedium *media, int n_media, const float4 *on, const float4 *df,
+                                             const uint4 *sd, const float4 *pv, const uint32_t *mid, uint32_t i,
+                                             float *feat)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     const uint32_t mi = mid ? mid[i] : 0u;
     const DevMedium &m = media[mi < (uint32_t)n_media ? mi : 0u];
     const float4 o = on[i], d = df[i];
@@ -377,6 +376,15 @@ __global__ void k_features(const DevMedium *media, int n_media, const float4 *on
     f[21] = 10.0f * amp;
     f[22] = tm > 0.0f ? fminf(step / tm, 1.0f) : 1.0f;
     f[23] = fminf(fmaxf(mean_value(m, o.x + near_t * d.x, o.y + near_t * d.y, o.z + near_t * d.z, id), -4.0f), 4.0f);
+}
+
+// n flights, or the live count in device memory (grid-stride)
+__global__ void k_features(const DevMedium *media, int n_media, const float4 *on, const float4 *df, const uint4 *sd,
+                           const float4 *pv, const uint32_t *mid, uint32_t n, const uint32_t *n_dev, float *feat)
+{
+    const uint32_t nl = n_dev ? min(*n_dev, n) : n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += gridDim.x * blockDim.x)
+        features_one(media, n_media, on, df, sd, pv, mid, i, feat);
 }
 
 // ---- fused inference -------------------------------------------------------------------
@@ -430,7 +438,8 @@ __device__ __forceinline__ void gelu_frag(float (&acc)[8][4], const float *bias,
 
 // Persistent: each block loads the weights once and its warps walk 16-flight tiles.
 __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *params, const float *feat,
-                                                 const float4 *on, const float4 *df, uint32_t n, float4 *out)
+                                                 const float4 *on, const float4 *df, uint32_t n_cap,
+                                                 const uint32_t *n_dev, float4 *out)
 {
     __shared__ __align__(16) bf sw[kWeights];
     __shared__ float sb[kBiases];
@@ -453,6 +462,7 @@ __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *para
     for (int k = tid; k < NOUT; k += blockDim.x) sb[6 * HID + 3 * WID + k] = params[O_B4 + k];
     __syncthreads();
     const int lane = tid & 31, gi = lane >> 2, ti = lane & 3;
+    const uint32_t n = n_dev ? min(*n_dev, n_cap) : n_cap;
     const long tiles = ((long)n + 15) / 16;
     for (long tile = (long)blockIdx.x * 4 + (tid >> 5); tile < tiles; tile += (long)gridDim.x * 4) {
     const long row0 = tile * 16;
@@ -882,9 +892,38 @@ int gpis_proposal_infer(gpis_proposal *p, const gpis_flight_soa *in, const float
         per_sm = 1;
     const unsigned blocks = (unsigned)std::min<long>(((long)n + 63) / 64, (long)sms * per_sm);
     k_propose<<<blocks, 128, 0, s>>>(p->pb, p->p, features, reinterpret_cast<const float4 *>(in->origin_near),
-                                     reinterpret_cast<const float4 *>(in->dir_far), n,
+                                     reinterpret_cast<const float4 *>(in->dir_far), n, nullptr,
                                      reinterpret_cast<float4 *>(intervals));
     PTRY(cudaGetLastError(), "proposal inference kernel");
+    return GPIS_OK;
+}
+
+// Inference on a batch whose live count is in device memory (the path tracer's
+// rounds); the parameters must be quiescent (gpis_internal_proposal_quiesce).
+__attribute__((visibility("hidden"))) int gpis_internal_infer_live(gpis_proposal *p, const gpis_flight_soa *in,
+                                                                   const float *features, float *intervals,
+                                                                   uint32_t cap, const uint32_t *n_dev,
+                                                                   void *cuda_stream)
+{
+    if (!p || !in || !features || !intervals || !n_dev) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    if (cap == 0) return GPIS_OK;
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_propose, 128, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const unsigned blocks = (unsigned)std::min<long>(((long)cap + 63) / 64, (long)sms * per_sm);
+    k_propose<<<blocks, 128, 0, static_cast<cudaStream_t>(cuda_stream)>>>(
+        p->pb, p->p, features, reinterpret_cast<const float4 *>(in->origin_near),
+        reinterpret_cast<const float4 *>(in->dir_far), cap, n_dev, reinterpret_cast<float4 *>(intervals));
+    PTRY(cudaGetLastError(), "proposal inference kernel");
+    return GPIS_OK;
+}
+
+__attribute__((visibility("hidden"))) int gpis_internal_proposal_quiesce(gpis_proposal *p)
+{
+    if (!p) return GPIS_EINVAL;
+    PTRY(cudaStreamSynchronize(p->stream), "synchronize proposal");
     return GPIS_OK;
 }
 
@@ -892,13 +931,15 @@ int gpis_proposal_infer(gpis_proposal *p, const gpis_flight_soa *in, const float
 
 namespace gpis {
 cudaError_t launch_features(const DevMedium *media, int n_media, const gpis_flight_soa &in, uint32_t n, float *feat,
-                            cudaStream_t s)
+                            cudaStream_t s, const uint32_t *n_dev)
 {
     if (n == 0) return cudaSuccess;
-    k_features<<<(n + 127) / 128, 128, 0, s>>>(media, n_media, reinterpret_cast<const float4 *>(in.origin_near),
-                                               reinterpret_cast<const float4 *>(in.dir_far),
-                                               reinterpret_cast<const uint4 *>(in.seeds),
-                                               reinterpret_cast<const float4 *>(in.prev), in.medium, n, feat);
+    unsigned blocks = (n + 127) / 128;
+    if (n_dev) blocks = std::min(blocks, 4096u);
+    k_features<<<blocks, 128, 0, s>>>(media, n_media, reinterpret_cast<const float4 *>(in.origin_near),
+                                      reinterpret_cast<const float4 *>(in.dir_far),
+                                      reinterpret_cast<const uint4 *>(in.seeds),
+                                      reinterpret_cast<const float4 *>(in.prev), in.medium, n, n_dev, feat);
     return cudaGetLastError();
 }
 }  // namespace gpis

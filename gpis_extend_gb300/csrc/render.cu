@@ -838,7 +838,13 @@ int cuda_fail(cudaError_t e, const char *what)
     } while (0)
 
 extern "C" int gpis_internal_submit_live(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa *out,
-                                         uint32_t cap, const uint32_t *n_dev, void *cuda_stream);
+                                         uint32_t cap, const uint32_t *n_dev, void *cuda_stream,
+                                         const float *intervals);
+extern "C" int gpis_internal_features_live(gpis_ctx *ctx, const gpis_flight_soa *in, float *features, uint32_t cap,
+                                           const uint32_t *n_dev, void *cuda_stream);
+extern "C" int gpis_internal_infer_live(gpis_proposal *p, const gpis_flight_soa *in, const float *features,
+                                        float *intervals, uint32_t cap, const uint32_t *n_dev, void *cuda_stream);
+extern "C" int gpis_internal_proposal_quiesce(gpis_proposal *p);
 extern "C" int gpis_internal_nee_live(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t cap,
                                       const uint32_t *n_dev, void *cuda_stream);
 extern "C" int gpis_internal_ctx_info(gpis_ctx *ctx, int *num_sms, int *profiling, int *prepare_runs);
@@ -903,10 +909,14 @@ int make_scene(gpis_ctx *ctx, const gpis_scene_desc &sc, RtScene &S, bool &specu
 // bounce loop until every path has ended, with the queue lengths in device
 // memory, so a round needs no host synchronization and is replayed from one
 // captured CUDA graph (launched directly while the context profiles its kernels).
-extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, uint32_t n_scenes, float *const *images,
-                                 gpis_render_stats *stats)
+extern "C" int gpis_render_batch_proposed(gpis_ctx *ctx, gpis_proposal *prop, const gpis_scene_desc *scenes,
+                                          uint32_t n_scenes, float *const *images, gpis_render_stats *stats)
 {
     if (!ctx || !scenes || !images || n_scenes == 0) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    if (prop) {
+        const int qrc = gpis_internal_proposal_quiesce(prop);
+        if (qrc) return qrc;
+    }
     std::vector<RtScene> hs(n_scenes);
     bool any_nee = false;
     uint32_t max_bounces = 0;
@@ -979,6 +989,12 @@ extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, u
     RT_TRY(mem.alloc(counts, 3), "allocate queue counters");
     RT_TRY(mem.alloc(n_paths, 1), "allocate path count");
     RT_TRY(mem.alloc(dcnt, 5), "allocate counters");
+    // the learned arm: features and proposed intervals of the distance queue
+    float *feats = nullptr, *ivals = nullptr;
+    if (prop) {
+        RT_TRY(mem.alloc(feats, (size_t)cap * 24), "allocate proposal features");
+        RT_TRY(mem.alloc(ivals, (size_t)cap * 4), "allocate proposal intervals");
+    }
     for (Queue *qq : {&q, &sq}) {
         const size_t m = qq == &q ? cap : 2 * (size_t)cap;
         RT_TRY(mem.alloc(qq->origin_near, m), "allocate queue");
@@ -1038,7 +1054,7 @@ extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, u
     }
     // the flight scratch for the largest batch, allocated before any capture (the
     // queue counters are zero here, so these launches trace nothing)
-    int rc = gpis_internal_submit_live(ctx, &sin, &sout, 2 * cap, counts + 1, st);
+    int rc = gpis_internal_submit_live(ctx, &sin, &sout, 2 * cap, counts + 1, st, nullptr);
     if (rc) return rc;
     if (any_nee) {
         rc = gpis_internal_nee_live(ctx, &nin, reinterpret_cast<float *>(eq.out), 2 * cap, counts + 2, st);
@@ -1051,7 +1067,14 @@ extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, u
         cudaError_t e = cudaMemsetAsync(counts, 0, 3 * sizeof(uint32_t), st);
         if (e != cudaSuccess) return cuda_fail(e, "clear queue counters");
         k_rt_advance<<<gs, tb, 0, st>>>(d_scenes, paths, n_paths, q, dcnt);
-        int r = gpis_internal_submit_live(ctx, &fin, &fout, cap, counts, st);
+        int r;
+        if (prop) {
+            r = gpis_internal_features_live(ctx, &fin, feats, cap, counts, st);
+            if (r) return r;
+            r = gpis_internal_infer_live(prop, &fin, feats, ivals, cap, counts, st);
+            if (r) return r;
+        }
+        r = gpis_internal_submit_live(ctx, &fin, &fout, cap, counts, st, ivals);
         if (r) return r;
         k_rt_event<<<gs, tb, 0, st>>>(d_scenes, paths, q, counts, sq, eq, direct, dcnt);
         if (any_nee) {
@@ -1059,7 +1082,7 @@ extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, u
             if (r) return r;
             k_rt_nee<<<gs, tb, 0, st>>>(d_scenes, paths, eq, counts, sq, direct);
         }
-        r = gpis_internal_submit_live(ctx, &sin, &sout, 2 * cap, counts + 1, st);
+        r = gpis_internal_submit_live(ctx, &sin, &sout, 2 * cap, counts + 1, st, nullptr);
         if (r) return r;
         k_rt_shadow<<<gs, tb, 0, st>>>(sq, counts, direct);
         k_rt_collect<<<gs, tb, 0, st>>>(paths, q.path, counts, direct);
@@ -1069,7 +1092,7 @@ extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, u
     // kernels of one round: advance, event, shadow, collect, tally, and per flight batch
     // prepare (when it runs), march, resume and finish; NEE adds its kernel and the shading
     const uint64_t per_batch = 3 + (prepare_runs ? 1 : 0);
-    const uint64_t per_round = 5 + 2 * per_batch + (any_nee ? 2 : 0);
+    const uint64_t per_round = 5 + 2 * per_batch + (any_nee ? 2 : 0) + (prop ? 2 : 0);
     const uint32_t rounds = 2 * max_bounces + 4;
     cudaGraphExec_t gexec = nullptr;
     struct GraphGuard { cudaGraphExec_t g; ~GraphGuard() { if (g) cudaGraphExecDestroy(g); } } gg{nullptr};
@@ -1142,6 +1165,12 @@ extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, u
         stats->passes = (uint32_t)passes.size();
     }
     return GPIS_OK;
+}
+
+extern "C" int gpis_render_batch(gpis_ctx *ctx, const gpis_scene_desc *scenes, uint32_t n_scenes, float *const *images,
+                                 gpis_render_stats *stats)
+{
+    return gpis_render_batch_proposed(ctx, nullptr, scenes, n_scenes, images, stats);
 }
 
 extern "C" int gpis_render(gpis_ctx *ctx, const gpis_scene_desc *scene, float *image_rgb, gpis_render_stats *stats)

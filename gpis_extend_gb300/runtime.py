@@ -146,13 +146,19 @@ class Context:
         abi.check(self.lib.gpis_tune_get(self.h, key, ctypes.byref(v)), "gpis_tune_get")
         return v.value
 
-    def render_batch(self, scenes):
-        """gpis_render_batch: returns (list of images (h, w, 3) float32, stats dict)."""
+    def render_batch(self, scenes, proposal=None):
+        """gpis_render_batch (gpis_render_batch_proposed with a Proposal): returns (list of
+        images (h, w, 3) float32, stats dict)."""
         imgs = [np.zeros((sc.height, sc.width, 3), np.float32) for sc in scenes]
         arr = (abi.SceneDesc * len(scenes))(*scenes)
         ptrs = (ctypes.c_void_p * len(scenes))(*[im.ctypes.data for im in imgs])
         st = abi.RenderStats()
-        abi.check(self.lib.gpis_render_batch(self.h, arr, len(scenes), ptrs, ctypes.byref(st)), "gpis_render_batch")
+        if proposal is None:
+            abi.check(self.lib.gpis_render_batch(self.h, arr, len(scenes), ptrs, ctypes.byref(st)),
+                      "gpis_render_batch")
+        else:
+            abi.check(self.lib.gpis_render_batch_proposed(self.h, proposal.h, arr, len(scenes), ptrs,
+                                                          ctypes.byref(st)), "gpis_render_batch_proposed")
         return imgs, {k: getattr(st, k) for k, _ in abi.RenderStats._fields_}
 
     def trace_pinned(self, pinned):

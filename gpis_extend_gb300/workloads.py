@@ -290,3 +290,19 @@ def config4_batch(n=64, seed=11, sizes=(64, 128, 256, 512, 1024), size_p=(0.35, 
         scenes.append(render_scene(width=size, height=size, spp=spp, max_bounces=max_bounces, medium=i,
                                    box_half=1.5 if kind == 0 else 2.0, sampler_seed=7 + i))
     return media, scenes
+
+
+def batch_flights(media, per_medium, seed=31, index_offset=0):
+    """Primary flights through every medium of an image batch (origins on a radius-4
+    sphere toward the region around the origin, cube 2), interleaved in one batch
+    with its medium stream: training data for the learned arm of the batch."""
+    parts = []
+    for k, d in enumerate(media):
+        b = torus_flights(per_medium, d, seed=seed + k, half=2.0, index_offset=index_offset + k * per_medium)
+        parts.append(b)
+    n = per_medium * len(media)
+    out = abi.FlightBatch(n)
+    for name in ("origin_near", "dir_far", "seeds", "prev"):
+        getattr(out, name)[:] = np.concatenate([getattr(p, name) for p in parts])
+    out.medium = np.repeat(np.arange(len(media), dtype=np.uint32), per_medium)
+    return out

@@ -490,6 +490,10 @@ int gpis_proposal_infer(gpis_proposal *prop, const gpis_flight_soa *in, const fl
  * gpis_proposal_infer (16-byte aligned).                                    */
 int gpis_flights_submit_proposed(gpis_ctx *ctx, const gpis_flight_soa *in, const float *intervals,
                                  const gpis_result_soa *out, uint32_t n, void *cuda_stream);
+/* gpis_render_batch with the learned arm: every distance-flight batch takes
+ * features, inference and the proposed march (identical images).            */
+int gpis_render_batch_proposed(gpis_ctx *ctx, gpis_proposal *prop, const gpis_scene_desc *scenes,
+                               uint32_t n_scenes, float *const *images, gpis_render_stats *stats);
 
 /* Last error message of the calling thread ("" when none). */
 const char *gpis_last_error(void);

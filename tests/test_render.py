@@ -169,3 +169,17 @@ def test_gpu_render_batch_matches_restatement_per_scene():
         c, _ = oracle.render(media[sc.medium], sc)
         close = np.all(np.abs(img - c) <= 1e-3 * np.abs(c) + 1e-7, axis=2)
         assert close.mean() >= 0.98, close.mean()
+
+
+@pytest.mark.gpu
+def test_gpu_render_batch_with_proposal_keeps_images():
+    """The learned arm inside the renderer (features, inference and the proposed march
+    for every distance-flight batch) gives the plain images bit for bit."""
+    from gpis_extend_gb300 import proposal, runtime
+    media, scenes = batch_scenes()
+    with runtime.Context(media) as ctx, runtime.Proposal(proposal.init_params(2)) as prop:
+        plain, ps = ctx.render_batch(scenes)
+        learned, ls = ctx.render_batch(scenes, proposal=prop)
+    for a, b in zip(plain, learned):
+        assert np.array_equal(a, b)
+    assert ls["launches"] > ps["launches"] and ls["graphed"] == 1
