@@ -552,27 +552,13 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        return float(t.item())
+    from gpis_extend_gb300 import replicas
+    red = replicas.Reducer(dist, device="cuda")
+    barrier, max_over_ranks, sum_over_ranks = red.barrier, red.max, red.sum
 
     desc = workloads.sphere_medium()
     n = args.flights
-    prim = workloads.sphere_flights(n, desc, index_offset=rank * n)
+    prim = workloads.sphere_flights(n, desc, index_offset=replicas.flight_range(n, rank))
     ctx = runtime.Context(desc)
     rec = ctx.trace_host(prim)
     sec, _ = workloads.secondary_flights(prim, rec, desc)

@@ -17,7 +17,10 @@
 // shadow flights and k_rt_shadow adds the light that got through.  Specular
 // events under the NEE or MIS scheme first queue their neePDF / neeGrad
 // queries (one batch of gpis_nee per round); k_rt_nee turns the answers into
-// shadow flights.  Rounds repeat until no path is alive.
+// shadow flights.  Every queue length stays in device memory, so a pass runs a
+// fixed 2 * bounces + 4 rounds (enough for every path to end: at most a forward
+// crossing and an event per bounce, plus entry and exit) replayed from one
+// captured CUDA graph, with no host synchronization between rounds.
 //
 // This file is compiled with -fmad=false: every float expression rounds as the
 // CPU restatement's (built with -ffp-contract=off), and path decisions use no
