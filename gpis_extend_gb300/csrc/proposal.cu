@@ -464,6 +464,27 @@ __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *para
     const int lane = tid & 31, gi = lane >> 2, ti = lane & 3;
     const uint32_t n = n_dev ? min(*n_dev, n_cap) : n_cap;
     const long tiles = ((long)n + 15) / 16;
+    // the GRU's B fragments and this lane's gate biases stay in registers for every
+    // tile: the recurrence would otherwise reload them from shared memory 8 times
+    // per tile (the kernel is bound by those loads)
+    uint32_t wih[12][2], whh[12][2][2];
+    float brz[2][4][2], bin_[4][2], bhn_[4][2];
+#pragma unroll
+    for (int t = 0; t < 12; ++t) {
+        bfrag(sw + S_WIH, NIN, t, 0, gi, ti, wih[t][0], wih[t][1]);
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt) bfrag(sw + S_WHH, HID, t, kt, gi, ti, whh[t][kt][0], whh[t][kt][1]);
+    }
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int c = nt * 8 + 2 * ti + q;
+            brz[0][nt][q] = sb[c] + sb[3 * HID + c];
+            brz[1][nt][q] = sb[HID + c] + sb[3 * HID + HID + c];
+            bin_[nt][q] = sb[2 * HID + c];
+            bhn_[nt][q] = sb[3 * HID + 2 * HID + c];
+        }
     for (long tile = (long)blockIdx.x * 4 + (tid >> 5); tile < tiles; tile += (long)gridDim.x * 4) {
     const long row0 = tile * 16;
     const long ra = min(row0 + gi, (long)n - 1), rb = min(row0 + gi + 8, (long)n - 1);
@@ -488,28 +509,21 @@ __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *para
 #pragma unroll
         for (int nt = 0; nt < 4; ++nt) {
             float gr[4] = {0, 0, 0, 0}, gz[4] = {0, 0, 0, 0}, gin[4] = {0, 0, 0, 0}, ghn[4] = {0, 0, 0, 0};
-            uint32_t b0, b1;
-            bfrag(sw + S_WIH, NIN, nt, 0, gi, ti, b0, b1);
-            mma_bf16(gr, xa0, xa1, 0u, 0u, b0, b1);
-            bfrag(sw + S_WIH, NIN, 4 + nt, 0, gi, ti, b0, b1);
-            mma_bf16(gz, xa0, xa1, 0u, 0u, b0, b1);
-            bfrag(sw + S_WIH, NIN, 8 + nt, 0, gi, ti, b0, b1);
-            mma_bf16(gin, xa0, xa1, 0u, 0u, b0, b1);
+            mma_bf16(gr, xa0, xa1, 0u, 0u, wih[nt][0], wih[nt][1]);
+            mma_bf16(gz, xa0, xa1, 0u, 0u, wih[4 + nt][0], wih[4 + nt][1]);
+            mma_bf16(gin, xa0, xa1, 0u, 0u, wih[8 + nt][0], wih[8 + nt][1]);
 #pragma unroll
             for (int kt = 0; kt < 2; ++kt) {
-                bfrag(sw + S_WHH, HID, nt, kt, gi, ti, b0, b1);
-                mma_bf16(gr, ha[kt][0], ha[kt][1], ha[kt][2], ha[kt][3], b0, b1);
-                bfrag(sw + S_WHH, HID, 4 + nt, kt, gi, ti, b0, b1);
-                mma_bf16(gz, ha[kt][0], ha[kt][1], ha[kt][2], ha[kt][3], b0, b1);
-                bfrag(sw + S_WHH, HID, 8 + nt, kt, gi, ti, b0, b1);
-                mma_bf16(ghn, ha[kt][0], ha[kt][1], ha[kt][2], ha[kt][3], b0, b1);
+                mma_bf16(gr, ha[kt][0], ha[kt][1], ha[kt][2], ha[kt][3], whh[nt][kt][0], whh[nt][kt][1]);
+                mma_bf16(gz, ha[kt][0], ha[kt][1], ha[kt][2], ha[kt][3], whh[4 + nt][kt][0], whh[4 + nt][kt][1]);
+                mma_bf16(ghn, ha[kt][0], ha[kt][1], ha[kt][2], ha[kt][3], whh[8 + nt][kt][0], whh[8 + nt][kt][1]);
             }
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                const int c = nt * 8 + 2 * ti + (e & 1);
-                const float r = sigm_fast(gr[e] + bih[c] + bhh[c]);
-                const float z = sigm_fast(gz[e] + bih[HID + c] + bhh[HID + c]);
-                const float nn = tanh_fast(gin[e] + bih[2 * HID + c] + r * (ghn[e] + bhh[2 * HID + c]));
+                const int q = e & 1;
+                const float r = sigm_fast(gr[e] + brz[0][nt][q]);
+                const float z = sigm_fast(gz[e] + brz[1][nt][q]);
+                const float nn = tanh_fast(gin[e] + bin_[nt][q] + r * (ghn[e] + bhn_[nt][q]));
                 hn[nt][e] = (1.0f - z) * nn + z * h[nt][e];
             }
         }
