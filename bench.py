@@ -647,7 +647,9 @@ def main():
                    "primary": prim.n, "secondary": sec.n, "l2": "inputs 512 MiB > L2 (no flush)",
                    "parallelism": f"replicas x{world} (disjoint flight ranges)", "schedule": schedule},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps * 2 * 3,
+        # per batch: k_prepare (the fast pass's set-up and the conditioning), the fast
+        # pass, the resume pass and k_finish; two batches per step
+        "gpu_launches": args.steps * 2 * 4,
         "roofline": roof,
         "counters": cnt,
         "clocks": clocks.summary(),

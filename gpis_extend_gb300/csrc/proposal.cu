@@ -315,6 +315,13 @@ __global__ void k_adam(float *p, const float *g, float *m1, float *m2, int n, fl
     pb[i] = __float2bfloat16_rn(v);
 }
 
+// out = o + bias over the 32 outputs of n flights
+__global__ void k_add_bias(const float *o, const float *bias, uint32_t n, float *out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n * NOUT) out[i] = o[i] + bias[i % NOUT];
+}
+
 __global__ void k_to_bf16(const float *p, int n, bf *pb)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -489,7 +496,7 @@ __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *para
     const long row0 = tile * 16;
     const long ra = min(row0 + gi, (long)n - 1), rb = min(row0 + gi + 8, (long)n - 1);
     const float *fa = feat + ra * NFEAT, *fb = feat + rb * NFEAT;
-    const float *bih = sb, *bhh = sb + 3 * HID, *b1 = sb + 6 * HID, *b2 = b1 + WID, *b3 = b2 + WID, *b4 = b3 + WID;
+    const float *b1 = sb + 6 * HID, *b2 = b1 + WID, *b3 = b2 + WID, *b4 = b3 + WID;
     // GRU
     float h[4][4];
 #pragma unroll
@@ -832,16 +839,9 @@ int gpis_proposal_forward(gpis_proposal *p, const float *features, uint32_t n, f
     if (rc) return rc;
     if (!outputs) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
     forward(p, features, n, p->stream);
-    // add the output bias the loss kernel adds in place
-    std::vector<float> b(NOUT);
-    PTRY(cudaMemcpyAsync(b.data(), p->p + O_B4, NOUT * sizeof(float), cudaMemcpyDeviceToHost, p->stream), "read bias");
-    PTRY(cudaMemcpyAsync(outputs, p->o, (size_t)n * NOUT * sizeof(float), cudaMemcpyDeviceToDevice, p->stream),
-         "copy outputs");
+    // the output bias (the loss kernel adds it in place during training)
+    k_add_bias<<<nb((size_t)n * NOUT), 256, 0, p->stream>>>(p->o, p->p + O_B4, n, outputs);
     PTRY(cudaStreamSynchronize(p->stream), "proposal forward");
-    std::vector<float> h((size_t)n * NOUT);
-    PTRY(cudaMemcpy(h.data(), outputs, h.size() * sizeof(float), cudaMemcpyDeviceToHost), "read outputs");
-    for (size_t i = 0; i < h.size(); ++i) h[i] += b[i % NOUT];
-    PTRY(cudaMemcpy(outputs, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice), "write outputs");
     PTRY(cudaGetLastError(), "proposal forward kernels");
     return GPIS_OK;
 }
