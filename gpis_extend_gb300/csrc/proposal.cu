@@ -26,6 +26,7 @@
 #include "../../include/gpis.h"
 #include "device_common.cuh"
 #include "flights.cuh"
+#include "umma.cuh"
 
 extern "C" int gpis_internal_set_error(int code, const char *msg);
 
@@ -604,6 +605,54 @@ __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *para
     }
 }
 
+// ---- tcgen05 self-check --------------------------------------------------------------
+// D[128 x N] = A[128 x K] B[N x K]^T through the tensor-memory path, one CTA: the
+// operands staged in the K-major no-swizzle layout, K / 16 MMAs issued by one
+// thread, completion on an mbarrier (bounded wait: err = 1 on time-out), the
+// accumulator read back by the four warps (32 rows each).  N % 32 == 0, N <= 128,
+// K % 16 == 0.
+__global__ void __launch_bounds__(128) k_tc_gemm_check(const bf *A, const bf *B, uint32_t N, uint32_t K, float *D,
+                                                        uint32_t *err)
+{
+    extern __shared__ __align__(128) unsigned char tc_smem[];
+    bf *sa = reinterpret_cast<bf *>(tc_smem);
+    bf *sbm = reinterpret_cast<bf *>(tc_smem + 128u * K * 2u);
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t i = tid; i < 128u * K; i += 128u) sa[umma::tile_offset(i / K, i % K, K) / 2] = A[i];
+    for (uint32_t i = tid; i < N * K; i += 128u) sbm[umma::tile_offset(i / K, i % K, K) / 2] = B[i];
+    if (tid == 0) umma::bar_init(&bar, 1);
+    if (tid < 32) umma::tmem_alloc(&tslot, 128);
+    umma::fence_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tslot;
+    if (tid == 0) {
+        for (uint32_t kb = 0; kb < K / 16; ++kb)
+            umma::mma(tmem, umma::tile_desc(sa, 0, kb, K), umma::tile_desc(sbm, 0, kb, K), umma::idesc_bf16_m128(N),
+                      kb > 0);
+        umma::commit(&bar);
+    }
+    const bool ok = umma::bar_wait(&bar, 0, 1u << 24);
+    umma::fence_after_sync();
+    if (ok) {
+        const uint32_t w = tid >> 5;
+        for (uint32_t c0 = 0; c0 < N; c0 += 32) {
+            float v[32];
+            umma::ld32(tmem + ((w * 32u) << 16) + c0, v);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) D[(size_t)tid * N + c0 + i] = v[i];
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1u);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (tid < 32) umma::tmem_free(tmem, 128);
+}
+
 }  // namespace prop
 }  // namespace gpis
 
@@ -884,6 +933,38 @@ int gpis_proposal_train_step(gpis_proposal *p, const float *features, const floa
         *loss = l / (float)n;
     }
     return GPIS_OK;
+}
+
+int gpis_debug_tc_gemm(const uint16_t *a_bf16, const uint16_t *b_bf16, uint32_t n, uint32_t k, float *d)
+{
+    if (!a_bf16 || !b_bf16 || !d) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    if (n == 0 || n > 128 || n % 32 || k == 0 || k > 128 || k % 16)
+        return gpis_internal_set_error(GPIS_EINVAL, "n must be a multiple of 32 up to 128, k of 16 up to 128");
+    void *da = nullptr, *db = nullptr, *dd = nullptr, *de = nullptr;
+    const size_t sa = 128u * k * 2u, sbb = (size_t)n * k * 2u, sd = 128u * n * 4u;
+    int rc = GPIS_OK;
+    if (cudaMalloc(&da, sa) != cudaSuccess || cudaMalloc(&db, sbb) != cudaSuccess || cudaMalloc(&dd, sd) != cudaSuccess ||
+        cudaMalloc(&de, 4) != cudaSuccess) {
+        rc = gpis_internal_set_error(GPIS_ENOMEM, "allocate check buffers");
+    } else {
+        cudaMemcpy(da, a_bf16, sa, cudaMemcpyHostToDevice);
+        cudaMemcpy(db, b_bf16, sbb, cudaMemcpyHostToDevice);
+        cudaMemset(de, 0, 4);
+        cudaFuncSetAttribute(k_tc_gemm_check, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sa + sbb));
+        k_tc_gemm_check<<<1, 128, sa + sbb>>>(static_cast<const bf *>(da), static_cast<const bf *>(db), n, k,
+                                              static_cast<float *>(dd), static_cast<uint32_t *>(de));
+        uint32_t err = 0;
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) e = cudaMemcpy(&err, de, 4, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(d, dd, sd, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = cfail(e, "tensor-core check");
+        else if (err) rc = gpis_internal_set_error(GPIS_EIO, "tensor-core check: MMA completion wait timed out");
+    }
+    cudaFree(da);
+    cudaFree(db);
+    cudaFree(dd);
+    cudaFree(de);
+    return rc;
 }
 
 int gpis_proposal_infer(gpis_proposal *p, const gpis_flight_soa *in, const float *features, float *intervals,

@@ -257,6 +257,19 @@ def debug_cells_3d(cells, seeds, impulses, order=0):
     return pos.cpu().numpy().reshape(n, impulses, 3), w.cpu().numpy().reshape(n, impulses)
 
 
+def debug_tc_gemm(a_bf16, b_bf16):
+    """D = A B^T on the tcgen05 path: A (128, K) and B (N, K) as uint16 BF16 bit
+    patterns; returns D (128, N) float32."""
+    lib = abi.load_library()
+    a = np.ascontiguousarray(a_bf16, np.uint16)
+    b = np.ascontiguousarray(b_bf16, np.uint16)
+    assert a.shape[0] == 128 and a.shape[1] == b.shape[1]
+    n, k = b.shape
+    d = np.zeros((128, n), np.float32)
+    abi.check(lib.gpis_debug_tc_gemm(a.ctypes.data, b.ctypes.data, n, k, d.ctypes.data), "gpis_debug_tc_gemm")
+    return d
+
+
 def se_splat_1d(q, c, scale):
     torch = _torch()
     lib = abi.load_library()

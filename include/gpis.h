@@ -495,6 +495,11 @@ int gpis_flights_submit_proposed(gpis_ctx *ctx, const gpis_flight_soa *in, const
 int gpis_render_batch_proposed(gpis_ctx *ctx, gpis_proposal *prop, const gpis_scene_desc *scenes,
                                uint32_t n_scenes, float *const *images, gpis_render_stats *stats);
 
+/* Tensor-core self-check: d[128 x n] = a[128 x k] * b[n x k]^T with BF16 inputs
+ * (row-major bit patterns) through the tcgen05 / tensor-memory path the proposal
+ * kernels use.  n a multiple of 32 up to 128, k of 16 up to 128.  Blocking.   */
+int gpis_debug_tc_gemm(const uint16_t *a_bf16, const uint16_t *b_bf16, uint32_t n, uint32_t k, float *d);
+
 /* Last error message of the calling thread ("" when none). */
 const char *gpis_last_error(void);
 

@@ -25,6 +25,27 @@ def random_targets(n, rng):
     return np.stack([rng.uniform(0.02, 0.98, n), (rng.random(n) < 0.7).astype(np.float64)], axis=1).astype(np.float32)
 
 
+def _bf16_bits(x):
+    """Round float32 to BF16 (nearest even); the bit patterns and their values."""
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+    return u, (u.astype(np.uint32) << 16).view(np.float32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,k", [(32, 16), (64, 32), (128, 128), (96, 48)])
+def test_gpu_tensor_core_gemm_check(gpu, n, k):
+    """The tcgen05 path (operand layout, descriptors, tensor-memory read-back)
+    against an FP64 product of the same BF16 operands; FP32 accumulation."""
+    from gpis_extend_gb300 import runtime
+    rng = np.random.default_rng(n * 1000 + k)
+    ab, av = _bf16_bits(rng.normal(size=(128, k)))
+    bb, bv = _bf16_bits(rng.normal(size=(n, k)))
+    d = runtime.debug_tc_gemm(ab, bb)
+    want = av.astype(np.float64) @ bv.astype(np.float64).T
+    assert np.abs(d - want).max() < 1e-4 * np.sqrt(k) * 4
+
+
 def test_reference_backward_matches_finite_differences(monkeypatch):
     monkeypatch.setattr(R, "bf16", lambda x: np.asarray(x, np.float64))
     rng = np.random.default_rng(0)
