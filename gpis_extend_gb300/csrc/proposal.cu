@@ -605,6 +605,269 @@ __global__ void __launch_bounds__(128) k_propose(const bf *wb, const float *para
     }
 }
 
+// ---- fused inference on the tensor-memory path ------------------------------------------
+// Each group of four warps walks 128-flight tiles: thread = flight = accumulator row.
+// One GRU step is one N = 128, K = 48 product of the operand [bf16(h_{j-1}) | x_j | 0]
+// with the gate matrix G, whose 128 rows are r, z (hidden and input weights side by
+// side, so the product sums both parts), the input part of n (hidden columns zero) and
+// the hidden part of n (input columns zero); the accumulator's four 32-column blocks
+// are those pre-activations.  The MLP layers are N = 64, 64, 64, 32 products.  One
+// thread of the group issues the MMAs; their completion arrives on the group's
+// mbarrier, the epilogues (gates, GELU, the dominant component) read the accumulator
+// rows with tcgen05.ld and write the next operand into shared memory.
+//
+// The GRU biases and the first layer's bias ride in the products: operand columns 34,
+// 35 (GRU) and 40, 41 (first layer) hold 1.0, and the matching weight columns the
+// bias split into two BF16 parts, hi = bf16(b) and lo = bf16(b - hi) (16 significant
+// bits; those weight columns multiply zero inputs in the network, which has two
+// inputs per step and 40 MLP inputs).  The other layers' biases are FP32 in shared memory.
+constexpr int TC_KG = 48;  // GRU / first-layer operand width: 32 hidden + 16 input columns
+constexpr uint32_t TC_GB = 0, TC_W1 = TC_GB + 128 * TC_KG * 2, TC_W2 = TC_W1 + WID * MLPIN * 2,
+                   TC_W3 = TC_W2 + WID * WID * 2, TC_W4 = TC_W3 + WID * WID * 2, TC_WEND = TC_W4 + NOUT * WID * 2,
+                   TC_A = 128 * TC_KG * 2, TC_Y = 128 * WID * 2, TC_GROUP = TC_A + TC_Y, TC_BIAS = (3 * WID + NOUT) * 4;
+constexpr uint32_t tc_smem_bytes(int groups) { return TC_WEND + groups * TC_GROUP + TC_BIAS; }
+constexpr uint32_t kTcWaitLimit = 1u << 22;
+
+// the operand row chunk of 8 BF16 columns starting at column 8 kb of row `row`
+__device__ __forceinline__ void put_chunk(unsigned char *tile, uint32_t row, uint32_t kb, uint32_t kdim, uint4 v)
+{
+    *reinterpret_cast<uint4 *>(tile + umma::tile_offset(row, kb * 8u, kdim)) = v;
+}
+
+// generic-proxy writes -> tensor core; group barrier; the group's first thread issues
+// D = A B^T (K / 16 MMAs) and commits to `bar`; every thread waits (bounded) and the
+// group agrees on the outcome, so that a time-out ends the tile loop of all 128
+// threads together (false, `fail` set, `phase` left at the outstanding commit)
+__device__ __forceinline__ bool tc_round(uint32_t gid, bool leader, uint32_t tmem, const unsigned char *a,
+                                         const unsigned char *b, uint32_t kdim, uint32_t n, uint64_t *bar,
+                                         uint32_t &phase, bool &fail)
+{
+    umma::fence_async_smem();
+    umma::fence_before_sync();
+    umma::sync_or(1 + gid, 128, false);
+    umma::fence_after_sync();
+    if (leader) {
+        for (uint32_t kb = 0; kb < kdim / 16; ++kb)
+            umma::mma(tmem, umma::tile_desc(a, 0, kb, kdim), umma::tile_desc(b, 0, kb, kdim),
+                      umma::idesc_bf16_m128(n), kb > 0);
+        umma::commit(bar);
+    }
+    const bool done = umma::bar_wait(bar, phase, kTcWaitLimit);
+    if (umma::sync_or(1 + gid, 128, !done)) {
+        fail = true;
+        return false;
+    }
+    phase ^= 1u;
+    umma::fence_after_sync();
+    return true;
+}
+
+// four FP32 values of shared memory; volatile, so that the loads stay in the loop
+// (hoisted out of the tile loop, the biases would take 224 registers)
+__device__ __forceinline__ float4 lds4(const float *p)
+{
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(umma::smem_u32(p)));
+    return v;
+}
+
+// GELU of 64 accumulator columns (+ bias from shared memory, or none: the bias is in the
+// product) into the next operand (K = 64)
+__device__ __forceinline__ void tc_gelu64(uint32_t t, const float *bias, unsigned char *y, uint32_t row)
+{
+#pragma unroll
+    for (uint32_t c0 = 0; c0 < 64; c0 += 32) {
+        float v[32];
+        umma::ld32(t + c0, v);
+        if (bias) {
+#pragma unroll
+            for (uint32_t c = 0; c < 32; c += 4) {
+                const float4 b = lds4(bias + c0 + c);
+                v[c] += b.x;
+                v[c + 1] += b.y;
+                v[c + 2] += b.z;
+                v[c + 3] += b.w;
+            }
+        }
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q) {
+            uint32_t w[4];
+#pragma unroll
+            for (uint32_t e = 0; e < 4; ++e) {
+                const uint32_t c = q * 8 + 2 * e;
+                w[e] = pack2f(gelu_fast(v[c]), gelu_fast(v[c + 1]));
+            }
+            put_chunk(y, row, c0 / 8 + q, WID, make_uint4(w[0], w[1], w[2], w[3]));
+        }
+    }
+}
+
+// the two BF16 parts of a bias, hi = bf16(b) and lo = bf16(b - hi)
+__device__ __forceinline__ bf bias_part(float b, uint32_t part)
+{
+    const bf hi = __float2bfloat16_rn(b);
+    return part ? __float2bfloat16_rn(b - __bfloat162float(hi)) : hi;
+}
+
+template <int GROUPS>
+__global__ void __launch_bounds__(128 * GROUPS, GROUPS == 1 ? 3 : 2) k_propose_tc(const bf *wb, const float *params,
+                                                                         const float *feat, const float4 *on,
+                                                                         const float4 *df, uint32_t n_cap,
+                                                                         const uint32_t *n_dev, float4 *out,
+                                                                         uint32_t *err)
+{
+    extern __shared__ __align__(128) unsigned char tsm[];
+    __shared__ __align__(8) uint64_t bars[GROUPS];
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x, gid = tid >> 7, row = tid & 127u;
+    unsigned char *gsh = tsm + TC_GB, *w1 = tsm + TC_W1, *w2 = tsm + TC_W2, *w3 = tsm + TC_W3, *w4 = tsm + TC_W4;
+    unsigned char *A = tsm + TC_WEND + gid * TC_GROUP, *Y = A + TC_A;
+    float *bm = reinterpret_cast<float *>(tsm + TC_WEND + GROUPS * TC_GROUP);  // b2, b3 (64), b4 (32)
+    // gate matrix: rows r (0..31), z (32..63), n input (64..95), n hidden (96..127);
+    // columns 0..31 hidden weights, 32, 33 input weights, 34, 35 the bias parts
+    const bf zero = __float2bfloat16_rn(0.0f);
+    for (uint32_t i = tid; i < 128u * TC_KG; i += blockDim.x) {
+        const uint32_t r = i / TC_KG, k = i % TC_KG, g = r >> 5, u = r & 31u;
+        bf v = zero;
+        if (k < HID) {
+            if (g != 2) v = wb[O_WHH + ((g == 3 ? 2u : g) * HID + u) * HID + k];
+        } else if (k < HID + 2) {
+            if (g != 3) v = wb[O_WIH + (g * HID + u) * NIN + (k - HID)];
+        } else if (k < HID + 4) {
+            const float b = g < 2 ? params[O_BIH + g * HID + u] + params[O_BHH + g * HID + u]
+                                  : (g == 2 ? params[O_BIH + 2 * HID + u] : params[O_BHH + 2 * HID + u]);
+            v = bias_part(b, k - HID - 2);
+        }
+        *reinterpret_cast<bf *>(gsh + umma::tile_offset(r, k, TC_KG)) = v;
+    }
+    // first layer: columns 0..39 weights, 40, 41 the bias parts, 42..47 zero
+    for (uint32_t i = tid; i < WID * MLPIN; i += blockDim.x) {
+        const uint32_t r = i / MLPIN, k = i % MLPIN;
+        const bf v = k < 40 ? wb[O_W1 + i] : (k < 42 ? bias_part(params[O_B1 + r], k - 40) : zero);
+        *reinterpret_cast<bf *>(w1 + umma::tile_offset(r, k, MLPIN)) = v;
+    }
+    for (uint32_t i = tid; i < WID * WID; i += blockDim.x) {
+        *reinterpret_cast<bf *>(w2 + umma::tile_offset(i / WID, i % WID, WID)) = wb[O_W2 + i];
+        *reinterpret_cast<bf *>(w3 + umma::tile_offset(i / WID, i % WID, WID)) = wb[O_W3 + i];
+    }
+    for (uint32_t i = tid; i < NOUT * WID; i += blockDim.x)
+        *reinterpret_cast<bf *>(w4 + umma::tile_offset(i / WID, i % WID, WID)) = wb[O_W4 + i];
+    for (uint32_t k = tid; k < WID; k += blockDim.x) {
+        bm[k] = params[O_B2 + k];
+        bm[WID + k] = params[O_B3 + k];
+    }
+    for (uint32_t k = tid; k < NOUT; k += blockDim.x) bm[2 * WID + k] = params[O_B4 + k];
+    // operand columns 40..47: (1, 1, 0 ..) for every product (the GRU's weight columns
+    // there are zero)
+    const uint32_t one2 = pack2f(1.0f, 1.0f);
+    put_chunk(A, row, 5, TC_KG, make_uint4(one2, 0u, 0u, 0u));
+    if (tid < GROUPS) umma::bar_init(&bars[tid], 1);
+    if (tid < 32) umma::tmem_alloc(&tslot, 128 * GROUPS);
+    umma::fence_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tslot + gid * 128u + (((tid >> 5) & 3u) << 21);  // lanes 32 (warp % 4) ..
+    const bool leader = row == 0;
+    uint64_t *bar = &bars[gid];
+    const uint32_t n = n_dev ? min(*n_dev, n_cap) : n_cap;
+    const uint32_t tiles = (n + 127u) / 128u;
+    uint32_t phase = 0;
+    bool fail = false;
+    for (uint32_t tile = blockIdx.x * GROUPS + gid; tile < tiles; tile += gridDim.x * GROUPS) {
+        const uint32_t r = tile * 128u + row;
+        const float *fr = feat + (size_t)min(r, n - 1) * NFEAT;
+        float h[HID];
+#pragma unroll
+        for (int u = 0; u < HID; ++u) h[u] = 0.0f;
+        bool ok = true;
+#pragma unroll 1
+        for (int j = 0; j < NHIST && ok; ++j) {
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q)
+                put_chunk(A, row, q, TC_KG,
+                          make_uint4(pack2f(h[8 * q], h[8 * q + 1]), pack2f(h[8 * q + 2], h[8 * q + 3]),
+                                     pack2f(h[8 * q + 4], h[8 * q + 5]), pack2f(h[8 * q + 6], h[8 * q + 7])));
+            const float2 x = reinterpret_cast<const float2 *>(fr)[j];
+            put_chunk(A, row, 4, TC_KG, make_uint4(pack2f(x.x, x.y), one2, 0u, 0u));
+            ok = tc_round(gid, leader, tmem, A, gsh, TC_KG, 128, bar, phase, fail);
+            if (!ok) break;
+#pragma unroll
+            for (uint32_t c0 = 0; c0 < HID; c0 += 8) {
+                float v[32];
+                umma::ld4x8(tmem + c0, tmem + 32 + c0, tmem + 64 + c0, tmem + 96 + c0, v);
+#pragma unroll
+                for (uint32_t i = 0; i < 8; ++i) {
+                    const float rg = sigm_fast(v[i]);
+                    const float zg = sigm_fast(v[8 + i]);
+                    const float nn = tanh_fast(fmaf(rg, v[24 + i], v[16 + i]));
+                    h[c0 + i] = fmaf(zg, h[c0 + i] - nn, nn);
+                }
+            }
+        }
+        if (!ok) break;
+        // MLP input: [h | globals | 0]
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q)
+            put_chunk(A, row, q, TC_KG,
+                      make_uint4(pack2f(h[8 * q], h[8 * q + 1]), pack2f(h[8 * q + 2], h[8 * q + 3]),
+                                 pack2f(h[8 * q + 4], h[8 * q + 5]), pack2f(h[8 * q + 6], h[8 * q + 7])));
+        const float4 g0 = reinterpret_cast<const float4 *>(fr)[4], g1 = reinterpret_cast<const float4 *>(fr)[5];
+        put_chunk(A, row, 4, TC_KG,
+                  make_uint4(pack2f(g0.x, g0.y), pack2f(g0.z, g0.w), pack2f(g1.x, g1.y), pack2f(g1.z, g1.w)));
+        if (!tc_round(gid, leader, tmem, A, w1, MLPIN, WID, bar, phase, fail)) break;
+        tc_gelu64(tmem, nullptr, Y, row);
+        if (!tc_round(gid, leader, tmem, Y, w2, WID, WID, bar, phase, fail)) break;
+        tc_gelu64(tmem, bm, Y, row);
+        if (!tc_round(gid, leader, tmem, Y, w3, WID, WID, bar, phase, fail)) break;
+        tc_gelu64(tmem, bm + WID, Y, row);
+        if (!tc_round(gid, leader, tmem, Y, w4, WID, NOUT, bar, phase, fail)) break;
+        float o[32];
+        umma::ld32(tmem, o);
+#pragma unroll
+        for (int c = 0; c < 28; c += 4) {
+            const float4 b = lds4(bm + 2 * WID + c);
+            o[c] += b.x;
+            o[c + 1] += b.y;
+            o[c + 2] += b.z;
+            o[c + 3] += b.w;
+        }
+        // the dominant component: the first of the largest logits
+        float best = -INFINITY, mlog = 0.0f, slog = 0.0f;
+        bool found = false;
+#pragma unroll
+        for (int k = 0; k < NCOMP; ++k) {
+            if (o[k] > best) {
+                best = o[k];
+                found = true;
+                mlog = o[8 + k];
+                slog = o[16 + k];
+            }
+        }
+        const float bmean = found ? sigm(mlog) : 0.0f;
+        const float bs = found ? softplus(slog) + 1e-3f : 1.0f;
+        const float q = sigm(o[24]);
+        if (r < n) {
+            const float4 a = on[r], b = df[r];
+            const float tm = b.w - a.w;
+            const float ua = fminf(fmaxf(bmean - 3.0f * bs, 0.0f), 1.0f);
+            const float ub = fminf(fmaxf(bmean + 3.0f * bs, 0.0f), 1.0f);
+            out[r] = make_float4(a.w + ua * tm, a.w + ub * tm, q, bmean);
+        }
+    }
+    // a group that gave up waits once more (bounded) for the MMAs it committed before
+    // the tensor memory is released
+    if (fail) {
+        if (leader) atomicExch(err, 1u);
+        umma::bar_wait(bar, phase, kTcWaitLimit);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (tid < 32) umma::tmem_free(tslot, 128 * GROUPS);
+}
+
 // ---- tcgen05 self-check --------------------------------------------------------------
 // D[128 x N] = A[128 x K] B[N x K]^T through the tensor-memory path, one CTA: the
 // operands staged in the K-major no-swizzle layout, K / 16 MMAs issued by one
@@ -672,6 +935,11 @@ struct gpis_proposal {
     float *h = nullptr, *gi = nullptr, *gh = nullptr, *r = nullptr, *z = nullptr, *nn = nullptr, *ghn = nullptr,
           *a1 = nullptr, *a2 = nullptr, *a3 = nullptr, *o = nullptr, *dof = nullptr, *dy = nullptr, *daf = nullptr,
           *du = nullptr, *dgif = nullptr, *dghf = nullptr, *dh = nullptr, *loss = nullptr;
+    // fused inference: GPIS_PROPOSAL_KERNEL_*, resident blocks per SM of each form, and
+    // the tensor-memory kernel's time-out flag (host-mapped, read by the next call)
+    int kernel = GPIS_PROPOSAL_KERNEL_TC2;
+    int sms = 1, per_sm_tc1 = 1, per_sm_tc2 = 1, per_sm_mma = 1;
+    uint32_t *tc_err_host = nullptr, *tc_err_dev = nullptr;
 };
 
 namespace {
@@ -808,6 +1076,38 @@ void backward(gpis_proposal *p, const float2 *tgt, uint32_t n, cudaStream_t s)
     }
 }
 
+// The fused inference launch: the tensor-memory kernel (two 128-flight groups or one
+// per block) unless the proposal selects the warp-MMA kernel or the features are not
+// 16-byte aligned (the tensor-memory kernel reads feature rows as float4).  A time-out
+// recorded by an earlier tensor-memory launch is reported here.
+int launch_infer(gpis_proposal *p, const gpis_flight_soa *in, const float *features, float *intervals, uint32_t cap,
+                 const uint32_t *n_dev, cudaStream_t s)
+{
+    if (*p->tc_err_host) {
+        *p->tc_err_host = 0;
+        return gpis_internal_set_error(GPIS_EIO, "proposal inference: tensor-core completion wait timed out");
+    }
+    const float4 *on = reinterpret_cast<const float4 *>(in->origin_near);
+    const float4 *df = reinterpret_cast<const float4 *>(in->dir_far);
+    float4 *out = reinterpret_cast<float4 *>(intervals);
+    int kernel = p->kernel;
+    if (reinterpret_cast<uintptr_t>(features) & 15u) kernel = GPIS_PROPOSAL_KERNEL_MMA;
+    if (kernel == GPIS_PROPOSAL_KERNEL_MMA) {
+        const unsigned blocks = (unsigned)std::min<long>(((long)cap + 63) / 64, (long)p->sms * p->per_sm_mma);
+        k_propose<<<blocks, 128, 0, s>>>(p->pb, p->p, features, on, df, cap, n_dev, out);
+    } else if (kernel == GPIS_PROPOSAL_KERNEL_TC1) {
+        const unsigned blocks = (unsigned)std::min<long>(((long)cap + 127) / 128, (long)p->sms * p->per_sm_tc1);
+        k_propose_tc<1><<<blocks, 128, tc_smem_bytes(1), s>>>(p->pb, p->p, features, on, df, cap, n_dev, out,
+                                                              p->tc_err_dev);
+    } else {
+        const unsigned blocks = (unsigned)std::min<long>(((long)cap + 255) / 256, (long)p->sms * p->per_sm_tc2);
+        k_propose_tc<2><<<blocks, 256, tc_smem_bytes(2), s>>>(p->pb, p->p, features, on, df, cap, n_dev, out,
+                                                              p->tc_err_dev);
+    }
+    PTRY(cudaGetLastError(), "proposal inference kernel");
+    return GPIS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -817,6 +1117,7 @@ uint32_t gpis_proposal_n_params(void) { return (uint32_t)N_PARAMS; }
 void gpis_proposal_destroy(gpis_proposal *p)
 {
     if (!p) return;
+    if (p->tc_err_host) cudaFreeHost(p->tc_err_host);
     for (void *v : p->act) cudaFree(v);
     cudaFree(p->p);
     cudaFree(p->g);
@@ -852,6 +1153,30 @@ int gpis_proposal_create(const float *params, gpis_proposal **out)
         cudaMalloc(&p->pb, N_PARAMS * sizeof(bf)) != cudaSuccess) {
         gpis_proposal_destroy(p);
         return gpis_internal_set_error(GPIS_ENOMEM, "allocate proposal parameters");
+    }
+    if (cudaHostAlloc(reinterpret_cast<void **>(&p->tc_err_host), sizeof(uint32_t), cudaHostAllocMapped) !=
+            cudaSuccess ||
+        cudaHostGetDevicePointer(reinterpret_cast<void **>(&p->tc_err_dev), p->tc_err_host, 0) != cudaSuccess) {
+        gpis_proposal_destroy(p);
+        return gpis_internal_set_error(GPIS_ENOMEM, "allocate proposal status flag");
+    }
+    *p->tc_err_host = 0;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(k_propose_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(1));
+        cudaFuncSetAttribute(k_propose_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(2));
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->per_sm_tc1, k_propose_tc<1>, 128, tc_smem_bytes(1)) !=
+                cudaSuccess || p->per_sm_tc1 < 1)
+            p->per_sm_tc1 = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->per_sm_tc2, k_propose_tc<2>, 256, tc_smem_bytes(2)) !=
+                cudaSuccess || p->per_sm_tc2 < 1)
+            p->per_sm_tc2 = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->per_sm_mma, k_propose, 128, 0) != cudaSuccess ||
+            p->per_sm_mma < 1)
+            p->per_sm_mma = 1;
+        cudaGetLastError();
     }
     std::vector<float> zero;
     if (!params) {
@@ -967,6 +1292,15 @@ int gpis_debug_tc_gemm(const uint16_t *a_bf16, const uint16_t *b_bf16, uint32_t 
     return rc;
 }
 
+int gpis_proposal_set_kernel(gpis_proposal *p, int kernel)
+{
+    if (!p) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    if (kernel != GPIS_PROPOSAL_KERNEL_TC2 && kernel != GPIS_PROPOSAL_KERNEL_TC1 && kernel != GPIS_PROPOSAL_KERNEL_MMA)
+        return gpis_internal_set_error(GPIS_EINVAL, "unknown proposal kernel");
+    p->kernel = kernel;
+    return GPIS_OK;
+}
+
 int gpis_proposal_infer(gpis_proposal *p, const gpis_flight_soa *in, const float *features, float *intervals,
                         uint32_t n, void *cuda_stream)
 {
@@ -980,17 +1314,7 @@ int gpis_proposal_infer(gpis_proposal *p, const gpis_flight_soa *in, const float
     cudaEventRecord(ev, p->stream);
     cudaStreamWaitEvent(s, ev, 0);
     cudaEventDestroy(ev);
-    int dev = 0, sms = 1, per_sm = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_propose, 128, 0) != cudaSuccess || per_sm < 1)
-        per_sm = 1;
-    const unsigned blocks = (unsigned)std::min<long>(((long)n + 63) / 64, (long)sms * per_sm);
-    k_propose<<<blocks, 128, 0, s>>>(p->pb, p->p, features, reinterpret_cast<const float4 *>(in->origin_near),
-                                     reinterpret_cast<const float4 *>(in->dir_far), n, nullptr,
-                                     reinterpret_cast<float4 *>(intervals));
-    PTRY(cudaGetLastError(), "proposal inference kernel");
-    return GPIS_OK;
+    return launch_infer(p, in, features, intervals, n, nullptr, s);
 }
 
 // Inference on a batch whose live count is in device memory (the path tracer's
@@ -1002,17 +1326,7 @@ __attribute__((visibility("hidden"))) int gpis_internal_infer_live(gpis_proposal
 {
     if (!p || !in || !features || !intervals || !n_dev) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
     if (cap == 0) return GPIS_OK;
-    int dev = 0, sms = 1, per_sm = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_propose, 128, 0) != cudaSuccess || per_sm < 1)
-        per_sm = 1;
-    const unsigned blocks = (unsigned)std::min<long>(((long)cap + 63) / 64, (long)sms * per_sm);
-    k_propose<<<blocks, 128, 0, static_cast<cudaStream_t>(cuda_stream)>>>(
-        p->pb, p->p, features, reinterpret_cast<const float4 *>(in->origin_near),
-        reinterpret_cast<const float4 *>(in->dir_far), cap, n_dev, reinterpret_cast<float4 *>(intervals));
-    PTRY(cudaGetLastError(), "proposal inference kernel");
-    return GPIS_OK;
+    return launch_infer(p, in, features, intervals, cap, n_dev, static_cast<cudaStream_t>(cuda_stream));
 }
 
 __attribute__((visibility("hidden"))) int gpis_internal_proposal_quiesce(gpis_proposal *p)

@@ -342,6 +342,11 @@ class Proposal:
                   "gpis_proposal_forward")
         return out
 
+    def set_kernel(self, kernel):
+        """The fused inference kernel: "tc2" (tcgen05, two 128-flight tiles per block),
+        "tc1" (one tile per block) or "mma" (warp-level mma.sync)."""
+        abi.check(self.lib.gpis_proposal_set_kernel(self.h, abi.PROPOSAL_KERNELS[kernel]), "gpis_proposal_set_kernel")
+
     def infer(self, dev, feats, stream=None, out=None):
         torch = _torch()
         s = stream if stream is not None else torch.cuda.current_stream()

@@ -483,9 +483,17 @@ int gpis_proposal_gradient(gpis_proposal *prop, const float *features, const flo
 int gpis_proposal_forward(gpis_proposal *prop, const float *features, uint32_t n, float *outputs);
 /* Fused inference (asynchronous, device pointers): per flight the dominant
  * component's interval [m - 3s, m + 3s] in t, the miss probability and m:
- * intervals[4 i .. 4 i + 3] = (t_a, t_b, q, m).                             */
+ * intervals[4 i .. 4 i + 3] = (t_a, t_b, q, m).  A time-out of the tensor
+ * cores' completion wait in an earlier call is returned as GPIS_EIO.        */
 int gpis_proposal_infer(gpis_proposal *prop, const gpis_flight_soa *in, const float *features, float *intervals,
                         uint32_t n, void *cuda_stream);
+/* The fused inference kernel: tcgen05 MMAs with tensor-memory accumulators, two
+ * 128-flight tiles per block (default) or one, or warp-level mma.sync (also
+ * taken when features is not 16-byte aligned).                              */
+#define GPIS_PROPOSAL_KERNEL_TC2 0
+#define GPIS_PROPOSAL_KERNEL_TC1 1
+#define GPIS_PROPOSAL_KERNEL_MMA 2
+int gpis_proposal_set_kernel(gpis_proposal *prop, int kernel);
 /* gpis_flights_submit with proposals: identical results; intervals from
  * gpis_proposal_infer (16-byte aligned).                                    */
 int gpis_flights_submit_proposed(gpis_ctx *ctx, const gpis_flight_soa *in, const float *intervals,

@@ -156,12 +156,16 @@ def test_gpu_adam_step_matches_reference(gpu):
 
 
 @pytest.mark.gpu
-def test_gpu_fused_inference_matches_unfused(gpu):
+@pytest.mark.parametrize("kernel", ["tc2", "tc1", "mma"])
+def test_gpu_fused_inference_matches_unfused(gpu, kernel):
+    """Each fused inference kernel (tcgen05 with two or one 128-flight tiles per
+    block, warp mma.sync) against the unfused BF16 forward."""
     torch, runtime = gpu
     desc = proposal.config2_medium()
     b = workloads.torus_flights(2048, desc)
     params = proposal.init_params(9)
     with runtime.Context(desc) as ctx, runtime.Proposal(params) as prop:
+        prop.set_kernel(kernel)
         dev = runtime.DeviceFlights(b)
         f = runtime.proposal_features(ctx, dev)
         iv = prop.infer(dev, f).cpu().numpy()
@@ -178,6 +182,37 @@ def test_gpu_fused_inference_matches_unfused(gpu):
     assert np.all(np.abs((iv[clear, 0] - near[clear]) / tm[clear] - ua[clear]) <= 2e-2)
     assert np.all(np.abs((iv[clear, 1] - near[clear]) / tm[clear] - ub[clear]) <= 2e-2)
     assert np.all(np.abs(iv[:, 2] - q) <= 1e-2)
+
+
+@pytest.mark.gpu
+def test_gpu_tensor_core_inference_tiles(gpu):
+    """The tcgen05 kernels with one and two tiles per block give the same bits; a
+    ragged batch (not a multiple of 128) gives the rows of the full batch; the
+    mma.sync kernel agrees to the BF16 rounding of the activations."""
+    torch, runtime = gpu
+    desc = proposal.config2_medium()
+    b = workloads.torus_flights(4096, desc, seed=5)
+    with runtime.Context(desc) as ctx, runtime.Proposal(proposal.init_params(4)) as prop:
+        dev = runtime.DeviceFlights(b)
+        f = runtime.proposal_features(ctx, dev)
+        got = {}
+        for k in ("tc2", "tc1", "mma"):
+            prop.set_kernel(k)
+            got[k] = prop.infer(dev, f).cpu().numpy()
+        prop.set_kernel("tc2")
+        part = runtime.DeviceFlights(b.subset(np.arange(1000)))
+        fp = f[:1000].contiguous()
+        ragged = prop.infer(part, fp).cpu().numpy()
+    assert np.array_equal(got["tc2"].view(np.uint32), got["tc1"].view(np.uint32))
+    assert np.array_equal(ragged.view(np.uint32), got["tc2"][:1000].view(np.uint32))
+    assert np.all(np.isfinite(got["tc2"]))
+    assert np.abs(got["tc2"][:, 2] - got["mma"][:, 2]).max() <= 1e-2
+    near, far = b.origin_near[:, 3], b.dir_far[:, 3]
+    m_tc = got["tc2"][:, 3]
+    m_mma = got["mma"][:, 3]
+    agree = np.abs(m_tc - m_mma) <= 2e-2
+    assert agree.mean() > 0.9
+    assert np.all((got["tc2"][:, 0] >= near - 1e-4) & (got["tc2"][:, 1] <= far + 1e-4))
 
 
 @pytest.mark.gpu
