@@ -275,6 +275,25 @@ def learned_arm(ctx, prop, batches, devs, steps, stream, plain_ms):
         b.record(stream)
         torch.cuda.synchronize()
         part[name] = a.elapsed_time(b)
+    # the fused inference alone with each of its kernels (the arm uses the default, tc2)
+    kernels = {}
+    for k in ("tc2", "tc1", "mma"):
+        kernels[k + "_blocks_per_sm"] = prop.occupancy(k)
+        prop.set_kernel(k)
+        for d, f, iv in zip(devs, feats, ivs):
+            prop.infer(d, f, stream, out=iv)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for d, f, iv in zip(devs, feats, ivs):
+            prop.infer(d, f, stream, out=iv)
+        b.record(stream)
+        torch.cuda.synchronize()
+        kernels[k] = a.elapsed_time(b)
+    prop.set_kernel("tc2")
+    for d, f, iv in zip(devs, feats, ivs):
+        prop.infer(d, f, stream, out=iv)
+    torch.cuda.synchronize()
     identical = all(torch.equal(p.view(torch.int32), d.rec.view(torch.int32)) for p, d in zip(plain, devs))
     inside, hits = 0.0, 0
     for b_, d, iv in zip(batches, devs, ivs):
@@ -285,7 +304,7 @@ def learned_arm(ctx, prop, batches, devs, steps, stream, plain_ms):
     value = n * steps / (ms * 1e-3)
     plain_value = n * steps / (plain_ms * 1e-3)
     return {"value": value, "unit": UNIT, "ms_per_step": ms / steps, "plain_value": plain_value,
-            "ratio_vs_plain": value / plain_value, "ms_per_part": part,
+            "ratio_vs_plain": value / plain_value, "ms_per_part": part, "inference_ms_by_kernel": kernels,
             "inside_interval": inside / max(1, hits), "miss_fallback_rate": 1.0 - inside / max(1, hits),
             "identical_to_plain": bool(identical),
             "equal_image_rmse": "every flight record equals the plain arm's bit for bit, so images and their "

@@ -388,6 +388,7 @@ def load_library(path=None):
         "gpis_debug_field": (c_int, [vp, vp, vp, vp, vp, vp, c_u32, vp]),
         "gpis_debug_tc_gemm": (c_int, [vp, vp, c_u32, c_u32, vp]),
         "gpis_proposal_set_kernel": (c_int, [vp, c_int]),
+        "gpis_proposal_occupancy": (c_int, [vp, c_int]),
         "gpis_se_splat_1d": (c_int, [vp, vp, vp, vp, ctypes.c_size_t, ctypes.c_float, vp]),
         "gpis_flights_submit_static": (c_int, [P(MediumDesc), P(FlightSoA), P(ResultSoA), c_u32, vp]),
         "gpis_medium_sample_distance": (c_int, [vp, c_u32, vp, vp, vp, vp, c_u32]),

@@ -1076,6 +1076,29 @@ void backward(gpis_proposal *p, const float2 *tgt, uint32_t n, cudaStream_t s)
     }
 }
 
+// Resident blocks per SM of a kernel with `dyn` bytes of dynamic shared memory (opted in
+// above 48 KB, with the shared-memory carveout at its maximum): the occupancy API's
+// answer, or, where it fails, the register and shared-memory limits from the kernel's
+// attributes; at least 1.
+int resident_blocks(const void *fn, int threads, uint32_t dyn, int dev)
+{
+    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    if (dyn > 48u * 1024u) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, dyn) != cudaSuccess || n < 1) {
+        cudaFuncAttributes a{};
+        int smem = 0, regs = 0;
+        cudaFuncGetAttributes(&a, fn);
+        cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&regs, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+        const long per_block = (long)dyn + (long)a.sharedSizeBytes + 1024;
+        const long by_regs = a.numRegs > 0 ? regs / ((long)a.numRegs * threads) : 1;
+        n = (int)std::min<long>(by_regs, smem / per_block);
+    }
+    cudaGetLastError();
+    return std::max(n, 1);
+}
+
 // The fused inference launch: the tensor-memory kernel (two 128-flight groups or one
 // per block) unless the proposal selects the warp-MMA kernel or the features are not
 // 16-byte aligned (the tensor-memory kernel reads feature rows as float4).  A time-out
@@ -1165,18 +1188,9 @@ int gpis_proposal_create(const float *params, gpis_proposal **out)
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_propose_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(1));
-        cudaFuncSetAttribute(k_propose_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(2));
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->per_sm_tc1, k_propose_tc<1>, 128, tc_smem_bytes(1)) !=
-                cudaSuccess || p->per_sm_tc1 < 1)
-            p->per_sm_tc1 = 1;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->per_sm_tc2, k_propose_tc<2>, 256, tc_smem_bytes(2)) !=
-                cudaSuccess || p->per_sm_tc2 < 1)
-            p->per_sm_tc2 = 1;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->per_sm_mma, k_propose, 128, 0) != cudaSuccess ||
-            p->per_sm_mma < 1)
-            p->per_sm_mma = 1;
-        cudaGetLastError();
+        p->per_sm_tc1 = resident_blocks(reinterpret_cast<const void *>(k_propose_tc<1>), 128, tc_smem_bytes(1), dev);
+        p->per_sm_tc2 = resident_blocks(reinterpret_cast<const void *>(k_propose_tc<2>), 256, tc_smem_bytes(2), dev);
+        p->per_sm_mma = resident_blocks(reinterpret_cast<const void *>(k_propose), 128, 0, dev);
     }
     std::vector<float> zero;
     if (!params) {
@@ -1299,6 +1313,15 @@ int gpis_proposal_set_kernel(gpis_proposal *p, int kernel)
         return gpis_internal_set_error(GPIS_EINVAL, "unknown proposal kernel");
     p->kernel = kernel;
     return GPIS_OK;
+}
+
+int gpis_proposal_occupancy(const gpis_proposal *p, int kernel)
+{
+    if (!p) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    if (kernel == GPIS_PROPOSAL_KERNEL_TC2) return p->per_sm_tc2;
+    if (kernel == GPIS_PROPOSAL_KERNEL_TC1) return p->per_sm_tc1;
+    if (kernel == GPIS_PROPOSAL_KERNEL_MMA) return p->per_sm_mma;
+    return gpis_internal_set_error(GPIS_EINVAL, "unknown proposal kernel");
 }
 
 int gpis_proposal_infer(gpis_proposal *p, const gpis_flight_soa *in, const float *features, float *intervals,

@@ -347,6 +347,12 @@ class Proposal:
         "tc1" (one tile per block) or "mma" (warp-level mma.sync)."""
         abi.check(self.lib.gpis_proposal_set_kernel(self.h, abi.PROPOSAL_KERNELS[kernel]), "gpis_proposal_set_kernel")
 
+    def occupancy(self, kernel):
+        """Resident blocks per SM of a fused inference kernel."""
+        n = int(self.lib.gpis_proposal_occupancy(self.h, abi.PROPOSAL_KERNELS[kernel]))
+        abi.check(min(n, 0), "gpis_proposal_occupancy")
+        return n
+
     def infer(self, dev, feats, stream=None, out=None):
         torch = _torch()
         s = stream if stream is not None else torch.cuda.current_stream()

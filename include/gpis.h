@@ -494,6 +494,9 @@ int gpis_proposal_infer(gpis_proposal *prop, const gpis_flight_soa *in, const fl
 #define GPIS_PROPOSAL_KERNEL_TC1 1
 #define GPIS_PROPOSAL_KERNEL_MMA 2
 int gpis_proposal_set_kernel(gpis_proposal *prop, int kernel);
+/* Resident blocks per SM of a fused inference kernel (its persistent grid is
+ * SMs x this); negative on error.                                           */
+int gpis_proposal_occupancy(const gpis_proposal *prop, int kernel);
 /* gpis_flights_submit with proposals: identical results; intervals from
  * gpis_proposal_infer (16-byte aligned).                                    */
 int gpis_flights_submit_proposed(gpis_ctx *ctx, const gpis_flight_soa *in, const float *intervals,
