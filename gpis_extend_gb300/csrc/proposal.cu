@@ -1077,23 +1077,32 @@ void backward(gpis_proposal *p, const float2 *tgt, uint32_t n, cudaStream_t s)
 }
 
 // Resident blocks per SM of a kernel with `dyn` bytes of dynamic shared memory (opted in
-// above 48 KB, with the shared-memory carveout at its maximum): the occupancy API's
-// answer, or, where it fails, the register and shared-memory limits from the kernel's
-// attributes; at least 1.
-int resident_blocks(const void *fn, int threads, uint32_t dyn, int dev)
+// above 48 KB, with the shared-memory carveout at its maximum); at least 1.  Kernels
+// without tensor memory take the occupancy API's answer.  For the tensor-memory
+// kernels the count follows from their resources: registers (allocated per warp in
+// units of 256), shared memory (1 KB reserved per block), threads, and the 512
+// tensor-memory columns of an SM (the occupancy API answers 1 for them, which would
+// leave half of the SM's register file and shared memory idle).
+int resident_blocks(const void *fn, int threads, uint32_t dyn, int dev, int tmem_cols)
 {
     cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
     if (dyn > 48u * 1024u) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, dyn) != cudaSuccess || n < 1) {
+    if (tmem_cols > 0 || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, dyn) != cudaSuccess ||
+        n < 1) {
         cudaFuncAttributes a{};
-        int smem = 0, regs = 0;
+        int smem = 0, regs = 0, max_threads = 0;
         cudaFuncGetAttributes(&a, fn);
         cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
         cudaDeviceGetAttribute(&regs, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&max_threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+        const long warps = (threads + 31) / 32;
+        const long per_warp = (((long)std::max(a.numRegs, 1) * 32 + 255) / 256) * 256;
         const long per_block = (long)dyn + (long)a.sharedSizeBytes + 1024;
-        const long by_regs = a.numRegs > 0 ? regs / ((long)a.numRegs * threads) : 1;
-        n = (int)std::min<long>(by_regs, smem / per_block);
+        long m = std::min<long>(regs / (per_warp * warps), smem / per_block);
+        m = std::min<long>(m, max_threads / threads);
+        if (tmem_cols > 0) m = std::min<long>(m, 512 / tmem_cols);
+        n = (int)m;
     }
     cudaGetLastError();
     return std::max(n, 1);
@@ -1188,9 +1197,11 @@ int gpis_proposal_create(const float *params, gpis_proposal **out)
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
-        p->per_sm_tc1 = resident_blocks(reinterpret_cast<const void *>(k_propose_tc<1>), 128, tc_smem_bytes(1), dev);
-        p->per_sm_tc2 = resident_blocks(reinterpret_cast<const void *>(k_propose_tc<2>), 256, tc_smem_bytes(2), dev);
-        p->per_sm_mma = resident_blocks(reinterpret_cast<const void *>(k_propose), 128, 0, dev);
+        p->per_sm_tc1 =
+            resident_blocks(reinterpret_cast<const void *>(k_propose_tc<1>), 128, tc_smem_bytes(1), dev, 128);
+        p->per_sm_tc2 =
+            resident_blocks(reinterpret_cast<const void *>(k_propose_tc<2>), 256, tc_smem_bytes(2), dev, 256);
+        p->per_sm_mma = resident_blocks(reinterpret_cast<const void *>(k_propose), 128, 0, dev, 0);
     }
     std::vector<float> zero;
     if (!params) {
