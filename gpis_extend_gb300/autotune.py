@@ -1,9 +1,8 @@
 """The schedule autotuner: times candidate values of the context's schedule knobs
 (gpis_tune_set) on the caller's own workload and keeps the fastest.
 
-Knobs: the fast pass's persistent grid (CTAs per SM), the rounds of fast and
-resume passes, the render's pass size (paths per wavefront pass) and the host
-pipeline's chunk.  None of them changes
+Knobs: the fast pass's persistent grid (CTAs per SM), the render's pass size
+(paths per wavefront pass) and the host pipeline's chunk.  None of them changes
 a result: every flight is independent of the grid and of its batch, so the
 tuner compares times only.
 """
@@ -46,26 +45,6 @@ def tune_march(ctx, devs, candidates=(0, 1, 2, 3, 4), reps=3):
     best = min(times, key=times.get)
     ctx.tune(abi.TUNE_MARCH_CTAS_PER_SM, best)
     return {"knob": "march_ctas_per_sm", "best": best, "ms": times}
-
-
-def tune_march_rounds(ctx, devs, candidates=(1, 2, 3), reps=3):
-    """Rounds of fast and resume passes per batch, timed on device-resident batches.
-    More rounds hand the flights a resume pass decides and that march on back to the
-    fast evaluator, at two launches a round.  Returns {candidate: ms} and leaves the
-    fastest set."""
-    times = {}
-
-    def run():
-        for d in devs:
-            ctx.submit(d)
-
-    for c in candidates:
-        ctx.tune(abi.TUNE_MARCH_ROUNDS, c)
-        run()
-        times[c] = _median_ms(run, reps)
-    best = min(times, key=times.get)
-    ctx.tune(abi.TUNE_MARCH_ROUNDS, best)
-    return {"knob": "march_rounds", "best": best, "ms": times}
 
 
 def tune_render(ctx, scenes, candidates=(1 << 20, 1 << 21, 1 << 22, 1 << 23), spp_cap=2, reps=1):

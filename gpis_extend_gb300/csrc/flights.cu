@@ -2535,9 +2535,8 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     // (queue2), except in the last round, which marches them to the end.  Counters per
     // round: fast pull, queue length, resume pull, queue2 length.
     uint32_t *w = b.work;
-    const int rounds = (a.rounds >= 1 && a.rounds <= kMarchRounds) ? a.rounds : kMarchRounds;
-    for (int k = 0; k < rounds; ++k) {
-        const bool last = k == rounds - 1;
+    for (int k = 0; k < kMarchRounds; ++k) {
+        const bool last = k == kMarchRounds - 1;
         const MarchRound fr = {k == 0 ? nullptr : b.queue2, k == 0 ? nullptr : w + 4 * (k - 1) + 3, b.queue,
                                w + 4 * k + 1, w + 4 * k};
         err = fast(fr);

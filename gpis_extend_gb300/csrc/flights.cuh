@@ -58,7 +58,6 @@ struct FlightArgs {
     int any_ns;                 // some medium has a nonstationary length scale
     int any_mr;                 // some medium blends multi-resolution levels
     uint32_t ctas_per_sm;       // fast-pass persistent grid: CTAs per SM (0: every resident CTA)
-    int rounds;                 // rounds of fast and resume passes, 1 .. kMarchRounds (0: all)
     const uint32_t *n_dev;      // may be null: the live flight count in device memory (<= n,
                                 // which is then the capacity the grids are sized for)
     const float4 *proposal;     // may be null: per flight the proposed crossing interval

@@ -276,7 +276,7 @@ struct gpis_ctx {
     double prof_ms[3] = {0, 0, 0};
     uint64_t prof_launches[3] = {0, 0, 0};
     // schedule knobs (gpis_tune_set; 0 = default)
-    uint64_t tune[4] = {0, 0, 0, 0};
+    uint64_t tune[3] = {0, 0, 0};
 };
 
 namespace {
@@ -486,7 +486,6 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.proposal = reinterpret_cast<const float4 *>(proposal);
     a.n_dev = n_dev;
     a.ctas_per_sm = (uint32_t)ctx->tune[GPIS_TUNE_MARCH_CTAS_PER_SM];
-    a.rounds = ctx->tune[GPIS_TUNE_MARCH_ROUNDS] ? (int)ctx->tune[GPIS_TUNE_MARCH_ROUNDS] : gpis::kMarchRounds;
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
     a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
     a.seeds = reinterpret_cast<const uint4 *>(in->seeds);
@@ -618,12 +617,12 @@ __attribute__((visibility("hidden"))) int gpis_internal_nee_live(gpis_ctx *ctx, 
     return GPIS_OK;
 }
 
+// SM count, whether per-kernel profiling is on, and whether a flight batch runs the
+// prepare kernel (conditioning media, or the stationary cooperative fast pass's set-up)
 int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value)
 {
     if (!ctx) return fail(GPIS_EINVAL, "null context");
-    if (key > GPIS_TUNE_MARCH_ROUNDS) return fail(GPIS_EINVAL, "unknown schedule knob");
-    if (key == GPIS_TUNE_MARCH_ROUNDS && value > (uint64_t)gpis::kMarchRounds)
-        return fail(GPIS_ERANGE, "march rounds must be <= 3");
+    if (key > GPIS_TUNE_HOST_CHUNK) return fail(GPIS_EINVAL, "unknown schedule knob");
     if (key == GPIS_TUNE_MARCH_CTAS_PER_SM && value > 64) return fail(GPIS_ERANGE, "CTAs per SM must be <= 64");
     if (key == GPIS_TUNE_RENDER_PASS_PATHS && value && (value < 4096 || value > (1ull << 26)))
         return fail(GPIS_ERANGE, "render pass size must be in [4096, 2^26]");
@@ -636,7 +635,7 @@ int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value)
 int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value)
 {
     if (!ctx || !value) return fail(GPIS_EINVAL, "null argument");
-    if (key > GPIS_TUNE_MARCH_ROUNDS) return fail(GPIS_EINVAL, "unknown schedule knob");
+    if (key > GPIS_TUNE_HOST_CHUNK) return fail(GPIS_EINVAL, "unknown schedule knob");
     *value = ctx->tune[key];
     return GPIS_OK;
 }
@@ -659,9 +658,7 @@ __attribute__((visibility("hidden"))) int gpis_internal_ctx_info(gpis_ctx *ctx, 
         const bool coop_plain = ctx->all_one_d && ctx->max_imp <= 8 && ctx->max_oct == 1 && !ctx->any_ns &&
                                 !ctx->all_grid && !ctx->any_mr;
         *prepare_runs = (ctx->any_cond || coop_plain) ? 1 : 0;
-        const int rounds =
-            ctx->tune[GPIS_TUNE_MARCH_ROUNDS] ? (int)ctx->tune[GPIS_TUNE_MARCH_ROUNDS] : gpis::kMarchRounds;
-        if (batch_kernels) *batch_kernels = 2 * rounds + 1 + *prepare_runs;
+        if (batch_kernels) *batch_kernels = 2 * gpis::kMarchRounds + 1 + *prepare_runs;
     }
     return GPIS_OK;
 }

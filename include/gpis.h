@@ -285,10 +285,6 @@ int gpis_nee_host(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n)
 #define GPIS_TUNE_RENDER_PASS_PATHS 1u   /* paths per render pass (default 2^22)     */
 #define GPIS_TUNE_HOST_CHUNK        2u   /* flights per chunk of the host pipeline
                                             (default 2^20)                          */
-#define GPIS_TUNE_MARCH_ROUNDS      3u   /* rounds of fast and resume passes, 1 to 3
-                                            (default 3): a flight decided by a resume
-                                            pass that marches on goes back to the
-                                            next round's fast pass                  */
 int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value);
 int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value);
 
