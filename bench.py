@@ -357,8 +357,7 @@ def run_learned(args):
         "e2e": {"value": None, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                 "note": "device-resident arms only; the host entry is measured by the default workload"},
         "learned": learned,
-        # per batch: features, inference, prepare, three rounds of fast and resume passes, finish
-        "gpu_launches": args.steps * 2 * 10,
+        "gpu_launches": args.steps * 2 * 6,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -667,9 +666,9 @@ def main():
                    "primary": prim.n, "secondary": sec.n, "l2": "inputs 512 MiB > L2 (no flush)",
                    "parallelism": f"replicas x{world} (disjoint flight ranges)", "schedule": schedule},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        # per batch: k_prepare (the fast pass's set-up and the conditioning), three
-        # rounds of fast and resume passes and k_finish; two batches per step
-        "gpu_launches": args.steps * 2 * 8,
+        # per batch: k_prepare (the fast pass's set-up and the conditioning), the fast
+        # pass, the resume pass and k_finish; two batches per step
+        "gpu_launches": args.steps * 2 * 4,
         "roofline": roof,
         "counters": cnt,
         "clocks": clocks.summary(),

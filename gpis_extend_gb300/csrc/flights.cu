@@ -1597,29 +1597,17 @@ __device__ __forceinline__ unsigned long long warp_sum(uint32_t v)
 
 // ---------------------------------------------------------------------------
 // k_march: persistent warps with per-lane refill.
-// One pass of the march: the flights it takes and the queue it hands flights on to.
-struct MarchRound {
-    const uint32_t *src;        // null: every flight (the first fast pass); else a queue
-    const uint32_t *src_n;      //   written by the previous kernel, and its length
-    uint32_t *dst;              // the flights handed on, and their count; null only for
-    uint32_t *dst_n;            //   the last resume pass
-    uint32_t *pull;             // work counter
-};
-
 // ---------------------------------------------------------------------------
-// RESUME = false: a fast pass.  Lanes march with the fast evaluator only; a flight
-// whose value comes within the band of zero or changes sign is saved to its resume
-// record and queued for the resume pass.  After the first round the fast pass takes
-// the flights a resume pass handed back and continues them from their records.
-// RESUME = true: a resume pass over the queued flights: the precise decision at the
-// saved point, the refinement and, when the point is not a crossing, the hand-back
-// to the next fast pass.  The last resume pass (no queue to hand on to) marches such
-// flights to their end itself, with precise decisions.
+// RESUME = false: the fast pass.  Lanes march with the fast evaluator only; a
+// flight whose value comes within the band of zero or changes sign is saved to
+// its resume record and left to the resume pass.
+// RESUME = true: the resume pass over the saved flights, with precise decisions,
+// the refinement and, after a rejected crossing candidate, the rest of the march.
 template <class Eval, bool RESUME>
-__global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a, MarchRound r)
+__global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
 {
     const int lane = threadIdx.x & 31;
-    uint32_t *work = r.pull;
+    uint32_t *work = a.work + (RESUME ? 2 : 0);
     const unsigned lt_mask = (1u << lane) - 1u;
     // 0.9 and 0.01 as float-float pairs (the reference's double constants)
     const FF kNine = {0.9f, -2.38418579e-08f};
@@ -1644,22 +1632,23 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a, M
     // its truncation-jump allowance, fixed and per step
     float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
     float prop_a = -INFINITY;   // start of the proposed crossing interval (learned proposal)
-    // the queue lengths were written by earlier kernels on this stream
-    const uint32_t n_live = r.src ? *r.src_n : live_n(a);
-    bool to_queue = false;      // this lane handed flight q_fid on in the last iteration
+    // the fast pass works through every flight; the resume pass through the queue of
+    // the flights the fast pass saved (written by the previous kernel on this stream)
+    const uint32_t n_live = RESUME ? a.work[1] : live_n(a);
+    bool to_queue = false;      // fast pass: this lane saved flight q_fid in the last iteration
     uint32_t q_fid = 0;
 
     for (;;) {
-        if (r.dst) {
-            // append the flights handed on in the last iteration to the next pass's
-            // queue, one atomic per warp (every lane passes here once per iteration)
+        if (!RESUME) {
+            // append the flights saved in the last iteration to the resume queue, one
+            // atomic per warp (every lane passes here once per iteration)
             const unsigned q_mask = __ballot_sync(FULL, to_queue);
             if (q_mask) {
                 const int ql = __ffs(q_mask) - 1;
                 uint32_t qb = 0;
-                if (lane == ql) qb = atomicAdd(r.dst_n, (uint32_t)__popc(q_mask));
+                if (lane == ql) qb = atomicAdd(a.work + 1, (uint32_t)__popc(q_mask));
                 qb = __shfl_sync(FULL, qb, ql);
-                if (to_queue) r.dst[qb + (uint32_t)__popc(q_mask & lt_mask)] = q_fid;
+                if (to_queue) a.queue[qb + (uint32_t)__popc(q_mask & lt_mask)] = q_fid;
                 to_queue = false;
             }
         }
@@ -1675,9 +1664,9 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a, M
                 if (pos >= n_live) {
                     drained = true;
                 } else {
-                    const uint32_t idx = r.src ? r.src[pos] : pos;
+                    const uint32_t idx = RESUME ? a.queue[pos] : pos;
                     fid = idx;
-                    if (!r.src) c_flights++;
+                    if (!RESUME) c_flights++;
                     prop_a = (!RESUME && a.proposal) ? a.proposal[idx].x : -INFINITY;
                     bool mok;
                     L.m = medium_of(a, idx, mok);
@@ -1731,17 +1720,6 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a, M
                             steps = 0;
                             ev.reset();
                             phase = PH_F0;
-                            if (r.src) {
-                                // handed back by a resume pass: continue from its record
-                                const uint4 rc = a.resume[idx];
-                                th = __uint_as_float(rc.x);
-                                tl = __uint_as_float(rc.y);
-                                pf = __uint_as_float(rc.z);
-                                steps = rc.w & 0xFFFFFFu;
-                                sign0 = (rc.w & (1u << 24)) ? -1 : 1;
-                                pf_precise = (rc.w & (1u << 25)) != 0;
-                                phase = (int)(rc.w >> 28);
-                            }
                         }
                     } else if (const FlightIn fl = load_flight(a, idx); !mok || !flight_valid(fl)) {
                         write_status(a, idx, 0.0f, 0.0f, 1.0f, 0u, GPIS_FLIGHT_INVALID_INPUT);
@@ -1766,8 +1744,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a, M
                         steps = 0;
                         ev.reset();
                         phase = PH_F0;
-                        if (!RESUME && r.src) rs = a.resume[idx];
-                        if (r.src) {
+                        if (RESUME) {
                             th = __uint_as_float(rs.x);
                             tl = __uint_as_float(rs.y);
                             pf = __uint_as_float(rs.z);
@@ -1794,13 +1771,14 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a, M
 #pragma unroll
         for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], eh, el);
         int id;
-        // a resume pass that hands flights on evaluates every point precisely (one code
-        // path for the warp's lanes: its flights only decide, refine and end at far);
-        // the last one marches on with the fast evaluator between precise decisions
-        const bool precise = RESUME && (r.dst || (phase != PH_MARCH && phase != PH_FAR));
-        const float f = precise ? field_precise(L, p[0], p[1], p[2], id)
-                                : ev.value(L, p[0], p[1], p[2], id, c_refills, live);
+        // the resume pass evaluates every point with the precise evaluator (one code
+        // path for the warp's lanes, whatever their phase); a marching value is then
+        // already the precise one, so PH_MARCH takes the PH_MARCH_P branch directly
+        // (the fast pass would re-evaluate the same point precisely before deciding)
+        const float f = RESUME ? field_precise(L, p[0], p[1], p[2], id)
+                               : ev.value(L, p[0], p[1], p[2], id, c_refills, live);
         if (Eval::kCollective && !live) continue;
+        if (RESUME && phase == PH_MARCH) phase = PH_MARCH_P;
         gpid = id;
         const int sg = f < 0.0f ? -1 : 1;
         bool done = false;
@@ -1948,9 +1926,6 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a, M
             t_end = {far_t, 0.0f};
             v_out = f;
         }
-        // a resume pass with a next round hands a decided flight that marches on back
-        // to the fast pass
-        if (RESUME && r.dst && !done && phase == PH_MARCH) pend = true;
         if (pend) {
             a.resume[fid] = pack_resume(th, tl, pf, steps, sign0, pf_precise, phase);
             to_queue = true;
@@ -2486,7 +2461,7 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     if (!coop_plain) b.setup = nullptr;     // the march kernels read set-up records only when written
     if (b.any_cond || b.setup) k_prepare<<<blocks, 128, 0, stream>>>(b);
     if (ev) cudaEventRecord(ev[1], stream);
-    cudaError_t err = cudaMemsetAsync(b.work, 0, kWorkCounters * sizeof(uint32_t), stream);
+    cudaError_t err = cudaMemsetAsync(b.work, 0, 4 * sizeof(uint32_t), stream);
     if (err != cudaSuccess) return err;
     // persistent grids: exactly the CTAs that are resident at once, never more
     // warps than flights
@@ -2505,46 +2480,30 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     if (ev) cudaEventRecord(ev[2], stream);
     // multi-resolution media take the generic evaluator (two levels per evaluation)
     const bool coop = a.one_d && a.max_imp <= 8 && a.max_oct == 1 && !a.any_mr;
-    auto fast = [&](const MarchRound &r) -> cudaError_t {
-        if (a.any_mr) {
-            const void *fn = (const void *)k_march<EvalGeneric, false>;
-            k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(b, r);
-        } else if (a.one_d && a.max_imp <= 8 && a.max_oct > 1) {
-            const void *fn = (const void *)k_march<EvalCoopOct, false>;
-            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemOct);
-            if (e != cudaSuccess) return e;
-            k_march<EvalCoopOct, false><<<grid(fn, kSmemOct), 256, kSmemOct, stream>>>(b, r);
-        } else if (coop && a.any_ns) {
-            const void *fn = (const void *)k_march<EvalCoop1D<8, false, true>, false>;
-            k_march<EvalCoop1D<8, false, true>, false><<<grid(fn), 256, 0, stream>>>(b, r);
-        } else if (coop && a.all_grid) {
-            const void *fn = (const void *)k_march<EvalCoop1D<8, true>, false>;
-            k_march<EvalCoop1D<8, true>, false><<<grid(fn), 256, 0, stream>>>(b, r);
-        } else if (coop) {
-            const void *fn = (const void *)k_march<EvalCoop1D<8>, false>;
-            k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(b, r);
-        } else {
-            const void *fn = (const void *)k_march<EvalGeneric, false>;
-            k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(b, r);
-        }
-        return cudaSuccess;
-    };
-    // Rounds of (fast pass, resume pass).  Round k's fast pass takes every flight (k = 0)
-    // or the flights resume pass k - 1 handed back (queue2) and queues the flights it
-    // saves (queue); resume pass k decides them and hands the ones that march on back
-    // (queue2), except in the last round, which marches them to the end.  Counters per
-    // round: fast pull, queue length, resume pull, queue2 length.
-    uint32_t *w = b.work;
-    for (int k = 0; k < kMarchRounds; ++k) {
-        const bool last = k == kMarchRounds - 1;
-        const MarchRound fr = {k == 0 ? nullptr : b.queue2, k == 0 ? nullptr : w + 4 * (k - 1) + 3, b.queue,
-                               w + 4 * k + 1, w + 4 * k};
-        err = fast(fr);
-        if (err != cudaSuccess) return err;
-        const MarchRound rr = {b.queue, w + 4 * k + 1, last ? nullptr : b.queue2, last ? nullptr : w + 4 * k + 3,
-                               w + 4 * k + 2};
+    if (a.any_mr) {
+        const void *fn = (const void *)k_march<EvalGeneric, false>;
+        k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(b);
+    } else if (a.one_d && a.max_imp <= 8 && a.max_oct > 1) {
+        const void *fn = (const void *)k_march<EvalCoopOct, false>;
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemOct);
+        if (e != cudaSuccess) return e;
+        k_march<EvalCoopOct, false><<<grid(fn, kSmemOct), 256, kSmemOct, stream>>>(b);
+    } else if (coop && a.any_ns) {
+        const void *fn = (const void *)k_march<EvalCoop1D<8, false, true>, false>;
+        k_march<EvalCoop1D<8, false, true>, false><<<grid(fn), 256, 0, stream>>>(b);
+    } else if (coop && a.all_grid) {
+        const void *fn = (const void *)k_march<EvalCoop1D<8, true>, false>;
+        k_march<EvalCoop1D<8, true>, false><<<grid(fn), 256, 0, stream>>>(b);
+    } else if (coop) {
+        const void *fn = (const void *)k_march<EvalCoop1D<8>, false>;
+        k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(b);
+    } else {
+        const void *fn = (const void *)k_march<EvalGeneric, false>;
+        k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(b);
+    }
+    {
         const void *fn = (const void *)k_march<EvalGeneric, true>;
-        k_march<EvalGeneric, true><<<grid(fn, 0, false), 256, 0, stream>>>(b, rr);
+        k_march<EvalGeneric, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
     }
     if (ev) cudaEventRecord(ev[3], stream);
     if (ev) cudaEventRecord(ev[4], stream);

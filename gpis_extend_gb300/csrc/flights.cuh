@@ -24,11 +24,6 @@ struct CondRec {
     uint32_t has_obs;       // has_gradient_observation
 };
 
-// Work counters per batch (per slice of the host pipeline): a pull counter and a
-// queue length for each of the march's fast and resume passes, three rounds.
-constexpr uint32_t kWorkCounters = 16;
-constexpr int kMarchRounds = 3;
-
 struct FlightArgs {
     const float4 *origin_near;
     const float4 *dir_far;
@@ -41,10 +36,10 @@ struct FlightArgs {
     uint32_t n;
     CondRec *cond;              // scratch, n records
     double *t_end;              // scratch, n values (double march parameter at the end point)
-    uint32_t *work;             // scratch, kWorkCounters counters zeroed before the march
-    uint32_t *queue;            // scratch, n: the flights a fast pass saved for the resume pass
-    uint32_t *queue2;           // scratch, n: the flights a resume pass decided and handed back
-                                // to the next fast pass
+    uint32_t *work;             // scratch, 4 counters zeroed before the march: march work,
+                                // resume-queue length, resume work, unused
+    uint32_t *queue;            // scratch, n: indices of the flights the fast pass saved for
+                                // the resume pass (work[1] of them)
     uint4 *resume;              // scratch, n saved march states
     float4 *setup;              // scratch, 4 per flight: the fast pass's per-flight set-up, written by
                                 // k_prepare when the stationary cooperative evaluator runs (else unused)

@@ -256,7 +256,7 @@ struct gpis_ctx {
     gpis::CondRec *d_cond = nullptr;
     double *d_tend = nullptr;
     uint4 *d_resume = nullptr;
-    uint32_t *d_queue = nullptr, *d_queue2 = nullptr;
+    uint32_t *d_queue = nullptr;
     float4 *d_setup = nullptr;
     uint32_t *d_work = nullptr;
     unsigned long long *d_counters = nullptr;
@@ -290,7 +290,6 @@ void release(gpis_ctx *c)
     cudaFree(c->d_tend);
     cudaFree(c->d_resume);
     cudaFree(c->d_queue);
-    cudaFree(c->d_queue2);
     cudaFree(c->d_setup);
     cudaFree(c->d_work);
     cudaFree(c->d_counters);
@@ -313,20 +312,17 @@ int ensure_scratch(gpis_ctx *c, size_t n)
     cudaFree(c->d_tend);
     cudaFree(c->d_resume);
     cudaFree(c->d_queue);
-    cudaFree(c->d_queue2);
     cudaFree(c->d_setup);
     c->d_cond = nullptr;
     c->d_tend = nullptr;
     c->d_resume = nullptr;
     c->d_queue = nullptr;
-    c->d_queue2 = nullptr;
     c->d_setup = nullptr;
     c->cap = 0;
     CUDA_TRY(cudaMalloc(&c->d_cond, cap * sizeof(gpis::CondRec)), "allocate conditioning scratch");
     CUDA_TRY(cudaMalloc(&c->d_tend, cap * sizeof(double)), "allocate end-parameter scratch");
     CUDA_TRY(cudaMalloc(&c->d_resume, cap * sizeof(uint4)), "allocate resume scratch");
     CUDA_TRY(cudaMalloc(&c->d_queue, cap * sizeof(uint32_t)), "allocate resume queue");
-    CUDA_TRY(cudaMalloc(&c->d_queue2, cap * sizeof(uint32_t)), "allocate continuation queue");
     CUDA_TRY(cudaMalloc(&c->d_setup, cap * 4 * sizeof(float4)), "allocate set-up scratch");
     c->cap = cap;
     return GPIS_OK;
@@ -451,7 +447,7 @@ int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
             rc = cuda_fail(e, "upload media");
             break;
         }
-        if ((e = cudaMalloc(&c->d_work, gpis::kWorkCounters * kMaxChunks * sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(e, "allocate work counters"); break; }
+        if ((e = cudaMalloc(&c->d_work, 4 * kMaxChunks * sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(e, "allocate work counters"); break; }
         if ((e = cudaMalloc(&c->d_counters, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "allocate counters"); break; }
         if ((e = cudaMemset(c->d_counters, 0, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "clear counters"); break; }
         if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(e, "create stream"); break; }
@@ -499,7 +495,6 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.t_end = ctx->d_tend + offset;
     a.work = work;
     a.queue = ctx->d_queue + offset;
-    a.queue2 = ctx->d_queue2 + offset;
     a.resume = ctx->d_resume + offset;
     a.setup = ctx->d_setup + 4 * offset;
     a.counters = ctx->d_counters;
@@ -646,10 +641,8 @@ __attribute__((visibility("hidden"))) uint32_t gpis_internal_render_pass(gpis_ct
                                                          : (1u << 22);
 }
 
-// prepare_runs: kernels of one flight batch (k_prepare when it runs, the march's
-// rounds, k_finish)
 __attribute__((visibility("hidden"))) int gpis_internal_ctx_info(gpis_ctx *ctx, int *num_sms, int *profiling,
-                                                                 int *prepare_runs, int *batch_kernels)
+                                                                 int *prepare_runs)
 {
     if (!ctx) return GPIS_EINVAL;
     if (num_sms) *num_sms = ctx->num_sms;
@@ -658,7 +651,6 @@ __attribute__((visibility("hidden"))) int gpis_internal_ctx_info(gpis_ctx *ctx, 
         const bool coop_plain = ctx->all_one_d && ctx->max_imp <= 8 && ctx->max_oct == 1 && !ctx->any_ns &&
                                 !ctx->all_grid && !ctx->any_mr;
         *prepare_runs = (ctx->any_cond || coop_plain) ? 1 : 0;
-        if (batch_kernels) *batch_kernels = 2 * gpis::kMarchRounds + 1 + *prepare_runs;
     }
     return GPIS_OK;
 }
@@ -760,7 +752,7 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis
         CUDA_TRY(cudaStreamWaitEvent(cs, ctx->ev_chunks[2 * k], 0), "wait for copies");
         gpis_flight_soa din{d_on + 4 * o, d_df + 4 * o, d_sd + 4 * o, d_pv + 4 * o, in->medium ? d_md + o : nullptr};
         gpis_result_soa dout{d_rec + 8 * o};
-        int rc = submit_slice(ctx, &din, &dout, (uint32_t)m, cs, o, ctx->d_work + gpis::kWorkCounters * k);
+        int rc = submit_slice(ctx, &din, &dout, (uint32_t)m, cs, o, ctx->d_work + 4 * k);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(ctx->ev_chunks[2 * k + 1], cs), "record kernel event");
     }

@@ -850,8 +850,7 @@ extern "C" int gpis_internal_infer_live(gpis_proposal *p, const gpis_flight_soa 
 extern "C" int gpis_internal_proposal_quiesce(gpis_proposal *p);
 extern "C" int gpis_internal_nee_live(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t cap,
                                       const uint32_t *n_dev, void *cuda_stream);
-extern "C" int gpis_internal_ctx_info(gpis_ctx *ctx, int *num_sms, int *profiling, int *prepare_runs,
-                                      int *batch_kernels);
+extern "C" int gpis_internal_ctx_info(gpis_ctx *ctx, int *num_sms, int *profiling, int *prepare_runs);
 extern "C" uint32_t gpis_internal_render_pass(gpis_ctx *ctx);
 
 namespace {
@@ -974,8 +973,7 @@ extern "C" int gpis_render_batch_proposed(gpis_ctx *ctx, gpis_proposal *prop, co
         max_segs = std::max<uint32_t>(max_segs, (uint32_t)passes[p].size());
     }
     int num_sms = 1, profiling = 0, prepare_runs = 1;
-    int batch_kernels = 0;
-    gpis_internal_ctx_info(ctx, &num_sms, &profiling, &prepare_runs, &batch_kernels);
+    gpis_internal_ctx_info(ctx, &num_sms, &profiling, &prepare_runs);
 
     DevBuf mem;
     RtScene *d_scenes;
@@ -1095,9 +1093,8 @@ extern "C" int gpis_render_batch_proposed(gpis_ctx *ctx, gpis_proposal *prop, co
         return GPIS_OK;
     };
     // kernels of one round: advance, event, shadow, collect, tally, and per flight batch
-    // prepare (when it runs), the march's rounds of fast and resume passes and finish;
-    // NEE adds its kernel and the shading
-    const uint64_t per_batch = (uint64_t)batch_kernels;
+    // prepare (when it runs), march, resume and finish; NEE adds its kernel and the shading
+    const uint64_t per_batch = 3 + (prepare_runs ? 1 : 0);
     const uint64_t per_round = 5 + 2 * per_batch + (any_nee ? 2 : 0) + (prop ? 2 : 0);
     const uint32_t rounds = 2 * max_bounces + 4;
     cudaGraphExec_t gexec = nullptr;
