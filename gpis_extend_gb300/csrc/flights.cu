@@ -1632,26 +1632,9 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     // its truncation-jump allowance, fixed and per step
     float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
     float prop_a = -INFINITY;   // start of the proposed crossing interval (learned proposal)
-    // the fast pass works through every flight; the resume pass through the queue of
-    // the flights the fast pass saved (written by the previous kernel on this stream)
-    const uint32_t n_live = RESUME ? a.work[1] : live_n(a);
-    bool to_queue = false;      // fast pass: this lane saved flight q_fid in the last iteration
-    uint32_t q_fid = 0;
+    const uint32_t n_live = live_n(a);
 
     for (;;) {
-        if (!RESUME) {
-            // append the flights saved in the last iteration to the resume queue, one
-            // atomic per warp (every lane passes here once per iteration)
-            const unsigned q_mask = __ballot_sync(FULL, to_queue);
-            if (q_mask) {
-                const int ql = __ffs(q_mask) - 1;
-                uint32_t qb = 0;
-                if (lane == ql) qb = atomicAdd(a.work + 1, (uint32_t)__popc(q_mask));
-                qb = __shfl_sync(FULL, qb, ql);
-                if (to_queue) a.queue[qb + (uint32_t)__popc(q_mask & lt_mask)] = q_fid;
-                to_queue = false;
-            }
-        }
         const bool need = phase == PH_IDLE && !drained;
         const unsigned need_mask = __ballot_sync(FULL, need);
         if (need_mask) {
@@ -1660,11 +1643,10 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
             if (lane == leader) base = atomicAdd(work, (uint32_t)__popc(need_mask));
             base = __shfl_sync(FULL, base, leader);
             if (need) {
-                const uint32_t pos = base + (uint32_t)__popc(need_mask & lt_mask);
-                if (pos >= n_live) {
+                const uint32_t idx = base + (uint32_t)__popc(need_mask & lt_mask);
+                if (idx >= n_live) {
                     drained = true;
                 } else {
-                    const uint32_t idx = RESUME ? a.queue[pos] : pos;
                     fid = idx;
                     if (!RESUME) c_flights++;
                     prop_a = (!RESUME && a.proposal) ? a.proposal[idx].x : -INFINITY;
@@ -1684,6 +1666,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                         if (!mok || !(flags & SF_VALID)) {
                             write_status(a, idx, 0.0f, 0.0f, 1.0f, 0u, GPIS_FLIGHT_INVALID_INPUT);
                             a.t_end[idx] = 0.0;
+                            a.resume[idx] = make_uint4(0u, 0u, 0u, 0u);
                             c_invalid++;
                         } else {
 #pragma unroll
@@ -1724,6 +1707,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     } else if (const FlightIn fl = load_flight(a, idx); !mok || !flight_valid(fl)) {
                         write_status(a, idx, 0.0f, 0.0f, 1.0f, 0u, GPIS_FLIGHT_INVALID_INPUT);
                         a.t_end[idx] = 0.0;
+                        a.resume[idx] = make_uint4(0u, 0u, 0u, 0u);
                         c_invalid++;
                     } else {
 #pragma unroll
@@ -1771,14 +1755,10 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
 #pragma unroll
         for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], eh, el);
         int id;
-        // the resume pass evaluates every point with the precise evaluator (one code
-        // path for the warp's lanes, whatever their phase); a marching value is then
-        // already the precise one, so PH_MARCH takes the PH_MARCH_P branch directly
-        // (the fast pass would re-evaluate the same point precisely before deciding)
-        const float f = RESUME ? field_precise(L, p[0], p[1], p[2], id)
-                               : ev.value(L, p[0], p[1], p[2], id, c_refills, live);
+        const bool precise = RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE);
+        const float f = precise ? field_precise(L, p[0], p[1], p[2], id)
+                                : ev.value(L, p[0], p[1], p[2], id, c_refills, live);
         if (Eval::kCollective && !live) continue;
-        if (RESUME && phase == PH_MARCH) phase = PH_MARCH_P;
         gpid = id;
         const int sg = f < 0.0f ? -1 : 1;
         bool done = false;
@@ -1928,12 +1908,11 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
         }
         if (pend) {
             a.resume[fid] = pack_resume(th, tl, pf, steps, sign0, pf_precise, phase);
-            to_queue = true;
-            q_fid = fid;
             phase = PH_IDLE;
         } else if (done) {
             write_status(a, fid, t_out, v_out, trans, steps, status | ((uint32_t)gpid << 8));
             a.t_end[fid] = (double)t_end.h + (double)t_end.l;
+            if (!RESUME) a.resume[fid] = make_uint4(0u, 0u, 0u, 0u);
             phase = PH_IDLE;
         }
     }

@@ -256,7 +256,6 @@ struct gpis_ctx {
     gpis::CondRec *d_cond = nullptr;
     double *d_tend = nullptr;
     uint4 *d_resume = nullptr;
-    uint32_t *d_queue = nullptr;
     float4 *d_setup = nullptr;
     uint32_t *d_work = nullptr;
     unsigned long long *d_counters = nullptr;
@@ -289,7 +288,6 @@ void release(gpis_ctx *c)
     cudaFree(c->d_cond);
     cudaFree(c->d_tend);
     cudaFree(c->d_resume);
-    cudaFree(c->d_queue);
     cudaFree(c->d_setup);
     cudaFree(c->d_work);
     cudaFree(c->d_counters);
@@ -311,18 +309,15 @@ int ensure_scratch(gpis_ctx *c, size_t n)
     cudaFree(c->d_cond);
     cudaFree(c->d_tend);
     cudaFree(c->d_resume);
-    cudaFree(c->d_queue);
     cudaFree(c->d_setup);
     c->d_cond = nullptr;
     c->d_tend = nullptr;
     c->d_resume = nullptr;
-    c->d_queue = nullptr;
     c->d_setup = nullptr;
     c->cap = 0;
     CUDA_TRY(cudaMalloc(&c->d_cond, cap * sizeof(gpis::CondRec)), "allocate conditioning scratch");
     CUDA_TRY(cudaMalloc(&c->d_tend, cap * sizeof(double)), "allocate end-parameter scratch");
     CUDA_TRY(cudaMalloc(&c->d_resume, cap * sizeof(uint4)), "allocate resume scratch");
-    CUDA_TRY(cudaMalloc(&c->d_queue, cap * sizeof(uint32_t)), "allocate resume queue");
     CUDA_TRY(cudaMalloc(&c->d_setup, cap * 4 * sizeof(float4)), "allocate set-up scratch");
     c->cap = cap;
     return GPIS_OK;
@@ -494,7 +489,7 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.cond = ctx->d_cond + offset;
     a.t_end = ctx->d_tend + offset;
     a.work = work;
-    a.queue = ctx->d_queue + offset;
+    a.queue = nullptr;
     a.resume = ctx->d_resume + offset;
     a.setup = ctx->d_setup + 4 * offset;
     a.counters = ctx->d_counters;

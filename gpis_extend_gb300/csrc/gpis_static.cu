@@ -36,8 +36,7 @@ constexpr size_t kOffCond = kOffCounters + 256;
 constexpr size_t kOffTEnd = kOffCond + kMax * sizeof(gpis::CondRec);
 constexpr size_t kOffResume = kOffTEnd + kMax * sizeof(double);
 constexpr size_t kOffSetup = kOffResume + kMax * sizeof(uint4);
-constexpr size_t kOffQueue = kOffSetup + kMax * 4 * sizeof(float4);
-constexpr size_t kBytes = kOffQueue + kMax * sizeof(uint32_t);
+constexpr size_t kBytes = kOffSetup + kMax * 4 * sizeof(float4);
 static_assert(sizeof(gpis::DevMedium) <= kOffWork, "medium table must fit its slot");
 
 // The working memory.  In host code this name is only a stand-in for the
@@ -121,7 +120,7 @@ extern "C" int gpis_flights_submit_static(const gpis_medium_desc *medium, const 
     a.cond = reinterpret_cast<gpis::CondRec *>(b + kOffCond);
     a.t_end = reinterpret_cast<double *>(b + kOffTEnd);
     a.work = reinterpret_cast<uint32_t *>(b + kOffWork);
-    a.queue = reinterpret_cast<uint32_t *>(b + kOffQueue);
+    a.queue = nullptr;
     a.resume = reinterpret_cast<uint4 *>(b + kOffResume);
     a.setup = reinterpret_cast<float4 *>(b + kOffSetup);
     a.counters = reinterpret_cast<unsigned long long *>(b + kOffCounters);
