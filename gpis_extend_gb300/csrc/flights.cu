@@ -238,9 +238,21 @@ __device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, floa
 
 // ---- 3D world-space noise, generic (no cache) ----------------------------------
 // Raw sum and gradient (world units), noise3D + cell3D (SparseConvolutionNoise.cpp:419-452).
-template <bool GRAD>
-__device__ void noise3d_generic(const DevMedium &m, float px, float py, float pz, uint32_t seed,
-                                float &v, float g[3])
+//
+// With BOUND, also the range of the raw sum over the segment [p, p + E] (E in cell
+// units, the segment inside p's cell, so that the 27 cells hold every impulse whose
+// support meets it): per impulse the kernel's largest value on the segment (at the
+// nearest point, with the least negative exponent coefficient kmax2 per squared cell
+// distance; 0 when the segment misses the support) and its smallest (at the farther
+// end, coefficient kmin2; 0 when the segment leaves the support).  A positive weight
+// adds [smallest, largest] to [lo, hi], a negative one [-largest, -smallest].  The
+// support tests are widened by kSupportEps against the float rounding of the points,
+// and the kernel values moved outward by 1e-5 against ex2.approx.
+constexpr float kSupportEps = 1e-4f;
+
+template <bool GRAD, bool BOUND>
+__device__ void noise3d_core(const DevMedium &m, float px, float py, float pz, uint32_t seed, float &v, float g[3],
+                             const float E[3], float ee, float kmax2, float kmin2, float &lo, float &hi)
 {
     const float kr = m.kr_world;
     const float p[3] = {px, py, pz};
@@ -255,6 +267,7 @@ __device__ void noise3d_generic(const DevMedium &m, float px, float py, float pz
     }
     const bool xfirst = (m.flags & MF_XYZ_ORDER) != 0;
     float sv = 0.0f, s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+    float blo = 0.0f, bhi = 0.0f;
     for (int dx = -1; dx <= 1; ++dx)
         for (int dy = -1; dy <= 1; ++dy)
             for (int dz = -1; dz <= 1; ++dz) {
@@ -285,10 +298,37 @@ __device__ void noise3d_generic(const DevMedium &m, float px, float py, float pz
                             s2 += w * (-2.0f * (ab2 * m.m3[2]) * e);
                         }
                     }
+                    if (BOUND) {
+                        const float ae = a0 * E[0] + a1 * E[1] + a2 * E[2];
+                        const float sn = fminf(fmaxf(-ae / ee, 0.0f), 1.0f);
+                        const float b2 = fmaxf(l2 + sn * (2.0f * ae + sn * ee), 0.0f);
+                        if (b2 < 1.0f + kSupportEps) {
+                            const float big = ex2_approx(kmax2 * b2) * 1.00001f;
+                            const float far2 = fmaxf(l2, l2 + 2.0f * ae + ee);
+                            const float small = far2 < 1.0f - kSupportEps ? ex2_approx(kmin2 * far2) * 0.99999f : 0.0f;
+                            if (wr >> 31) {
+                                blo += small;
+                                bhi += big;
+                            } else {
+                                blo -= big;
+                                bhi -= small;
+                            }
+                        }
+                    }
                 }
             }
     v = sv;
     if (GRAD) { g[0] = s0; g[1] = s1; g[2] = s2; }
+    if (BOUND) { lo = blo; hi = bhi; }
+}
+
+template <bool GRAD>
+__device__ void noise3d_generic(const DevMedium &m, float px, float py, float pz, uint32_t seed,
+                                float &v, float g[3])
+{
+    const float E[3] = {0.0f, 0.0f, 0.0f};
+    float lo, hi;
+    noise3d_core<GRAD, false>(m, px, py, pz, seed, v, g, E, 1.0f, 0.0f, 0.0f, lo, hi);
 }
 
 // 3D conditioning splat (value and gradient) of the coefficients c at p.
@@ -1180,6 +1220,121 @@ struct EvalGeneric {
     }
 };
 
+// 3D stationary single-octave media with step skipping.  The value is EvalGeneric's
+// (the same arithmetic); a march step that plans a segment [p, p + D d] also gets the
+// range of the field over it: the raw noise sum's range (noise3d_core), the
+// conditioning splat's exact range along the segment (its exponent is a quadratic in
+// the segment parameter; the Renewal+ gradient terms bounded by their largest
+// magnitude), and the mean within its Lipschitz slope times the segment length.  The
+// segment ends inside p's cell (less kSupportEps of a cell), where the 27 cells hold
+// every impulse that reaches it.  When the range keeps the sign of f with a margin
+// above the float evaluations' error, every step on the segment keeps it too and the
+// reference would march past: those steps are skipped.
+struct EvalSkip3D {
+    static constexpr bool kCollective = false;
+    static constexpr int kMinBlocks = 2;
+    static constexpr bool kGeneral = true;
+    static constexpr bool kSkip = false;
+    static constexpr bool kSkip3D = true;
+    float want;          // planned segment length (world units along d; 0: none)
+    float dlen;          // the segment's length actually bounded
+    float f_lo, f_hi;    // the field's range over it
+
+    __device__ __forceinline__ void reset() { want = 0.0f; dlen = 0.0f; }
+    __device__ __forceinline__ void bind(const PcgJump *) {}
+    __device__ __forceinline__ void plan(float len) { want = len; }
+
+    __device__ __forceinline__ float value(const LaneField &L, const float d[3], float px, float py, float pz, int &id,
+                                           uint32_t &refills, bool)
+    {
+        const DevMedium &m = *L.m;
+        refills += 27;
+        float len = want;
+        want = 0.0f;
+        dlen = 0.0f;
+        const float kr = m.kr_world;
+        // the segment's end inside p's cell: the distance to the cell's faces along d
+        if (len > 0.0f && m.skip_mean_lip >= 0.0f) {
+            const float p[3] = {px, py, pz};
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float q = __fdiv_rn(p[i], kr);
+                const float fr = __fsub_rn(q, floorf(q));
+                const float di = d[i] / kr;   // cells per unit of t
+                float room = 1e30f;
+                if (di > 0.0f) room = (1.0f - kSupportEps - fr) / di;
+                else if (di < 0.0f) room = (fr - kSupportEps) / -di;
+                len = fminf(len, room);
+            }
+        } else {
+            len = 0.0f;
+        }
+        float v, g[3], lo = 0.0f, hi = 0.0f;
+        if (len > 0.0f) {
+            const float E[3] = {len * d[0] / kr, len * d[1] / kr, len * d[2] / kr};
+            const float ee = E[0] * E[0] + E[1] * E[1] + E[2] * E[2];
+            const float kr2 = kr * kr;
+            const float kmax2 = fmaxf(fmaxf(m.kexp3d[0], m.kexp3d[1]), m.kexp3d[2]) * kr2;
+            const float kmin2 = fminf(fminf(m.kexp3d[0], m.kexp3d[1]), m.kexp3d[2]) * kr2;
+            noise3d_core<false, true>(m, px, py, pz, L.seed, v, g, E, ee, kmax2, kmin2, lo, hi);
+        } else {
+            noise3d_generic<false>(m, px, py, pz, L.seed, v, g);
+        }
+        float noise = v * m.inv_norm3d;
+        float nlo = lo * m.inv_norm3d, nhi = hi * m.inv_norm3d;
+        const float p[3] = {px, py, pz};
+        if (L.cond) {
+            float cv, cg[3];
+            cond3d(m, L.c3, L.o, p, cv, cg);
+            noise += cv;
+            if (len > 0.0f) {
+                // exponent -log2e Q(s), Q(s) = C + 2 B s + A s^2 over s in [0, 1]
+                float A = 0.0f, B = 0.0f, C = 0.0f, gh = 0.0f, eh = 0.0f;
+                const CondOct &co = L.c3.oct[0];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const float ab = p[i] - L.o[i], ew = len * d[i];
+                    A += m.m3c[i] * ew * ew;
+                    B += m.m3c[i] * ab * ew;
+                    C += m.m3c[i] * ab * ab;
+                    gh += ab * m.m3c[i] * co.gs[i];
+                    eh += ew * m.m3c[i] * co.gs[i];
+                }
+                const float sn = A > 0.0f ? fminf(fmaxf(-B / A, 0.0f), 1.0f) : 0.0f;
+                const float qmin = fmaxf(C + sn * (2.0f * B + sn * A), 0.0f);
+                const float qmax = fmaxf(C, C + 2.0f * B + A);
+                const float fmax = ex2_approx(-LOG2E * qmin) * 1.00001f;
+                const float fmin = ex2_approx(-LOG2E * qmax) * 0.99999f;
+                const float vlo = co.vs >= 0.0f ? co.vs * fmin : co.vs * fmax;
+                const float vhi = co.vs >= 0.0f ? co.vs * fmax : co.vs * fmin;
+                const float gb = 2.0f * fmax * (fabsf(gh) + fabsf(eh)) * 1.00001f;
+                nlo += vlo - gb;
+                nhi += vhi + gb;
+            }
+        }
+        const float mu = lane_mean(L, px, py, pz, id);
+        if (len > 0.0f) {
+            const float dn = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            const float dm = m.skip_mean_lip * len * dn * 1.0001f;
+            const float sg = L.sigma;
+            f_lo = (sg >= 0.0f ? sg * nlo : sg * nhi) + mu - dm;
+            f_hi = (sg >= 0.0f ? sg * nhi : sg * nlo) + mu + dm;
+            dlen = len;
+        }
+        return L.sigma * noise + mu;
+    }
+
+    // steps of length `step` after p that keep the sign of f (f the value at p)
+    __device__ __forceinline__ int skips(float f, float step, int cap) const
+    {
+        if (!(dlen > 0.0f)) return 0;
+        const float margin = 1e-5f + 1e-6f * fmaxf(fabsf(f_lo), fabsf(f_hi));
+        const bool keep = f > 0.0f ? f_lo > margin : (f < 0.0f && f_hi < -margin);
+        if (!keep) return 0;
+        return (int)fminf(floorf(dlen / step * (1.0f - 1e-6f)), (float)cap);
+    }
+};
+
 // 1D evaluator with the three-cell impulse window in registers.  Each cached
 // impulse is its position t_i in [0,1) with the sign of its weight in the sign bit.
 template <int NMAX>
@@ -1566,6 +1721,24 @@ enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE
 
 // most march steps one evaluation may skip (fast pass)
 constexpr int kMaxSkip = 8;
+// at most this many steps skipped per evaluation of a 3D medium (the segment also ends
+// inside the query's cell)
+constexpr int kMaxSkip3D = 32;
+
+template <class E> struct IsSkip3D { static constexpr bool value = false; };
+template <> struct IsSkip3D<EvalSkip3D> { static constexpr bool value = true; };
+
+template <class Eval>
+__device__ __forceinline__ float eval_at(Eval &ev, const LaneField &L, const float *, const float p[3], int &id,
+                                         uint32_t &refills, bool live)
+{
+    return ev.value(L, p[0], p[1], p[2], id, refills, live);
+}
+__device__ __forceinline__ float eval_at(EvalSkip3D &ev, const LaneField &L, const float *d, const float p[3],
+                                         int &id, uint32_t &refills, bool live)
+{
+    return ev.value(L, d, p[0], p[1], p[2], id, refills, live);
+}
 // before a proposed crossing interval the cap is this (every skipped step is still certified)
 constexpr int kMaxSkipProposed = 16;
 
@@ -1756,8 +1929,16 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
         for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], eh, el);
         int id;
         const bool precise = RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE);
+        if constexpr (IsSkip3D<Eval>::value) {
+            // a marching step of a 3D medium asks for the field's range over the next
+            // steps: about half of |f| at the last step, and at least two steps
+            if (!RESUME && phase == PH_MARCH) {
+                const float len = fminf(0.5f * fabsf(pf), (float)kMaxSkip3D * step);
+                ev.plan(len >= 2.0f * step ? len : 0.0f);
+            }
+        }
         const float f = precise ? field_precise(L, p[0], p[1], p[2], id)
-                                : ev.value(L, p[0], p[1], p[2], id, c_refills, live);
+                                : eval_at(ev, L, d, p, id, c_refills, live);
         if (Eval::kCollective && !live) continue;
         gpid = id;
         const int sg = f < 0.0f ? -1 : 1;
@@ -1840,6 +2021,9 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     // counts, so the warp runs the longest lane's loop
                     const float cap = th < prop_a ? (float)kMaxSkipProposed : (float)kMaxSkip;
                     if (af > per) skip = (int)fminf(af / per, cap);
+                }
+                if constexpr (IsSkip3D<Eval>::value) {
+                    if (!RESUME) skip = ev.skips(f, step, kMaxSkip3D);
                 }
                 for (;;) {
                     if (!t_less(th, tl, far_t)) {
@@ -2476,6 +2660,10 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     } else if (coop) {
         const void *fn = (const void *)k_march<EvalCoop1D<8>, false>;
         k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(b);
+    } else if (a.three_d && a.max_oct == 1 && !a.any_ns) {
+        // 3D stationary single-octave media: the generic evaluator with step skipping
+        const void *fn = (const void *)k_march<EvalSkip3D, false>;
+        k_march<EvalSkip3D, false><<<grid(fn), 256, 0, stream>>>(b);
     } else {
         const void *fn = (const void *)k_march<EvalGeneric, false>;
         k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(b);
