@@ -1569,22 +1569,8 @@ struct EvalCoopOct {
     int rot[kOctMax];
     uint32_t valid;         // bit o: octave o's window is filled
     const PcgJump *sj;
-    // Step skipping: a marching step may plan a segment [p, p + D d]; the evaluation
-    // then also bounds the field over it (see value)
-    float want;             // planned length (world units along d; 0: none)
-    float dlen;             // the length bounded
-    float f_lo, f_hi;       // the field's range over it
 
-    __device__ __forceinline__ void reset() { valid = 0u; want = 0.0f; dlen = 0.0f; }
-    __device__ __forceinline__ void plan(float len) { want = len; }
-    __device__ __forceinline__ int skips(float f, float step, int cap) const
-    {
-        if (!(dlen > 0.0f)) return 0;
-        const float margin = 1e-5f + 1e-6f * fmaxf(fabsf(f_lo), fabsf(f_hi));
-        const bool keep = f > 0.0f ? f_lo > margin : (f < 0.0f && f_hi < -margin);
-        if (!keep) return 0;
-        return (int)fminf(floorf(dlen / step * (1.0f - 1e-6f)), (float)cap);
-    }
+    __device__ __forceinline__ void reset() { valid = 0u; }
     __device__ __forceinline__ void bind(const PcgJump *t)
     {
         extern __shared__ float4 dsm_oct[];
@@ -1632,18 +1618,7 @@ struct EvalCoopOct {
         __syncwarp();
     }
 
-    // The value, and with a planned segment [p, p + D d] the field's range over it:
-    // the segment ends inside every octave's current cell (less kSupportEps), so each
-    // octave's three-cell window holds every impulse that reaches it; the local scale
-    // ls stays within ls(p) +- its slope bound times the segment's lateral length; per
-    // impulse the kernel's largest value (nearest offset, largest ls; 0 when the
-    // segment misses the widened support) and smallest (farthest offset, smallest ls;
-    // 0 when the segment leaves the narrowed support) give [smallest, largest] for a
-    // positive weight and [-largest, -smallest] for a negative one, times the
-    // normalisation's range; the conditioning splats are bounded by their exact
-    // Gaussian range and the largest magnitude of the derivative term; the mean moves
-    // by at most its slope bound times the length.
-    __device__ __forceinline__ float value(const LaneField &L, const float *d, float px, float py, float pz,
+    __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
                                            int &id, uint32_t &refills, bool live)
     {
         const int lane = threadIdx.x & 31;
@@ -1653,63 +1628,6 @@ struct EvalCoopOct {
         const float kexp = L.kexp / (ls * ls);
         const float inv_norm = inv_norm_1d(m, ls);
         const float ca = splat_cov_1d(ls, L.ls_o);
-        // ---- the planned segment: its length inside every octave's cell, the range
-        // of the local scale over it and the per-octave cell-coordinate rates
-        float len = (live && m.skip_mean_lip >= 0.0f) ? want : 0.0f;
-        want = 0.0f;
-        dlen = 0.0f;
-        float ls_lo = ls, ls_hi = ls;
-        float ux = 0.0f, uy = 0.0f, uz = 0.0f;   // d in the octave-0 isotropic frame, per unit t
-        if (len > 0.0f) {
-            ux = m.l_inv[0] * d[0];
-            uy = m.l_inv[1] * d[1];
-            uz = m.l_inv[2] * d[2];
-            if (m.ls_kind) {
-                ux /= m.ls_max;
-                uy /= m.ls_max;
-                uz /= m.ls_max;
-                const float *q = m.ls_params;
-                const float g = fabsf(q[1]) * sqrtf(q[2] * q[2] + q[3] * q[3]) / m.ls_max;
-                const float dl = g * len * sqrtf(d[0] * d[0] + d[2] * d[2]) * 1.0001f + 1e-6f;
-                ls_lo = fmaxf(ls - dl, (q[0] - fabsf(q[1])) / m.ls_max * 0.9999f);
-                ls_hi = ls + dl;
-                if (!(ls_lo > 0.0f)) len = 0.0f;
-            }
-        }
-        if (len > 0.0f) {
-            // each octave's cell fraction, computed as the evaluation below computes it
-            float cx = __fmul_rn(m.l_inv[0], px), cy = __fmul_rn(m.l_inv[1], py), cz = __fmul_rn(m.l_inv[2], pz);
-            if (m.ls_kind) {
-                cx = __fdiv_rn(cx, m.ls_max);
-                cy = __fdiv_rn(cy, m.ls_max);
-                cz = __fdiv_rn(cz, m.ls_max);
-            }
-            for (int o = 0; o < n_oct; ++o) {
-                const float sc = oct_scale(m, o);
-                float qx = cx, qy = cy, qz = cz;
-                if (sc != 1.0f) {
-                    if ((m.oct_pow2 >> o) & 1u) {
-                        const float inv = m.oct_inv[o];
-                        qx = __fmul_rn(qx, inv); qy = __fmul_rn(qy, inv); qz = __fmul_rn(qz, inv);
-                    } else {
-                        qx = __fdiv_rn(qx, sc); qy = __fdiv_rn(qy, sc); qz = __fdiv_rn(qz, sc);
-                    }
-                }
-                const float tg = __fdiv_rn(dot3_rn(L.n[0], L.n[1], L.n[2], qx, qy, qz), L.kr);
-                const float fr = __fsub_rn(tg, floorf(tg));
-                const float u = (L.n[0] * ux + L.n[1] * uy + L.n[2] * uz) / (sc * L.kr);
-                // the segment stays 1e-3 of a cell inside the faces (the float rounding
-                // of the skipped points' coordinates is far below)
-                float room = 1e30f;
-                if (u > 0.0f) room = (1.0f - 1e-3f - fr) / u;
-                else if (u < 0.0f) room = (fr - 1e-3f) / -u;
-                len = fminf(len, fmaxf(room, 0.0f));
-            }
-        }
-        const bool bound = len > 0.0f;
-        const float kexp_hi = L.kexp / (ls_hi * ls_hi), kexp_lo = L.kexp / (ls_lo * ls_lo);
-        const float inv_lo = inv_norm_1d(m, ls_hi), inv_hi = inv_norm_1d(m, ls_lo);
-        float r_lo = 0.0f, r_hi = 0.0f;
         // the isotropic position (divided by the maximum lateral scale) once; each
         // octave divides it by its length multiplier, a multiply when that is a
         // power of two (the same rounding as ray_coord_oct's division)
@@ -1763,9 +1681,6 @@ struct EvalCoopOct {
             }
             if (!act) continue;
             float acc0 = 0.0f, acc1 = 0.0f;
-            float blo = 0.0f, bhi = 0.0f;
-            // the cell-coordinate offset of the segment's end
-            const float du = bound ? len * (L.n[0] * ux + L.n[1] * uy + L.n[2] * uz) / (sc * L.kr) : 0.0f;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const float tl = __fsub_rn(frac, (float)(c - 1));
@@ -1782,66 +1697,19 @@ struct EvalCoopOct {
                         const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(sgn) & 0x80000000u));
                         if (j & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
                         else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
-                        if (bound) {
-                            const float te = tp + du;
-                            const float amin = (tp < 0.0f) != (te < 0.0f) ? 0.0f : fminf(fabsf(tp), fabsf(te));
-                            const float amax = fmaxf(fabsf(tp), fabsf(te));
-                            if (amin < 1.0f + kSupportEps && !(sgn != sgn) && fabsf(sgn) < 2.0f) {
-                                const float big = ex2_approx(kexp_hi * (amin * amin)) * 1.00001f;
-                                const float small =
-                                    amax < 1.0f - kSupportEps ? ex2_approx(kexp_lo * (amax * amax)) * 0.99999f : 0.0f;
-                                if (__float_as_uint(sgn) & 0x80000000u) {
-                                    blo -= big;
-                                    bhi -= small;
-                                } else {
-                                    blo += small;
-                                    bhi += big;
-                                }
-                            }
-                        }
                     }
                 }
             }
             float nk = (acc0 + acc1) * inv_norm;
-            float nlo = fminf(blo * inv_lo, blo * inv_hi), nhi = fmaxf(bhi * inv_lo, bhi * inv_hi);
             if (L.cond) {
                 float vs, gz, oz;
                 lane_cond_1d(L, o, sc, vs, gz, oz);
                 const Cov1D kc = cov1d(z - oz, ca);
                 nk += vs * kc.k0 + gz * kc.k1;
-                if (bound) {
-                    // d = z - oz over the segment (iso units), ia2 = 1 / ca^2 over the ls range
-                    const float d0 = z - oz, d1 = d0 + du * L.kr;
-                    const float dmin = (d0 < 0.0f) != (d1 < 0.0f) ? 0.0f : fminf(fabsf(d0), fabsf(d1));
-                    const float dmax = fmaxf(fabsf(d0), fabsf(d1));
-                    float ia_lo = 1.0f, ia_hi = 1.0f;
-                    if (m.ls_kind) {
-                        ia_lo = 2.0f / (ls_hi * ls_hi + L.ls_o * L.ls_o) * 0.9999f;
-                        ia_hi = 2.0f / (ls_lo * ls_lo + L.ls_o * L.ls_o) * 1.0001f;
-                    }
-                    const float k0hi = ex2_approx((-0.25f * LOG2E) * ia_lo * dmin * dmin) * 1.00001f;
-                    const float k0lo = ex2_approx((-0.25f * LOG2E) * ia_hi * dmax * dmax) * 0.99999f;
-                    const float k1m = fminf(0.42888194f * sqrtf(ia_hi), 0.5f * ia_hi * dmax * k0hi) * 1.0001f;
-                    nlo += (vs >= 0.0f ? vs * k0lo : vs * k0hi) - fabsf(gz) * k1m;
-                    nhi += (vs >= 0.0f ? vs * k0hi : vs * k0lo) + fabsf(gz) * k1m;
-                }
             }
-            const float so = m.n_oct == 1 ? L.sigma : oct_sigma(m, o);
-            total += so * nk;
-            if (bound) {
-                r_lo += so >= 0.0f ? so * nlo : so * nhi;
-                r_hi += so >= 0.0f ? so * nhi : so * nlo;
-            }
+            total += (m.n_oct == 1 ? L.sigma : oct_sigma(m, o)) * nk;
         }
-        const float mu = lane_mean(L, px, py, pz, id);
-        if (bound) {
-            const float dn = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-            const float dm = m.skip_mean_lip * len * dn * 1.0001f;
-            f_lo = r_lo + mu - dm;
-            f_hi = r_hi + mu + dm;
-            dlen = len;
-        }
-        return total + mu;
+        return total + lane_mean(L, px, py, pz, id);
     }
 };
 
@@ -1853,14 +1721,12 @@ enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE
 
 // most march steps one evaluation may skip (fast pass)
 constexpr int kMaxSkip = 8;
-// at most this many steps skipped per evaluation by a range bound (the segment also
-// ends inside the query's cell)
+// at most this many steps skipped per evaluation of a 3D medium (the segment also ends
+// inside the query's cell)
 constexpr int kMaxSkip3D = 32;
 
-// evaluators that bound the field over a planned segment (step skipping by range)
 template <class E> struct IsSkip3D { static constexpr bool value = false; };
 template <> struct IsSkip3D<EvalSkip3D> { static constexpr bool value = true; };
-template <> struct IsSkip3D<EvalCoopOct> { static constexpr bool value = true; };
 
 template <class Eval>
 __device__ __forceinline__ float eval_at(Eval &ev, const LaneField &L, const float *, const float p[3], int &id,
@@ -1869,11 +1735,6 @@ __device__ __forceinline__ float eval_at(Eval &ev, const LaneField &L, const flo
     return ev.value(L, p[0], p[1], p[2], id, refills, live);
 }
 __device__ __forceinline__ float eval_at(EvalSkip3D &ev, const LaneField &L, const float *d, const float p[3],
-                                         int &id, uint32_t &refills, bool live)
-{
-    return ev.value(L, d, p[0], p[1], p[2], id, refills, live);
-}
-__device__ __forceinline__ float eval_at(EvalCoopOct &ev, const LaneField &L, const float *d, const float p[3],
                                          int &id, uint32_t &refills, bool live)
 {
     return ev.value(L, d, p[0], p[1], p[2], id, refills, live);
@@ -2069,8 +1930,8 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
         int id;
         const bool precise = RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE);
         if constexpr (IsSkip3D<Eval>::value) {
-            // a marching step asks for the field's range over the next steps: about
-            // half of |f| at the last step, and at least two steps
+            // a marching step of a 3D medium asks for the field's range over the next
+            // steps: about half of |f| at the last step, and at least two steps
             if (!RESUME && phase == PH_MARCH) {
                 const float len = fminf(0.5f * fabsf(pf), (float)kMaxSkip3D * step);
                 ev.plan(len >= 2.0f * step ? len : 0.0f);
