@@ -1569,8 +1569,9 @@ struct EvalCoopOct {
     int rot[kOctMax];
     uint32_t valid;         // bit o: octave o's window is filled
     const PcgJump *sj;
+    float last_ls;          // the local scale at the last evaluated point
 
-    __device__ __forceinline__ void reset() { valid = 0u; }
+    __device__ __forceinline__ void reset() { valid = 0u; last_ls = 1.0f; }
     __device__ __forceinline__ void bind(const PcgJump *t)
     {
         extern __shared__ float4 dsm_oct[];
@@ -1625,6 +1626,7 @@ struct EvalCoopOct {
         const DevMedium &m = *L.m;
         const int n_oct = live ? (int)m.n_oct : 0;
         const float ls = live ? ns_scale(m, px, pz) : 1.0f;
+        last_ls = ls;
         const float kexp = L.kexp / (ls * ls);
         const float inv_norm = inv_norm_1d(m, ls);
         const float ca = splat_cov_1d(ls, L.ls_o);
@@ -1724,6 +1726,78 @@ constexpr int kMaxSkip = 8;
 // at most this many steps skipped per evaluation of a 3D medium (the segment also ends
 // inside the query's cell)
 constexpr int kMaxSkip3D = 32;
+
+// Step skipping for multi-octave and nonstationary 1D media (EvalCoopOct): a
+// Lipschitz bound along the ray over the next kMaxSkip3D steps, from the local
+// scale's range there.  Octave k's noise is A(ls) S_k + C_k with S_k the sum of at
+// most 3N truncated splats exp(-(z_k - z_i)^2 / (2 ls^2)) in the octave's iso
+// coordinate z_k (|dz_k/dt| <= |l_inv o d| / (ls_max sc_k)), A(ls) = inv_norm1d
+// ls^-1/2 the normalisation and C_k the conditioning splats.  Per splat |dK/dz| <=
+// e^-1/2 / ls and |dK/dls| <= 2 / (e ls); |S_k| <= 3N; |dA/dls| = A / (2 ls); the
+// conditioning kernels k0 = exp(-ia2 d^2 / 4), k1 = -ia2 d k0 / 2 with ia2 = 2 /
+// (ls^2 + ls_o^2) (1 when stationary) have |dk0/dd| <= 0.42888 sqrt(ia2), |dk1/dd|
+// <= ia2 / 2, |dk0/dia2| <= 1 / (e ia2), |dk1/dia2| <= 0.84 / sqrt(ia2) and
+// |dia2/dls| <= 4 ls / (ls^2 + ls_o^2)^2; ls changes by at most |q1| sqrt(q2^2 +
+// q3^2) / ls_max per unit of lateral (x, z) travel.  Every bound takes the worst
+// local scale of the range.  A splat jumps by at most exp(-kr^2 / (2 ls_hi^2)) where
+// the query crosses its support, and 2N (cells crossed + 1) crossings per octave
+// are allowed for, as for single-octave media.  Returns the steps after the
+// evaluated point that keep the sign of f (margins as for single-octave media).
+__device__ __forceinline__ int oct_skip_count(const DevMedium &m, const LaneField &L, const float d[3], float ls_p,
+                                              float f, float step, int cap)
+{
+    if (m.skip_mean_lip < 0.0f) return 0;
+    const float span = (float)cap * step;
+    float ls_lo = ls_p, ls_hi = ls_p, dls = 0.0f;
+    const float lx = m.l_inv[0] * d[0], ly = m.l_inv[1] * d[1], lz = m.l_inv[2] * d[2];
+    float dn = sqrtf(lx * lx + ly * ly + lz * lz) * 1.0001f;
+    if (m.ls_kind) {
+        const float *q = m.ls_params;
+        dls = fabsf(q[1]) * sqrtf(q[2] * q[2] + q[3] * q[3]) / m.ls_max * sqrtf(d[0] * d[0] + d[2] * d[2]) * 1.0001f;
+        const float glo = (q[0] - fabsf(q[1])) / m.ls_max, ghi = (q[0] + fabsf(q[1])) / m.ls_max;
+        ls_lo = fmaxf(ls_p - dls * span - 1e-6f, glo * 0.9999f);
+        ls_hi = fminf(ls_p + dls * span + 1e-6f, ghi * 1.0001f);
+        if (!(ls_lo > 0.0f)) return 0;
+        dn /= m.ls_max;
+    }
+    const float n3 = 3.0f * (float)m.n_imp;
+    const float a_lo = m.inv_norm1d * rsqrtf(ls_lo) * 1.0001f;    // the largest normalisation
+    const float e_h = 0.60653066f, e_1 = 0.36787944f;
+    const float jump = expf(-0.5f * m.kr_iso * m.kr_iso / (ls_hi * ls_hi)) * 1.0001f;
+    const float ia_hi = m.ls_kind ? 2.0f / (ls_lo * ls_lo + L.ls_o * L.ls_o) : 1.0f;
+    const float ia_lo = m.ls_kind ? 2.0f / (ls_hi * ls_hi + L.ls_o * L.ls_o) : 1.0f;
+    const float dia = m.ls_kind ? 4.0f * ls_hi / ((ls_lo * ls_lo + L.ls_o * L.ls_o) * (ls_lo * ls_lo + L.ls_o * L.ls_o))
+                                : 0.0f;
+    float lip = m.skip_mean_lip * sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    float j0 = 0.0f, j1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kOctMax; ++k) {
+        if (k >= (int)m.n_oct) break;
+        const float sg = fabsf(oct_sigma(m, k));
+        const float sc = oct_scale(m, k);
+        const float dz = dn / sc;
+        float slope = a_lo * n3 * (e_h / ls_lo * dz + 2.0f * e_1 / ls_lo * dls) + n3 * a_lo / (2.0f * ls_lo) * dls;
+        if (L.cond) {
+            float vs, gz, oz;
+            lane_cond_1d(L, k, sc, vs, gz, oz);
+            slope += (0.42888194f * sqrtf(ia_hi) * fabsf(vs) + 0.5f * ia_hi * fabsf(gz)) * dz;
+            if (m.ls_kind)
+                slope += (fabsf(vs) * e_1 / ia_lo + fabsf(gz) * 0.84f * rsqrtf(ia_lo)) * dia * dls;
+        }
+        lip += sg * slope;
+        const float jn = sg * a_lo * jump * 2.0f * (float)m.n_imp * 1.01f;
+        j0 += 3.0f * jn;
+        j1 += jn * (step * dz / m.kr_iso);
+    }
+    lip *= 1.01f;
+    const float af = fabsf(f) * (1.0f - 1e-6f) - 1e-5f - j0;
+    const float per = lip * step + j1;
+    if (!(af > per)) return 0;
+    return (int)fminf(af / per, (float)cap);
+}
+
+template <class E> struct IsOct { static constexpr bool value = false; };
+template <> struct IsOct<EvalCoopOct> { static constexpr bool value = true; };
 
 template <class E> struct IsSkip3D { static constexpr bool value = false; };
 template <> struct IsSkip3D<EvalSkip3D> { static constexpr bool value = true; };
@@ -2024,6 +2098,9 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 }
                 if constexpr (IsSkip3D<Eval>::value) {
                     if (!RESUME) skip = ev.skips(f, step, kMaxSkip3D);
+                }
+                if constexpr (IsOct<Eval>::value) {
+                    if (!RESUME) skip = oct_skip_count(*L.m, L, d, ev.last_ls, f, step, kMaxSkip3D);
                 }
                 for (;;) {
                     if (!t_less(th, tl, far_t)) {

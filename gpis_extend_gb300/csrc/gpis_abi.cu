@@ -181,11 +181,10 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         m.oct_inv[k] = 1.0f / m.oct_scale[k];
         if (pow2) m.oct_pow2 |= 1u << k;
     }
-    // Lipschitz bounds for step skipping: stationary single-octave media (1D or 3D
-    // noise) with a mean whose slope is bounded (SDFs are 1-Lipschitz; a linear mean
-    // has the slope of its scaled normal)
+    // The mean's slope bound for step skipping (SDFs are 1-Lipschitz; a linear mean
+    // has the slope of its scaled normal); not for multi-resolution media
     m.skip_mean_lip = -1.0f;
-    if (d.n_octaves == 1 && d.ls_kind == GPIS_LS_CONSTANT) {
+    if (!multires) {
         switch (d.mean_kind) {
         case GPIS_MEAN_SPHERE: case GPIS_MEAN_TORUS: case GPIS_MEAN_TORUS_PLANE: m.skip_mean_lip = 1.0f; break;
         case GPIS_MEAN_HOMOGENEOUS: m.skip_mean_lip = 0.0f; break;
