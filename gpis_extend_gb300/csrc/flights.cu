@@ -1723,6 +1723,8 @@ enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE
 
 // most march steps one evaluation may skip (fast pass)
 constexpr int kMaxSkip = 8;
+// multi-octave media (EvalCoopOct): their evaluation costs more than the skip loop
+constexpr int kMaxSkipOct = 16;
 // at most this many steps skipped per evaluation of a 3D medium (the segment also ends
 // inside the query's cell)
 constexpr int kMaxSkip3D = 32;
@@ -2100,7 +2102,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     if (!RESUME) skip = ev.skips(f, step, kMaxSkip3D);
                 }
                 if constexpr (IsOct<Eval>::value) {
-                    if (!RESUME) skip = oct_skip_count(*L.m, L, d, ev.last_ls, f, step, kMaxSkip3D);
+                    if (!RESUME) skip = oct_skip_count(*L.m, L, d, ev.last_ls, f, step, kMaxSkipOct);
                 }
                 for (;;) {
                     if (!t_less(th, tl, far_t)) {
