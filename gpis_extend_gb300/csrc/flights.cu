@@ -1435,8 +1435,9 @@ struct EvalCoop1D {
     int base;
     bool valid;
     const PcgJump *sj;      // the jump table in shared memory
+    float last_ls;          // nonstationary: the local scale at the last evaluated point
 
-    __device__ __forceinline__ void reset() { valid = false; base = 0; }
+    __device__ __forceinline__ void reset() { valid = false; base = 0; last_ls = 1.0f; }
     __device__ __forceinline__ void bind(const PcgJump *t) { sj = t; }
 
     template <int S>
@@ -1490,6 +1491,7 @@ struct EvalCoop1D {
         float z, kexp = L.kexp, inv_norm = L.inv_norm, ca = 1.0f;
         if (NS && L.ns) {
             const float ls = ns_scale(*L.m, px, pz);
+            last_ls = ls;
             z = ray_coord_oct(*L.m, L.n, px, py, pz, 1.0f);
             kexp = L.kexp / (ls * ls);
             inv_norm = inv_norm_1d(*L.m, ls);
@@ -1723,15 +1725,14 @@ enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE
 
 // most march steps one evaluation may skip (fast pass)
 constexpr int kMaxSkip = 8;
-// multi-octave media (EvalCoopOct): their evaluation costs more than the skip loop
-constexpr int kMaxSkipOct = 16;
 // at most this many steps skipped per evaluation of a 3D medium (the segment also ends
 // inside the query's cell)
 constexpr int kMaxSkip3D = 32;
 
-// Step skipping for multi-octave and nonstationary 1D media (EvalCoopOct): a
-// Lipschitz bound along the ray over the next kMaxSkip3D steps, from the local
-// scale's range there.  Octave k's noise is A(ls) S_k + C_k with S_k the sum of at
+// Step skipping for multi-octave and nonstationary 1D media (EvalCoopOct, and
+// EvalCoop1D's nonstationary form): a Lipschitz bound along the ray over the next
+// `cap` steps, from the local scale's range there (multi-octave evaluations cost
+// more than the warp's skip loop, so they may skip 16 steps; single-octave ones 8).  Octave k's noise is A(ls) S_k + C_k with S_k the sum of at
 // most 3N truncated splats exp(-(z_k - z_i)^2 / (2 ls^2)) in the octave's iso
 // coordinate z_k (|dz_k/dt| <= |l_inv o d| / (ls_max sc_k)), A(ls) = inv_norm1d
 // ls^-1/2 the normalisation and C_k the conditioning splats.  Per splat |dK/dz| <=
@@ -1798,8 +1799,10 @@ __device__ __forceinline__ int oct_skip_count(const DevMedium &m, const LaneFiel
     return (int)fminf(af / per, (float)cap);
 }
 
-template <class E> struct IsOct { static constexpr bool value = false; };
-template <> struct IsOct<EvalCoopOct> { static constexpr bool value = true; };
+// the evaluators whose fast pass skips by oct_skip_count, and the cap of each
+template <class E> struct IsOct { static constexpr bool value = false; static constexpr int cap = 0; };
+template <> struct IsOct<EvalCoopOct> { static constexpr bool value = true; static constexpr int cap = 16; };
+template <> struct IsOct<EvalCoop1D<8, false, true>> { static constexpr bool value = true; static constexpr int cap = 8; };
 
 template <class E> struct IsSkip3D { static constexpr bool value = false; };
 template <> struct IsSkip3D<EvalSkip3D> { static constexpr bool value = true; };
@@ -2102,7 +2105,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     if (!RESUME) skip = ev.skips(f, step, kMaxSkip3D);
                 }
                 if constexpr (IsOct<Eval>::value) {
-                    if (!RESUME) skip = oct_skip_count(*L.m, L, d, ev.last_ls, f, step, kMaxSkipOct);
+                    if (!RESUME) skip = oct_skip_count(*L.m, L, d, ev.last_ls, f, step, IsOct<Eval>::cap);
                 }
                 for (;;) {
                     if (!t_less(th, tl, far_t)) {

@@ -108,7 +108,12 @@ def test_gpu_nonstationary_flights_vs_oracle(ns, octaves, mr):
     desc = workloads.torus_plane_medium(nonstationary=bool(ns), octaves=octaves, multires=mr)
     prim = workloads.sphere_flights(1 << 14, desc)
     with runtime.Context(desc) as ctx:
+        ctx.counters(reset=True)
         rec = ctx.trace_host(prim)
+        cnt = ctx.counters(reset=True)
+        if not mr:
+            # the fast pass skips certified steps (the slope bound at the local scale's range)
+            assert cnt["skipped_steps"] > 0.1 * cnt["steps"], cnt
         flights_vs_oracle(desc, prim, rec)
         rec_cpu = oracle.trace_flights(desc, prim)
         sec, _ = workloads.secondary_flights(prim, rec_cpu, desc)
