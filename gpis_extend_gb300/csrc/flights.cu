@@ -2107,6 +2107,15 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 if constexpr (IsOct<Eval>::value) {
                     if (!RESUME) skip = oct_skip_count(*L.m, L, d, ev.last_ls, f, step, IsOct<Eval>::cap);
                 }
+                if constexpr (RESUME) {
+                    // a flight that marches on after a decision skips by the same slope bound
+                    // (1D media); the value before a later crossing is then no longer the
+                    // last one evaluated, so the refinement re-evaluates it
+                    if (L.m->flags & MF_ONE_D) {
+                        skip = oct_skip_count(*L.m, L, d, ns_scale(*L.m, p[0], p[2]), f, step, kMaxSkip);
+                        if (skip > 0) pf_precise = false;
+                    }
+                }
                 for (;;) {
                     if (!t_less(th, tl, far_t)) {
                         phase = PH_FAR;
