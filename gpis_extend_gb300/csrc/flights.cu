@@ -1870,6 +1870,9 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     Eval ev;
     ev.reset();
     ev.bind(s_jump);
+    // the resume pass marches 3D flights on with the range-bounded evaluator
+    EvalSkip3D ev3;
+    ev3.reset();
     LaneField L;
     lane_field_idle(L, a.media);
     int phase = PH_IDLE;
@@ -2016,8 +2019,18 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 ev.plan(len >= 2.0f * step ? len : 0.0f);
             }
         }
+        bool use3 = false;
+        if constexpr (RESUME) {
+            const DevMedium &m3 = *L.m;
+            use3 = !precise && phase == PH_MARCH && !(m3.flags & MF_ONE_D) && m3.n_oct == 1 && m3.ls_kind == 0u;
+            if (use3) {
+                const float len = fminf(0.5f * fabsf(pf), (float)kMaxSkip3D * step);
+                ev3.plan(len >= 2.0f * step ? len : 0.0f);
+            }
+        }
         const float f = precise ? field_precise(L, p[0], p[1], p[2], id)
-                                : eval_at(ev, L, d, p, id, c_refills, live);
+                                : (use3 ? ev3.value(L, d, p[0], p[1], p[2], id, c_refills, live)
+                                        : eval_at(ev, L, d, p, id, c_refills, live));
         if (Eval::kCollective && !live) continue;
         gpid = id;
         const int sg = f < 0.0f ? -1 : 1;
@@ -2109,12 +2122,14 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 }
                 if constexpr (RESUME) {
                     // a flight that marches on after a decision skips by the same slope bound
-                    // (1D media); the value before a later crossing is then no longer the
-                    // last one evaluated, so the refinement re-evaluates it
-                    if (L.m->flags & MF_ONE_D) {
+                    // (1D media) or range bound (3D media); the value before a later
+                    // crossing is then no longer the last one evaluated, so the refinement
+                    // re-evaluates it
+                    if (L.m->flags & MF_ONE_D)
                         skip = oct_skip_count(*L.m, L, d, ns_scale(*L.m, p[0], p[2]), f, step, kMaxSkip);
-                        if (skip > 0) pf_precise = false;
-                    }
+                    else if (use3)
+                        skip = ev3.skips(f, step, kMaxSkip3D);
+                    if (skip > 0) pf_precise = false;
                 }
                 for (;;) {
                     if (!t_less(th, tl, far_t)) {
