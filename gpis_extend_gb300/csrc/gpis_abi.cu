@@ -717,24 +717,10 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis
     // previous chunk out (another) overlap the flight kernels, and the chunks'
     // kernels alternate between two compute streams on disjoint slices of the
     // scratch, so one chunk's tail overlaps the next chunk's start.
-    // The chunks ramp up and down (per/8, per/4, per/2, per, ..., per, per/2, per/4,
-    // per/8): the first kernels wait for a short copy in and the last copy out is short.
     const uint32_t chunk = ctx->tune[GPIS_TUNE_HOST_CHUNK] ? (uint32_t)ctx->tune[GPIS_TUNE_HOST_CHUNK] : (1u << 20);
     uint32_t per = n > 3 * (uint64_t)chunk ? chunk : n;
-    if ((n + per - 1) / per > kMaxChunks - 6) per = (n + kMaxChunks - 7) / (kMaxChunks - 6);
-    std::vector<uint32_t> bounds{0};
-    {
-        const uint32_t r1 = per >> 3, r2 = per >> 2, r3 = per >> 1;
-        const bool ramp = per < n && r1 >= 4096 && (uint64_t)n >= 2ull * (r1 + r2 + r3) + per;
-        uint32_t at = 0;
-        if (ramp)
-            for (uint32_t r : {r1, r2, r3}) bounds.push_back(at += r);
-        const uint32_t tail = ramp ? r1 + r2 + r3 : 0u;
-        while (n - at > tail) bounds.push_back(at += std::min<uint32_t>(per, n - at - tail));
-        if (ramp)
-            for (uint32_t r : {r3, r2, r1}) bounds.push_back(at += r);
-    }
-    const uint32_t chunks = (uint32_t)bounds.size() - 1;
+    if ((n + per - 1) / per > kMaxChunks) per = (n + kMaxChunks - 1) / kMaxChunks;
+    const uint32_t chunks = (n + per - 1) / per;
     int rc0 = ensure_scratch(ctx, n);
     if (rc0) return rc0;
     while (ctx->ev_chunks.size() < 2 * (size_t)chunks) {
@@ -744,7 +730,7 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis
     }
     cudaStream_t s = ctx->stream, hs = ctx->h2d_stream, ds = ctx->d2h_stream;
     for (uint32_t k = 0; k < chunks; ++k) {
-        const size_t o = bounds[k], m = bounds[k + 1] - bounds[k];
+        const size_t o = (size_t)k * per, m = std::min<size_t>(per, n - o);
         const size_t b16 = m * 16;
         CUDA_TRY(cudaMemcpyAsync(d_on + 4 * o, in->origin_near + 4 * o, b16, cudaMemcpyHostToDevice, hs), "copy origins");
         CUDA_TRY(cudaMemcpyAsync(d_df + 4 * o, in->dir_far + 4 * o, b16, cudaMemcpyHostToDevice, hs), "copy directions");
@@ -767,7 +753,7 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis
     // results out after every chunk is enqueued: a copy to pageable memory blocks the
     // calling thread until it is done, which must not hold back the later chunks
     for (uint32_t k = 0; k < chunks; ++k) {
-        const size_t o = bounds[k], m = bounds[k + 1] - bounds[k];
+        const size_t o = (size_t)k * per, m = std::min<size_t>(per, n - o);
         CUDA_TRY(cudaStreamWaitEvent(ds, ctx->ev_chunks[2 * k + 1], 0), "wait for kernels");
         CUDA_TRY(cudaMemcpyAsync(out->rec + 8 * o, d_rec + 8 * o, 2 * m * 16, cudaMemcpyDeviceToHost, ds),
                  "copy results");
