@@ -514,7 +514,10 @@ def run_image(args):
                      "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
                      "kernel": "k_march (fast + resume passes) inside gpis_render (one profiled render)",
                      "flops_per_eval": fpe, "evals": evals, "march_ms": kms[1],
-                     "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, best of 5, measured in this run"},
+                     "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, best of 5, measured in this run",
+            "ops32": {"per_eval": ops_eval, "achieved": ops_achieved, "peak": ops_peak, "unit": "Tops/s",
+                      "frac": (ops_achieved / ops_peak) if ops_peak else None,
+                      "peak_source": f"{sms} SMs x {roofline.LANES_PER_SM} 32-bit lanes x the sampled SM clock"}},
         "image": {"mean": float(img.mean()), "max": float(img.max())},
         "counters": cnt,
         "clocks": clocks.summary(),
@@ -649,6 +652,14 @@ def main():
     tr = load_traffic()
     if tr and tr.get("bytes_per_flight"):
         traffic = tr["bytes_per_flight"] * flights_per_step / 2.0
+    # beside the flops: all 32-bit operations of the reference formulation (flops plus
+    # the hash, PCG and compare work) against the SMs' 32-bit lane throughput at the
+    # clock sampled during the timed region
+    ops_eval = roofline.flops_per_eval_1d(8) + roofline.int_ops_per_eval_1d(8)
+    ops_achieved = evals_march * ops_eval / march_launches / (march_ms * 1e-3) / 1e12
+    sm_mhz = clocks.summary().get("sm_mhz") or 0.0
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    ops_peak = sms * roofline.LANES_PER_SM * sm_mhz * 1e6 / 1e12 if sm_mhz else None
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if peak else None, "traffic": traffic,
             "kernel": "k_march<EvalCoop1D<8>> fast pass + k_march<EvalGeneric> resume pass",

@@ -13,7 +13,8 @@ with FMA = 2 flops and exp = 1 op, independent of how the kernel computes it:
   conditioning splats and mean.
 
 The integer work of the cell hash and the PCG draws (3 hashes, 6 warm-up draws
-and 6N draws per evaluation in the reference) is not counted as flops.
+and 6N draws per evaluation in the reference) is not counted as flops; it is
+counted separately below as 32-bit operations.
 """
 
 FLOPS_PER_INSIDE_IMPULSE = 9
@@ -30,6 +31,29 @@ def flops_per_eval_3d(impulses_per_cell):
     # form, exp, weighted accumulate); 60 flops of overhead (evaluateNoise3D).
     impulses = 27 * impulses_per_cell
     return impulses * 5 + impulses * 0.155 * 20 + 60
+
+
+# Integer and compare work of one 1D evaluation in the reference formulation, reported
+# beside the flops (the path's arithmetic is mostly this): 32-bit operations counted
+# from MathUtil::xxhash32(Vec2u) (MathUtil.hpp:190-198: a multiply-add and an add, the
+# rotate, three multiplies and three xor-shifts = 12) and UniformSampler::nextI
+# (UniformSampler.hpp:44-51: the 64-bit multiply-add as three 32-bit multiply-adds and
+# a carried add, the 64-bit xor-shift, the extract and the variable rotate = 17), plus
+# BitManip::normalizedUint (shift, or, subtract = 3).  Per cell: the hash, set_state
+# and the two warm-up draws; per impulse: two draws with their float conversion, the
+# Bernoulli select and the inside test (difference and compare) = 6 more.
+INT_OPS_HASH2 = 12
+INT_OPS_DRAW = 17 + 3
+INT_OPS_PER_CELL = INT_OPS_HASH2 + 1 + 2 * INT_OPS_DRAW
+INT_OPS_PER_IMPULSE = 2 * INT_OPS_DRAW + 6
+
+
+def int_ops_per_eval_1d(impulses_per_cell):
+    return 3 * INT_OPS_PER_CELL + 3 * impulses_per_cell * INT_OPS_PER_IMPULSE
+
+
+# 32-bit lanes per SM that execute integer and FP32 operations (Blackwell SM: 4 x 32)
+LANES_PER_SM = 128
 
 
 # Flight record traffic: 4 input streams of 16 B and 2 result records of 16 B.
