@@ -1890,14 +1890,9 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     const uint32_t n_live = live_n(a);
 
     for (;;) {
-        // the resume pass pulls again for lanes whose flight the fast pass finished, so
-        // that fewer lanes sit out the next evaluation (a few rounds at most)
-#pragma unroll 1
-        for (int pull_round = 0; pull_round < (RESUME ? 4 : 1); ++pull_round) {
         const bool need = phase == PH_IDLE && !drained;
         const unsigned need_mask = __ballot_sync(FULL, need);
-        if (!need_mask) break;
-        {
+        if (need_mask) {
             const int leader = __ffs(need_mask) - 1;
             uint32_t base = 0;
             if (lane == leader) base = atomicAdd(work, (uint32_t)__popc(need_mask));
@@ -2000,7 +1995,6 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     }
                 }
             }
-        }
         }
         const bool live = phase != PH_IDLE;
         if (!__any_sync(FULL, live)) {
