@@ -986,77 +986,6 @@ __device__ float noise1d_precise(const DevMedium &m, float z, uint32_t seed, flo
     return __fdiv_rn(sv, __fsqrt_rn(var));
 }
 
-// The three-cell impulse window of a thread's last precise 1D evaluation, in shared
-// memory (slot j of the thread at col[j * 256], 256 threads per block): the precise
-// evaluations of one flight in the resume pass (the crossing step, the step before it
-// and the refinement points) lie within a step of each other and almost always in the
-// same cells, so all but the first read the impulses instead of drawing them.  Each
-// entry is the position t_i with the sign of the weight in the sign bit.  The window is
-// keyed by the medium, the seed and the middle cell.
-struct PreciseWindow {
-    float *col;
-    const DevMedium *m;
-    uint32_t seed;
-    int base;
-};
-constexpr int kWinStride = 256;
-
-__device__ __forceinline__ void window_fill(PreciseWindow &W, const DevMedium &m, int cell, uint32_t seed, int slot)
-{
-    const uint32_t s = xxhash2((uint32_t)cell, seed) + 1u;
-    for (uint32_t k = 0; k < m.n_imp; ++k) {
-        const float ti = unit_float(pcg_draw(c_jump[2 + 2 * k], s));
-        const uint32_t wr = pcg_draw(c_jump[3 + 2 * k], s);
-        W.col[(slot * 8 + (int)k) * kWinStride] = __uint_as_float(__float_as_uint(ti) | ((wr >> 31) ? 0u : 0x80000000u));
-    }
-}
-
-// noise1d_precise's arithmetic, op for op, with the impulses from the window (media
-// with at most 8 impulses per cell)
-__device__ float noise1d_precise_win(const DevMedium &m, float z, uint32_t seed, float ls, PreciseWindow &W)
-{
-    const float kr = m.kr_iso;
-    const float tg = __fdiv_rn(z, kr);
-    const float fl = floorf(tg);
-    const float frac = __fsub_rn(tg, fl);
-    const int ci = (int)fl;
-    if (W.m != &m || W.seed != seed || W.base != ci) {
-        if (W.m == &m && W.seed == seed && ci == W.base + 1) {
-            for (int j = 0; j < 16; ++j) W.col[j * kWinStride] = W.col[(j + 8) * kWinStride];
-            window_fill(W, m, ci + 1, seed, 2);
-        } else if (W.m == &m && W.seed == seed && ci == W.base - 1) {
-            for (int j = 15; j >= 0; --j) W.col[(j + 8) * kWinStride] = W.col[j * kWinStride];
-            window_fill(W, m, ci - 1, seed, 0);
-        } else {
-            for (int dx = -1; dx <= 1; ++dx) window_fill(W, m, ci + dx, seed, dx + 1);
-        }
-        W.m = &m;
-        W.seed = seed;
-        W.base = ci;
-    }
-    const float den = __fmul_rn(2.0f, __fmul_rn(ls, ls));
-    float sv = 0.0f;
-    for (int dx = -1; dx <= 1; ++dx) {
-        const float tl = __fsub_rn(frac, (float)dx);
-        const float a = __fmul_rn(kr, tl);
-        float cv = 0.0f;
-        for (uint32_t k = 0; k < m.n_imp; ++k) {
-            const float q = W.col[((dx + 1) * 8 + (int)k) * kWinStride];
-            const float ti = fabsf(q);
-            const float tp = __fsub_rn(tl, ti);
-            if (fabsf(tp) < 1.0f) {
-                const float ab = __fsub_rn(a, __fmul_rn(kr, ti));
-                const float e = expf(-__fdiv_rn(__fmul_rn(ab, ab), den));
-                cv = __fadd_rn(cv, (__float_as_uint(q) & 0x80000000u) ? -e : e);
-            }
-        }
-        sv = __fadd_rn(sv, cv);
-    }
-    if (ls == 1.0f) return __fdiv_rn(sv, m.norm1d);
-    const float var = (float)((double)m.var1d_c * (1.7724538509055159 * (double)ls));
-    return __fdiv_rn(sv, __fsqrt_rn(var));
-}
-
 __device__ float noise3d_precise(const DevMedium &m, float px, float py, float pz, uint32_t seed)
 {
     const float kr = m.kr_world;
@@ -1148,7 +1077,7 @@ __device__ float mean_plus_precise(const DevMedium &m, float an, float x, float 
     return __fadd_rn(s, e);
 }
 
-__device__ float field_precise(const LaneField &L, float px, float py, float pz, int &id, PreciseWindow *W = nullptr)
+__device__ float field_precise(const LaneField &L, float px, float py, float pz, int &id)
 {
     const DevMedium &m = *L.m;
     if (!(m.flags & MF_ONE_D)) {
@@ -1194,8 +1123,7 @@ __device__ float field_precise(const LaneField &L, float px, float py, float pz,
         const float sc = oct_scale(m, k);
         const float z = m.n_oct == 1 && m.ls_kind == 0u ? ray_coord(L.li, L.n, px, py, pz)
                                                           : ray_coord_oct(m, L.n, px, py, pz, sc);
-        float noise = (W && m.n_oct == 1 && m.n_imp <= 8) ? noise1d_precise_win(m, z, L.seed, ls, *W)
-                                                          : noise1d_precise(m, z, L.seed + oct_seed(m, k), ls);
+        float noise = noise1d_precise(m, z, L.seed + oct_seed(m, k), ls);
         if (L.cond) {
             // covarianceKernel1DVal / 1stGrad (GPFunctions.cpp:850-862) at the local
             // scale a: den2 = 2 (a sqrt2)^2 in float, the derivative in double
@@ -1945,9 +1873,6 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     // the resume pass marches 3D flights on with the range-bounded evaluator
     EvalSkip3D ev3;
     ev3.reset();
-    // and keeps each thread's last precise 1D impulse window (256 threads per block)
-    __shared__ float s_win[RESUME ? 24 * kWinStride : 1];
-    PreciseWindow win{s_win + threadIdx.x, nullptr, 0u, 0};
     LaneField L;
     lane_field_idle(L, a.media);
     int phase = PH_IDLE;
@@ -2103,7 +2028,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 ev3.plan(len >= 2.0f * step ? len : 0.0f);
             }
         }
-        const float f = precise ? field_precise(L, p[0], p[1], p[2], id, RESUME ? &win : nullptr)
+        const float f = precise ? field_precise(L, p[0], p[1], p[2], id)
                                 : (use3 ? ev3.value(L, d, p[0], p[1], p[2], id, c_refills, live)
                                         : eval_at(ev, L, d, p, id, c_refills, live));
         if (Eval::kCollective && !live) continue;
