@@ -36,9 +36,8 @@ struct FlightArgs {
     uint32_t n;
     CondRec *cond;              // scratch, n records
     double *t_end;              // scratch, n values (double march parameter at the end point)
-    uint32_t *work;             // scratch, 4 counters zeroed before the march: march work,
-                                // resume-queue length, resume work, unused
-    uint32_t *queue;            // scratch, n flight indices handed to the resume pass
+    uint32_t *work;             // scratch, 4 counters zeroed before the march: the fast pass's
+                                // and the resume pass's work counters (0 and 2)
     uint4 *resume;              // scratch, n saved march states
     float4 *setup;              // scratch, 4 per flight: the fast pass's per-flight set-up, written by
                                 // k_prepare when the stationary cooperative evaluator runs (else unused)

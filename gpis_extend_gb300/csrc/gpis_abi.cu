@@ -488,7 +488,6 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.cond = ctx->d_cond + offset;
     a.t_end = ctx->d_tend + offset;
     a.work = work;
-    a.queue = nullptr;
     a.resume = ctx->d_resume + offset;
     a.setup = ctx->d_setup + 4 * offset;
     a.counters = ctx->d_counters;

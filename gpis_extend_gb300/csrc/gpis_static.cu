@@ -120,7 +120,6 @@ extern "C" int gpis_flights_submit_static(const gpis_medium_desc *medium, const 
     a.cond = reinterpret_cast<gpis::CondRec *>(b + kOffCond);
     a.t_end = reinterpret_cast<double *>(b + kOffTEnd);
     a.work = reinterpret_cast<uint32_t *>(b + kOffWork);
-    a.queue = nullptr;
     a.resume = reinterpret_cast<uint4 *>(b + kOffResume);
     a.setup = reinterpret_cast<float4 *>(b + kOffSetup);
     a.counters = reinterpret_cast<unsigned long long *>(b + kOffCounters);
