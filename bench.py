@@ -623,6 +623,7 @@ def main():
     pin_p = runtime.PinnedFlights(prim)
     pin_s = runtime.PinnedFlights(sec)
     schedule.append(autotune.tune_host_chunk(ctx, [pin_p, pin_s]))
+    schedule.append(autotune.tune_host_direct(ctx, [pin_p, pin_s]))
     ctx.trace_pinned(pin_p)
     ctx.trace_pinned(pin_s)
     barrier()

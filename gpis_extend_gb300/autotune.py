@@ -2,7 +2,8 @@
 (gpis_tune_set) on the caller's own workload and keeps the fastest.
 
 Knobs: the fast pass's persistent grid (CTAs per SM), the render's pass size
-(paths per wavefront pass) and the host pipeline's chunk.  None of them changes
+(paths per wavefront pass), the host pipeline's chunk and whether it runs on
+page-locked host streams in place.  None of them changes
 a result: every flight is independent of the grid and of its batch, so the
 tuner compares times only.
 """
@@ -87,3 +88,24 @@ def tune_host_chunk(ctx, pinned, candidates=(1 << 18, 1 << 19, 1 << 20, 1 << 21)
     best = min(times, key=times.get)
     ctx.tune(abi.TUNE_HOST_CHUNK, best)
     return {"knob": "host_chunk", "best": best, "ms": times}
+
+
+def tune_host_direct(ctx, pinned, reps=3):
+    """Staged copies (0) or the kernels on the page-locked streams in place (1), timed on
+    pinned batches (wall time of the blocking call).  Returns {candidate: ms} and
+    leaves the fastest set."""
+    times = {}
+    for c in (0, 1):
+        ctx.tune(abi.TUNE_HOST_DIRECT, c)
+        for p in pinned:
+            ctx.trace_pinned(p)
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            for p in pinned:
+                ctx.trace_pinned(p)
+            ts.append((time.perf_counter() - t0) * 1e3)
+        times[c] = float(np.median(ts))
+    best = min(times, key=times.get)
+    ctx.tune(abi.TUNE_HOST_DIRECT, best)
+    return {"knob": "host_direct", "best": best, "ms": times}

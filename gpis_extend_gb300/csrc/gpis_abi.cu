@@ -274,7 +274,7 @@ struct gpis_ctx {
     double prof_ms[3] = {0, 0, 0};
     uint64_t prof_launches[3] = {0, 0, 0};
     // schedule knobs (gpis_tune_set; 0 = default)
-    uint64_t tune[3] = {0, 0, 0};
+    uint64_t tune[4] = {0, 0, 0, 0};
 };
 
 namespace {
@@ -299,6 +299,18 @@ void release(gpis_ctx *c)
     if (c->d2h_stream) cudaStreamDestroy(c->d2h_stream);
     for (cudaEvent_t e : c->ev_chunks) cudaEventDestroy(e);
     delete c;
+}
+
+// page-locked host memory the device maps at the same address (the kernels can use
+// the pointer as it is)
+bool host_mapped(const void *p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost && a.devicePointer == p;
 }
 
 int ensure_scratch(gpis_ctx *c, size_t n)
@@ -610,7 +622,8 @@ __attribute__((visibility("hidden"))) int gpis_internal_nee_live(gpis_ctx *ctx, 
 int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value)
 {
     if (!ctx) return fail(GPIS_EINVAL, "null context");
-    if (key > GPIS_TUNE_HOST_CHUNK) return fail(GPIS_EINVAL, "unknown schedule knob");
+    if (key > GPIS_TUNE_HOST_DIRECT) return fail(GPIS_EINVAL, "unknown schedule knob");
+    if (key == GPIS_TUNE_HOST_DIRECT && value > 1) return fail(GPIS_ERANGE, "host direct mode is 0 or 1");
     if (key == GPIS_TUNE_MARCH_CTAS_PER_SM && value > 64) return fail(GPIS_ERANGE, "CTAs per SM must be <= 64");
     if (key == GPIS_TUNE_RENDER_PASS_PATHS && value && (value < 4096 || value > (1ull << 26)))
         return fail(GPIS_ERANGE, "render pass size must be in [4096, 2^26]");
@@ -623,7 +636,7 @@ int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value)
 int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value)
 {
     if (!ctx || !value) return fail(GPIS_EINVAL, "null argument");
-    if (key > GPIS_TUNE_HOST_CHUNK) return fail(GPIS_EINVAL, "unknown schedule knob");
+    if (key > GPIS_TUNE_HOST_DIRECT) return fail(GPIS_EINVAL, "unknown schedule knob");
     *value = ctx->tune[key];
     return GPIS_OK;
 }
@@ -696,6 +709,33 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis
     if (n == 0) return GPIS_OK;
     if (!in->origin_near || !in->dir_far || !in->seeds || !out->rec)
         return fail(GPIS_EINVAL, "flight streams origin_near, dir_far, seeds and rec are required");
+    if (ctx->tune[GPIS_TUNE_HOST_DIRECT] && host_mapped(in->origin_near) && host_mapped(in->dir_far) &&
+        host_mapped(in->seeds) && (!in->prev || host_mapped(in->prev)) && (!in->medium || host_mapped(in->medium)) &&
+        host_mapped(out->rec)) {
+        // in place: the kernels read the flights and write the records over the host link
+        int rc = ensure_scratch(ctx, n);
+        if (rc) return rc;
+        gpis_flight_soa din = *in;
+        float *zero_prev = nullptr;
+        if (!din.prev) {
+            // the prev stream is read for every flight: zeros in the staging area
+            const size_t need = (size_t)n * 16;
+            if (need > ctx->stage_cap) {
+                cudaFree(ctx->d_stage);
+                ctx->d_stage = nullptr;
+                ctx->stage_cap = 0;
+                CUDA_TRY(cudaMalloc(&ctx->d_stage, need), "allocate staging");
+                ctx->stage_cap = need;
+            }
+            zero_prev = reinterpret_cast<float *>(ctx->d_stage);
+            CUDA_TRY(cudaMemsetAsync(zero_prev, 0, need, ctx->stream), "clear prev");
+            din.prev = zero_prev;
+        }
+        rc = submit_slice(ctx, &din, out, n, ctx->stream, 0, ctx->d_work);
+        if (rc) return rc;
+        CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize flights");
+        return GPIS_OK;
+    }
     const size_t rec16 = (size_t)n * 16;
     const size_t need = rec16 * 4 + (size_t)n * 4 + 64 + rec16 * 2;
     if (need > ctx->stage_cap) {

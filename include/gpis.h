@@ -285,6 +285,12 @@ int gpis_nee_host(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n)
 #define GPIS_TUNE_RENDER_PASS_PATHS 1u   /* paths per render pass (default 2^22)     */
 #define GPIS_TUNE_HOST_CHUNK        2u   /* flights per chunk of the host pipeline
                                             (default 2^20)                          */
+#define GPIS_TUNE_HOST_DIRECT       3u   /* 1: gpis_flights_trace_host runs the kernels on
+                                            page-locked host streams in place (the GPU
+                                            reads and writes them over the host link, no
+                                            staging copies) when every stream is
+                                            page-locked and mapped; 0 (default): staged,
+                                            chunked copies                             */
 int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value);
 int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value);
 

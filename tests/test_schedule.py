@@ -21,6 +21,18 @@ def test_gpu_knobs_keep_results():
         for chunk in (4096, 1 << 14):
             ctx.tune(abi.TUNE_HOST_CHUNK, chunk)
             assert np.array_equal(ctx.trace_host(prim).view(np.uint32), ref.view(np.uint32)), chunk
+        # in place on page-locked streams, and staged again
+        pin = runtime.PinnedFlights(prim)
+        for direct in (1, 0):
+            ctx.tune(abi.TUNE_HOST_DIRECT, direct)
+            pin.rec.zero_()
+            ctx.trace_pinned(pin)
+            assert np.array_equal(pin.results().view(np.uint32), ref.view(np.uint32)), direct
+        # pageable streams take the staged path whatever the knob
+        ctx.tune(abi.TUNE_HOST_DIRECT, 1)
+        assert np.array_equal(ctx.trace_host(prim).view(np.uint32), ref.view(np.uint32))
+        with pytest.raises(abi.GpisError):
+            ctx.tune(abi.TUNE_HOST_DIRECT, 2)
         with pytest.raises(abi.GpisError):
             ctx.tune(abi.TUNE_MARCH_CTAS_PER_SM, 1000)
         with pytest.raises(abi.GpisError):
