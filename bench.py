@@ -164,9 +164,18 @@ def cpu_baseline(desc, prim, sec, target_s=8.0):
     oracle.trace_flights(desc, prim.subset(np.arange(m2)), n_threads=0)
     oracle.trace_flights(desc, sec.subset(np.arange(s2)), n_threads=0)
     dt = time.perf_counter() - t0
+    # beside it, one thread on a smaller sample (about a second)
+    m1 = int(min(prim.n, max(1024, rate / cores)))
+    s1 = min(m1, sec.n)
+    t1 = time.perf_counter()
+    oracle.trace_flights(desc, prim.subset(np.arange(m1)), n_threads=1)
+    oracle.trace_flights(desc, sec.subset(np.arange(s1)), n_threads=1)
+    dt1 = time.perf_counter() - t1
     return {"value": (m2 + s2) / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"first {m2} primary + first {s2} secondary flights of the workload, "
-                      f"oracle (C restatement, float mode) on {cores} threads, {dt:.1f} s"}
+                      f"oracle (C restatement, float mode) on {cores} threads, {dt:.1f} s",
+            "one_thread": {"value": (m1 + s1) / dt1, "unit": UNIT,
+                           "sample": f"first {m1} primary + first {s1} secondary flights, {dt1:.1f} s"}}
 
 
 def run_reference(args, world, rank):
