@@ -1115,8 +1115,9 @@ int resident_blocks(const void *fn, int threads, uint32_t dyn, int dev, int tmem
 int launch_infer(gpis_proposal *p, const gpis_flight_soa *in, const float *features, float *intervals, uint32_t cap,
                  const uint32_t *n_dev, cudaStream_t s)
 {
-    if (*p->tc_err_host) {
-        *p->tc_err_host = 0;
+    volatile uint32_t *flag = p->tc_err_host;   // written by the device through the mapping
+    if (*flag) {
+        *flag = 0;
         return gpis_internal_set_error(GPIS_EIO, "proposal inference: tensor-core completion wait timed out");
     }
     const float4 *on = reinterpret_cast<const float4 *>(in->origin_near);
