@@ -11,12 +11,12 @@ from gpis_extend_gb300 import abi, workloads
 from oracle import oracle
 
 
-def draw_media(n, seed=11, allow_3d=True):
+def draw_media(n, seed=11, allow_3d=True, only_3d=False):
     rng = np.random.default_rng(seed)
     media = []
     for i in range(n):
         kind = rng.integers(0, 4)
-        one_d = (not allow_3d) or rng.random() < 0.75
+        one_d = not only_3d and ((not allow_3d) or rng.random() < 0.75)
         octaves = int(rng.integers(1, 4)) if one_d else 1
         ns = one_d and rng.random() < 0.3
         ctx = abi.CTX_RENEWAL_PLUS if rng.random() < 0.5 else abi.CTX_RENEWAL
@@ -67,12 +67,15 @@ def test_oracle_mixed_batch_equals_per_medium():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("allow_3d", [False, True])
-def test_gpu_mixed_media_one_launch(allow_3d):
+@pytest.mark.parametrize("mode", ["1d", "mixed", "3d"])
+def test_gpu_mixed_media_one_launch(mode):
+    """1D media only (the octave and nonstationary fast passes with their skipping),
+    1D and 3D media together (the generic fast pass) and 3D media only (the 3D fast
+    pass with its range-bound skipping, per-lane media)."""
     from gpis_extend_gb300 import runtime
     from test_gpu_parity import flights_vs_oracle
-    media = draw_media(16, allow_3d=allow_3d)
-    batch, parts, order = mixed_batch(media, 256 if not allow_3d else 96)
+    media = draw_media(16, allow_3d=mode != "1d", only_3d=mode == "3d")
+    batch, parts, order = mixed_batch(media, 256 if mode == "1d" else 96)
     with runtime.Context(media) as ctx:
         rec = ctx.trace_host(batch)
     flights_vs_oracle(media[0], batch, rec, check_grad=True, media=media)
