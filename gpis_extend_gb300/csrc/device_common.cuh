@@ -288,6 +288,17 @@ __device__ __forceinline__ FF ff_div_ff(float a, FF b)
     return ff_norm(q, __fdiv_rn(r, b.h));
 }
 
+// 1 / sqrt(a) as a float-float pair (about 43 significant bits): the float reciprocal
+// square root and one Newton step r + r (1 - a r^2) / 2 in float-float.  Replaces the
+// double division by a double square root where the result is rounded to float.
+__device__ __forceinline__ FF ff_rsqrt(FF a)
+{
+    const float r = rsqrtf(a.h);
+    const FF ar2 = ff_mul(a, ff_prod(r, r));
+    const FF e = ff_add_f({-ar2.h, -ar2.l}, 1.0f);
+    return ff_add_f(ff_mul_f(e, 0.5f * r), r);
+}
+
 // a <= c for a float-float a and the double c = ch + cl.
 __device__ __forceinline__ bool ff_le(FF a, float ch, float cl)
 {
@@ -425,16 +436,24 @@ __device__ __forceinline__ float mean_value(const DevMedium &m, float x, float y
     }
 }
 
-// Mean gradient in double where the reference evaluates it in double.
+// Mean gradient as the reference evaluates it (in double for the sphere, to float).
 __device__ __forceinline__ void mean_grad(const DevMedium &m, float x, float y, float z, float g[3])
 {
     const float *q = m.mean_params;
     int id;
     switch (m.mean_kind) {
     case 0: {
-        const double dx = (double)x - q[0], dy = (double)y - q[1], dz = (double)z - q[2];
-        const double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
-        g[0] = (float)(dx * inv); g[1] = (float)(dy * inv); g[2] = (float)(dz * inv);
+        // (p - c).normalized() in double, rounded to float: the differences are exact
+        // float-float pairs, the squared length and its reciprocal square root are
+        // carried in float-float (the double path's FP64 division and square root run
+        // at a small fraction of the FP32 rate)
+        float ex, ey, ez;
+        const FF dx = {two_sum(x, -q[0], ex), 0.0f}, dy = {two_sum(y, -q[1], ey), 0.0f},
+                 dz = {two_sum(z, -q[2], ez), 0.0f};
+        const FF ddx = {dx.h, ex}, ddy = {dy.h, ey}, ddz = {dz.h, ez};
+        const FF inv = ff_rsqrt(ff_add(ff_add(ff_sq(ddx), ff_sq(ddy)), ff_sq(ddz)));
+        const FF gx = ff_mul(ddx, inv), gy = ff_mul(ddy, inv), gz = ff_mul(ddz, inv);
+        g[0] = __fadd_rn(gx.h, gx.l); g[1] = __fadd_rn(gy.h, gy.l); g[2] = __fadd_rn(gz.h, gz.l);
         return;
     }
     case 1:

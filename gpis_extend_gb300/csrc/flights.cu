@@ -2245,13 +2245,19 @@ __device__ __forceinline__ void finish_one(const FlightArgs &a, uint32_t i)
         return;
     }
     const double t = a.t_end[i];
-    // ro + normalize(rd) * t in double (GaussianProcessMedium.cpp:307, 401)
-    const double dx = fl.d[0], dy = fl.d[1], dz = fl.d[2];
-    const double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+    // ro + normalize(rd) * t in double, rounded to float (GaussianProcessMedium.cpp:307,
+    // 401), carried in float-float: the squared length of rd is exact, its reciprocal
+    // square root good to about 43 bits, and t splits exactly into two floats
+    const float th = __double2float_rn(t);
+    const FF tt = {th, __double2float_rn(t - (double)th)};
+    const FF inv = ff_rsqrt(ff_add(ff_add(ff_prod(fl.d[0], fl.d[0]), ff_prod(fl.d[1], fl.d[1])),
+                                   ff_prod(fl.d[2], fl.d[2])));
     float p[3];
-    p[0] = (float)((double)fl.o[0] + dx * inv * t);
-    p[1] = (float)((double)fl.o[1] + dy * inv * t);
-    p[2] = (float)((double)fl.o[2] + dz * inv * t);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const FF q = ff_add_f(ff_mul(ff_mul_f(inv, fl.d[j]), tt), fl.o[j]);
+        p[j] = __fadd_rn(q.h, q.l);
+    }
     const bool cond = conditioned(m, fl);
     CondRec c = {};
     if (cond) c = a.cond[i];

@@ -350,7 +350,7 @@ __device__ __forceinline__ void features_one(const DevMedium *media, int n_media
         const float mv = mean_value(m, x, y, z, id);
         float g[3];
         if (m.mean_kind == GPIS_MEAN_SPHERE) {
-            // float form of the sphere's gradient (mean_grad takes the reference's double path)
+            // float form of the sphere's gradient (mean_grad emulates the reference's double path)
             const float *c = m.mean_params;
             const float dx = x - c[0], dy = y - c[1], dz = z - c[2];
             const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
