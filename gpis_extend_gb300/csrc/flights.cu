@@ -780,8 +780,19 @@ __device__ __forceinline__ void prepare_one(const FlightArgs &a, uint32_t i)
     const bool valid = mok && flight_valid(fl);
     const bool cond = valid && conditioned(m, fl);
     CondRec c = {};
-    if (cond) c = make_condition(m, fl);
-    if (a.any_cond) a.cond[i] = c;
+    if (cond) {
+        c = make_condition(m, fl);
+        // only conditioned flights' records are read; a 1D single-octave medium's
+        // readers take the first octave's coefficients and the transverse observation
+        float4 *cr = reinterpret_cast<float4 *>(a.cond + i);
+        const float4 *cs = reinterpret_cast<const float4 *>(&c);
+        if ((m.flags & MF_ONE_D) && m.n_oct == 1 && !(m.flags & MF_MULTIRES)) {
+            cr[0] = cs[0];
+            cr[4] = cs[4];
+        } else {
+            a.cond[i] = c;
+        }
+    }
     if (!a.setup) return;
     float4 *s = a.setup + 4 * (size_t)i;
     if (!valid || !(m.flags & MF_ONE_D)) {

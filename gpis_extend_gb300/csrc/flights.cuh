@@ -2,6 +2,7 @@
 // flight kernels (flights.cu).
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -23,6 +24,8 @@ struct CondRec {
     float tgn[3];           // target_gradient_noise (1D transverse law)
     uint32_t has_obs;       // has_gradient_observation
 };
+static_assert(sizeof(CondRec) == 80 && offsetof(CondRec, tgn) == 64, "conditioning record layout (k_prepare "
+                                                                      "writes 1D single-octave records by float4)");
 
 struct FlightArgs {
     const float4 *origin_near;
