@@ -274,6 +274,7 @@ __device__ __forceinline__ FF ff_sq(FF a)
 
 __device__ __forceinline__ FF ff_sqrt(FF a)
 {
+    if (!(a.h > 0.0f)) return {__fsqrt_rn(a.h), 0.0f};   // 0 (or NaN below 0), no 0 / 0
     const float r = __fsqrt_rn(a.h);
     const FF r2 = ff_prod(r, r);
     const float e = __fadd_rn(__fsub_rn(__fsub_rn(a.h, r2.h), r2.l), a.l);

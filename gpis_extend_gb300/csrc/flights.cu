@@ -1066,20 +1066,24 @@ __device__ float mean_plus_precise(const DevMedium &m, float an, float x, float 
         return __fadd_rn(tot.h, tot.l);
     }
     if (m.mean_kind == 4 || m.mean_kind == 5) {
-        // the torus (and the union with the plane y = q[5]) in double, uncontracted
-        const double dx = __dsub_rn((double)x, (double)q[0]);
-        const double dy = __dsub_rn((double)y, (double)q[1]);
-        const double dz = __dsub_rn((double)z, (double)q[2]);
-        const double rxz = __dsub_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dz, dz))), (double)q[3]);
-        double mean = __dsub_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(rxz, rxz), __dmul_rn(dy, dy))), (double)q[4]);
+        // the torus (and the union with the plane y = q[5]), which the reference evaluates
+        // in double, in float-float: the differences are exact pairs, the square roots
+        // good to about 46 bits, the sum with the noise rounded to float once
+        float e0, e1, e2;
+        const float h0 = two_sum(x, -q[0], e0), h1 = two_sum(y, -q[1], e1), h2 = two_sum(z, -q[2], e2);
+        const FF dy = {h1, e1};
+        const FF rxz = ff_add_f(ff_sqrt(ff_add(ff_sq({h0, e0}), ff_sq({h2, e2}))), -q[3]);
+        FF mean = ff_add_f(ff_sqrt(ff_add(ff_sq(rxz), ff_sq(dy))), -q[4]);
         if (m.mean_kind == 5) {
-            const double pl = __dsub_rn((double)y, (double)q[5]);
-            if (pl < mean) {
+            float e5;
+            const FF pl = {two_sum(y, -q[5], e5), e5};
+            if (pl.h < mean.h || (pl.h == mean.h && pl.l < mean.l)) {
                 id = 1;
                 mean = pl;
             }
         }
-        return (float)__dadd_rn((double)an, mean);
+        const FF tot = ff_add_f(mean, an);
+        return __fadd_rn(tot.h, tot.l);
     }
     // float means (homogeneous, grid): (float)((double)an + mean) is the rounded exact sum
     const float mv = mean_value(m, x, y, z, id);
