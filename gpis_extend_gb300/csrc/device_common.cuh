@@ -82,6 +82,7 @@ struct DevMedium {
     // mean's Lipschitz constant along a ray, the noise's per iso unit and the
     // largest jump of one truncated splat (noise units)
     float skip_mean_lip;
+    float skip_noise_lip;   // 3 N e^{-1/2} / norm1d per iso unit
     float skip_jump;        // e^{-kr^2/2} / norm1d per truncation crossing
     float oct_inv[4];       // 1 / oct_scale[k], exact where the scale is a power of two
     uint32_t oct_pow2;      // bit k: oct_scale[k] is a power of two (x / s == x * oct_inv[k])

@@ -748,40 +748,28 @@ __device__ __forceinline__ CondRec make_condition(const DevMedium &m, const Flig
 // every lane busy instead of inside the march, where it runs for the few lanes
 // that start a flight while the rest of the warp waits.  Four float4 per flight:
 // {frame normal, origin coordinate}, {value scale, gradient scale, step, t0},
-// {skip slope a, slope per impulse b, jump per impulse c, segment in cells dmax}
-// (skip_local_params), {seed, flags (1 valid, 2 conditioned, 4 first scatter), -, -}.
+// {skip slope, skip jump, skip jump per step, -}, {seed, flags (1 valid, 2
+// conditioned, 4 first scatter), -, -}.
 enum : uint32_t { SF_VALID = 1u, SF_COND = 2u, SF_FIRST = 4u };
 
-// most march steps one evaluation may skip (fast pass)
-constexpr int kMaxSkip = 8;
-// before a proposed crossing interval the cap is this (every skipped step is still certified)
-constexpr int kMaxSkipProposed = 16;
-
-// Step skipping of stationary 1D single-octave media with the count of impulses that
-// can reach the next steps (the cooperative evaluator counts them in its window): over a
-// segment of the ray whose iso coordinate stays within dmax cells of the query, only the
-// impulses whose support (half-width one cell) meets the segment contribute, each with a
-// slope of at most e^-1/2 per iso unit (the normalised noise) and a jump of at most
-// exp(-kr^2 / 2) at each of its two support boundaries.  With count such impulses the
-// field's slope along the ray is at most a + b count per unit t and its jumps c count:
-// a the mean's slope bound plus the conditioning splats' (0.429 |vs| + 0.5 |gz| per iso
-// unit), b and c those per-impulse bounds times sigma and dz = |l_inv o d| (iso units per
-// unit t), all inflated by 1 %; dmax covers nsteps steps.  a < 0: no skipping.
-__device__ __forceinline__ void skip_local_params(const DevMedium &m, const float d[3], float sigma, bool cond,
-                                                  float vs, float gsz, float step, int nsteps, float &a, float &b,
-                                                  float &c, float &dmax)
+__device__ __forceinline__ void skip_params(const DevMedium &m, const float d[3], float sigma, bool cond, float vs,
+                                            float gsz, float step, float &lip, float &j0, float &j1)
 {
-    a = -1.0f;
-    b = c = dmax = 0.0f;
+    // |df/dt| <= mean slope + sigma (noise + conditioning slopes) dz/dt with
+    // dz/dt = |l_inv o d| (iso units per world unit); a truncated splat jumps by at
+    // most skip_jump where the query crosses its support, and an iso interval of
+    // D cells holds at most 2 N (D + 1) such crossings
+    lip = -1.0f;
+    j0 = j1 = 0.0f;
     if (m.skip_mean_lip < 0.0f) return;
     const float lx = m.l_inv[0] * d[0], ly = m.l_inv[1] * d[1], lz = m.l_inv[2] * d[2];
     const float dz = sqrtf(lx * lx + ly * ly + lz * lz) * 1.0001f;
     const float sg = fabsf(sigma);
     const float cslope = cond ? 0.42888194f * fabsf(vs) + 0.5f * fabsf(gsz) : 0.0f;
-    a = (m.skip_mean_lip + sg * cslope * dz) * 1.01f;
-    b = sg * 0.60653066f * m.inv_norm1d * dz * 1.01f;
-    c = 2.0f * sg * m.skip_jump * 1.01f;
-    dmax = (float)nsteps * step * dz / m.kr_iso * 1.0001f;
+    lip = (m.skip_mean_lip + sg * (m.skip_noise_lip + cslope) * dz) * 1.01f;
+    const float jn = sg * m.skip_jump * 2.0f * (float)m.n_imp * 1.01f;
+    j0 = jn * 3.0f;
+    j1 = jn * (step * dz / m.kr_iso);
 }
 
 __device__ __forceinline__ void prepare_one(const FlightArgs &a, uint32_t i)
@@ -818,13 +806,12 @@ __device__ __forceinline__ void prepare_one(const FlightArgs &a, uint32_t i)
     float step = __fdiv_rn(__fsub_rn(fl.far_t, fl.near_t), (float)m.min_step);
     if (m.step_size < step) step = m.step_size;
     const float t0 = __fadd_rn(fl.near_t, __fmul_rn(step, fl.jitter));
-    float sa, sb, sc, sdmax;
-    skip_local_params(m, fl.d, m.sigma, cond, vs, gsz, step, a.proposal ? kMaxSkipProposed : kMaxSkip, sa, sb, sc,
-                      sdmax);
+    float lip, j0, j1;
+    skip_params(m, fl.d, m.sigma, cond, vs, gsz, step, lip, j0, j1);
     const uint32_t flags = SF_VALID | (cond ? SF_COND : 0u) | ((fl.flags & GPIS_FLAG_FIRST_SCATTER) ? SF_FIRST : 0u);
     s[0] = make_float4(f.n[0], f.n[1], f.n[2], ozc);
     s[1] = make_float4(vs, gsz, step, t0);
-    s[2] = make_float4(sa, sb, sc, sdmax);
+    s[2] = make_float4(lip, j0, j1, 0.0f);
     s[3] = make_float4(__uint_as_float(fl.noise_seed), __uint_as_float(flags), 0.0f, 0.0f);
 }
 
@@ -854,7 +841,6 @@ struct LaneField {
     bool ns;                // nonstationary length scale
     float ls_o;             // kernel scale at the origin (conditioning)
     float mr_ow[2];         // multi-resolution: the origin's weights of the low and high level
-    float sdmax;            // step skipping: the cells the next skipped steps may span
 };
 
 // Safe contents for a lane without a flight (collective evaluators run every lane).
@@ -869,7 +855,6 @@ __device__ __forceinline__ void lane_field_idle(LaneField &L, const DevMedium *m
     L.cond = false;
     L.c3 = CondRec{};
     L.o[0] = L.o[1] = L.o[2] = 0.0f;
-    L.sdmax = 0.0f;
     L.mean_kind = 1u;
 #pragma unroll
     for (int k = 0; k < 6; ++k) L.mq[k] = 0.0f;
@@ -1466,9 +1451,8 @@ struct EvalCoop1D {
     bool valid;
     const PcgJump *sj;      // the jump table in shared memory
     float last_ls;          // nonstationary: the local scale at the last evaluated point
-    int near_cnt;           // step skipping: the impulses that can reach the next L.sdmax cells
 
-    __device__ __forceinline__ void reset() { valid = false; base = 0; last_ls = 1.0f; near_cnt = 0; }
+    __device__ __forceinline__ void reset() { valid = false; base = 0; last_ls = 1.0f; }
     __device__ __forceinline__ void bind(const PcgJump *t) { sj = t; }
 
     template <int S>
@@ -1555,10 +1539,6 @@ struct EvalCoop1D {
             refills += full ? 3u : 1u;
         }
         float acc0 = 0.0f, acc1 = 0.0f;
-        int cnt = 0;
-        // the segment's reach: tp grows along the ray by up to L.sdmax cells; an impulse
-        // counts while tp < 1 and tp + sdmax > -1 (widened by 1e-4 against rounding)
-        const float lo_reach = -1.0f - 1e-4f - L.sdmax;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const float tl = __fsub_rn(frac, (float)(c - 1));
@@ -1570,15 +1550,7 @@ struct EvalCoop1D {
                 const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(s) & 0x80000000u));
                 if (k & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
                 else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
-                if (kSkip) cnt += (tp < 1.0f + 1e-4f && tp > lo_reach) ? 1 : 0;
             }
-        }
-        if (kSkip) {
-            // a segment that leaves the query's cell meets the impulses of the cells beyond
-            // the window: all of them count
-            const float reach = frac + L.sdmax;
-            if (reach >= 1.0f - 1e-4f) cnt += (int)L.n_imp * (int)floorf(reach + 1e-4f);
-            near_cnt = cnt;
         }
         float noise = (acc0 + acc1) * inv_norm;
         if (L.cond) {
@@ -1766,6 +1738,8 @@ struct EvalCoopOct {
 // refinement point.
 enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE, PH_FAR };
 
+// most march steps one evaluation may skip (fast pass)
+constexpr int kMaxSkip = 8;
 // at most this many steps skipped per evaluation of a 3D medium (the segment also ends
 // inside the query's cell)
 constexpr int kMaxSkip3D = 32;
@@ -1859,6 +1833,8 @@ __device__ __forceinline__ float eval_at(EvalSkip3D &ev, const LaneField &L, con
 {
     return ev.value(L, d, p[0], p[1], p[2], id, refills, live);
 }
+// before a proposed crossing interval the cap is this (every skipped step is still certified)
+constexpr int kMaxSkipProposed = 16;
 
 // Fast values farther than this from zero have the sign of the precise value
 // (the fast evaluator differs from the precise one by a few 1e-8).
@@ -1924,7 +1900,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     uint32_t c_skipped = 0;
     // step skipping (fast pass): the field's Lipschitz constant along this ray and
     // its truncation-jump allowance, fixed and per step
-    float skip_a = -1.0f, skip_b = 0.0f, skip_c = 0.0f;
+    float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
     float prop_a = -INFINITY;   // start of the proposed crossing interval (learned proposal)
     const uint32_t n_live = live_n(a);
 
@@ -1988,10 +1964,9 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                             L.inv_norm = m.inv_norm1d;
                             step = s1.z;
                             t0 = s1.w;
-                            skip_a = s2.x;
-                            skip_b = s2.y;
-                            skip_c = s2.z;
-                            L.sdmax = s2.w;
+                            skip_lip = s2.x;
+                            skip_j0 = s2.y;
+                            skip_j1 = s2.z;
                             max_steps = m.max_steps;
                             th = near_t;
                             tl = 0.0f;
@@ -2015,12 +1990,9 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                         if (m.step_size < step) step = m.step_size;
                         t0 = __fadd_rn(near_t, __fmul_rn(step, fl.jitter));
                         max_steps = m.max_steps;
-                        skip_a = -1.0f;
-                        L.sdmax = 0.0f;
+                        skip_lip = -1.0f;
                         if (Eval::kSkip && !RESUME)
-                            skip_local_params(m, d, L.sigma, L.cond, L.vs, L.gsz, step,
-                                              a.proposal ? kMaxSkipProposed : kMaxSkip, skip_a, skip_b, skip_c,
-                                              L.sdmax);
+                            skip_params(m, d, L.sigma, L.cond, L.vs, L.gsz, step, skip_lip, skip_j0, skip_j1);
                         th = near_t;
                         tl = 0.0f;
                         steps = 0;
@@ -2142,25 +2114,20 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 pf_precise = phase == PH_MARCH_P;
                 ff_add(th, tl, step);
                 phase = PH_MARCH;
-                // Step skipping: over the next k steps |f(t) - f| <= (a + b n) |t - t_j| plus
-                // the jumps c n, n the impulses that can reach those steps (counted by the
-                // evaluator in its window), so while that stays below |f| (less a margin for
-                // the fast value's error and the reference's float evaluation) every skipped
+                // Step skipping: over the next k steps |f(t) - f| <= skip_lip |t - t_j| plus
+                // the jump allowance, so while that stays below |f| (less a margin for the
+                // fast value's error and the reference's float evaluation) every skipped
                 // step has the sign of f and the reference would march past it.  Skipped
                 // steps are counted as marched; the resume pass re-evaluates the step before
                 // a crossing, so no skipped value is ever needed.
                 int skip = 0;
-                if constexpr (Eval::kSkip) {
-                    if (!RESUME && skip_a >= 0.0f) {
-                        const float cnt = (float)ev.near_cnt;
-                        const float af = fabsf(f) * (1.0f - 1e-6f) - 1e-5f - skip_c * cnt;
-                        const float per = (skip_a + skip_b * cnt) * step;
-                        // at most kMaxSkip per evaluation (the segment the count covers; and
-                        // the lanes of a warp skip different counts, so the warp runs the
-                        // longest lane's loop)
-                        const float cap = th < prop_a ? (float)kMaxSkipProposed : (float)kMaxSkip;
-                        if (af > per) skip = (int)fminf(af / per, cap);
-                    }
+                if (Eval::kSkip && !RESUME && skip_lip >= 0.0f) {
+                    const float af = fabsf(f) * (1.0f - 1e-6f) - 1e-5f - skip_j0;
+                    const float per = skip_lip * step + skip_j1;
+                    // at most kMaxSkip per evaluation: the lanes of a warp skip different
+                    // counts, so the warp runs the longest lane's loop
+                    const float cap = th < prop_a ? (float)kMaxSkipProposed : (float)kMaxSkip;
+                    if (af > per) skip = (int)fminf(af / per, cap);
                 }
                 if constexpr (IsSkip3D<Eval>::value) {
                     if (!RESUME) skip = ev.skips(f, step, kMaxSkip3D);

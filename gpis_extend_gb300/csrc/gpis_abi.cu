@@ -224,6 +224,7 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         default: break;
         }
     }
+    m.skip_noise_lip = (float)(3.0 * m.n_imp * std::exp(-0.5) / (double)m.norm1d);
     m.skip_jump = (float)(std::exp(-0.5 * (double)m.kr_iso * m.kr_iso) / (double)m.norm1d);
     m.step_size = d.step_size;
     m.min_step = d.min_step;
