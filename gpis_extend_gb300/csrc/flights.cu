@@ -1350,87 +1350,6 @@ struct EvalSkip3D {
     }
 };
 
-// 1D evaluator with the three-cell impulse window in registers.  Each cached
-// impulse is its position t_i in [0,1) with the sign of its weight in the sign bit.
-template <int NMAX>
-struct EvalCached1D {
-    static constexpr bool kCollective = false;
-    float cache[3][NMAX];
-    int base;
-    bool valid;
-
-    __device__ __forceinline__ void reset() { valid = false; base = 0; }
-    __device__ __forceinline__ void bind(const PcgJump *) {}
-
-    __device__ __forceinline__ void gen(float (&dst)[NMAX], int cell, uint32_t seed, uint32_t n_imp)
-    {
-        const uint32_t s = xxhash2((uint32_t)cell, seed) + 1u;
-#pragma unroll
-        for (int k = 0; k < NMAX; ++k) {
-            if ((uint32_t)k < n_imp) {
-                const uint32_t r1 = pcg_draw(c_jump[2 + 2 * k], s);
-                const uint32_t r2 = pcg_draw(c_jump[3 + 2 * k], s);
-                const float t = unit_float(r1);
-                dst[k] = __uint_as_float(__float_as_uint(t) | (~r2 & 0x80000000u));
-            } else {
-                dst[k] = __int_as_float(0x7f800000);
-            }
-        }
-    }
-
-    __device__ __forceinline__ float value(const LaneField &L, float px, float py, float pz,
-                                           int &id, uint32_t &refills, bool)
-    {
-        const float z = ray_coord(L.li, L.n, px, py, pz);
-        const float tg = __fdiv_rn(z, L.kr);
-        const float fl = floorf(tg);
-        const float frac = __fsub_rn(tg, fl);
-        const int ci = (int)fl;
-        if (!valid || ci != base) {
-            const uint32_t n_imp = L.m->n_imp;
-            if (valid && ci == base + 1) {
-#pragma unroll
-                for (int k = 0; k < NMAX; ++k) { cache[0][k] = cache[1][k]; cache[1][k] = cache[2][k]; }
-                gen(cache[2], ci + 1, L.seed, n_imp);
-                refills += 1;
-            } else if (valid && ci == base - 1) {
-#pragma unroll
-                for (int k = 0; k < NMAX; ++k) { cache[2][k] = cache[1][k]; cache[1][k] = cache[0][k]; }
-                gen(cache[0], ci - 1, L.seed, n_imp);
-                refills += 1;
-            } else {
-                gen(cache[0], ci - 1, L.seed, n_imp);
-                gen(cache[1], ci, L.seed, n_imp);
-                gen(cache[2], ci + 1, L.seed, n_imp);
-                refills += 3;
-            }
-            base = ci;
-            valid = true;
-        }
-        float acc0 = 0.0f, acc1 = 0.0f;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const float tl = __fsub_rn(frac, (float)(c - 1));
-#pragma unroll
-            for (int k = 0; k < NMAX; ++k) {
-                const float s = cache[c][k];
-                const float tp = __fsub_rn(tl, fabsf(s));
-                const float e = ex2_approx(L.kexp * (tp * tp));
-                const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(s) & 0x80000000u));
-                if (k & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
-                else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
-            }
-        }
-        float noise = (acc0 + acc1) * L.inv_norm;
-        if (L.cond) {
-            const Cov1D k = cov1d(z - L.ozc);
-            noise += L.vs * k.k0 + L.gsz * k.k1;
-        }
-        return L.sigma * noise + lane_mean(L, px, py, pz, id);
-    }
-};
-
-
 // 1D evaluator with the three-cell impulse window in registers and a
 // warp-cooperative refill: the lanes whose query entered a new cell are
 // gathered by a ballot and the whole warp generates their cells, one impulse per
