@@ -306,12 +306,6 @@ __device__ __forceinline__ bool ff_le(FF a, float ch, float cl)
     return a.h < ch || (a.h == ch && a.l <= cl);
 }
 
-// double-precision point (refinement and gradient points are rare).
-__device__ __forceinline__ float dd_point(float o, float d, double t)
-{
-    return (float)__dadd_rn((double)o, __dmul_rn(t, (double)d));
-}
-
 __device__ __forceinline__ float ex2_approx(float x)
 {
     float y;
