@@ -148,34 +148,48 @@ def load_traffic():
         return None
 
 
-def cpu_baseline(desc, prim, sec, target_s=8.0):
-    """The oracle on all host cores over a bounded sample of the same flights."""
+def cpu_baseline(desc, prim, sec, gpu_recs=None):
+    """The oracle on all host cores over the whole workload (every primary and
+    secondary flight of one step), timed; its records are the parity check of the
+    GPU's records of the same flights (gpu_recs: primary, secondary).  Beside it,
+    one thread on a sample of about a second."""
     from oracle import oracle
     cores = os.cpu_count() or 1
-    m = 4096
     t0 = time.perf_counter()
-    oracle.trace_flights(desc, prim.subset(np.arange(m)), n_threads=0)
-    oracle.trace_flights(desc, sec.subset(np.arange(min(m, sec.n))), n_threads=0)
+    rp = oracle.trace_flights(desc, prim, n_threads=0)
+    rs = oracle.trace_flights(desc, sec, n_threads=0)
     dt = time.perf_counter() - t0
-    rate = (m + min(m, sec.n)) / dt
-    m2 = int(min(prim.n, max(4096, rate * target_s / 2)))
-    s2 = min(m2, sec.n)
-    t0 = time.perf_counter()
-    oracle.trace_flights(desc, prim.subset(np.arange(m2)), n_threads=0)
-    oracle.trace_flights(desc, sec.subset(np.arange(s2)), n_threads=0)
-    dt = time.perf_counter() - t0
-    # beside it, one thread on a smaller sample (about a second)
-    m1 = int(min(prim.n, max(1024, rate / cores)))
+    rate = (prim.n + sec.n) / dt
+    m1 = int(min(prim.n, max(1024, rate / cores / 2)))
     s1 = min(m1, sec.n)
     t1 = time.perf_counter()
     oracle.trace_flights(desc, prim.subset(np.arange(m1)), n_threads=1)
     oracle.trace_flights(desc, sec.subset(np.arange(s1)), n_threads=1)
     dt1 = time.perf_counter() - t1
-    return {"value": (m2 + s2) / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"first {m2} primary + first {s2} secondary flights of the workload, "
-                      f"oracle (C restatement, float mode) on {cores} threads, {dt:.1f} s",
+    base = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"the whole workload: {prim.n} primary + {sec.n} secondary flights, oracle (C restatement, "
+                      f"float mode) on {cores} threads, {dt:.1f} s",
             "one_thread": {"value": (m1 + s1) / dt1, "unit": UNIT,
                            "sample": f"first {m1} primary + first {s1} secondary flights, {dt1:.1f} s"}}
+    parity = None
+    if gpu_recs is not None:
+        parity = {}
+        for name, g, c in (("primary", gpu_recs[0], rp), ("secondary", gpu_recs[1], rs)):
+            parity[name] = oracle.compare_flights(g, c, desc.sigma, 1.5)
+        tot = {k: sum(parity[x][k] for x in ("primary", "secondary"))
+               for k in ("flights", "hit_disagreements", "hits", "t_outliers", "t_outliers_backoff",
+                         "t_outliers_other")}
+        tot["hit_agreement"] = 1.0 - tot["hit_disagreements"] / max(1, tot["flights"])
+        tot["hits_within_t_tol"] = 1.0 - tot["t_outliers"] / max(1, tot["hits"])
+        tot["bars"] = ("hit/miss agreement >= 0.9999; |dt| <= 1e-4 x scene scale (1.5) on >= 0.9999 of hits, "
+                       "every outlier a back-off case; miss values within 1e-5 of sigma; normals within 2e-3")
+        tot["pass"] = bool(tot["hit_agreement"] >= 0.9999 and tot["hits_within_t_tol"] >= 0.9999
+                           and tot["t_outliers_other"] == 0
+                           and all(parity[x]["status_agreement"] == 1.0 and parity[x]["miss_t_equal"] == 1.0
+                                   and parity[x]["miss_value_within_tol"] >= 0.9999
+                                   and parity[x]["normals_within_tol"] >= 0.999 for x in ("primary", "secondary")))
+        parity["all"] = tot
+    return base, parity
 
 
 def run_reference(args, world, rank):
@@ -546,6 +560,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=1 << 16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-ref-gpu", action="store_true")
     ap.add_argument("--workload", default="flights", choices=["flights", "image0", "image2", "learned", "batch"])
     ap.add_argument("--spp-scale", type=float, default=1.0)
     ap.add_argument("--train-flights", type=int, default=1 << 22)
@@ -706,7 +721,32 @@ def main():
             learned = {"error": f"{type(e).__name__}: {e}"}
         line["learned"] = learned
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(desc, prim, sec)
+        # the oracle over every flight of the step, timed as the CPU baseline; its
+        # records check the GPU's records of the last timed step flight by flight
+        ctx.submit(dev_p, stream)
+        ctx.submit(dev_s, stream)
+        torch.cuda.synchronize()
+        gpu_recs = (dev_p.results(), dev_s.results())
+        line["cpu_baseline"], line["parity"] = cpu_baseline(desc, prim, sec, gpu_recs)
+    if rank == 0 and world == 1 and not args.no_ref_gpu:
+        # the GPU baseline to beat: the reference's own traceSegments kernel
+        # (RaySegmentBatch.cu, compiled unmodified) and the flight kernels on the
+        # same flights over the sphere SDF baked into a 256^3 grid (the only mean
+        # that kernel supports); device time per pass with CUDA events
+        try:
+            from oracle import ref_gpu_baseline as rgb
+            if rgb.available():
+                r = rgb.compare(args.flights, reps=5, grid_res=256)
+                line["ref_gpu_kernel"] = {
+                    "value": r["reference_flights_per_s"], "unit": UNIT,
+                    "flight_kernels_value": r["flight_kernels_flights_per_s"], "ratio": r["speedup_total"],
+                    "hit_agreement": {k: v["hit_agreement"] for k, v in r["flights"].items()},
+                    "t_agreement": {k: v["t_agreement"] for k, v in r["flights"].items()},
+                    "workload": r["workload"], "passes": r["flights"]}
+            else:
+                line["ref_gpu_kernel"] = {"unavailable": "reference cubin not built (needs the reference tree)"}
+        except Exception as e:  # noqa: BLE001
+            line["ref_gpu_kernel"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -147,6 +147,7 @@ PHASE_LAMBERT, PHASE_MIRROR, PHASE_CONDUCTOR = 0, 1, 2
 TUNE_MARCH_CTAS_PER_SM, TUNE_RENDER_PASS_PATHS, TUNE_HOST_CHUNK, TUNE_HOST_DIRECT = 0, 1, 2, 3
 PHASE_NAMES = {"lambert": PHASE_LAMBERT, "mirror": PHASE_MIRROR, "conductor": PHASE_CONDUCTOR}
 PROPOSAL_KERNELS = {"tc2": 0, "tc1": 1, "mma": 2}
+PROPOSAL_WAIT_DEFAULT = 1 << 22
 # ConductorBsdf's default material, copper (ConductorBsdf.cpp:24-27)
 CU_ETA = (0.200438, 0.924033, 1.10221)
 CU_K = (3.91295, 2.45285, 2.14219)
@@ -389,6 +390,7 @@ def load_library(path=None):
         "gpis_debug_tc_gemm": (c_int, [vp, vp, c_u32, c_u32, vp]),
         "gpis_proposal_set_kernel": (c_int, [vp, c_int]),
         "gpis_proposal_occupancy": (c_int, [vp, c_int]),
+        "gpis_proposal_set_wait_limit": (c_int, [vp, c_u32]),
         "gpis_se_splat_1d": (c_int, [vp, vp, vp, vp, ctypes.c_size_t, ctypes.c_float, vp]),
         "gpis_flights_submit_static": (c_int, [P(MediumDesc), P(FlightSoA), P(ResultSoA), c_u32, vp]),
         "gpis_medium_sample_distance": (c_int, [vp, c_u32, vp, vp, vp, vp, c_u32]),

@@ -67,7 +67,7 @@ def build(force=False, verbose=False):
             f.write(f"== {src}\n{log}\n")
     objs = [o for o, _ in results]
     tmp = LIB + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static" if False else "-cudart=static"]
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart=static"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

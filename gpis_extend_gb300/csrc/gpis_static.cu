@@ -11,6 +11,7 @@
 // and result streams.
 #include <cmath>
 #include <cstring>
+#include <cstdint>
 #include <mutex>
 
 #include "../../include/gpis.h"
@@ -86,6 +87,12 @@ extern "C" int gpis_flights_submit_static(const gpis_medium_desc *medium, const 
     if (n == 0) return GPIS_OK;
     if (!in->origin_near || !in->dir_far || !in->seeds || !out->rec)
         return fail(GPIS_EINVAL, "flight streams origin_near, dir_far, seeds and rec are required");
+    // the kernels move these streams as 16-byte vectors: a misaligned pointer is
+    // an error here, before anything is launched
+    for (const void *p : {(const void *)in->origin_near, (const void *)in->dir_far, (const void *)in->seeds,
+                          (const void *)in->prev, (const void *)out->rec})
+        if (p && (reinterpret_cast<uintptr_t>(p) & 15u))
+            return fail(GPIS_EINVAL, "flight and result streams must be 16-byte aligned");
     if (medium->mean_kind == GPIS_MEAN_GRID)
         return fail(GPIS_ENOTSUP, "a grid mean needs device memory; use gpis_ctx_create instead");
     gpis::DevMedium m;
@@ -98,8 +105,11 @@ extern "C" int gpis_flights_submit_static(const gpis_medium_desc *medium, const 
     void *base = nullptr;
     rc = setup_device(dev, &base);
     if (rc) return rc;
-    int sms = 1;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // the fast pass's persistent grid is the occupancy maximum (ctas_per_sm 0):
+    // there is no context here to carry an autotuned value
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return fail(GPIS_ENODEV, "querying the device's multiprocessor count failed");
     char *b = static_cast<char *>(base);
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
     // The array keeps the previous call's contents: the medium table is written

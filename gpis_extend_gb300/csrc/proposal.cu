@@ -626,7 +626,7 @@ constexpr uint32_t TC_GB = 0, TC_W1 = TC_GB + 128 * TC_KG * 2, TC_W2 = TC_W1 + W
                    TC_W3 = TC_W2 + WID * WID * 2, TC_W4 = TC_W3 + WID * WID * 2, TC_WEND = TC_W4 + NOUT * WID * 2,
                    TC_A = 128 * TC_KG * 2, TC_Y = 128 * WID * 2, TC_GROUP = TC_A + TC_Y, TC_BIAS = (3 * WID + NOUT) * 4;
 constexpr uint32_t tc_smem_bytes(int groups) { return TC_WEND + groups * TC_GROUP + TC_BIAS; }
-constexpr uint32_t kTcWaitLimit = 1u << 22;
+constexpr uint32_t kTcWaitLimit = GPIS_PROPOSAL_WAIT_DEFAULT;
 
 // the operand row chunk of 8 BF16 columns starting at column 8 kb of row `row`
 __device__ __forceinline__ void put_chunk(unsigned char *tile, uint32_t row, uint32_t kb, uint32_t kdim, uint4 v)
@@ -640,7 +640,7 @@ __device__ __forceinline__ void put_chunk(unsigned char *tile, uint32_t row, uin
 // threads together (false, `fail` set, `phase` left at the outstanding commit)
 __device__ __forceinline__ bool tc_round(uint32_t gid, bool leader, uint32_t tmem, const unsigned char *a,
                                          const unsigned char *b, uint32_t kdim, uint32_t n, uint64_t *bar,
-                                         uint32_t &phase, bool &fail)
+                                         uint32_t &phase, bool &fail, uint32_t wait_limit)
 {
     umma::fence_async_smem();
     umma::fence_before_sync();
@@ -652,7 +652,7 @@ __device__ __forceinline__ bool tc_round(uint32_t gid, bool leader, uint32_t tme
                       umma::idesc_bf16_m128(n), kb > 0);
         umma::commit(bar);
     }
-    const bool done = umma::bar_wait(bar, phase, kTcWaitLimit);
+    const bool done = umma::bar_wait(bar, phase, wait_limit);
     if (umma::sync_or(1 + gid, 128, !done)) {
         fail = true;
         return false;
@@ -716,7 +716,7 @@ __global__ void __launch_bounds__(128 * GROUPS, GROUPS == 1 ? 3 : 2) k_propose_t
                                                                          const float *feat, const float4 *on,
                                                                          const float4 *df, uint32_t n_cap,
                                                                          const uint32_t *n_dev, float4 *out,
-                                                                         uint32_t *err)
+                                                                         uint32_t *err, uint32_t wait_limit)
 {
     extern __shared__ __align__(128) unsigned char tsm[];
     __shared__ __align__(8) uint64_t bars[GROUPS];
@@ -792,7 +792,7 @@ __global__ void __launch_bounds__(128 * GROUPS, GROUPS == 1 ? 3 : 2) k_propose_t
                                      pack2f(h[8 * q + 4], h[8 * q + 5]), pack2f(h[8 * q + 6], h[8 * q + 7])));
             const float2 x = reinterpret_cast<const float2 *>(fr)[j];
             put_chunk(A, row, 4, TC_KG, make_uint4(pack2f(x.x, x.y), one2, 0u, 0u));
-            ok = tc_round(gid, leader, tmem, A, gsh, TC_KG, 128, bar, phase, fail);
+            ok = tc_round(gid, leader, tmem, A, gsh, TC_KG, 128, bar, phase, fail, wait_limit);
             if (!ok) break;
 #pragma unroll
             for (uint32_t c0 = 0; c0 < HID; c0 += 8) {
@@ -817,13 +817,13 @@ __global__ void __launch_bounds__(128 * GROUPS, GROUPS == 1 ? 3 : 2) k_propose_t
         const float4 g0 = reinterpret_cast<const float4 *>(fr)[4], g1 = reinterpret_cast<const float4 *>(fr)[5];
         put_chunk(A, row, 4, TC_KG,
                   make_uint4(pack2f(g0.x, g0.y), pack2f(g0.z, g0.w), pack2f(g1.x, g1.y), pack2f(g1.z, g1.w)));
-        if (!tc_round(gid, leader, tmem, A, w1, MLPIN, WID, bar, phase, fail)) break;
+        if (!tc_round(gid, leader, tmem, A, w1, MLPIN, WID, bar, phase, fail, wait_limit)) break;
         tc_gelu64(tmem, nullptr, Y, row);
-        if (!tc_round(gid, leader, tmem, Y, w2, WID, WID, bar, phase, fail)) break;
+        if (!tc_round(gid, leader, tmem, Y, w2, WID, WID, bar, phase, fail, wait_limit)) break;
         tc_gelu64(tmem, bm, Y, row);
-        if (!tc_round(gid, leader, tmem, Y, w3, WID, WID, bar, phase, fail)) break;
+        if (!tc_round(gid, leader, tmem, Y, w3, WID, WID, bar, phase, fail, wait_limit)) break;
         tc_gelu64(tmem, bm + WID, Y, row);
-        if (!tc_round(gid, leader, tmem, Y, w4, WID, NOUT, bar, phase, fail)) break;
+        if (!tc_round(gid, leader, tmem, Y, w4, WID, NOUT, bar, phase, fail, wait_limit)) break;
         float o[32];
         umma::ld32(tmem, o);
 #pragma unroll
@@ -857,8 +857,8 @@ __global__ void __launch_bounds__(128 * GROUPS, GROUPS == 1 ? 3 : 2) k_propose_t
             out[r] = make_float4(a.w + ua * tm, a.w + ub * tm, q, bmean);
         }
     }
-    // a group that gave up waits once more (bounded) for the MMAs it committed before
-    // the tensor memory is released
+    // a group that gave up waits once more for the MMAs it committed before the
+    // tensor memory is released, with the default bound whatever wait_limit was
     if (fail) {
         if (leader) atomicExch(err, 1u);
         umma::bar_wait(bar, phase, kTcWaitLimit);
@@ -940,6 +940,8 @@ struct gpis_proposal {
     int kernel = GPIS_PROPOSAL_KERNEL_TC2;
     int sms = 1, per_sm_tc1 = 1, per_sm_tc2 = 1, per_sm_mma = 1;
     uint32_t *tc_err_host = nullptr, *tc_err_dev = nullptr;
+    // polls of the tensor-memory kernel's completion wait per MMA round
+    uint32_t wait_limit = GPIS_PROPOSAL_WAIT_DEFAULT;
 };
 
 namespace {
@@ -1131,11 +1133,11 @@ int launch_infer(gpis_proposal *p, const gpis_flight_soa *in, const float *featu
     } else if (kernel == GPIS_PROPOSAL_KERNEL_TC1) {
         const unsigned blocks = (unsigned)std::min<long>(((long)cap + 127) / 128, (long)p->sms * p->per_sm_tc1);
         k_propose_tc<1><<<blocks, 128, tc_smem_bytes(1), s>>>(p->pb, p->p, features, on, df, cap, n_dev, out,
-                                                              p->tc_err_dev);
+                                                              p->tc_err_dev, p->wait_limit);
     } else {
         const unsigned blocks = (unsigned)std::min<long>(((long)cap + 255) / 256, (long)p->sms * p->per_sm_tc2);
         k_propose_tc<2><<<blocks, 256, tc_smem_bytes(2), s>>>(p->pb, p->p, features, on, df, cap, n_dev, out,
-                                                              p->tc_err_dev);
+                                                              p->tc_err_dev, p->wait_limit);
     }
     PTRY(cudaGetLastError(), "proposal inference kernel");
     return GPIS_OK;
@@ -1324,6 +1326,13 @@ int gpis_proposal_set_kernel(gpis_proposal *p, int kernel)
     if (kernel != GPIS_PROPOSAL_KERNEL_TC2 && kernel != GPIS_PROPOSAL_KERNEL_TC1 && kernel != GPIS_PROPOSAL_KERNEL_MMA)
         return gpis_internal_set_error(GPIS_EINVAL, "unknown proposal kernel");
     p->kernel = kernel;
+    return GPIS_OK;
+}
+
+int gpis_proposal_set_wait_limit(gpis_proposal *p, uint32_t polls)
+{
+    if (!p) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
+    p->wait_limit = polls;
     return GPIS_OK;
 }
 

@@ -347,6 +347,12 @@ class Proposal:
         "tc1" (one tile per block) or "mma" (warp-level mma.sync)."""
         abi.check(self.lib.gpis_proposal_set_kernel(self.h, abi.PROPOSAL_KERNELS[kernel]), "gpis_proposal_set_kernel")
 
+    def set_wait_limit(self, polls=None):
+        """Polls of the tensor-memory kernel's completion wait per MMA round (None:
+        the default); 0 makes the wait time out, reported by the next infer."""
+        polls = abi.PROPOSAL_WAIT_DEFAULT if polls is None else int(polls)
+        abi.check(self.lib.gpis_proposal_set_wait_limit(self.h, polls), "gpis_proposal_set_wait_limit")
+
     def occupancy(self, kernel):
         """Resident blocks per SM of a fused inference kernel."""
         n = int(self.lib.gpis_proposal_occupancy(self.h, abi.PROPOSAL_KERNELS[kernel]))

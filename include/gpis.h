@@ -352,9 +352,13 @@ int gpis_se_splat_1d(const float *queries, const float *centers, float *values,
  * caller provides device flight and result streams as for gpis_flights_submit.
  * Larger batches fail with GPIS_ERANGE.  The first call on a device, with that
  * device current, looks up the array's device address and uploads a constant
- * table; make that first call before any stream capture.  All calls share the
- * array, so calls that overlap on the GPU (other streams, other host threads)
- * race: serialize them.                                                      */
+ * table; make that first call before any stream capture.  That set-up is kept
+ * for the life of the process: after cudaDeviceReset (or anything else that
+ * destroys the device's primary context) this entry point must not be called
+ * again on that device.  All calls share the array, so calls that overlap on
+ * the GPU (other streams, other host threads) race: serialize them.  Streams
+ * must be 16-byte aligned (GPIS_EINVAL otherwise, before any launch).  The
+ * march grid is the occupancy maximum, not a context's autotuned value.     */
 #define GPIS_STATIC_MAX_FLIGHTS 65536u
 int gpis_flights_submit_static(const gpis_medium_desc *medium, const gpis_flight_soa *in,
                                const gpis_result_soa *out, uint32_t n, void *cuda_stream);
@@ -500,6 +504,15 @@ int gpis_proposal_infer(gpis_proposal *prop, const gpis_flight_soa *in, const fl
 #define GPIS_PROPOSAL_KERNEL_TC1 1
 #define GPIS_PROPOSAL_KERNEL_MMA 2
 int gpis_proposal_set_kernel(gpis_proposal *prop, int kernel);
+/* Polls of the tensor-memory inference kernel's bounded completion wait per
+ * MMA round (default GPIS_PROPOSAL_WAIT_DEFAULT; each poll is one
+ * mbarrier.try_wait).  When a round's wait runs out, the kernel's threads stop
+ * together, wait for the MMAs already committed with the default bound, free
+ * their tensor memory and set a flag; the next gpis_proposal_infer returns
+ * GPIS_EIO and clears it.  0 makes every wait run out at once: the way to
+ * exercise that path.  No counterpart in the reference.                      */
+#define GPIS_PROPOSAL_WAIT_DEFAULT (1u << 22)
+int gpis_proposal_set_wait_limit(gpis_proposal *prop, uint32_t polls);
 /* Resident blocks per SM of a fused inference kernel (its persistent grid is
  * SMs x this); negative on error.                                           */
 int gpis_proposal_occupancy(const gpis_proposal *prop, int kernel);

@@ -260,3 +260,52 @@ def render_rows(desc, scene, row0, rows, n_threads=0):
     c = counts.sum(axis=0)
     return img[row0:row0 + rows], {"distance_flights": int(c[0]), "shadow_flights": int(c[1]),
                                    "medium_events": int(c[2]), "failed": int(c[3])}
+
+
+def compare_flights(rec_gpu, rec_cpu, sigma, scene_scale, t_tol_rel=1e-4, value_tol=1e-5, grad_tol=2e-3):
+    """Parity statistics of two sets of flight records of the same inputs (the GPU's
+    and this oracle's): the bars of the flight path, counted rather than asserted.
+
+    * status agreement, hit / miss (transmittance 0/1) agreement;
+    * hits on both sides: |dt| <= t_tol_rel * scene_scale; hits outside it that are
+      back-off cases (one side returned t = 0 after the reference refinement's x0.9
+      back-off reached 0.01, SparseConvolutionNoiseMedium.cpp:309-330) and the rest;
+    * misses on both sides: t equal, the value at farT within value_tol of the noise
+      scale sigma (relative above sigma);
+    * gradients of hits with |dt| <= 1e-6: relative L2 <= grad_tol.
+    """
+    g, c = abi.unpack_results(rec_gpu), abi.unpack_results(rec_cpu)
+    n = len(g["hit"])
+    agree = g["hit"] == c["hit"]
+    both = agree & g["hit"]
+    dt = np.abs(g["t"][both].astype(np.float64) - c["t"][both])
+    t_tol = t_tol_rel * scene_scale
+    bad = dt > t_tol
+    backoff = (g["t"][both] == 0) | (c["t"][both] == 0)
+    miss = agree & ~g["hit"]
+    s = max(float(sigma), 1e-6)
+    vtol = value_tol * s * np.maximum(1.0, np.abs(c["value"][miss]) / s)
+    v_ok = np.abs(g["value"][miss].astype(np.float64) - c["value"][miss]) <= vtol
+    close_t = both.copy()
+    close_t[both] = dt <= 1e-6
+    gg, cg = g["grad"][close_t], c["grad"][close_t]
+    rel = np.linalg.norm(gg - cg, axis=1) / np.maximum(1e-6, np.linalg.norm(cg, axis=1))
+    hits = int(both.sum())
+    return {
+        "flights": int(n),
+        "status_agreement": float((g["status"] == c["status"]).mean()) if n else 1.0,
+        "hit_agreement": float(agree.mean()) if n else 1.0,
+        "hit_disagreements": int((~agree).sum()),
+        "hits": hits,
+        "t_tol": t_tol,
+        "hits_within_t_tol": float(1.0 - bad.mean()) if hits else 1.0,
+        "t_outliers": int(bad.sum()),
+        "t_outliers_backoff": int((bad & backoff).sum()),
+        "t_outliers_other": int((bad & ~backoff).sum()),
+        "max_dt_non_backoff": float(dt[~backoff].max()) if (~backoff).any() else 0.0,
+        "misses": int(miss.sum()),
+        "miss_t_equal": float((g["t"][miss] == c["t"][miss]).mean()) if miss.any() else 1.0,
+        "miss_value_within_tol": float(v_ok.mean()) if miss.any() else 1.0,
+        "normals_compared": int(close_t.sum()),
+        "normals_within_tol": float((rel <= grad_tol).mean()) if close_t.any() else 1.0,
+    }

@@ -131,37 +131,36 @@ def agreement(ref_out, rec):
     return float(agree.mean()), float(np.mean(dt <= 1.5e-4)) if both.any() else 1.0, int(ok.sum())
 
 
-def main():
+def compare(n_flights=1 << 22, reps=5, grid_res=256):
+    """Both kernels on the same baked-grid flights (primary, then the conditioned
+    secondaries at the flight kernels' hits): per pass the device time per launch
+    (CUDA events, mean over reps after a warm-up), flights/s and agreement."""
     import torch
     from gpis_extend_gb300 import runtime
 
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--flights", type=int, default=1 << 22)
-    ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--grid", type=int, default=256)
-    args = ap.parse_args()
-    grid = sphere_grid(args.grid)
+    grid = sphere_grid(grid_res)
     desc = grid_medium(grid)
-    prim = workloads.sphere_flights(args.flights, desc)
-    res = {"workload": f"sphere SDF baked to a {args.grid}^3 grid, sigma 0.05, l 0.1, N 8, 1D Renewal+ UNI",
+    prim = workloads.sphere_flights(n_flights, desc)
+    res = {"workload": f"sphere SDF baked to a {grid_res}^3 grid, sigma 0.05, l 0.1, N 8, 1D Renewal+ UNI, "
+                       f"{n_flights} primary flights + their conditioned secondaries",
            "flights": {}}
     with runtime.Context(desc) as ctx:
         rec = ctx.trace_host(prim)
         sec, _ = workloads.secondary_flights(prim, rec, desc)
         stream = torch.cuda.current_stream()
         for name, batch in (("primary", prim), ("secondary", sec)):
-            ref_out, ref_ms, ref_e2e = run(batch, grid, desc, reps=args.reps)
+            ref_out, ref_ms, ref_e2e = run(batch, grid, desc, reps=reps)
             dev = runtime.DeviceFlights(batch)
             ctx.submit(dev, stream)
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            for _ in range(args.reps):
+            for _ in range(reps):
                 ctx.submit(dev, stream)
             e1.record(stream)
             torch.cuda.synchronize()
-            ours_ms = e0.elapsed_time(e1) / args.reps
+            ours_ms = e0.elapsed_time(e1) / reps
             ours_rec = ctx.trace_host(batch)
             hit_agree, t_agree, n_ok = agreement(ref_out, ours_rec)
             res["flights"][name] = {
@@ -173,8 +172,20 @@ def main():
                 "compared": n_ok}
     tot_ref = sum(v["reference_kernel_ms"] for v in res["flights"].values())
     tot_ours = sum(v["flight_kernels_ms"] for v in res["flights"].values())
+    n_all = sum(v["n"] for v in res["flights"].values())
+    res["reference_flights_per_s"] = n_all / (tot_ref * 1e-3)
+    res["flight_kernels_flights_per_s"] = n_all / (tot_ours * 1e-3)
     res["speedup_total"] = tot_ref / tot_ours
-    print(json.dumps(res))
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--flights", type=int, default=1 << 22)
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--grid", type=int, default=256)
+    args = ap.parse_args()
+    print(json.dumps(compare(args.flights, args.reps, args.grid)))
 
 
 if __name__ == "__main__":

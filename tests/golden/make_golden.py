@@ -6,7 +6,7 @@ tangent-frame code compiled from the reference tree (oracle/Makefile, target
 "ref").  It is only runnable where the reference tree is present; the JSON it
 writes is committed so the tests never need the reference at run time.
 
-    python tests/golden/make_golden.py [--ref /path/to/reference]
+    python tests/golden/make_golden.py --ref /path/to/reference   (or GPIS_REFERENCE=...)
 """
 import argparse
 import json
@@ -20,8 +20,10 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("GPIS_REFERENCE"))
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("the reference tree is required: --ref <path> or GPIS_REFERENCE")
     subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={args.ref}"])
     out = subprocess.check_output([os.path.join(ROOT, "oracle", "_ref", "ref_golden")])
     doc = json.loads(out)

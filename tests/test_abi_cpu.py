@@ -90,3 +90,20 @@ def test_ctx_create_fails_loudly_without_gpu(lib):
     h = ctypes.c_void_p()
     rc = lib.gpis_ctx_create(ctypes.byref(d), 1, ctypes.byref(h))
     assert rc == abi.GPIS_ENODEV and not h.value
+
+
+def test_static_entry_rejects_misaligned_streams_before_launch(lib):
+    # a stream pointer offset by 4 bytes (a sub-slice of a float buffer) is refused
+    # with GPIS_EINVAL before the entry point touches the device; the addresses are
+    # never dereferenced
+    d = workloads.sphere_medium()
+    soa = abi.FlightSoA()
+    res = abi.ResultSoA()
+    soa.origin_near = 0x10000
+    soa.dir_far = 0x20000 + 4
+    soa.seeds = 0x30000
+    soa.prev = 0x40000
+    res.rec = 0x50000
+    rc = lib.gpis_flights_submit_static(ctypes.byref(d), ctypes.byref(soa), ctypes.byref(res), 128, None)
+    assert rc == abi.GPIS_EINVAL
+    assert b"16-byte" in lib.gpis_last_error()

@@ -185,6 +185,36 @@ def test_gpu_fused_inference_matches_unfused(gpu, kernel):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["tc2", "tc1"])
+def test_gpu_tensor_core_wait_time_out_is_reported(gpu, kernel):
+    """The tensor-memory kernel's bounded completion wait, made to run out: with a
+    poll limit of 0 every MMA round gives up at once, the threads stop together,
+    wait (with the default bound) for the MMAs already committed, free their
+    tensor memory and raise the flag.  The next call reports GPIS_EIO without
+    launching; with the limit restored the call after succeeds and gives the same
+    intervals as before (the context is still usable)."""
+    torch, runtime = gpu
+    desc = proposal.config2_medium()
+    b = workloads.torus_flights(1024, desc, seed=3)
+    with runtime.Context(desc) as ctx, runtime.Proposal(proposal.init_params(2)) as prop:
+        prop.set_kernel(kernel)
+        dev = runtime.DeviceFlights(b)
+        f = runtime.proposal_features(ctx, dev)
+        good = prop.infer(dev, f).cpu().numpy()
+        prop.set_wait_limit(0)
+        prop.infer(dev, f)
+        torch.cuda.synchronize()
+        prop.set_wait_limit()
+        with pytest.raises(abi.GpisError) as e:
+            prop.infer(dev, f)
+        assert e.value.code == abi.GPIS_EIO
+        assert "timed out" in str(e.value)
+        again = prop.infer(dev, f).cpu().numpy()
+        torch.cuda.synchronize()
+    assert np.array_equal(again.view(np.uint32), good.view(np.uint32))
+
+
+@pytest.mark.gpu
 def test_gpu_tensor_core_inference_tiles(gpu):
     """The tcgen05 kernels with one and two tiles per block give the same bits; a
     ragged batch (not a multiple of 128) gives the rows of the full batch; the

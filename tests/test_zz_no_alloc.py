@@ -40,17 +40,30 @@ def compare(a, b):
     assert np.all(np.linalg.norm(ga["grad"] - gb["grad"], axis=1) <= 2e-3 * np.maximum(ref, 1e-6))
 
 
-def test_static_entry_matches_context_entry_twice():
+MEDIA = {
+    # 1D, one octave: the stationary cooperative fast pass and its set-up records
+    "sphere_1d": (lambda: workloads.sphere_medium(), workloads.sphere_flights, 1.5),
+    # 3D world-space noise: full conditioning records and the generic evaluator
+    "sphere_3d": (lambda: workloads.sphere_medium(one_d=False), workloads.sphere_flights, 1.5),
+    # 1D, three octaves, nonstationary length scale: the octave fast pass
+    "torus_octaves": (lambda: workloads.torus_plane_medium(), workloads.torus_flights, 2.0),
+}
+
+
+@pytest.mark.parametrize("kind", sorted(MEDIA))
+def test_static_entry_matches_context_entry_twice(kind):
     import torch
     from gpis_extend_gb300 import build
     build.build()
     assert torch.cuda.is_available()
     stream = torch.cuda.current_stream()
-    desc = workloads.sphere_medium()
-    prim = workloads.sphere_flights(8192, desc, index_offset=12345)
+    make_desc, make_flights, half = MEDIA[kind]
+    desc = make_desc()
+    n = 2048 if kind == "sphere_3d" else 8192
+    prim = make_flights(n, desc, index_offset=12345)
     with runtime.Context(desc) as ctx:
         ref1 = ctx.trace_host(prim)
-        sec, _ = workloads.secondary_flights(prim, ref1, desc)
+        sec, _ = workloads.secondary_flights(prim, ref1, desc, half=half)
         ref2 = ctx.trace_host(sec)
     # first call: primary flights; second call: conditioned secondaries (the
     # conditioning records of the working array are rewritten by this call)
