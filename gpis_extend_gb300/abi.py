@@ -388,6 +388,7 @@ def load_library(path=None):
         "gpis_debug_cells_3d": (c_int, [vp, vp, c_u32, c_u32, c_u32, vp, vp]),
         "gpis_debug_field": (c_int, [vp, vp, vp, vp, vp, vp, c_u32, vp]),
         "gpis_debug_tc_gemm": (c_int, [vp, vp, c_u32, c_u32, vp]),
+        "gpis_debug_exp": (c_int, [vp, vp, c_u32]),
         "gpis_proposal_set_kernel": (c_int, [vp, c_int]),
         "gpis_proposal_occupancy": (c_int, [vp, c_int]),
         "gpis_proposal_set_wait_limit": (c_int, [vp, c_u32]),

@@ -313,6 +313,117 @@ __device__ __forceinline__ float ex2_approx(float x)
     return y;
 }
 
+// ---- correctly rounded exp ---------------------------------------------------
+// e^x rounded to the nearest float, the exp of the precise evaluator (the oracle
+// evaluates the reference's float exp as (float)exp((double)x), the correctly
+// rounded value).  Tang's table-driven method (P. T. P. Tang, "Table-driven
+// implementation of the exponential function in IEEE floating-point arithmetic",
+// ACM TOMS 15(2), 1989) carried in float-float: x = (64 m + j) ln2 / 64 + r with
+// |r| <= ln2 / 128, e^x = 2^m 2^(j/64) e^r, the table 2^(j/64) as float pairs
+// (hi + lo, generated from the definition to 60 digits), e^r - 1 as
+// r + r^2/2 (exact products) + r^3/6 + r^4/24 + r^5/120, one rounding at the end.
+// Relative error about 2^-46 before the rounding: it differs from the correctly
+// rounded value on about 1e-8 of the arguments in [-90, 0] (checked exhaustively
+// on every third float there).  Arguments below -87 (results near the denormal
+// range, which never decide a sum) take expf.
+static __constant__ float2 c_exp2_64[64] = {
+    {0x1.0000000000000p+0f, 0x0.0p+0f},
+    {0x1.02c9a40000000p+0f, -0x1.887fa00000000p-28f},
+    {0x1.059b0e0000000p+0f, -0x1.9d4f520000000p-25f},
+    {0x1.0874520000000p+0f, -0x1.e2990e0000000p-26f},
+    {0x1.0b55860000000p+0f, 0x1.9f31220000000p-25f},
+    {0x1.0e3ec40000000p+0f, -0x1.a585cc0000000p-25f},
+    {0x1.11301e0000000p+0f, -0x1.fdb4960000000p-25f},
+    {0x1.1429aa0000000p+0f, 0x1.d525bc0000000p-25f},
+    {0x1.172b840000000p+0f, -0x1.c157420000000p-27f},
+    {0x1.1a35be0000000p+0f, 0x1.6df96e0000000p-25f},
+    {0x1.1d48740000000p+0f, -0x1.d2e8ca0000000p-25f},
+    {0x1.2063b80000000p+0f, 0x1.0c519a0000000p-25f},
+    {0x1.2387a60000000p+0f, 0x1.ceac480000000p-25f},
+    {0x1.26b4560000000p+0f, 0x1.789f380000000p-26f},
+    {0x1.29e9e00000000p+0f, -0x1.5c04240000000p-25f},
+    {0x1.2d285a0000000p+0f, 0x1.b900c20000000p-26f},
+    {0x1.306fe00000000p+0f, 0x1.4636e20000000p-25f},
+    {0x1.33c08c0000000p+0f, -0x1.b37d200000000p-25f},
+    {0x1.371a740000000p+0f, -0x1.18aac60000000p-25f},
+    {0x1.3a7db40000000p+0f, -0x1.634c020000000p-25f},
+    {0x1.3dea640000000p+0f, 0x1.8246840000000p-25f},
+    {0x1.4160a20000000p+0f, 0x1.f72e2a0000000p-28f},
+    {0x1.44e0860000000p+0f, 0x1.8624b40000000p-30f},
+    {0x1.486a2c0000000p+0f, -0x1.47d8660000000p-25f},
+    {0x1.4bfdae0000000p+0f, -0x1.593abc0000000p-25f},
+    {0x1.4f9b280000000p+0f, -0x1.2c5a6c0000000p-25f},
+    {0x1.5342b60000000p+0f, -0x1.2c56100000000p-25f},
+    {0x1.56f4740000000p+0f, -0x1.295b040000000p-25f},
+    {0x1.5ab07e0000000p+0f, -0x1.5bd5ec0000000p-27f},
+    {0x1.5e76f20000000p+0f, -0x1.4a5bd60000000p-25f},
+    {0x1.6247ec0000000p+0f, -0x1.f8b5500000000p-25f},
+    {0x1.6623880000000p+0f, 0x1.2a91120000000p-27f},
+    {0x1.6a09e60000000p+0f, 0x1.9fcef40000000p-26f},
+    {0x1.6dfb240000000p+0f, -0x1.cd72e80000000p-27f},
+    {0x1.71f75e0000000p+0f, 0x1.1d8bee0000000p-25f},
+    {0x1.75feb60000000p+0f, -0x1.37b3060000000p-25f},
+    {0x1.7a11480000000p+0f, -0x1.829fd00000000p-25f},
+    {0x1.7e2f340000000p+0f, -0x1.2616340000000p-25f},
+    {0x1.82589a0000000p+0f, -0x1.accc7c0000000p-26f},
+    {0x1.868d9a0000000p+0f, -0x1.2edb440000000p-26f},
+    {0x1.8ace540000000p+0f, 0x1.15506e0000000p-27f},
+    {0x1.8f1aea0000000p+0f, -0x1.baa2320000000p-26f},
+    {0x1.93737c0000000p+0f, -0x1.e647440000000p-25f},
+    {0x1.97d82a0000000p+0f, -0x1.0d8d840000000p-31f},
+    {0x1.9c49180000000p+0f, 0x1.51f8480000000p-27f},
+    {0x1.a0c6680000000p+0f, -0x1.2886a60000000p-26f},
+    {0x1.a5503c0000000p+0f, -0x1.b83b540000000p-25f},
+    {0x1.a9e6b60000000p+0f, -0x1.50c0480000000p-25f},
+    {0x1.ae89fa0000000p+0f, -0x1.a94b140000000p-26f},
+    {0x1.b33a2c0000000p+0f, -0x1.ec3a820000000p-26f},
+    {0x1.b7f7700000000p+0f, -0x1.a094380000000p-25f},
+    {0x1.bcc1ea0000000p+0f, -0x1.f687c60000000p-25f},
+    {0x1.c199be0000000p+0f, -0x1.3d56b20000000p-27f},
+    {0x1.c67f120000000p+0f, 0x1.cafa2a0000000p-25f},
+    {0x1.cb720e0000000p+0f, -0x1.8837cc0000000p-27f},
+    {0x1.d072d40000000p+0f, 0x1.40f1300000000p-25f},
+    {0x1.d5818e0000000p+0f, -0x1.822dbc0000000p-27f},
+    {0x1.da9e600000000p+0f, 0x1.ed99420000000p-27f},
+    {0x1.dfc9740000000p+0f, -0x1.908c940000000p-25f},
+    {0x1.e502ee0000000p+0f, 0x1.e2cffe0000000p-26f},
+    {0x1.ea4afa0000000p+0f, 0x1.52486c0000000p-27f},
+    {0x1.efa1be0000000p+0f, 0x1.cc2b440000000p-25f},
+    {0x1.f507660000000p+0f, -0x1.246eb00000000p-26f},
+    {0x1.fa7c180000000p+0f, 0x1.9e90d80000000p-28f},
+};
+
+__device__ __forceinline__ float cr_expf(float x)
+{
+    if (!(x > -87.0f)) return expf(x);
+    const float kf = rintf(x * 0x1.715476p+6f);   // 64 / ln2
+    const int k = (int)kf;
+    const float c_hi = 0x1.62e43p-7f, c_lo = -0x1.05c61p-35f;   // ln2 / 64 = c_hi + c_lo + O(2^-60)
+    const float ph = __fmul_rn(kf, c_hi);
+    float pl = __fmaf_rn(kf, c_hi, -ph);
+    pl = __fmaf_rn(kf, c_lo, pl);
+    const float rh = __fsub_rn(x, ph);   // exact (Sterbenz)
+    const float r = __fsub_rn(rh, pl);
+    const float rl = __fsub_rn(__fsub_rn(rh, r), pl);
+    const float s2h = __fmul_rn(r, r);
+    float s2l = __fmaf_rn(r, r, -s2h);
+    s2l = __fmaf_rn(__fmul_rn(2.0f, r), rl, s2l);
+    const float h2h = __fmul_rn(0.5f, s2h), h2l = __fmul_rn(0.5f, s2l);
+    const float tail = __fmul_rn(__fmul_rn(r, s2h),
+                                 __fmaf_rn(r, __fmaf_rn(r, 0x1.111112p-7f, 0x1.555556p-5f), 0x1.555556p-3f));
+    float ql;
+    const float qh = two_sum(r, h2h, ql);
+    ql = __fadd_rn(ql, __fadd_rn(rl, __fadd_rn(h2l, tail)));
+    const float2 t = c_exp2_64[k & 63];
+    const float ah = __fmul_rn(t.x, qh);
+    float al = __fmaf_rn(t.x, qh, -ah);
+    al = __fadd_rn(al, __fmaf_rn(t.x, ql, __fmaf_rn(t.y, qh, t.y)));
+    float sl;
+    const float sh = two_sum(t.x, ah, sl);
+    const float y = __fadd_rn(sh, __fadd_rn(sl, al));
+    return __fmul_rn(y, __int_as_float(((k >> 6) + 127) << 23));
+}
+
 // ---- means (MeanFunction::mean / dmean_da) -------------------------------------
 __device__ __forceinline__ float grid_voxel(const DevMedium &m, int x, int y, int z)
 {

@@ -374,6 +374,23 @@ __device__ __forceinline__ void normal_draws(uint32_t seed, int pair, float &z0,
     normal_pair(pcg_draw(c_jump[2 + 2 * pair], seed), pcg_draw(c_jump[3 + 2 * pair], seed), z0, z1);
 }
 
+// Box-Muller as the reference evaluates it, in double (Gaussian.cpp:23-35; PI is
+// the float constant of Angle.hpp:8, so 2*PI is formed in float before it meets
+// the double u2): the pair of draws `pair` of the normal-seed stream.  One pair per
+// conditioned flight (its conditioning gradient), where the transverse draws enter
+// the along-ray coefficient through the rounding of the frame transforms.
+__device__ __forceinline__ void normal_draws_double(uint32_t seed, int pair, double &z0, double &z1)
+{
+    const double u1 = (double)unit_float(pcg_draw(c_jump[2 + 2 * pair], seed));
+    const double u2 = (double)unit_float(pcg_draw(c_jump[3 + 2 * pair], seed));
+    const double r = sqrt(-2.0 * log(1.0 - u1));
+    const float two_pi = 2.0f * 3.1415926536f;
+    double sn, cs;
+    sincos((double)two_pi * u2, &sn, &cs);
+    z0 = r * cs;
+    z1 = r * sn;
+}
+
 // correlatedGradientMoments (SparseConvolutionNoise.cpp:13-22)
 __device__ __forceinline__ void corr_moments(float dist, float &factor, float &variance)
 {
@@ -490,10 +507,47 @@ __device__ __forceinline__ void noise1d_level(const DevMedium &m, const FlightIn
 // 244-295): both levels' base gradients, a normal pair per level at the start of
 // the ray (pairs 0, 1) and at its end (pairs 2, 3), each level's gradient taken
 // to world space through its own frame and scale, blended by the level weights.
+__device__ void noise1d_precise_vd(const DevMedium &m, float z, uint32_t seed, float ls, float &value, float &deriv);
+
 __device__ void noise_gradient_mr(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
-                                  const float p[3], float t_segment, float &value, float g[3])
+                                  const float p[3], float t_segment, float &value, float g[3],
+                                  bool precise = false)
 {
     const MrLevels lv = mr_levels(m, ls_value_precise(m, p[0], p[2]));
+    if (precise && !cond && t_segment == 0.0f) {
+        // the conditioning's value and birth gradient at the origin, operation for
+        // operation: each level's precise value and derivative, the double normal
+        // pairs (low level first), the level frames and scales, the blend unfused
+        Frame f;
+        ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+        float v[2], dv[2];
+#pragma unroll 1
+        for (int j = 0; j < 2; ++j) {
+            const float z = ray_coord_oct(m, f.n, p[0], p[1], p[2], lv.s[j]);
+            noise1d_precise_vd(m, z, fl.noise_seed + lv.seed[j], 1.0f, v[j], dv[j]);
+        }
+        value = __fadd_rn(__fmul_rn(lv.w[0], v[0]), __fmul_rn(lv.w[1], v[1]));
+        const double s2 = 1.4142135381698608;   // (double)sqrtf(2.f)
+        float gw[2][3];
+#pragma unroll 1
+        for (int j = 0; j < 2; ++j) {
+            double z0, z1;
+            normal_draws_double(fl.normal_seed, j, z0, z1);
+            const float gq[3] = {__fadd_rn((float)(z0 / s2 * 1.0), 0.0f), __fadd_rn((float)(z1 / s2 * 1.0), 0.0f),
+                                 __fadd_rn(0.0f, dv[j])};
+            Frame fj;
+            ray_frame_level(m, fl.d, lv.s[j], fj);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float gi = __fadd_rn(__fadd_rn(__fmul_rn(fj.t[i], gq[0]), __fmul_rn(fj.b[i], gq[1])),
+                                           __fmul_rn(fj.n[i], gq[2]));
+                gw[j][i] = __fdiv_rn(__fmul_rn(m.l_inv[i], gi), lv.s[j]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) g[i] = __fadd_rn(__fmul_rn(lv.w[0], gw[0][i]), __fmul_rn(lv.w[1], gw[1][i]));
+        return;
+    }
     float ow[2] = {1.0f, 1.0f};
     if (cond) {
         const MrLevels lo = mr_levels(m, ls_value_precise(m, fl.o[0], fl.o[2]));
@@ -543,15 +597,28 @@ __device__ void noise_gradient_mr(const DevMedium &m, const FlightIn &fl, const 
 
 // Noise of octave k at p with its world gradient (evaluateGradientNoise1D /
 // evaluateNoise3D gradient).  cond: the octave's conditioning splats are active.
+__device__ void noise1d_precise_vd(const DevMedium &m, float z, uint32_t seed, float ls, float &value, float &deriv);
+__device__ float mean_plus_precise(const DevMedium &m, float an, float x, float y, float z, int &id);
+__device__ void noise3d_precise_grad(const DevMedium &m, float px, float py, float pz, uint32_t seed, float &value,
+                                     float g[3]);
+
+// precise: the noise value and its derivative along the ray (1D) or gradient (3D)
+// come from the precise evaluator (the conditioning at a flight's origin), else
+// from the generic one
 __device__ __forceinline__ void noise_gradient_oct(const DevMedium &m, const FlightIn &fl, const CondRec &c, bool cond,
-                                   const float p[3], float t_segment, int oc, float &value, float g[3])
+                                   const float p[3], float t_segment, int oc, float &value, float g[3],
+                                   bool precise = false)
 {
     if (!(m.flags & MF_ONE_D)) {
-        float v, gg[3];
-        noise3d_generic<true>(m, p[0], p[1], p[2], fl.noise_seed, v, gg);
-        value = v * m.inv_norm3d;
+        if (precise) {
+            noise3d_precise_grad(m, p[0], p[1], p[2], fl.noise_seed, value, g);
+        } else {
+            float v, gg[3];
+            noise3d_generic<true>(m, p[0], p[1], p[2], fl.noise_seed, v, gg);
+            value = v * m.inv_norm3d;
 #pragma unroll
-        for (int i = 0; i < 3; ++i) g[i] = gg[i] * m.inv_norm3d;
+            for (int i = 0; i < 3; ++i) g[i] = gg[i] * m.inv_norm3d;
+        }
         if (cond) {
             float cv, cg[3];
             cond3d(m, c, fl.o, p, cv, cg);
@@ -562,7 +629,7 @@ __device__ __forceinline__ void noise_gradient_oct(const DevMedium &m, const Fli
         return;
     }
     if (m.flags & MF_MULTIRES) {
-        noise_gradient_mr(m, fl, c, cond, p, t_segment, value, g);
+        noise_gradient_mr(m, fl, c, cond, p, t_segment, value, g, precise);
         return;
     }
     const CondOct &co = c.oct[oc];
@@ -570,12 +637,16 @@ __device__ __forceinline__ void noise_gradient_oct(const DevMedium &m, const Fli
     Frame f;
     ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
     const float z = ray_coord_oct(m, f.n, p[0], p[1], p[2], sc);
-    const float ls = ns_scale(m, p[0], p[2]);
+    const float ls = precise ? ns_scale_precise(m, p[0], p[2]) : ns_scale(m, p[0], p[2]);
     float v, dv;
-    noise1d_generic<true>(m, z, fl.noise_seed + oct_seed(m, oc), v, dv, ls);
-    const float inrm = inv_norm_1d(m, ls);
-    v *= inrm;
-    dv *= inrm;
+    if (precise) {
+        noise1d_precise_vd(m, z, fl.noise_seed + oct_seed(m, oc), ls, v, dv);
+    } else {
+        noise1d_generic<true>(m, z, fl.noise_seed + oct_seed(m, oc), v, dv, ls);
+        const float inrm = inv_norm_1d(m, ls);
+        v *= inrm;
+        dv *= inrm;
+    }
     float gcx = 0.0f, gcy = 0.0f;
     if (cond) {
         const float oz = ray_coord_oct(m, f.n, fl.o[0], fl.o[1], fl.o[2], sc);
@@ -599,6 +670,29 @@ __device__ __forceinline__ void noise_gradient_oct(const DevMedium &m, const Fli
         gl[0] = m0 + s * z0;
         gl[1] = m1 + s * z1;
         gl[2] = dv;
+    } else if (precise && t_segment == 0.0f) {
+        // the birth gradient of the conditioning (grad_noise at the origin), operation
+        // for operation: the double draws scaled by 1/sqrt(2) and 1/splat scale in
+        // double, rounded to float, taken to world space through the frame and the
+        // inverse length scales (evaluateGradientNoise1D, SparseConvolutionNoise.cpp:
+        // 178-296; TangentFrame::toGlobal; transformGradLocaltoWorld)
+        const float scx = splat_cov_1d(ls, ls);
+        const double xs = 1.0 / (double)scx;
+        double z0, z1;
+        normal_draws_double(nseed, 0, z0, z1);
+        const double s2 = 1.4142135381698608;   // (double)sqrtf(2.f)
+        const float gx0 = (float)(z0 / s2 * xs), gy0 = (float)(z1 / s2 * xs);
+        const float gq[3] = {__fadd_rn(gx0, gcx), __fadd_rn(gy0, gcy), __fadd_rn(0.0f, dv)};
+        const float sdiv = m.ls_kind ? m.ls_max : 1.0f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float gi = __fadd_rn(__fadd_rn(__fmul_rn(f.t[i], gq[0]), __fmul_rn(f.b[i], gq[1])),
+                                       __fmul_rn(f.n[i], gq[2]));
+            float gw = __fdiv_rn(__fmul_rn(m.l_inv[i], gi), sdiv);
+            if (sc != 1.0f) gw = __fdiv_rn(gw, sc);
+            g[i] = gw;
+        }
+        return;
     } else {
         const float scx = splat_cov_1d(ls, ls);
         const float xs = 1.0f / scx;
@@ -670,7 +764,7 @@ __device__ __forceinline__ void condition_octave(const DevMedium &m, const Fligh
         float gi[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) gi[i] = (m.l_aniso[i] * delta[i]) * mul;
-        const float ls = ns_scale(m, fl.o[0], fl.o[2]);
+        const float ls = ns_scale_precise(m, fl.o[0], fl.o[2]);
         const float sc = splat_cov_1d(ls, ls);
         const float s2 = sc * sc;
         const float gx = dot3_rn(f.t[0], f.t[1], f.t[2], gi[0], gi[1], gi[2]);
@@ -690,9 +784,44 @@ __device__ __forceinline__ void condition_octave(const DevMedium &m, const Fligh
             c.has_obs = 1u;
         }
     } else {
+        // delta / (-2 * (l_inv^2 * 0.25)), the inverse of sparseConvNoiseOneOverSecondDerivative's
+        // diagonal applied as the division it is (GPFunctions.cpp:723-749)
 #pragma unroll
-        for (int i = 0; i < 3; ++i) co.gs[i] = delta[i] * m.d2inv3[i];
+        for (int i = 0; i < 3; ++i) {
+            const float inv2 = __fmul_rn(m.l_inv[i], m.l_inv[i]);
+            const float d2 = __fmul_rn(-2.0f, __fmul_rn(inv2, 0.25f));
+            co.gs[i] = inv2 > 0.0f ? __fdiv_rn(delta[i], d2) : 0.0f;
+        }
     }
+}
+
+// The mean gradient as the reference evaluates it in double and rounds to float
+// (dmean_da): the torus (and its union with the plane) in FP64 with the
+// operations unfused (once per conditioned flight); the other means as mean_grad.
+__device__ __forceinline__ void mean_grad_precise(const DevMedium &m, float px, float py, float pz, float g[3])
+{
+    if (m.mean_kind != 4 && m.mean_kind != 5) {
+        mean_grad(m, px, py, pz, g);
+        return;
+    }
+    const float *q = m.mean_params;
+    const double x = __dsub_rn((double)px, (double)q[0]), y = __dsub_rn((double)py, (double)q[1]),
+                 z = __dsub_rn((double)pz, (double)q[2]);
+    const double rxz = __dsqrt_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(z, z)));
+    const double s = __dsub_rn(rxz, (double)q[3]);
+    const double len = __dsqrt_rn(__dadd_rn(__dmul_rn(s, s), __dmul_rn(y, y)));
+    if (m.mean_kind == 5) {
+        const double t = __dsub_rn(len, (double)q[4]);
+        const double pl = __dsub_rn((double)py, (double)q[5]);
+        if (pl < t) {
+            g[0] = 0.0f; g[1] = 1.0f; g[2] = 0.0f;
+            return;
+        }
+    }
+    const double dr = __ddiv_rn(s, len), dy = __ddiv_rn(y, len);
+    g[0] = rxz > 0.0 ? (float)__ddiv_rn(__dmul_rn(dr, x), rxz) : 0.0f;
+    g[1] = (float)dy;
+    g[2] = rxz > 0.0 ? (float)__ddiv_rn(__dmul_rn(dr, z), rxz) : 0.0f;
 }
 
 // Conditioning coefficients of a flight at its origin (conditioning,
@@ -704,38 +833,44 @@ __device__ __forceinline__ CondRec make_condition(const DevMedium &m, const Flig
     CondRec c = {};
     const float *p = fl.o;
     int id;
-    const float mean = mean_value(m, p[0], p[1], p[2], id);
+    // the mean as the reference rounds it (float of the double mean) and the noise
+    // from the precise evaluator, so that the conditioned field at the origin
+    // leaves the residual the reference leaves
+    const float mean = mean_plus_precise(m, 0.0f, p[0], p[1], p[2], id);
     float mg[3] = {0.0f, 0.0f, 0.0f};
-    if (m.flags & MF_RENEWAL_PLUS) mean_grad(m, p[0], p[1], p[2], mg);
+    if (m.flags & MF_RENEWAL_PLUS) mean_grad_precise(m, p[0], p[1], p[2], mg);
     const CondRec none = {};
     const int n = (m.flags & MF_ONE_D) ? (int)m.n_oct : 1;
     if (n == 1) {
         float v, g[3];
-        noise_gradient_oct(m, fl, none, false, p, 0.0f, 0, v, g);
+        noise_gradient_oct(m, fl, none, false, p, 0.0f, 0, v, g, true);
         condition_octave(m, fl, 0, v, g, fl.prev_v, fl.prev_g, mean, mg, c);
         return c;
     }
     float v[4], g[4][3];
-    for (int k = 0; k < n; ++k) noise_gradient_oct(m, fl, none, false, p, 0.0f, k, v[k], g[k]);
-    float total = 0.0f, sum_v = 0.0f, sum_g[3] = {0.0f, 0.0f, 0.0f};
+    for (int k = 0; k < n; ++k) noise_gradient_oct(m, fl, none, false, p, 0.0f, k, v[k], g[k], true);
+    // the shares in the restatement's float operations, unfused
+    float total = 0.0f;
+    for (int k = 0; k < n; ++k) total = __fadd_rn(total, __fmul_rn(oct_sigma(m, k), oct_sigma(m, k)));
+    float sum_v = 0.0f, sum_g[3] = {0.0f, 0.0f, 0.0f};
     for (int k = 0; k < n; ++k) {
         const float sk = oct_sigma(m, k);
-        total += sk * sk;
-        sum_v += sk * v[k];
+        sum_v = __fadd_rn(sum_v, __fmul_rn(sk, v[k]));
 #pragma unroll
-        for (int i = 0; i < 3; ++i) sum_g[i] += sk * g[k][i];
+        for (int i = 0; i < 3; ++i) sum_g[i] = __fadd_rn(sum_g[i], __fmul_rn(sk, g[k][i]));
     }
-    const float resid = (fl.prev_v - mean) - sum_v;
+    const float resid = __fsub_rn(__fsub_rn(fl.prev_v, mean), sum_v);
     float resid_g[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) resid_g[i] = (fl.prev_g[i] - mg[i]) - sum_g[i];
+    for (int i = 0; i < 3; ++i) resid_g[i] = __fsub_rn(__fsub_rn(fl.prev_g[i], mg[i]), sum_g[i]);
     for (int k = 0; k < n; ++k) {
         const float sk = oct_sigma(m, k);
-        const float share = sk * sk / total;
-        const float tv = mean + sk * v[k] + share * resid;
+        const float share = __fdiv_rn(__fmul_rn(sk, sk), total);
+        const float tv = __fadd_rn(__fadd_rn(mean, __fmul_rn(sk, v[k])), __fmul_rn(share, resid));
         float tg[3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) tg[i] = mg[i] + sk * g[k][i] + share * resid_g[i];
+        for (int i = 0; i < 3; ++i)
+            tg[i] = __fadd_rn(__fadd_rn(mg[i], __fmul_rn(sk, g[k][i])), __fmul_rn(share, resid_g[i]));
         condition_octave(m, fl, k, v[k], g[k], tv, tg, mean, mg, c);
     }
     return c;
@@ -957,7 +1092,8 @@ __device__ __forceinline__ void lane_cond_1d(const LaneField &L, int k, float sc
 
 // ---- precise evaluation ------------------------------------------------------
 // The reference's float formulation op for op: every splat as
-// expf(-((kr*t - kr*t_i)^2 / 2)) (GPFunctions.cpp:845-848), cell sums in impulse
+// exp(-((kr*t - kr*t_i)^2 / 2)) (GPFunctions.cpp:845-848) with the exp correctly
+// rounded (cr_expf, as the oracle evaluates the reference's float exp), cell sums in impulse
 // order, cells summed in order, division by the rounded normalisation, the
 // conditioning splats of evaluateNoise1DNormalized, and the mean in double
 // (emulated in float-float for the sphere) added as
@@ -985,7 +1121,7 @@ __device__ float noise1d_precise(const DevMedium &m, float z, uint32_t seed, flo
             const float tp = __fsub_rn(tl, ti);
             if (fabsf(tp) < 1.0f) {
                 const float ab = __fsub_rn(a, __fmul_rn(kr, ti));
-                const float e = expf(-__fdiv_rn(__fmul_rn(ab, ab), den));
+                const float e = cr_expf(-__fdiv_rn(__fmul_rn(ab, ab), den));
                 cv = __fadd_rn(cv, (wr >> 31) ? e : -e);
             }
         }
@@ -995,6 +1131,123 @@ __device__ float noise1d_precise(const DevMedium &m, float z, uint32_t seed, flo
     // sparseConvNoiseVariance1D: impulseDensity/kernelRadius * sqrt(pi) * localScale
     const float var = (float)((double)m.var1d_c * (1.7724538509055159 * (double)ls));
     return __fdiv_rn(sv, __fsqrt_rn(var));
+}
+
+// a * b / c rounded once to float: the product exact as a float pair, the quotient
+// carried with its remainder (the reference evaluates such terms in double and
+// rounds the result to float; the two agree but where the exact value lies within
+// about 2^-46 of a rounding boundary)
+__device__ __forceinline__ float rn_mul_div(float a, float b, float c)
+{
+    const float ph = __fmul_rn(a, b);
+    const float pl = __fmaf_rn(a, b, -ph);
+    const float qh = __fdiv_rn(ph, c);
+    const float rem = __fadd_rn(__fmaf_rn(-qh, c, ph), pl);
+    return __fadd_rn(qh, __fdiv_rn(rem, c));
+}
+
+// noise1d_precise with the derivative d/dz of the normalized noise: per splat
+// (float)(-2.0 * ab / den * f) as the reference's splattingKernel1D1stGrad
+// evaluates it in double (GPFunctions.cpp:859-863), summed as the value.  The
+// conditioning at a flight's origin takes both from here.
+__device__ void noise1d_precise_vd(const DevMedium &m, float z, uint32_t seed, float ls, float &value, float &deriv)
+{
+    const float kr = m.kr_iso;
+    const float tg = __fdiv_rn(z, kr);
+    const float fl = floorf(tg);
+    const float frac = __fsub_rn(tg, fl);
+    const int ci = (int)fl;
+    const float den = __fmul_rn(2.0f, __fmul_rn(ls, ls));
+    float sv = 0.0f, sg = 0.0f;
+    for (int dx = -1; dx <= 1; ++dx) {
+        const float tl = __fsub_rn(frac, (float)dx);
+        const float a = __fmul_rn(kr, tl);
+        const uint32_t s = xxhash2((uint32_t)(ci + dx), seed) + 1u;
+        float cv = 0.0f, cg = 0.0f;
+        for (uint32_t k = 0; k < m.n_imp; ++k) {
+            const float ti = unit_float(pcg_draw(c_jump[2 + 2 * k], s));
+            const uint32_t wr = pcg_draw(c_jump[3 + 2 * k], s);
+            const float tp = __fsub_rn(tl, ti);
+            if (fabsf(tp) < 1.0f) {
+                const float ab = __fsub_rn(a, __fmul_rn(kr, ti));
+                const float e = cr_expf(-__fdiv_rn(__fmul_rn(ab, ab), den));
+                const float gr = rn_mul_div(__fmul_rn(-2.0f, ab), e, den);
+                cv = __fadd_rn(cv, (wr >> 31) ? e : -e);
+                cg = __fadd_rn(cg, (wr >> 31) ? gr : -gr);
+            }
+        }
+        sv = __fadd_rn(sv, cv);
+        sg = __fadd_rn(sg, cg);
+    }
+    float nrm = m.norm1d;
+    if (ls != 1.0f) nrm = __fsqrt_rn((float)((double)m.var1d_c * (1.7724538509055159 * (double)ls)));
+    value = __fdiv_rn(sv, nrm);
+    deriv = __fdiv_rn(sg, nrm);
+}
+
+// noise3d_precise with the world gradient of the normalized noise: per splat
+// (-2 (ab_c M_c)) f as the reference's splattingKernel3D1stGrad (GPFunctions.cpp:
+// 814-821), summed per cell and over the cells in the value's order.
+__device__ void noise3d_precise_grad(const DevMedium &m, float px, float py, float pz, uint32_t seed, float &value,
+                                     float g[3])
+{
+    const float kr = m.kr_world;
+    const float p[3] = {px, py, pz};
+    float fr[3];
+    int ijk[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float q = __fdiv_rn(p[i], kr);
+        const float fl = floorf(q);
+        fr[i] = __fsub_rn(q, fl);
+        ijk[i] = (int)fl;
+    }
+    const bool xfirst = (m.flags & MF_XYZ_ORDER) != 0;
+    float sv = 0.0f, s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz) {
+                const float t0 = __fsub_rn(fr[0], (float)dx), t1 = __fsub_rn(fr[1], (float)dy),
+                            t2 = __fsub_rn(fr[2], (float)dz);
+                const uint32_t s = xxhash4((uint32_t)(ijk[2] + dz), (uint32_t)(ijk[1] + dy),
+                                           (uint32_t)(ijk[0] + dx), seed) + 1u;
+                float cv = 0.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
+                for (uint32_t k = 0; k < m.n_imp; ++k) {
+                    const int b = 2 + 4 * (int)k;
+                    const float r0 = unit_float(pcg_draw(c_jump[b], s));
+                    const float r1 = unit_float(pcg_draw(c_jump[b + 1], s));
+                    const float r2 = unit_float(pcg_draw(c_jump[b + 2], s));
+                    const uint32_t wr = pcg_draw(c_jump[b + 3], s);
+                    const float ix = xfirst ? r0 : r2, iy = r1, iz = xfirst ? r2 : r0;
+                    const float a0 = __fsub_rn(t0, ix), a1 = __fsub_rn(t1, iy), a2 = __fsub_rn(t2, iz);
+                    const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(a0, a0), __fmul_rn(a1, a1)), __fmul_rn(a2, a2));
+                    if (l2 < 1.0f) {
+                        const float b0 = __fsub_rn(__fmul_rn(kr, t0), __fmul_rn(kr, ix));
+                        const float b1 = __fsub_rn(__fmul_rn(kr, t1), __fmul_rn(kr, iy));
+                        const float b2 = __fsub_rn(__fmul_rn(kr, t2), __fmul_rn(kr, iz));
+                        float q = __fmul_rn(__fmul_rn(b0, m.m3[0]), b0);
+                        q = __fadd_rn(q, __fmul_rn(__fmul_rn(b1, m.m3[1]), b1));
+                        q = __fadd_rn(q, __fmul_rn(__fmul_rn(b2, m.m3[2]), b2));
+                        const float e = cr_expf(-q);
+                        const float g0 = __fmul_rn(__fmul_rn(-2.0f, __fmul_rn(b0, m.m3[0])), e);
+                        const float g1 = __fmul_rn(__fmul_rn(-2.0f, __fmul_rn(b1, m.m3[1])), e);
+                        const float g2 = __fmul_rn(__fmul_rn(-2.0f, __fmul_rn(b2, m.m3[2])), e);
+                        const bool pos = (wr >> 31) != 0;
+                        cv = __fadd_rn(cv, pos ? e : -e);
+                        c0 = __fadd_rn(c0, pos ? g0 : -g0);
+                        c1 = __fadd_rn(c1, pos ? g1 : -g1);
+                        c2 = __fadd_rn(c2, pos ? g2 : -g2);
+                    }
+                }
+                sv = __fadd_rn(sv, cv);
+                s0 = __fadd_rn(s0, c0);
+                s1 = __fadd_rn(s1, c1);
+                s2 = __fadd_rn(s2, c2);
+            }
+    value = __fdiv_rn(sv, m.norm3d);
+    g[0] = __fdiv_rn(s0, m.norm3d);
+    g[1] = __fdiv_rn(s1, m.norm3d);
+    g[2] = __fdiv_rn(s2, m.norm3d);
 }
 
 __device__ float noise3d_precise(const DevMedium &m, float px, float py, float pz, uint32_t seed)
@@ -1036,7 +1289,7 @@ __device__ float noise3d_precise(const DevMedium &m, float px, float py, float p
                         float q = __fmul_rn(__fmul_rn(b0, m.m3[0]), b0);
                         q = __fadd_rn(q, __fmul_rn(__fmul_rn(b1, m.m3[1]), b1));
                         q = __fadd_rn(q, __fmul_rn(__fmul_rn(b2, m.m3[2]), b2));
-                        const float e = expf(-q);
+                        const float e = cr_expf(-q);
                         cv = __fadd_rn(cv, (wr >> 31) ? e : -e);
                     }
                 }
@@ -1092,16 +1345,37 @@ __device__ float mean_plus_precise(const DevMedium &m, float an, float x, float 
     return __fadd_rn(s, e);
 }
 
+// The 3D conditioning splats' value at p as the reference's float expressions give
+// it: splattingKernel3D(p, origin, isCov) * value_scale plus splattingKernel3DGrad's
+// value row sum_c gs_c * (-2 (ab_c M_c)) f (GPFunctions.cpp:555-580, 784-843).
+__device__ __forceinline__ float cond3d_value_precise(const DevMedium &m, const CondRec &c, const float o[3],
+                                                      const float p[3])
+{
+    float ab[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) ab[i] = __fsub_rn(p[i], o[i]);
+    float absq = __fmul_rn(__fmul_rn(ab[0], m.m3c[0]), ab[0]);
+    absq = __fadd_rn(absq, __fmul_rn(__fmul_rn(ab[1], m.m3c[1]), ab[1]));
+    absq = __fadd_rn(absq, __fmul_rn(__fmul_rn(ab[2], m.m3c[2]), ab[2]));
+    const float f = cr_expf(-absq);
+    const CondOct &co = c.oct[0];
+    float gv = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float g1 = __fmul_rn(__fmul_rn(-2.0f, __fmul_rn(ab[i], m.m3c[i])), f);
+        gv = __fadd_rn(gv, __fmul_rn(g1, co.gs[i]));
+    }
+    return __fadd_rn(__fmul_rn(f, co.vs), gv);
+}
+
 __device__ float field_precise(const LaneField &L, float px, float py, float pz, int &id)
 {
     const DevMedium &m = *L.m;
     if (!(m.flags & MF_ONE_D)) {
         float noise = noise3d_precise(m, px, py, pz, L.seed);
         if (L.cond) {
-            float cv, cg[3];
             const float p[3] = {px, py, pz};
-            cond3d(m, L.c3, L.o, p, cv, cg);
-            noise = __fadd_rn(noise, cv);
+            noise = __fadd_rn(noise, cond3d_value_precise(m, L.c3, L.o, p));
         }
         return mean_plus_precise(m, __fmul_rn(L.sigma, noise), px, py, pz, id);
     }
@@ -1117,7 +1391,7 @@ __device__ float field_precise(const LaneField &L, float px, float py, float pz,
                 const float oz = ray_coord_oct(m, L.n, L.o[0], L.o[1], L.o[2], lv.s[j]);
                 const float d = __fsub_rn(z, oz);
                 const float den2 = m.cov_den2;
-                const float k0 = expf(-__fdiv_rn(__fmul_rn(d, d), den2));
+                const float k0 = cr_expf(-__fdiv_rn(__fmul_rn(d, d), den2));
                 const float r = -2.0f * d;
                 const float qh = __fdiv_rn(r, den2);
                 const float ql = __fdiv_rn(__fmaf_rn(-qh, den2, r), den2);
@@ -1151,7 +1425,7 @@ __device__ float field_precise(const LaneField &L, float px, float py, float pz,
                 den2 = (float)(2.0 * (double)__fmul_rn(s2, s2));
             }
             const float d = __fsub_rn(z, oz);
-            const float k0 = expf(-__fdiv_rn(__fmul_rn(d, d), den2));
+            const float k0 = cr_expf(-__fdiv_rn(__fmul_rn(d, d), den2));
             // (float)(-2 d / den2 * k0) with the quotient and product carried in
             // float-float: the double expression's rounding without FP64 division
             const float r = -2.0f * d;
@@ -2223,6 +2497,13 @@ __global__ void __launch_bounds__(128) k_finish(FlightArgs a)
 // ---------------------------------------------------------------------------
 // Unit-level kernels.
 // ---------------------------------------------------------------------------
+// cr_expf at n arguments (its check against the correctly rounded exponential)
+__global__ void k_debug_exp(const float *x, float *y, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = cr_expf(x[i]);
+}
+
 __global__ void k_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n,
                                  uint32_t imp, float *pos, float *weight)
 {
@@ -2722,6 +3003,12 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     if (ev) cudaEventRecord(ev[4], stream);
     k_finish<<<blocks, 128, 0, stream>>>(b);
     if (ev) cudaEventRecord(ev[5], stream);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_exp(const float *x, float *y, uint32_t n, cudaStream_t s)
+{
+    if (n) k_debug_exp<<<(n + 255) / 256, 256, 0, s>>>(x, y, n);
     return cudaGetLastError();
 }
 

@@ -78,6 +78,7 @@ cudaError_t launch_nee(const FlightArgs &a, const float4 *point_t, const float4 
                        cudaStream_t stream);
 
 // Unit-level kernels (synchronous wrappers live in gpis_abi.cu).
+cudaError_t launch_debug_exp(const float *x, float *y, uint32_t n, cudaStream_t s);
 cudaError_t launch_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n,
                                   uint32_t impulses, float *pos, float *weight, cudaStream_t s);
 cudaError_t launch_debug_cells_3d(const int32_t *cells, const uint32_t *seeds, uint32_t n,

@@ -915,6 +915,14 @@ void gpis_flight_seeds(const gpis_medium_desc *d, const uint32_t pss[4], uint32_
     if (normal_seed) *normal_seed = h_xx4(pss[0], pss[1], pss[2], pss[3]) + h_xx1(scene_seed) + 1u;
 }
 
+int gpis_debug_exp(const float *x, float *y, uint32_t n)
+{
+    if (n && (!x || !y)) return fail(GPIS_EINVAL, "null argument");
+    CUDA_TRY(gpis::launch_debug_exp(x, y, n, 0), "launch");
+    CUDA_TRY(cudaDeviceSynchronize(), "synchronize");
+    return GPIS_OK;
+}
+
 int gpis_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n, uint32_t impulses,
                         float *pos, float *weight)
 {

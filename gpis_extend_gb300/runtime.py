@@ -231,6 +231,15 @@ class Context:
         return out.cpu().numpy()
 
 
+def debug_exp(x):
+    """gpis_debug_exp: the precise evaluator's exponential at the float32 arguments x."""
+    torch = _torch()
+    xs = torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
+    ys = torch.empty_like(xs)
+    abi.check(abi.load_library().gpis_debug_exp(xs.data_ptr(), ys.data_ptr(), xs.numel()), "gpis_debug_exp")
+    return ys.cpu().numpy()
+
+
 def debug_cells_1d(cells, seeds, impulses):
     torch = _torch()
     lib = abi.load_library()

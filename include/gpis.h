@@ -321,6 +321,11 @@ int gpis_debug_cells_1d(const uint32_t *cells, const uint32_t *seeds, uint32_t n
 int gpis_debug_cells_3d(const int32_t *cells, const uint32_t *seeds, uint32_t n,
                         uint32_t impulses, uint32_t xyz_order, float *pos, float *weight);
 
+/* The precise evaluator's exponential at n arguments (device pointers,
+ * blocking): e^x rounded to the nearest float (the oracle's definition of the
+ * reference's float exp).  Unit-level check; no counterpart in the reference. */
+int gpis_debug_exp(const float *x, float *y, uint32_t n);
+
 /* Field evaluation at n points (device pointers): points/dirs n x 4 floats,
  * seeds n x 4 words as in the flight seed stream, prev n x 4 floats.  The
  * conditioning of each point's flight is built from (origin = points of the

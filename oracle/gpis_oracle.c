@@ -7,7 +7,13 @@
  * Precision: "float mode" keeps every float/double choice of the reference
  * C++ (Vec3f vs Vec3d, double march parameter t, float field values).  The
  * reference was built with MSVC, whose <cmath> resolves exp/sqrt of a float
- * argument to the float overloads; this file uses expf/sqrtf there.  Build
+ * argument to the float overloads.  sqrtf is correctly rounded everywhere; the
+ * float exp is not specified by IEEE 754 and differs between C libraries in the
+ * last bit (glibc's expf differs from the correctly rounded value on about 1e-4
+ * of the splat arguments), so this file evaluates the reference's float exp as
+ * the correctly rounded float of e^x, rexpf(x) = (float)exp((double)x): a value
+ * that any implementation can reproduce, which the GPU's precise evaluator
+ * does.  Build
  * with -ffp-contract=off so that no multiply-add is fused (SSE2 x86-64 and the
  * reference CPU build have no FMA contraction).
  *
@@ -28,6 +34,9 @@ static volatile float mr_base_v = 2.5f;
 #define MR_LEVEL_MAX 16
 
 #include <math.h>
+
+/* the reference's float exp, correctly rounded (see the header) */
+static inline float rexpf(float x) { return (float)exp((double)x); }
 #include <pthread.h>
 #include <stdatomic.h>
 #include <stdlib.h>
@@ -544,7 +553,7 @@ static void noise1d_f(const om_t *m, float z, uint32_t seed, float ls, float out
             if (tp * tp < 1.0f) {
                 float ab = kr * tl - kr * ti;
                 float den = 2.0f * (ls * ls);   /* splattingKernel1DVal, GPFunctions.cpp:845-848 */
-                float f = expf(-(ab * ab / den));
+                float f = rexpf(-(ab * ab / den));
                 float gr = (float)(-2.0 * (double)ab / (double)den * (double)f);
                 cv += wi * f;
                 cg += wi * gr;
@@ -595,7 +604,7 @@ static void cov1d_f(float d, float a, float out[4])
        double overload (integer argument), the product is passed as float. */
     float s2 = (float)((double)a * sqrt(2));
     float den2 = (float)(2.0 * (double)(s2 * s2));
-    float f = expf(-(d * d / den2));
+    float f = rexpf(-(d * d / den2));
     float g1 = (float)(-2.0 * (double)d / (double)den2 * (double)f);
     float den4 = (float)(4.0 * (double)(a * a));
     float gr = (float)(-2.0 * (double)d / (double)den4);
@@ -789,7 +798,7 @@ static void noise3d(const real_t *r, const float p[3], int dbl, double out[4])
                             float absq = ab[0] * M[0] * ab[0];
                             absq += ab[1] * M[1] * ab[1];
                             absq += ab[2] * M[2] * ab[2];
-                            float f = expf(-absq);
+                            float f = rexpf(-absq);
                             cf[0] += wi * f;
                             for (int c = 0; c < 3; ++c) cf[1 + c] += wi * (-2.f * (ab[c] * M[c]) * f);
                         } else {
@@ -839,7 +848,7 @@ static void noise3d_norm(const real_t *r, const float p[3], int cond, int dbl, d
         float absq = ab[0] * M[0] * ab[0];
         absq += ab[1] * M[1] * ab[1];
         absq += ab[2] * M[2] * ab[2];
-        float f = expf(-absq);
+        float f = rexpf(-absq);
         float dp[3], g1[3];
         for (int i = 0; i < 3; ++i) {
             dp[i] = -2.f * (ab[i] * M[i]);

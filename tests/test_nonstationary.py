@@ -134,17 +134,24 @@ PRECISE_MEDIA = {
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", sorted(PRECISE_MEDIA))
 def test_gpu_precise_field_matches_oracle_float_mode(name):
-    """The march's precise evaluator against the oracle's float-mode field value on
-    unconditioned points: within 8 ulp of the field scale everywhere and bit-exact
-    on most points (CUDA's expf is within 2 ulp, the C library's within about half
-    an ulp, so the 24 splats of a sum can move its last bits)."""
+    """The march's precise evaluator against the oracle's float-mode field value,
+    on unconditioned points and on points of conditioned (secondary) flights,
+    their origins included, where the field is zero up to rounding.  Both sides
+    round the exponential correctly and repeat the reference's float operations,
+    so the values are bit-exact but where a transcendental of the length-scale
+    field or the float-float mean rounds differently: within 8 ulp of the field
+    scale everywhere, bit-exact on >= 99.9 % of the points of stationary media
+    and >= 99 % of the others."""
     from gpis_extend_gb300 import runtime
     desc = PRECISE_MEDIA[name]()
     rng = np.random.default_rng(sum(map(ord, name)))
     n = 4000 if desc.one_d_sampling else 800
     o, d, seeds, prev = birth_points(n, rng)
-    seeds[:, 2] = abi.FLAG_FIRST_SCATTER
+    # the first half unconditioned; the second half conditioned, a quarter of it at
+    # the origin itself
+    seeds[: n // 2, 2] = abi.FLAG_FIRST_SCATTER
     t = rng.uniform(0.0, 0.5, n)
+    t[n // 2: n // 2 + n // 8] = 0.0
     p = (o.astype(np.float64) + d * t[:, None]).astype(np.float32)
     with runtime.Context(desc) as ctx:
         out = ctx.debug_field(o, p, d, seeds, prev)
@@ -152,9 +159,11 @@ def test_gpu_precise_field_matches_oracle_float_mode(name):
     exact = out[:, 6] == ref
     ulp = np.spacing(np.maximum(np.abs(ref), np.float32(desc.sigma)))
     err = np.abs(out[:, 6].astype(np.float64) - ref) / ulp
-    print(name, "bit-exact fraction", exact.mean(), "max ulp", err.max())
+    print(name, "bit-exact fraction", exact.mean(), "(unconditioned", exact[: n // 2].mean(), ", conditioned",
+          exact[n // 2:].mean(), ") max ulp", err.max())
     assert np.all(err <= 8), (name, err.max(), np.argmax(err))
-    assert exact.mean() >= 0.75, (name, exact.mean())
+    stationary = desc.ls_kind == abi.LS_CONSTANT
+    assert exact.mean() >= (0.999 if stationary else 0.99), (name, exact.mean())
     ids = out[:, 7].view(np.int32)
     ref_id = np.array([oracle.field(desc, o[i], d[i], p[i], seeds[i], prev[i])[5] for i in range(n)])
     if desc.mean_kind == abi.MEAN_TORUS_PLANE:
