@@ -23,6 +23,7 @@ enum : uint32_t {
     MF_TRANSVERSE = 1u << 4,     // exact SE transverse law applies
     MF_XYZ_ORDER = 1u << 5,      // next3D drawn x first
     MF_MULTIRES = 1u << 6,       // 2-level multi-resolution blend of the length scale
+    MF_ISO3D = 1u << 7,          // 3D noise in isotropic ray space (isotropic_3D_sampling)
 };
 
 // Levels of the multi-resolution grid: scales 2.5^L for L in [-kMrLevels, kMrLevels).
@@ -94,7 +95,18 @@ struct DevMedium {
     float mr_log_base;
     float mr_pow[2 * kMrLevels];
     int32_t mr_seed[2 * kMrLevels];
+    // 3D brute-force nonstationary noise in world space: the noise-seed offset
+    // floor(log(ls_max) / log(2.5f)) of its kernelSpatialScale ls_max
+    int32_t ns3_seed;
+    float imp_density;      // impulseDensity as given (the 3D normalisation's numerator)
 };
+
+// A 3D medium outside the stationary world-space form: isotropic ray space,
+// a nonstationary length scale or the multi-resolution grid.
+__host__ __device__ inline bool general_3d(const DevMedium &m)
+{
+    return !(m.flags & MF_ONE_D) && ((m.flags & (MF_ISO3D | MF_MULTIRES)) || m.ls_kind != 0u);
+}
 
 struct PcgJump {
     uint32_t alo, ahi;      // multiplier M^k

@@ -599,6 +599,9 @@ __device__ void noise_gradient_mr(const DevMedium &m, const FlightIn &fl, const 
 // evaluateNoise3D gradient).  cond: the octave's conditioning splats are active.
 __device__ void noise1d_precise_vd(const DevMedium &m, float z, uint32_t seed, float ls, float &value, float &deriv);
 __device__ float mean_plus_precise(const DevMedium &m, float an, float x, float y, float z, int &id);
+template <bool GRAD, bool PRECISE>
+__device__ int noise3d_gen(const DevMedium &m, const float p[3], const float d[3], const CondRec *c, const float o[3],
+                           uint32_t seed, float &v, float g[3]);
 __device__ void noise3d_precise_grad(const DevMedium &m, float px, float py, float pz, uint32_t seed, float &value,
                                      float g[3]);
 
@@ -609,6 +612,12 @@ __device__ __forceinline__ void noise_gradient_oct(const DevMedium &m, const Fli
                                    const float p[3], float t_segment, int oc, float &value, float g[3],
                                    bool precise = false)
 {
+    if (general_3d(m)) {
+        // isotropic, nonstationary or multi-resolution 3D noise: the precise
+        // evaluation (the conditioning and the end-point gradient take it)
+        noise3d_gen<true, true>(m, p, fl.d, cond ? &c : nullptr, fl.o, fl.noise_seed, value, g);
+        return;
+    }
     if (!(m.flags & MF_ONE_D)) {
         if (precise) {
             noise3d_precise_grad(m, p[0], p[1], p[2], fl.noise_seed, value, g);
@@ -739,6 +748,65 @@ __device__ __forceinline__ void write_status(const FlightArgs &a, uint32_t i, fl
     a.out[2 * i + 1] = make_float4(0.0f, trans, __uint_as_float(steps), __uint_as_float(status));
 }
 
+// conditioning3D (SparseConvolutionNoise.cpp:498-574) for isotropic, nonstationary
+// or multi-resolution 3D media; co.vs holds (target - mean) / amplitude - noise.
+// The multi-resolution value scale is divided by w_low + w_high.  Renewal+: the
+// world residual of the gradient; in isotropic ray space it is taken to the
+// isotropic frame and times -2 (the inverse of -2 * 0.25 I), then divided by
+// w_low / s_low + w_high / s_high or times sqr(ls(o) / ls_max); in world space it is
+// divided by -2 * (l_inv^2 * 0.25) (the diagonal inverse written as the division),
+// then divided by w_low / s_low^2 + w_high / s_high^2 or times sqr(ls(o)).
+__device__ __forceinline__ void condition_3d_general(const DevMedium &m, const FlightIn &fl, const float g[3],
+                                                     const float tg[3], const float mg[3], float amp, CondOct &co)
+{
+    const bool mr = (m.flags & MF_MULTIRES) != 0;
+    MrLevels lv = {};
+    if (mr) {
+        lv = mr_levels(m, ls_value_precise(m, fl.o[0], fl.o[2]));
+        co.vs = __fdiv_rn(co.vs, __fadd_rn(lv.w[0], lv.w[1]));
+    }
+    if (!(m.flags & MF_RENEWAL_PLUS)) return;
+    float delta[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) delta[i] = __fsub_rn(__fdiv_rn(__fsub_rn(tg[i], mg[i]), amp), g[i]);
+    if (m.flags & MF_ISO3D) {
+        Frame f;
+        ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
+        const float sw = m.ls_kind ? m.ls_max : 1.0f;
+        float gi[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) gi[i] = __fmul_rn(__fmul_rn(m.l_aniso[i], delta[i]), sw);
+        co.gs[0] = __fmul_rn(-2.0f, dot3_rn(f.t[0], f.t[1], f.t[2], gi[0], gi[1], gi[2]));
+        co.gs[1] = __fmul_rn(-2.0f, dot3_rn(f.b[0], f.b[1], f.b[2], gi[0], gi[1], gi[2]));
+        co.gs[2] = __fmul_rn(-2.0f, dot3_rn(f.n[0], f.n[1], f.n[2], gi[0], gi[1], gi[2]));
+        if (mr) {
+            const float dv = __fadd_rn(__fdiv_rn(lv.w[0], lv.s[0]), __fdiv_rn(lv.w[1], lv.s[1]));
+#pragma unroll
+            for (int i = 0; i < 3; ++i) co.gs[i] = __fdiv_rn(co.gs[i], dv);
+        } else {
+            const float a = ns_scale_precise(m, fl.o[0], fl.o[2]);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) co.gs[i] = __fmul_rn(co.gs[i], __fmul_rn(a, a));
+        }
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float inv2 = __fmul_rn(m.l_inv[i], m.l_inv[i]);
+        co.gs[i] = __fdiv_rn(delta[i], __fmul_rn(-2.0f, __fmul_rn(inv2, 0.25f)));
+    }
+    if (mr) {
+        const float dv = __fadd_rn(__fdiv_rn(lv.w[0], __fmul_rn(lv.s[0], lv.s[0])),
+                                   __fdiv_rn(lv.w[1], __fmul_rn(lv.s[1], lv.s[1])));
+#pragma unroll
+        for (int i = 0; i < 3; ++i) co.gs[i] = __fdiv_rn(co.gs[i], dv);
+    } else {
+        const float ls = m.ls_kind ? ls_value_precise(m, fl.o[0], fl.o[2]) : 1.0f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) co.gs[i] = __fmul_rn(co.gs[i], __fmul_rn(ls, ls));
+    }
+}
+
 // One octave's coefficients from its target value and gradient at the origin
 // (conditioning1D / conditioning3D, SparseConvolutionNoise.cpp:498-656).
 __device__ __forceinline__ void condition_octave(const DevMedium &m, const FlightIn &fl, int k, float v,
@@ -749,6 +817,10 @@ __device__ __forceinline__ void condition_octave(const DevMedium &m, const Fligh
     if (amp == 0.0f) return;
     CondOct &co = c.oct[k];
     co.vs = (tv - mean) / amp - v;
+    if (general_3d(m)) {
+        condition_3d_general(m, fl, g, tg, mg, amp, co);
+        return;
+    }
     // the multi-resolution splats carry both levels' weights (conditioning1D, :602-633)
     const float mrn = (m.flags & MF_MULTIRES) ? mr_norm(mr_levels(m, ls_value_precise(m, fl.o[0], fl.o[2]))) : 1.0f;
     if (m.flags & MF_MULTIRES) co.vs = __fdiv_rn(co.vs, mrn);
@@ -976,6 +1048,7 @@ struct LaneField {
     bool ns;                // nonstationary length scale
     float ls_o;             // kernel scale at the origin (conditioning)
     float mr_ow[2];         // multi-resolution: the origin's weights of the low and high level
+    float d[3];             // the flight's direction (isotropic-space 3D noise)
 };
 
 // Safe contents for a lane without a flight (collective evaluators run every lane).
@@ -997,6 +1070,7 @@ __device__ __forceinline__ void lane_field_idle(LaneField &L, const DevMedium *m
     L.ns = false;
     L.ls_o = 1.0f;
     L.mr_ow[0] = L.mr_ow[1] = 1.0f;
+    L.d[0] = 0.0f; L.d[1] = 0.0f; L.d[2] = 1.0f;
 }
 
 // A lane's registers for flight fl of medium m; cond points at its conditioning record.
@@ -1015,6 +1089,8 @@ __device__ __forceinline__ void lane_field_setup(LaneField &L, const DevMedium &
     L.ns = m.ls_kind != 0u;
     L.ls_o = 1.0f;
     L.mr_ow[0] = L.mr_ow[1] = 1.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) L.d[k] = fl.d[k];
     if (GENERAL && (m.flags & MF_MULTIRES) && L.cond) {
         const MrLevels lo = mr_levels(m, ls_value_precise(m, fl.o[0], fl.o[2]));
         L.mr_ow[0] = lo.w[0];
@@ -1250,6 +1326,280 @@ __device__ void noise3d_precise_grad(const DevMedium &m, float px, float py, flo
     g[2] = __fdiv_rn(s2, m.norm3d);
 }
 
+// ---- 3D noise outside the stationary world form --------------------------------
+// Isotropic ray space (isotropic_3D_sampling: evaluateNoise3DIsotropicRayNormalized,
+// SparseConvolutionNoise.cpp:348-377), the brute-force nonstationary length scale
+// and the multi-resolution grid (evaluateNoise3D, :142-165), world or isotropic.
+// One evaluation runs per level: the point in the level's space, the lattice of
+// 27 cells with the level's kernel radius and inverse covariance, the
+// normalisation, the gradient back to world space and the conditioning splats.
+// PRECISE repeats the reference's float operations (cr_expf, unfused); the march's
+// decisions near zero, the conditioning and the end-point gradient take it.
+
+// One level: kernelRadius, kernelSpatialScale and its noise-seed offset.
+struct Lv3 {
+    float kr, ks;
+    uint32_t seed_add;
+};
+
+// The levels at p with their weights (one, or the two of the multi-resolution
+// grid around ls(p)).  kernelRadius: the isotropic localScale, or in world space
+// (kernelScale * localScale) * the largest anisotropic length, localScale being
+// the level's scale or, by brute force, the largest lateral scale
+// (GPFunctions.cpp:711-719, 1253-1258).
+__device__ __forceinline__ int levels3(const DevMedium &m, float px, float pz, bool precise, Lv3 lv[2], float w[2])
+{
+    const bool iso = (m.flags & MF_ISO3D) != 0;
+    const float mtx = fmaxf(fmaxf(m.l_aniso[0], m.l_aniso[1]), m.l_aniso[2]);
+    if (m.flags & MF_MULTIRES) {
+        const MrLevels L = mr_levels(m, precise ? ls_value_precise(m, px, pz) : ls_value(m, px, pz));
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            lv[j].ks = L.s[j];
+            lv[j].seed_add = L.seed[j];
+            lv[j].kr = iso ? m.kr_iso : __fmul_rn(__fmul_rn(m.kr_iso, L.s[j]), mtx);
+            w[j] = L.w[j];
+        }
+        return 2;
+    }
+    const bool ns = m.ls_kind != 0u;
+    lv[0].kr = iso ? m.kr_iso : __fmul_rn(__fmul_rn(m.kr_iso, ns ? m.ls_max : 1.0f), mtx);
+    lv[0].ks = (!iso && ns) ? m.ls_max : 1.0f;
+    lv[0].seed_add = (!iso && ns) ? (uint32_t)m.ns3_seed : 0u;
+    w[0] = 1.0f;
+    w[1] = 0.0f;
+    return 1;
+}
+
+// getInvCovMtx's diagonal (GPFunctions.cpp:784-812): world space (the inverse
+// squared length scales over sqr(globalScale)) or isotropic space (identity), times
+// 0.5 for a covariance splat, over sqr(localScale), times 0.5.
+__device__ __forceinline__ void inv_cov3(const DevMedium &m, bool iso, bool is_cov, float a, float gs, float M[3])
+{
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float v = iso ? 1.0f : __fmul_rn(m.l_inv[i], m.l_inv[i]);
+        if (!iso && gs != 1.0f) v = __fdiv_rn(v, __fmul_rn(gs, gs));
+        if (is_cov) v = __fmul_rn(v, 0.5f);
+        v = __fdiv_rn(v, __fmul_rn(a, a));
+        M[i] = __fmul_rn(v, 0.5f);
+    }
+}
+
+// noise3D + cell3D (SparseConvolutionNoise.cpp:419-452) at the point q of a level's
+// space: the raw sum and its gradient (q units).
+template <bool GRAD, bool PRECISE>
+__device__ void lattice3(const DevMedium &m, const float q[3], float kr, const float M[3], uint32_t seed, float &v,
+                         float g[3])
+{
+    float fr[3];
+    int ijk[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float t = __fdiv_rn(q[i], kr);
+        const float fl = floorf(t);
+        fr[i] = __fsub_rn(t, fl);
+        ijk[i] = (int)fl;
+    }
+    const bool xfirst = (m.flags & MF_XYZ_ORDER) != 0;
+    float sv = 0.0f, s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz) {
+                const float t0 = __fsub_rn(fr[0], (float)dx), t1 = __fsub_rn(fr[1], (float)dy),
+                            t2 = __fsub_rn(fr[2], (float)dz);
+                const uint32_t s = xxhash4((uint32_t)(ijk[2] + dz), (uint32_t)(ijk[1] + dy),
+                                           (uint32_t)(ijk[0] + dx), seed) + 1u;
+                float cv = 0.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
+                for (uint32_t k = 0; k < m.n_imp; ++k) {
+                    const int b = 2 + 4 * (int)k;
+                    const float r0 = unit_float(pcg_draw(c_jump[b], s));
+                    const float r1 = unit_float(pcg_draw(c_jump[b + 1], s));
+                    const float r2 = unit_float(pcg_draw(c_jump[b + 2], s));
+                    const uint32_t wr = pcg_draw(c_jump[b + 3], s);
+                    const float ix = xfirst ? r0 : r2, iy = r1, iz = xfirst ? r2 : r0;
+                    const float a0 = __fsub_rn(t0, ix), a1 = __fsub_rn(t1, iy), a2 = __fsub_rn(t2, iz);
+                    const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(a0, a0), __fmul_rn(a1, a1)), __fmul_rn(a2, a2));
+                    if (l2 < 1.0f) {
+                        const bool pos = (wr >> 31) != 0;
+                        if (PRECISE) {
+                            const float b0 = __fsub_rn(__fmul_rn(kr, t0), __fmul_rn(kr, ix));
+                            const float b1 = __fsub_rn(__fmul_rn(kr, t1), __fmul_rn(kr, iy));
+                            const float b2 = __fsub_rn(__fmul_rn(kr, t2), __fmul_rn(kr, iz));
+                            float qq = __fmul_rn(__fmul_rn(b0, M[0]), b0);
+                            qq = __fadd_rn(qq, __fmul_rn(__fmul_rn(b1, M[1]), b1));
+                            qq = __fadd_rn(qq, __fmul_rn(__fmul_rn(b2, M[2]), b2));
+                            const float e = cr_expf(-qq);
+                            cv = __fadd_rn(cv, pos ? e : -e);
+                            if (GRAD) {
+                                const float g0 = __fmul_rn(__fmul_rn(-2.0f, __fmul_rn(b0, M[0])), e);
+                                const float g1 = __fmul_rn(__fmul_rn(-2.0f, __fmul_rn(b1, M[1])), e);
+                                const float g2 = __fmul_rn(__fmul_rn(-2.0f, __fmul_rn(b2, M[2])), e);
+                                c0 = __fadd_rn(c0, pos ? g0 : -g0);
+                                c1 = __fadd_rn(c1, pos ? g1 : -g1);
+                                c2 = __fadd_rn(c2, pos ? g2 : -g2);
+                            }
+                        } else {
+                            const float b0 = kr * a0, b1 = kr * a1, b2 = kr * a2;
+                            const float e = ex2_approx(-LOG2E * (M[0] * b0 * b0 + M[1] * b1 * b1 + M[2] * b2 * b2));
+                            const float w = pos ? 1.0f : -1.0f;
+                            cv += w * e;
+                            if (GRAD) {
+                                c0 += w * (-2.0f * (b0 * M[0]) * e);
+                                c1 += w * (-2.0f * (b1 * M[1]) * e);
+                                c2 += w * (-2.0f * (b2 * M[2]) * e);
+                            }
+                        }
+                    }
+                }
+                if (PRECISE) {
+                    sv = __fadd_rn(sv, cv);
+                    if (GRAD) { s0 = __fadd_rn(s0, c0); s1 = __fadd_rn(s1, c1); s2 = __fadd_rn(s2, c2); }
+                } else {
+                    sv += cv;
+                    if (GRAD) { s0 += c0; s1 += c1; s2 += c2; }
+                }
+            }
+    v = sv;
+    if (GRAD) { g[0] = s0; g[1] = s1; g[2] = s2; }
+}
+
+// sqrt(sparseConvNoiseVariance3D) as the reference rounds it (GPFunctions.cpp:751-764,
+// 1260-1263): impulseDensity / kr^3 in float, the determinant and the scales' cubes
+// in double, pi^1.5 = pow(M_PI, 1.5).
+__device__ __forceinline__ float norm3(const DevMedium &m, bool iso, float kr, float gs, float a)
+{
+    const float ud = __fdiv_rn(m.imp_density, __fmul_rn(__fmul_rn(kr, kr), kr));
+    double det = 1.0;
+    if (!iso) {
+        const float detf = __fmul_rn(__fmul_rn(m.l_aniso[0], m.l_aniso[1]), m.l_aniso[2]);
+        det = __dmul_rn((double)detf, __dmul_rn(__dmul_rn((double)gs, (double)gs), (double)gs));
+    }
+    det = __dmul_rn(det, __dmul_rn(__dmul_rn((double)a, (double)a), (double)a));
+    const double pi15 = 0x1.645f7c63f2c6bp+2;
+    return __fsqrt_rn((float)__dmul_rn((double)ud, __dmul_rn(pi15, det)));
+}
+
+// One level: the normalized noise value (and world gradient) at p with the
+// conditioning splats of c (null: none) about the flight's origin o.
+template <bool GRAD, bool PRECISE>
+__device__ void noise3d_level_gen(const DevMedium &m, const float p[3], const float d[3], const CondRec *c,
+                                  const float o[3], const Lv3 &lv, uint32_t seed, float &v, float g[3])
+{
+    const bool iso = (m.flags & MF_ISO3D) != 0;
+    const float a = m.ls_kind ? (PRECISE ? ns_scale_precise(m, p[0], p[2]) : ns_scale(m, p[0], p[2])) : 1.0f;
+    const float gs = iso ? 1.0f : lv.ks;
+    // transformPosDirWorldtoLocal / transformGradLocaltoWorld scale: the largest
+    // lateral scale by brute force, else the level's scale
+    const float S = m.ls_kind ? m.ls_max : lv.ks;
+    float q[3];
+    Frame f;
+    if (iso) {
+        ray_frame(m, d[0], d[1], d[2], f);
+        float pi[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) pi[i] = __fdiv_rn(__fmul_rn(m.l_inv[i], p[i]), S);
+        q[0] = dot3_rn(f.t[0], f.t[1], f.t[2], pi[0], pi[1], pi[2]);
+        q[1] = dot3_rn(f.b[0], f.b[1], f.b[2], pi[0], pi[1], pi[2]);
+        q[2] = dot3_rn(f.n[0], f.n[1], f.n[2], pi[0], pi[1], pi[2]);
+    } else {
+        q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+    }
+    float M[3];
+    inv_cov3(m, iso, false, a, gs, M);
+    float sv, sg[3];
+    lattice3<GRAD, PRECISE>(m, q, lv.kr, M, seed + lv.seed_add, sv, sg);
+    const float nf = norm3(m, iso, lv.kr, gs, a);
+    v = __fdiv_rn(sv, nf);
+    // a vector of the level's space to world space (TangentFrame::toGlobal, then
+    // transformGradLocaltoWorld)
+    auto to_world = [&](const float x[3], float y[3]) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float gi = __fadd_rn(__fadd_rn(__fmul_rn(f.t[i], x[0]), __fmul_rn(f.b[i], x[1])),
+                                       __fmul_rn(f.n[i], x[2]));
+            y[i] = __fdiv_rn(__fmul_rn(m.l_inv[i], gi), S);
+        }
+    };
+    if (GRAD) {
+        float gw[3] = {sg[0], sg[1], sg[2]};
+        if (iso) to_world(sg, gw);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) g[i] = __fdiv_rn(gw[i], nf);
+    }
+    if (!c) return;
+    float Mc[3];
+    inv_cov3(m, iso, true, a, gs, Mc);
+    float ab[3];
+    if (iso) {
+        float oi[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) oi[i] = __fdiv_rn(__fmul_rn(m.l_inv[i], o[i]), S);
+        ab[0] = __fsub_rn(q[0], dot3_rn(f.t[0], f.t[1], f.t[2], oi[0], oi[1], oi[2]));
+        ab[1] = __fsub_rn(q[1], dot3_rn(f.b[0], f.b[1], f.b[2], oi[0], oi[1], oi[2]));
+        ab[2] = __fsub_rn(q[2], dot3_rn(f.n[0], f.n[1], f.n[2], oi[0], oi[1], oi[2]));
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) ab[i] = __fsub_rn(p[i], o[i]);
+    }
+    float absq = __fmul_rn(__fmul_rn(ab[0], Mc[0]), ab[0]);
+    absq = __fadd_rn(absq, __fmul_rn(__fmul_rn(ab[1], Mc[1]), ab[1]));
+    absq = __fadd_rn(absq, __fmul_rn(__fmul_rn(ab[2], Mc[2]), ab[2]));
+    const float fk = PRECISE ? cr_expf(-absq) : ex2_approx(-LOG2E * absq);
+    const CondOct &co = c->oct[0];
+    float dp[3], g1[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        dp[i] = __fmul_rn(-2.0f, __fmul_rn(ab[i], Mc[i]));
+        g1[i] = __fmul_rn(dp[i], fk);
+    }
+    float gv = 0.0f;
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) gv = __fadd_rn(gv, __fmul_rn(g1[cc], co.gs[cc]));
+    v = __fadd_rn(v, __fadd_rn(__fmul_rn(fk, co.vs), gv));
+    if (GRAD) {
+        float dg[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float gg = 0.0f;
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                const float h = __fsub_rn(__fmul_rn(dp[cc], dp[j]), cc == j ? __fmul_rn(2.0f, Mc[cc]) : 0.0f);
+                gg = __fadd_rn(gg, __fmul_rn(__fmul_rn(h, fk), co.gs[cc]));
+            }
+            dg[j] = __fadd_rn(__fmul_rn(g1[j], co.vs), gg);
+        }
+        float dw[3] = {dg[0], dg[1], dg[2]};
+        if (iso) to_world(dg, dw);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) g[j] = __fadd_rn(g[j], dw[j]);
+    }
+}
+
+// The normalized 3D noise (and world gradient) at p: one level or the blend of two.
+// Returns the cells regenerated.
+template <bool GRAD, bool PRECISE>
+__device__ int noise3d_gen(const DevMedium &m, const float p[3], const float d[3], const CondRec *c, const float o[3],
+                           uint32_t seed, float &v, float g[3])
+{
+    Lv3 lv[2];
+    float w[2];
+    const int n = levels3(m, p[0], p[2], PRECISE, lv, w);
+    if (n == 1) {
+        noise3d_level_gen<GRAD, PRECISE>(m, p, d, c, o, lv[0], seed, v, g);
+        return 27;
+    }
+    float v0, v1, g0[3] = {0.0f, 0.0f, 0.0f}, g1[3] = {0.0f, 0.0f, 0.0f};
+    noise3d_level_gen<GRAD, PRECISE>(m, p, d, c, o, lv[0], seed, v0, g0);
+    noise3d_level_gen<GRAD, PRECISE>(m, p, d, c, o, lv[1], seed, v1, g1);
+    v = __fadd_rn(__fmul_rn(w[0], v0), __fmul_rn(w[1], v1));
+    if (GRAD) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) g[i] = __fadd_rn(__fmul_rn(w[0], g0[i]), __fmul_rn(w[1], g1[i]));
+    }
+    return 54;
+}
+
 __device__ float noise3d_precise(const DevMedium &m, float px, float py, float pz, uint32_t seed)
 {
     const float kr = m.kr_world;
@@ -1371,6 +1721,12 @@ __device__ __forceinline__ float cond3d_value_precise(const DevMedium &m, const 
 __device__ float field_precise(const LaneField &L, float px, float py, float pz, int &id)
 {
     const DevMedium &m = *L.m;
+    if (general_3d(m)) {
+        const float p[3] = {px, py, pz};
+        float v, g[3];
+        noise3d_gen<false, true>(m, p, L.d, L.cond ? &L.c3 : nullptr, L.o, L.seed, v, g);
+        return mean_plus_precise(m, __fmul_rn(L.sigma, v), px, py, pz, id);
+    }
     if (!(m.flags & MF_ONE_D)) {
         float noise = noise3d_precise(m, px, py, pz, L.seed);
         if (L.cond) {
@@ -1456,7 +1812,7 @@ struct EvalGeneric {
     {
         const DevMedium &m = *L.m;
         float noise;
-        if (m.flags & MF_MULTIRES) {
+        if ((m.flags & MF_MULTIRES) && (m.flags & MF_ONE_D)) {
             const MrLevels lv = mr_levels(m, ls_value(m, px, pz));
             noise = 0.0f;
 #pragma unroll 1
@@ -1496,6 +1852,11 @@ struct EvalGeneric {
             return noise + lane_mean(L, px, py, pz, id);
         }
         float v, g[3];
+        if (general_3d(m)) {
+            const float p[3] = {px, py, pz};
+            refills += noise3d_gen<false, false>(m, p, L.d, L.cond ? &L.c3 : nullptr, L.o, L.seed, v, g);
+            return L.sigma * v + lane_mean(L, px, py, pz, id);
+        }
         noise3d_generic<false>(m, px, py, pz, L.seed, v, g);
         noise = v * m.inv_norm3d;
         if (L.cond) {
@@ -2218,7 +2579,11 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
 #pragma unroll
         for (int k = 0; k < 3; ++k) p[k] = ff_point(L.o[k], d[k], eh, el);
         int id;
-        const bool precise = RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE);
+        // the value at farT of isotropic, nonstationary or multi-resolution 3D media
+        // is the precise one too (their fast evaluator's normalisation and level
+        // weights round differently)
+        const bool precise = (RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE)) ||
+                             (!Eval::kCollective && phase == PH_FAR && general_3d(*L.m));
         if constexpr (IsSkip3D<Eval>::value) {
             // a marching step of a 3D medium asks for the field's range over the next
             // steps: about half of |f| at the last step, and at least two steps
@@ -2230,7 +2595,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
         bool use3 = false;
         if constexpr (RESUME) {
             const DevMedium &m3 = *L.m;
-            use3 = !precise && phase == PH_MARCH && !(m3.flags & MF_ONE_D) && m3.n_oct == 1 && m3.ls_kind == 0u;
+            use3 = !precise && phase == PH_MARCH && !(m3.flags & MF_ONE_D) && m3.n_oct == 1 && !general_3d(m3);
             if (use3) {
                 const float len = fminf(0.5f * fabsf(pf), (float)kMaxSkip3D * step);
                 ev3.plan(len >= 2.0f * step ? len : 0.0f);
@@ -2558,7 +2923,7 @@ __global__ void k_debug_field(const DevMedium *mp, const float4 *origins, const 
     float v = 0.0f, g[3] = {0.0f, 0.0f, 0.0f}, fv_noise;
     // value and derivative parts of the noise (the 1D xy entries are the
     // conditioning splats); several octaves report amplitude-weighted sums
-    if (m.flags & MF_MULTIRES) {
+    if ((m.flags & MF_MULTIRES) && (m.flags & MF_ONE_D)) {
         Frame f;
         ray_frame(m, fl.d[0], fl.d[1], fl.d[2], f);
         const MrLevels lv = mr_levels(m, ls_value_precise(m, p[0], p[2]));
@@ -2987,7 +3352,7 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     } else if (coop) {
         const void *fn = (const void *)k_march<EvalCoop1D<8>, false>;
         k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(b);
-    } else if (a.three_d && a.max_oct == 1 && !a.any_ns) {
+    } else if (a.three_d && a.max_oct == 1 && !a.any_ns && !a.any_gen3d) {
         // 3D stationary single-octave media: the generic evaluator with step skipping
         const void *fn = (const void *)k_march<EvalSkip3D, false>;
         k_march<EvalSkip3D, false><<<grid(fn), 256, 0, stream>>>(b);

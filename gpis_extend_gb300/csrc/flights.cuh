@@ -53,6 +53,8 @@ struct FlightArgs {
     int all_grid;               // all media have a grid mean
     int any_ns;                 // some medium has a nonstationary length scale
     int any_mr;                 // some medium blends multi-resolution levels
+    int any_gen3d;              // some 3D medium is isotropic, nonstationary or multi-resolution
+                                // (the general 3D evaluator, no 3D step skipping)
     uint32_t ctas_per_sm;       // fast-pass persistent grid: CTAs per SM (0: every resident CTA)
     const uint32_t *n_dev;      // may be null: the live flight count in device memory (<= n,
                                 // which is then the capacity the grids are sized for)

@@ -64,8 +64,8 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         if (!std::isfinite(d.mean_params[i])) return fail(GPIS_EINVAL, "mean parameters must be finite");
     if (d.n_octaves < 1 || d.n_octaves > 4) return fail(GPIS_EINVAL, "n_octaves must be in 1..4");
     if (d.ls_kind > GPIS_LS_SINCOS) return fail(GPIS_EINVAL, "unknown ls_kind");
-    if ((d.ls_kind != GPIS_LS_CONSTANT || d.n_octaves != 1) && !d.one_d_sampling)
-        return fail(GPIS_ENOTSUP, "nonstationary and multi-octave fields need 1D_sampling");
+    if (d.n_octaves != 1 && !d.one_d_sampling)
+        return fail(GPIS_ENOTSUP, "multi-octave fields need 1D_sampling");
     if (d.ls_kind != GPIS_LS_CONSTANT) {
         if (!(std::isfinite(d.ls_max) && d.ls_max > 0.0f)) return fail(GPIS_EINVAL, "ls_max must be finite and > 0");
         for (int i = 0; i < 4; ++i)
@@ -86,8 +86,6 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         for (uint32_t k = 0; k < d.n_octaves; ++k)
             if (!std::isfinite(d.octave_sigma[k]) || !(std::isfinite(d.octave_scale[k]) && d.octave_scale[k] > 0.0f))
                 return fail(GPIS_EINVAL, "octave sigma must be finite and octave scale finite and > 0");
-    if (d.isotropic_3d_sampling && !d.one_d_sampling)
-        return fail(GPIS_ENOTSUP, "isotropic_3D_sampling is not supported");
     if (d.mean_kind > GPIS_MEAN_TORUS_PLANE) return fail(GPIS_EINVAL, "unknown mean kind");
     if (d.mean_kind == GPIS_MEAN_GRID) {
         const gpis_mean_grid *g = d.grid;
@@ -144,6 +142,7 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         flags |= gpis::MF_TRANSVERSE;
     if (d.impulse_xyz_order) flags |= gpis::MF_XYZ_ORDER;
     if (multires) flags |= gpis::MF_MULTIRES;
+    if (d.isotropic_3d_sampling && !d.one_d_sampling) flags |= gpis::MF_ISO3D;
     m.flags = flags;
     m.mean_kind = d.mean_kind;
     std::memcpy(m.mean_params, d.mean_params, sizeof(m.mean_params));
@@ -170,6 +169,10 @@ int derive_medium(const gpis_medium_desc &d, gpis::DevMedium &m)
         m.mr_pow[l + gpis::kMrLevels] = sc;
         m.mr_seed[l + gpis::kMrLevels] = (int32_t)std::floor(std::log(sc) / m.mr_log_base);
     }
+    m.imp_density = d.impulse_density;
+    m.ns3_seed = 0;
+    if (d.ls_kind != GPIS_LS_CONSTANT && !multires)
+        m.ns3_seed = (int32_t)std::floor(std::log((float)m.ls_max) / m.mr_log_base);
     m.n_oct = d.n_octaves;
     for (int k = 0; k < 4; ++k) {
         const bool on = (uint32_t)k < d.n_octaves && d.n_octaves > 1;
@@ -249,7 +252,8 @@ struct gpis_ctx {
     int n_media = 0;
     gpis::DevMedium *d_media = nullptr;
     std::vector<float *> d_grids;
-    bool any_cond = false, all_one_d = true, all_three_d = true, all_grid = true, any_ns = false, any_mr = false;
+    bool any_cond = false, all_one_d = true, all_three_d = true, all_grid = true, any_ns = false, any_mr = false,
+         any_gen3d = false;
     uint32_t max_imp = 0, max_oct = 1;
     // scratch of the flight kernels
     gpis::CondRec *d_cond = nullptr;
@@ -446,6 +450,7 @@ int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
             c->all_grid = c->all_grid && m.mean_kind == GPIS_MEAN_GRID;
             c->any_ns = c->any_ns || m.ls_kind != 0u;
             c->any_mr = c->any_mr || (m.flags & gpis::MF_MULTIRES) != 0u;
+            c->any_gen3d = c->any_gen3d || gpis::general_3d(m);
         }
         if (rc) break;
         if ((e = cudaMalloc(&c->d_media, host.size() * sizeof(gpis::DevMedium))) != cudaSuccess) { rc = cuda_fail(e, "allocate media"); break; }
@@ -511,6 +516,7 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.all_grid = ctx->all_grid;
     a.any_ns = ctx->any_ns;
     a.any_mr = ctx->any_mr;
+    a.any_gen3d = ctx->any_gen3d;
     for (const void *p : {(const void *)in->origin_near, (const void *)in->dir_far, (const void *)in->seeds,
                           (const void *)in->prev, (const void *)out->rec})
         if (p && (reinterpret_cast<uintptr_t>(p) & 15u))

@@ -141,6 +141,7 @@ extern "C" int gpis_flights_submit_static(const gpis_medium_desc *medium, const 
     a.all_grid = m.mean_kind == GPIS_MEAN_GRID;
     a.any_ns = m.ls_kind != 0u;
     a.any_mr = (m.flags & gpis::MF_MULTIRES) != 0u;
+    a.any_gen3d = gpis::general_3d(m);
     if (gpis::launch_flights(a, sms, s) != cudaSuccess) return fail(GPIS_EIO, "launching the flight kernels failed");
     return GPIS_OK;
 }

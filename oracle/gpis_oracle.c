@@ -223,6 +223,7 @@ typedef struct {
     float kr_world;          /* splattingKernelRadius(false, 1), GPFunctions.cpp:711-718 */
     float ls_max;            /* sparseConvNoiseMaxLateralScale */
     int multires;            /* 2-level multi-resolution blend (SparseConvolutionNoise.cpp:47-49) */
+    int iso3d;               /* 3D noise in isotropic ray space (isotropic_3D_sampling) */
     /* grid mean copy */
     const float *grid_vox;
 } om_t;
@@ -235,7 +236,8 @@ static int om_init(om_t *m, const gpis_medium_desc *d)
         return GPIS_EINVAL;
     if (d->n_octaves < 1 || d->n_octaves > 4) return GPIS_EINVAL;
     if (d->mean_kind == GPIS_MEAN_GRID && (!d->grid || !d->grid->voxels)) return GPIS_EINVAL;
-    if ((d->ls_kind != GPIS_LS_CONSTANT || d->n_octaves != 1) && !d->one_d_sampling) return GPIS_ENOTSUP;
+    /* octaves are this restatement's composition of 1D realizations */
+    if (d->n_octaves != 1 && !d->one_d_sampling) return GPIS_ENOTSUP;
     if (d->ls_kind != GPIS_LS_CONSTANT && !(d->ls_max > 0.0f)) return GPIS_EINVAL;
     /* _multiResolutionGrid = !isStationaryKernel() && useMultiResolutionGrid() */
     m->multires = d->multires && d->ls_kind != GPIS_LS_CONSTANT;
@@ -249,6 +251,7 @@ static int om_init(om_t *m, const gpis_medium_desc *d)
             return GPIS_ERANGE;
     }
     m->n_imp = (uint32_t)d->impulse_density;
+    m->iso3d = d->isotropic_3d_sampling && !d->one_d_sampling;
     m->activate_cond = !d->single_realization &&
         (d->correlation_context == GPIS_CTX_RENEWAL || d->correlation_context == GPIS_CTX_RENEWAL_PLUS);
     m->scheme = GPIS_SCHEME_UNI;
@@ -730,7 +733,7 @@ static void noise1d_norm(const real_t *r, const float p[3], const float dir[3], 
                      : (double)(info[2] * (float)lo[k] + info[3] * (float)hi[k]);
 }
 
-/* --- 3D noise (world space) -------------------------------------------- */
+/* --- 3D noise ---------------------------------------------------------- */
 
 static inline void draw3(pcg_t *g, uint32_t order, float p[3])
 {
@@ -745,12 +748,14 @@ static inline void draw3(pcg_t *g, uint32_t order, float p[3])
     }
 }
 
-/* getInvCovMtx diagonal (GPFunctions.cpp:784-812), isCov and local scale a. */
-static inline void inv_cov_diag(const om_t *m, int is_cov, float a, float sc, float M[3])
+/* getInvCovMtx diagonal (GPFunctions.cpp:784-812): world space (the inverse
+ * squared length scales over sqr(globalScale)) or isotropic space (identity),
+ * isCov, then over sqr(localScale) a, times 0.5. */
+static inline void inv_cov3(const om_t *m, int iso, int is_cov, float a, float gs, float M[3])
 {
     for (int i = 0; i < 3; ++i) {
-        float v = m->l_inv[i] * m->l_inv[i];
-        if (sc != 1.0f) v = v / (sc * sc);
+        float v = iso ? 1.0f : m->l_inv[i] * m->l_inv[i];
+        if (!iso && gs != 1.0f) v /= gs * gs;
         if (is_cov) v *= 0.5f;
         v /= a * a;
         v *= 0.5f;
@@ -758,20 +763,60 @@ static inline void inv_cov_diag(const om_t *m, int is_cov, float a, float sc, fl
     }
 }
 
-/* noise3D + cell3D (SparseConvolutionNoise.cpp:419-452), world space. */
-static void noise3d(const real_t *r, const float p[3], int dbl, double out[4])
+/* One level of evaluateNoise3D (SparseConvolutionNoise.cpp:142-165): the cell size
+ * kernelRadius, the kernelSpatialScale and its seed offset floor(log(s)/log(2.5)). */
+typedef struct { float kr, ks; uint32_t seed_add; } lv3_t;
+
+/* The levels of a 3D evaluation at p: one (stationary: world kernelRadius and
+ * worldSamplingSpatialScale 1; brute-force nonstationary: both at the largest
+ * lateral scale, GPFunctions.cpp:1241-1258; isotropic: kernelRadius = localScale
+ * and kernelSpatialScale 1) or the two of the multi-resolution grid around ls(p)
+ * with their weights (kernelScaleLevelRatio). */
+static int levels3(const om_t *m, const float p[3], lv3_t lv[2], float w[2])
 {
-    const om_t *m = r->m;
-    float sc = oct_scale(m, r->octave);
-    const float kr = m->kr_world * sc;
-    uint32_t seed = r->noise_seed + oct_seed(m, r->octave);
-    float ls = ns_scale(m, p);
-    float M[3];
-    inv_cov_diag(m, 0, ls, sc, M);
+    const float mtx = fmaxf(fmaxf(m->l_aniso[0], m->l_aniso[1]), m->l_aniso[2]);
+    if (m->multires) {
+        float info[4];
+        level_ratio(m, p, info);
+        for (int j = 0; j < 2; ++j) {
+            lv[j].ks = info[j];
+            lv[j].seed_add = level_seed(info[j]);
+            lv[j].kr = m->iso3d ? m->d.kernel_scale : m->d.kernel_scale * info[j] * mtx;
+        }
+        w[0] = info[2];
+        w[1] = info[3];
+        return 2;
+    }
+    lv[0].kr = m->iso3d ? m->kr_iso : m->kr_world;
+    lv[0].ks = m->iso3d ? 1.0f : m->ls_max;
+    lv[0].seed_add = level_seed(lv[0].ks);
+    w[0] = 1.0f;
+    w[1] = 0.0f;
+    return 1;
+}
+
+/* The isotropic ray-space frame of a direction and a point's coordinates in it
+ * (evaluateNoise3DIsotropicRayNormalized, SparseConvolutionNoise.cpp:348-360). */
+static void iso_ray_point(const om_t *m, const float p[3], const float dir[3], float ks, frame_t *f, float q[3])
+{
+    float diso[3], dn[3], piso[3];
+    w2l_pos(m, dir, 1.0f, diso);
+    normalize3f(diso, dn);
+    frame_make(dn, f);
+    w2l_pos(m, p, ks, piso);
+    frame_to_local(f, piso, q);
+}
+
+/* noise3D + cell3D (SparseConvolutionNoise.cpp:419-452) at the point q of the
+ * level's space: raw sum and gradient.  dbl: the same impulse set (float inside
+ * test), every value in FP64. */
+static void lattice3(const om_t *m, const float q[3], float kr, const float M[3], uint32_t seed, int dbl,
+                     double out[4])
+{
     float pg[3], fr[3];
     int ijk[3];
     for (int i = 0; i < 3; ++i) {
-        pg[i] = p[i] / kr;
+        pg[i] = q[i] / kr;
         float fl = floorf(pg[i]);
         fr[i] = pg[i] - fl;
         ijk[i] = (int)fl;
@@ -804,7 +849,7 @@ static void noise3d(const real_t *r, const float p[3], int dbl, double out[4])
                         } else {
                             double ab[3], absq = 0.0;
                             for (int c = 0; c < 3; ++c) {
-                                ab[c] = (double)kr * ((double)p[c] / (double)kr - (double)(ijk[c] + (c == 0 ? dx : c == 1 ? dy : dz)) - (double)pi[c]);
+                                ab[c] = (double)kr * ((double)q[c] / (double)kr - (double)(ijk[c] + (c == 0 ? dx : c == 1 ? dy : dz)) - (double)pi[c]);
                                 absq += ab[c] * (double)M[c] * ab[c];
                             }
                             double f = exp(-absq);
@@ -815,75 +860,152 @@ static void noise3d(const real_t *r, const float p[3], int dbl, double out[4])
                 }
                 for (int c = 0; c < 4; ++c) sf[c] += cf[c];
             }
-    /* sparseConvNoiseVariance3D (GPFunctions.cpp:751-764) */
-    float ud = m->d.impulse_density / (kr * kr * kr);
-    float detf = m->l_aniso[0] * m->l_aniso[1] * m->l_aniso[2];
-    double det = (double)detf * pow((double)sc, 3) * pow((double)ls, 3);
-    float var = (float)((double)ud * (pow(M_PI, 1.5) * det));
-    if (!dbl) {
-        float nf = sqrtf(var);
-        for (int c = 0; c < 4; ++c) out[c] = sf[c] / nf;
-    } else {
-        double vd = (double)m->d.impulse_density / ((double)kr * kr * kr) * pow(M_PI, 1.5) *
-                    (double)m->l_aniso[0] * m->l_aniso[1] * m->l_aniso[2] * pow((double)sc, 3) * pow((double)ls, 3);
-        double nd = sqrt(vd);
-        for (int c = 0; c < 4; ++c) out[c] = sd[c] / nd;
-    }
+    for (int c = 0; c < 4; ++c) out[c] = dbl ? sd[c] : (double)sf[c];
 }
 
-/* evaluateNoise3DNormalized with conditioning (SparseConvolutionNoise.cpp:308-317;
- * splattingKernel3D / 3DGrad, GPFunctions.cpp:555-580, 814-843). */
-static void noise3d_norm(const real_t *r, const float p[3], int cond, int dbl, double out[4])
+/* sqrt(sparseConvNoiseVariance3D) (GPFunctions.cpp:751-764; nonstationary
+ * 1260-1263): float as the reference rounds it, and FP64. */
+static void norm3(const om_t *m, int iso, float kr, float gs, float a, float *nf, double *nd)
+{
+    float ud = m->d.impulse_density / (kr * kr * kr);
+    double det = 1.0, detd = 1.0;
+    if (!iso) {
+        float detf = m->l_aniso[0] * m->l_aniso[1] * m->l_aniso[2];
+        det = (double)detf * pow((double)gs, 3);
+        detd = (double)m->l_aniso[0] * m->l_aniso[1] * m->l_aniso[2] * pow((double)gs, 3);
+    }
+    det *= pow((double)a, 3);
+    detd *= pow((double)a, 3);
+    float var = (float)((double)ud * (pow(M_PI, 1.5) * det));
+    *nf = sqrtf(var);
+    *nd = sqrt((double)m->d.impulse_density / ((double)kr * kr * kr) * pow(M_PI, 1.5) * detd);
+}
+
+/* One level: evaluateNoise3DNormalized (world, :308-317) or
+ * evaluateNoise3DIsotropicRayNormalized (:348-377) with its conditioning splats
+ * (splattingKernel3D / 3DGrad, GPFunctions.cpp:555-580, 814-843).  out = (value,
+ * world gradient) of the normalized noise. */
+static void noise3d_level(const real_t *r, const float p[3], const float dir[3], int cond, int dbl,
+                          const lv3_t *L, double out[4])
 {
     const om_t *m = r->m;
-    noise3d(r, p, dbl, out);
+    const int iso = m->iso3d;
+    const float a = ns_scale(m, p);
+    const uint32_t seed = r->noise_seed + oct_seed(m, r->octave) + L->seed_add;
+    const float gs = iso ? 1.0f : L->ks;
+    float q[3];
+    frame_t f;
+    if (iso) iso_ray_point(m, p, dir, L->ks, &f, q);
+    else { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+    float M[3];
+    inv_cov3(m, iso, 0, a, gs, M);
+    double s4[4];
+    lattice3(m, q, L->kr, M, seed, dbl, s4);
+    float nf;
+    double nd;
+    norm3(m, iso, L->kr, gs, a, &nf, &nd);
+    if (!dbl) {
+        float g[3] = {(float)s4[1], (float)s4[2], (float)s4[3]};
+        if (iso) {
+            float gi[3];
+            frame_to_global(&f, g, gi);
+            l2w_grad(m, gi, L->ks, g);
+        }
+        out[0] = (float)s4[0] / nf;
+        for (int c = 0; c < 3; ++c) out[1 + c] = g[c] / nf;
+    } else {
+        double g[3] = {s4[1], s4[2], s4[3]};
+        if (iso) {
+            double gi[3];
+            for (int i = 0; i < 3; ++i) gi[i] = (double)f.t[i] * g[0] + (double)f.b[i] * g[1] + (double)f.n[i] * g[2];
+            const double sdiv = (double)ns_transform_scale(m, L->ks);
+            for (int i = 0; i < 3; ++i) g[i] = (double)m->l_inv[i] * gi[i] / sdiv;
+        }
+        out[0] = s4[0] / nd;
+        for (int c = 0; c < 3; ++c) out[1 + c] = g[c] / nd;
+    }
     if (!(m->activate_cond && cond)) return;
     const coef_t *c = &r->c3;
-    float sc = oct_scale(m, r->octave);
-    float ls = ns_scale(m, p);
-    float M[3];
-    inv_cov_diag(m, 1, ls, sc, M);
+    float Mc[3];
+    inv_cov3(m, iso, 1, a, gs, Mc);
+    float ab[3];
+    if (iso) {
+        float oiso[3], oq[3];
+        w2l_pos(m, c->origin, L->ks, oiso);
+        frame_to_local(&f, oiso, oq);
+        for (int i = 0; i < 3; ++i) ab[i] = q[i] - oq[i];
+    } else {
+        for (int i = 0; i < 3; ++i) ab[i] = p[i] - c->origin[i];
+    }
     if (!dbl) {
-        float ab[3] = {p[0] - c->origin[0], p[1] - c->origin[1], p[2] - c->origin[2]};
-        float absq = ab[0] * M[0] * ab[0];
-        absq += ab[1] * M[1] * ab[1];
-        absq += ab[2] * M[2] * ab[2];
-        float f = rexpf(-absq);
+        float absq = ab[0] * Mc[0] * ab[0];
+        absq += ab[1] * Mc[1] * ab[1];
+        absq += ab[2] * Mc[2] * ab[2];
+        float fk = rexpf(-absq);
         float dp[3], g1[3];
         for (int i = 0; i < 3; ++i) {
-            dp[i] = -2.f * (ab[i] * M[i]);
-            g1[i] = dp[i] * f;
+            dp[i] = -2.f * (ab[i] * Mc[i]);
+            g1[i] = dp[i] * fk;
         }
         float add[4];
-        add[0] = f * c->value_scale;
+        add[0] = fk * c->value_scale;
         for (int i = 0; i < 3; ++i) add[1 + i] = g1[i] * c->value_scale;
         /* sum_c gs_c * (grad1st_c, grad2nd(c, .)) */
         float gv = 0.0f, gg[3] = {0, 0, 0};
         for (int cc = 0; cc < 3; ++cc) {
             gv += g1[cc] * c->gs[cc];
             for (int j = 0; j < 3; ++j) {
-                float h = dp[cc] * dp[j] - (cc == j ? 2.f * M[cc] : 0.0f);
-                gg[j] += (h * f) * c->gs[cc];
+                float h = dp[cc] * dp[j] - (cc == j ? 2.f * Mc[cc] : 0.0f);
+                gg[j] += (h * fk) * c->gs[cc];
             }
         }
+        float dg[3] = {add[1] + gg[0], add[2] + gg[1], add[3] + gg[2]};
+        if (iso) {
+            float gi[3];
+            frame_to_global(&f, dg, gi);
+            l2w_grad(m, gi, L->ks, dg);
+        }
         out[0] = (float)out[0] + (add[0] + gv);
-        for (int j = 0; j < 3; ++j) out[1 + j] = (float)out[1 + j] + (add[1 + j] + gg[j]);
+        for (int j = 0; j < 3; ++j) out[1 + j] = (float)out[1 + j] + dg[j];
     } else {
-        double ab[3], absq = 0.0;
-        for (int i = 0; i < 3; ++i) {
-            ab[i] = (double)p[i] - (double)c->origin[i];
-            absq += ab[i] * ab[i] * M[i];
-        }
-        double f = exp(-absq), dp[3];
-        for (int i = 0; i < 3; ++i) dp[i] = -2.0 * ab[i] * M[i];
-        out[0] += f * c->value_scale;
-        for (int j = 0; j < 3; ++j) out[1 + j] += dp[j] * f * c->value_scale;
+        double absq = 0.0;
+        for (int i = 0; i < 3; ++i) absq += (double)ab[i] * ab[i] * Mc[i];
+        double fk = exp(-absq), dp[3], dg[3] = {0, 0, 0};
+        for (int i = 0; i < 3; ++i) dp[i] = -2.0 * ab[i] * Mc[i];
+        out[0] += fk * c->value_scale;
+        for (int j = 0; j < 3; ++j) dg[j] += dp[j] * fk * c->value_scale;
         for (int cc = 0; cc < 3; ++cc) {
-            out[0] += dp[cc] * f * c->gs[cc];
+            out[0] += dp[cc] * fk * c->gs[cc];
             for (int j = 0; j < 3; ++j)
-                out[1 + j] += (dp[cc] * dp[j] - (cc == j ? 2.0 * M[cc] : 0.0)) * f * c->gs[cc];
+                dg[j] += (dp[cc] * dp[j] - (cc == j ? 2.0 * Mc[cc] : 0.0)) * fk * c->gs[cc];
         }
+        if (iso) {
+            double gi[3];
+            for (int i = 0; i < 3; ++i) gi[i] = (double)f.t[i] * dg[0] + (double)f.b[i] * dg[1] + (double)f.n[i] * dg[2];
+            const double sdiv = (double)ns_transform_scale(m, L->ks);
+            for (int i = 0; i < 3; ++i) dg[i] = (double)m->l_inv[i] * gi[i] / sdiv;
+        }
+        for (int j = 0; j < 3; ++j) out[1 + j] += dg[j];
     }
+}
+
+/* evaluateNoise3D (SparseConvolutionNoise.cpp:142-165): one level, or the blend
+ * w_low * noise_low + w_high * noise_high of the multi-resolution grid. */
+static void noise3d_norm(const real_t *r, const float p[3], const float dir[3], int cond, int dbl, double out[4])
+{
+    lv3_t lv[2];
+    float w[2];
+    const int n = levels3(r->m, p, lv, w);
+    if (n == 1) {
+        noise3d_level(r, p, dir, cond, dbl, &lv[0], out);
+        return;
+    }
+    double lo[4], hi[4];
+    noise3d_level(r, p, dir, cond, dbl, &lv[0], lo);
+    noise3d_level(r, p, dir, cond, dbl, &lv[1], hi);
+    for (int k = 0; k < 4; ++k)
+        out[k] = dbl ? (double)w[0] * lo[k] + (double)w[1] * hi[k]
+                     : (double)(w[0] * (float)lo[k] + w[1] * (float)hi[k]);
 }
 
 /* --- gradient sampling, conditioning ------------------------------------ */
@@ -1140,7 +1262,7 @@ static void conditioning_1d(real_t *r, const float p[3], const float dir[3], flo
     }
 }
 
-static void conditioning_3d(real_t *r, const float p[3], float target_val,
+static void conditioning_3d(real_t *r, const float p[3], const float dir[3], float target_val,
                             const float target_grad[3], float mean, const float mgrad[3])
 {
     const om_t *m = r->m;
@@ -1149,24 +1271,49 @@ static void conditioning_3d(real_t *r, const float p[3], float target_val,
     memcpy(c->origin, p, sizeof(float) * 3);
     float amp = amplitude(r);
     if (amp == 0) return;
+    float info[4] = {1.0f, 1.0f, 1.0f, 0.0f};
+    if (m->multires) level_ratio(m, p, info);
     double n4[4];
-    noise3d_norm(r, p, 0, 0, n4);
+    noise3d_norm(r, p, dir, 0, 0, n4);
     c->value_scale = (target_val - mean) / amp - (float)n4[0];
-    if (m->d.correlation_context == GPIS_CTX_RENEWAL_PLUS) {
-        float sc = oct_scale(m, r->octave);
-        float ls = ns_scale(m, p);
-        for (int i = 0; i < 3; ++i) {
-            float delta = (target_grad[i] - mgrad[i]) / amp - (float)n4[1 + i];
-            /* sparseConvNoiseOneOverSecondDerivative (GPFunctions.cpp:723-749): the inverse
-               of -2*(0.25*l_inv^2) for a diagonal covariance. */
-            float inv2 = m->l_inv[i] * m->l_inv[i];
-            float d2 = -2.f * (inv2 * 0.25f);
-            float g = delta / d2;
-            g *= (sc * sc);               /* octave length-scale multiplier */
-            g *= m->ls_max * m->ls_max;   /* sqr(sparseConvNoiseLateralScale), :564 */
-            (void)ls;
-            c->gs[i] = g;
+    if (m->multires) c->value_scale /= info[2] + info[3];
+    if (m->d.correlation_context != GPIS_CTX_RENEWAL_PLUS) return;
+    float delta[3];
+    for (int i = 0; i < 3; ++i) delta[i] = (target_grad[i] - mgrad[i]) / amp - (float)n4[1 + i];
+    if (m->iso3d) {
+        /* the world residual to isotropic (ray) space, times the inverse of the
+           isotropic second derivative -2 * 0.25 I, which is -2 I exactly */
+        float gi[3], diso[3], dn[3], gl[3];
+        w2l_grad(m, delta, 1.0f, gi);
+        w2l_pos(m, dir, 1.0f, diso);
+        normalize3f(diso, dn);
+        frame_t f;
+        frame_make(dn, &f);
+        frame_to_local(&f, gi, gl);
+        for (int i = 0; i < 3; ++i) c->gs[i] = -2.f * gl[i];
+        if (m->multires) {
+            const float dv = info[2] / info[0] + info[3] / info[1];
+            for (int i = 0; i < 3; ++i) c->gs[i] /= dv;
+        } else {
+            const float a = ns_scale(m, p);
+            for (int i = 0; i < 3; ++i) c->gs[i] *= a * a;
         }
+        return;
+    }
+    for (int i = 0; i < 3; ++i) {
+        /* sparseConvNoiseOneOverSecondDerivative (GPFunctions.cpp:723-749): the inverse
+           of -2*(0.25*l_inv^2) for a diagonal covariance, restated as the division */
+        float inv2 = m->l_inv[i] * m->l_inv[i];
+        float d2 = -2.f * (inv2 * 0.25f);
+        c->gs[i] = delta[i] / d2;
+    }
+    if (m->multires) {
+        const float dv = info[2] / (info[0] * info[0]) + info[3] / (info[1] * info[1]);
+        for (int i = 0; i < 3; ++i) c->gs[i] /= dv;
+    } else {
+        /* sqr(sparseConvNoiseLateralScale(p)): ls(p) itself by brute force, 1 stationary */
+        const float ls = ls_field(m, p);
+        for (int i = 0; i < 3; ++i) c->gs[i] *= ls * ls;
     }
 }
 
@@ -1201,7 +1348,7 @@ static void oct_noise(const field_t *F, int k, const float p[3], int cond, int d
     if (F->m->d.one_d_sampling)
         noise1d_norm(&F->oct[k], p, F->dir, cond, dbl, out);
     else
-        noise3d_norm(&F->oct[k], p, cond, dbl, out);
+        noise3d_norm(&F->oct[k], p, F->dir, cond, dbl, out);
 }
 
 /* evaluateValue (SparseConvolutionNoise.cpp:114-130): amplitude*noise + mean. */
@@ -1237,7 +1384,7 @@ static void field_grad(const field_t *F, const float p[3], float t_segment, floa
             grad_noise_1d(&F->oct[k], p, t_segment, F->dir, 1, ng);
         } else {
             double n4[4];
-            noise3d_norm(&F->oct[k], p, 1, 0, n4);
+            noise3d_norm(&F->oct[k], p, F->dir, 1, 0, n4);
             ng[0] = (float)n4[1]; ng[1] = (float)n4[2]; ng[2] = (float)n4[3];
         }
         float amp = amplitude(&F->oct[k]);
@@ -1260,7 +1407,7 @@ static void field_condition(field_t *F, const float p[3], float target_val, cons
     else mg[0] = mg[1] = mg[2] = 0.0f;
     if (F->n == 1) {
         if (m->d.one_d_sampling) conditioning_1d(&F->oct[0], p, F->dir, target_val, target_grad, mean, mg);
-        else conditioning_3d(&F->oct[0], p, target_val, target_grad, mean, mg);
+        else conditioning_3d(&F->oct[0], p, F->dir, target_val, target_grad, mean, mg);
         return;
     }
     /* Octaves (1D): the residual of the value, and of the gradient under

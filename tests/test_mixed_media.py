@@ -11,14 +11,17 @@ from gpis_extend_gb300 import abi, workloads
 from oracle import oracle
 
 
-def draw_media(n, seed=11, allow_3d=True, only_3d=False):
+def draw_media(n, seed=11, allow_3d=True, only_3d=False, spaces=False):
+    """spaces: the 3D media cycle through isotropic ray space, a brute-force
+    nonstationary length scale and the multi-resolution grid (in isotropic space
+    every other time)."""
     rng = np.random.default_rng(seed)
     media = []
     for i in range(n):
         kind = rng.integers(0, 4)
         one_d = not only_3d and ((not allow_3d) or rng.random() < 0.75)
         octaves = int(rng.integers(1, 4)) if one_d else 1
-        ns = one_d and rng.random() < 0.3
+        ns = (one_d and rng.random() < 0.3) or (spaces and not one_d and i % 3 != 0)
         ctx = abi.CTX_RENEWAL_PLUS if rng.random() < 0.5 else abi.CTX_RENEWAL
         ell = float(rng.uniform(0.02, 0.3))
         params = dict(sigma=float(rng.uniform(0.02, 0.06)), length_scale=ell if not ns else 1.0, kernel_scale=3.0,
@@ -35,6 +38,10 @@ def draw_media(n, seed=11, allow_3d=True, only_3d=False):
             params.update(mean_kind=abi.MEAN_TORUS_PLANE, mean_params=(0, 0, 0, 1.0, 0.35, -0.5))
         if ns:
             params.update(ls_kind=abi.LS_SINCOS, ls_params=(0.6 * ell, 0.4 * ell, 3.0, 2.0), ls_max=ell)
+        if spaces and not one_d:
+            params.update(isotropic_3d_sampling=int(i % 3 == 0 or i % 6 == 5), multires=int(i % 3 == 2))
+            if i % 3 == 2:
+                params.update(length_scale=1.0)
         if octaves > 1:
             params.update(n_octaves=octaves, octave_sigma=[params["sigma"] / 2 ** k for k in range(octaves)],
                           octave_scale=[0.5 ** k for k in range(octaves)],
@@ -67,14 +74,15 @@ def test_oracle_mixed_batch_equals_per_medium():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["1d", "mixed", "3d"])
+@pytest.mark.parametrize("mode", ["1d", "mixed", "3d", "3d_spaces"])
 def test_gpu_mixed_media_one_launch(mode):
     """1D media only (the octave and nonstationary fast passes with their skipping),
-    1D and 3D media together (the generic fast pass) and 3D media only (the 3D fast
-    pass with its range-bound skipping, per-lane media)."""
+    1D and 3D media together (the generic fast pass), 3D media only (the 3D fast
+    pass with its range-bound skipping, per-lane media) and 3D media in isotropic
+    space, nonstationary and on the multi-resolution grid (the generic evaluator)."""
     from gpis_extend_gb300 import runtime
     from test_gpu_parity import flights_vs_oracle
-    media = draw_media(16, allow_3d=mode != "1d", only_3d=mode == "3d")
+    media = draw_media(16, allow_3d=mode != "1d", only_3d=mode.startswith("3d"), spaces=mode == "3d_spaces")
     batch, parts, order = mixed_batch(media, 256 if mode == "1d" else 96)
     with runtime.Context(media) as ctx:
         rec = ctx.trace_host(batch)
