@@ -99,6 +99,8 @@ int gor_medium_transmittance(const gpis_medium_desc *desc, const gpis_ray *rays,
  * counts[4] += {distance flights, shadow flights, medium events, failed paths}. */
 int gor_render(const gpis_medium_desc *md, const gpis_scene_desc *sc, float *image, uint64_t counts[4],
                uint32_t row0, uint32_t rows);
+int gor_render_span(const gpis_medium_desc *md, const gpis_scene_desc *sc, float *image, uint64_t counts[4],
+                    uint32_t row, uint32_t col0, uint32_t cols);
 
 /* Elementwise SE splat in FP64 (the SeSplat1DTest expectation, SeSplat1DTest.cpp:72-84). */
 void gor_se_splat_1d(const float *q, const float *c, uint32_t n, float scale,

@@ -59,6 +59,7 @@ def lib():
                 "gor_medium_sample_distance": (c_int, [M, vp, vp, vp, vp, u32]),
                 "gor_medium_transmittance": (c_int, [M, vp, vp, vp, vp, u32]),
                 "gor_render": (c_int, [M, ctypes.POINTER(abi.SceneDesc), vp, vp, u32, u32]),
+                "gor_render_span": (c_int, [M, ctypes.POINTER(abi.SceneDesc), vp, vp, u32, u32, u32]),
             }
             for k, (r, a) in sigs.items():
                 f = getattr(L, k)
@@ -238,6 +239,31 @@ def render(desc, scene, n_threads=0):
     c = counts.sum(axis=0)
     return img, {"distance_flights": int(c[0]), "shadow_flights": int(c[1]), "medium_events": int(c[2]),
                  "failed": int(c[3])}
+
+
+def render_band(desc, scene, row0, rows, n_threads=0, span=16):
+    """Rows [row0, row0 + rows) of the restatement's image, each row split into spans
+    of `span` pixels over a thread pool (a band of a large image at full spp);
+    returns (rows, counts dict)."""
+    from concurrent.futures import ThreadPoolExecutor
+    h, w = scene.height, scene.width
+    img = np.zeros((h, w, 3), np.float32)
+    n_threads = n_threads or os.cpu_count() or 1
+    jobs = [(r, c) for r in range(row0, row0 + rows) for c in range(0, w, span)]
+    counts = np.zeros((len(jobs), 4), np.uint64)
+    L = lib()
+
+    def run(k):
+        r, c = jobs[k]
+        rc = L.gor_render_span(ctypes.byref(desc), ctypes.byref(scene), _p(img), _p(counts[k]), r, c, span)
+        if rc:
+            raise abi.GpisError(f"oracle render failed: {rc}", rc)
+
+    with ThreadPoolExecutor(n_threads) as ex:
+        list(ex.map(run, range(len(jobs))))
+    c = counts.sum(axis=0)
+    return img[row0:row0 + rows], {"distance_flights": int(c[0]), "shadow_flights": int(c[1]),
+                                   "medium_events": int(c[2]), "failed": int(c[3])}
 
 
 def render_rows(desc, scene, row0, rows, n_threads=0):

@@ -450,3 +450,27 @@ int gor_render(const gpis_medium_desc *md, const gpis_scene_desc *sc, float *ima
     }
     return GPIS_OK;
 }
+
+/* Columns [col0, col0 + cols) of one row (a band of the image rendered over many
+ * threads); the same paths as gor_render. */
+int gor_render_span(const gpis_medium_desc *md, const gpis_scene_desc *sc, float *image, uint64_t counts[4],
+                    uint32_t row, uint32_t col0, uint32_t cols)
+{
+    if (!md || !sc || !image || sc->width == 0 || sc->height == 0 || sc->spp == 0) return GPIS_EINVAL;
+    if (sc->phase > GPIS_PHASE_CONDUCTOR || row >= sc->height) return GPIS_EINVAL;
+    pt_counts_t cnt = {0, 0, 0, 0};
+    for (uint32_t x = col0; x < col0 + cols && x < sc->width; ++x) {
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        for (uint32_t s = 0; s < sc->spp; ++s) {
+            float l[3];
+            trace_path(md, sc, x, row, s, l, &cnt);
+            for (int c = 0; c < 3; ++c) acc[c] = acc[c] + l[c];
+        }
+        float *px = image + 3 * ((size_t)row * sc->width + x);
+        for (int c = 0; c < 3; ++c) px[c] = acc[c] / (float)sc->spp;
+    }
+    if (counts) {
+        counts[0] += cnt.distance; counts[1] += cnt.shadow; counts[2] += cnt.events; counts[3] += cnt.failed;
+    }
+    return GPIS_OK;
+}
