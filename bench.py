@@ -264,10 +264,53 @@ def learned_arm(ctx, prop, batches, devs, steps, stream, plain_ms):
     the arm's summary (flights/s, ratio to the plain arm, interval statistics, identity
     of every record with the plain records)."""
     import torch
-    from gpis_extend_gb300 import proposal, runtime
+    from gpis_extend_gb300 import abi, autotune, proposal, runtime
     plain = [d.rec.clone() for d in devs]
     feats = [torch.empty((d.n, 24), dtype=torch.float32, device="cuda") for d in devs]
     ivs = [torch.empty((d.n, 4), dtype=torch.float32, device="cuda") for d in devs]
+
+    # the ceiling of this use of a proposal: the true crossing of every flight (from
+    # the plain records) as its interval, so the march may skip up to `cap` certified
+    # steps per evaluation everywhere before the crossing; the march alone is timed
+    def true_intervals(d, rec):
+        r = rec.view(-1, 8)
+        hit = r[:, 5] == 0.0
+        far = d.dir_far[:, 3]
+        ta = torch.where(hit, r[:, 0], far)
+        iv = torch.zeros((d.n, 4), dtype=torch.float32, device="cuda")
+        iv[:, 0] = ta
+        iv[:, 1] = ta
+        iv[:, 2] = (~hit).float()
+        return iv
+
+    true_ivs = [true_intervals(d, p) for d, p in zip(devs, plain)]
+
+    def march_ms(intervals, reps):
+        for d, iv in zip(devs, intervals):
+            runtime.submit_proposed(ctx, d, iv, stream)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            for d, iv in zip(devs, intervals):
+                runtime.submit_proposed(ctx, d, iv, stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    plain_march = plain_ms / steps
+    ceiling = {}
+    for cap in (16, 64, 256):
+        ctx.tune(abi.TUNE_PROPOSED_SKIP_CAP, cap)
+        ms_c = march_ms(true_ivs, max(2, steps // 2))
+        same = all(torch.equal(p.view(torch.int32), d.rec.view(torch.int32)) for p, d in zip(plain, devs))
+        ceiling[str(cap)] = {"march_ms_per_step": ms_c, "ratio_vs_plain": plain_march / ms_c,
+                             "identical_to_plain": bool(same)}
+    for d, f, iv in zip(devs, feats, ivs):
+        runtime.proposal_features(ctx, d, stream, out=f)
+        prop.infer(d, f, stream, out=iv)
+    torch.cuda.synchronize()
+    sched = autotune.tune_proposed_cap(ctx, devs, ivs)
 
     def step():
         for d, f, iv in zip(devs, feats, ivs):
@@ -328,6 +371,11 @@ def learned_arm(ctx, prop, batches, devs, steps, stream, plain_ms):
     plain_value = n * steps / (plain_ms * 1e-3)
     return {"value": value, "unit": UNIT, "ms_per_step": ms / steps, "plain_value": plain_value,
             "ratio_vs_plain": value / plain_value, "ms_per_part": part, "inference_ms_by_kernel": kernels,
+            "plain_march_ms_per_step": plain_march, "schedule": sched,
+            "ceiling_true_interval": ceiling,
+            "ceiling_note": "the march with every flight's true crossing as its interval (skip cap per "
+                            "evaluation before it), features and inference excluded: the most this use "
+                            "of any proposal can buy",
             "inside_interval": inside / max(1, hits), "miss_fallback_rate": 1.0 - inside / max(1, hits),
             "identical_to_plain": bool(identical),
             "equal_image_rmse": "every flight record equals the plain arm's bit for bit, so images and their "
@@ -335,8 +383,16 @@ def learned_arm(ctx, prop, batches, devs, steps, stream, plain_ms):
 
 
 def run_learned(args):
-    """The learned-proposal workload on the three-octave torus-plane field: 10^7
-    training flights from the plain kernels, then plain vs learned on a fresh set."""
+    """The learned-proposal workload on its own line."""
+    line = learned_workload(args)
+    print(json.dumps(line), flush=True)
+
+
+def learned_workload(args):
+    """The learned-proposal workload on the three-octave torus-plane field: about 10^7
+    training flights from the plain kernels (primaries and their conditioned
+    secondaries), then plain vs learned on a fresh set, with the ceiling of the
+    proposal's use beside it.  Returns the line."""
     import torch
     from gpis_extend_gb300 import build, proposal, runtime, workloads
     build.build()
@@ -383,9 +439,9 @@ def run_learned(args):
         "gpu_launches": args.steps * 2 * 6,
         "clocks": clocks.summary(),
     }
-    print(json.dumps(line), flush=True)
     prop.close()
     ctx.close()
+    return line
 
 
 def run_batch(args):
@@ -563,7 +619,7 @@ def main():
     ap.add_argument("--no-ref-gpu", action="store_true")
     ap.add_argument("--workload", default="flights", choices=["flights", "image0", "image2", "learned", "batch"])
     ap.add_argument("--spp-scale", type=float, default=1.0)
-    ap.add_argument("--train-flights", type=int, default=1 << 22)
+    ap.add_argument("--train-flights", type=int, default=5_200_000)
     ap.add_argument("--train-steps", type=int, default=1200)
     ap.add_argument("--size", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0)
@@ -720,6 +776,23 @@ def main():
         except Exception as e:  # noqa: BLE001
             learned = {"error": f"{type(e).__name__}: {e}"}
         line["learned"] = learned
+    if rank == 0 and world == 1 and not args.no_learned:
+        # the learned arm on its own configuration: the three-octave torus-plane
+        # field, 2^22 primaries and their secondaries per step, a network trained on
+        # about 10^7 flights of that field
+        try:
+            l3 = learned_workload(args)
+            lr = l3["learned"]
+            line["learned_config3"] = {
+                "workload": l3["config"]["workload"], "flights_per_step": l3["config"]["flights_per_step"],
+                "value": lr["value"], "plain_value": lr["plain_value"], "ratio_vs_plain": lr["ratio_vs_plain"],
+                "ms_per_step": lr["ms_per_step"], "plain_ms_per_step": l3["plain"]["ms_per_step"],
+                "ms_per_part": lr["ms_per_part"], "ceiling_true_interval": lr["ceiling_true_interval"],
+                "schedule": lr["schedule"], "inside_interval": lr["inside_interval"],
+                "miss_fallback_rate": lr["miss_fallback_rate"], "identical_to_plain": lr["identical_to_plain"],
+                "train": l3["config"]["train"]}
+        except Exception as e:  # noqa: BLE001
+            line["learned_config3"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # the oracle over every flight of the step, timed as the CPU baseline; its
         # records check the GPU's records of the last timed step flight by flight

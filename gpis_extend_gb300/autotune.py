@@ -3,7 +3,8 @@
 
 Knobs: the fast pass's persistent grid (CTAs per SM), the render's pass size
 (paths per wavefront pass), the host pipeline's chunk and whether it runs on
-page-locked host streams in place.  None of them changes
+page-locked host streams in place, and the skip cap before a proposed crossing
+interval.  None of them changes
 a result: every flight is independent of the grid and of its batch, so the
 tuner compares times only.
 """
@@ -109,3 +110,24 @@ def tune_host_direct(ctx, pinned, reps=3):
     best = min(times, key=times.get)
     ctx.tune(abi.TUNE_HOST_DIRECT, best)
     return {"knob": "host_direct", "best": best, "ms": times}
+
+
+def tune_proposed_cap(ctx, devs, intervals, candidates=(16, 32, 64), reps=3):
+    """The most steps one evaluation may skip before a flight's proposed interval,
+    timed on the proposed march of device-resident batches with their intervals
+    (every skipped step is certified, so the records do not depend on it).  Returns
+    {candidate: ms} and leaves the fastest set."""
+    from . import runtime
+    times = {}
+
+    def run():
+        for d, iv in zip(devs, intervals):
+            runtime.submit_proposed(ctx, d, iv)
+
+    for c in candidates:
+        ctx.tune(abi.TUNE_PROPOSED_SKIP_CAP, c)
+        run()
+        times[c] = _median_ms(run, reps)
+    best = min(times, key=times.get)
+    ctx.tune(abi.TUNE_PROPOSED_SKIP_CAP, best)
+    return {"knob": "proposed_skip_cap", "best": best, "ms": times}

@@ -2387,7 +2387,8 @@ __device__ __forceinline__ float eval_at(EvalSkip3D &ev, const LaneField &L, con
 {
     return ev.value(L, d, p[0], p[1], p[2], id, refills, live);
 }
-// before a proposed crossing interval the cap is this (every skipped step is still certified)
+// before a proposed crossing interval the cap is this by default (every skipped step is
+// still certified; GPIS_TUNE_PROPOSED_SKIP_CAP sets it)
 constexpr int kMaxSkipProposed = 16;
 
 // Fast values farther than this from zero have the sign of the precise value
@@ -2456,6 +2457,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     // its truncation-jump allowance, fixed and per step
     float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
     float prop_a = -INFINITY;   // start of the proposed crossing interval (learned proposal)
+    const int prop_cap = a.prop_cap ? (int)a.prop_cap : kMaxSkipProposed;
     const uint32_t n_live = live_n(a);
 
     for (;;) {
@@ -2684,14 +2686,16 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     const float per = skip_lip * step + skip_j1;
                     // at most kMaxSkip per evaluation: the lanes of a warp skip different
                     // counts, so the warp runs the longest lane's loop
-                    const float cap = th < prop_a ? (float)kMaxSkipProposed : (float)kMaxSkip;
+                    const float cap = th < prop_a ? (float)prop_cap : (float)kMaxSkip;
                     if (af > per) skip = (int)fminf(af / per, cap);
                 }
                 if constexpr (IsSkip3D<Eval>::value) {
                     if (!RESUME) skip = ev.skips(f, step, kMaxSkip3D);
                 }
                 if constexpr (IsOct<Eval>::value) {
-                    if (!RESUME) skip = oct_skip_count(*L.m, L, d, ev.last_ls, f, step, IsOct<Eval>::cap);
+                    if (!RESUME)
+                        skip = oct_skip_count(*L.m, L, d, ev.last_ls, f, step,
+                                              th < prop_a ? max(IsOct<Eval>::cap, prop_cap) : IsOct<Eval>::cap);
                 }
                 if constexpr (RESUME) {
                     // a flight that marches on after a decision skips by the same slope bound

@@ -291,6 +291,10 @@ int gpis_nee_host(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n)
                                             staging copies) when every stream is
                                             page-locked and mapped; 0 (default): staged,
                                             chunked copies                             */
+#define GPIS_TUNE_PROPOSED_SKIP_CAP 4u   /* gpis_flights_submit_proposed: the most steps
+                                            one evaluation may skip before a flight's
+                                            proposed interval, 8..256 (default 16; every
+                                            skipped step is still certified)            */
 int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value);
 int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value);
 
