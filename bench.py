@@ -667,7 +667,7 @@ def main():
     stream = torch.cuda.current_stream()
     # the schedule: the fast pass's persistent grid from the autotuner, on these flights
     from gpis_extend_gb300 import autotune
-    schedule = [autotune.tune_march(ctx, [dev_p, dev_s])]
+    schedule = [autotune.tune_fast_window(ctx, [dev_p, dev_s]), autotune.tune_march(ctx, [dev_p, dev_s])]
 
     # ---- device-resident throughput --------------------------------------------
     for _ in range(args.warmup):
@@ -740,6 +740,8 @@ def main():
     ops_peak = sms * roofline.LANES_PER_SM * sm_mhz * 1e6 / 1e12 if sm_mhz else None
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if peak else None, "traffic": traffic,
+            "traffic_source": ((tr or {}).get("source", "") + "; DRAM bytes per flight of that capture times "
+                               "the flights of one launch, not measured in this run") if traffic else None,
             "kernel": "k_march<EvalCoop1D<8>> fast pass + k_march<EvalGeneric> resume pass",
             "march_ms_per_launch": march_ms,
             "kernel_ms_per_step": [k / max(1, args.steps) for k in kms],

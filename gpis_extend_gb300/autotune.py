@@ -3,8 +3,8 @@
 
 Knobs: the fast pass's persistent grid (CTAs per SM), the render's pass size
 (paths per wavefront pass), the host pipeline's chunk and whether it runs on
-page-locked host streams in place, and the skip cap before a proposed crossing
-interval.  None of them changes
+page-locked host streams in place, the skip cap before a proposed crossing
+interval, and where the stationary 1D fast pass keeps its impulse window.  None of them changes
 a result: every flight is independent of the grid and of its batch, so the
 tuner compares times only.
 """
@@ -131,3 +131,22 @@ def tune_proposed_cap(ctx, devs, intervals, candidates=(16, 32, 64), reps=3):
     best = min(times, key=times.get)
     ctx.tune(abi.TUNE_PROPOSED_SKIP_CAP, best)
     return {"knob": "proposed_skip_cap", "best": best, "ms": times}
+
+
+def tune_fast_window(ctx, devs, reps=3):
+    """Where the stationary 1D fast pass keeps each lane's three-cell impulse window:
+    0 shared memory, 1 registers; timed on device-resident batches.  Returns
+    {candidate: ms} and leaves the fastest set."""
+    times = {}
+
+    def run():
+        for d in devs:
+            ctx.submit(d)
+
+    for c in (0, 1):
+        ctx.tune(abi.TUNE_FAST_WINDOW, c)
+        run()
+        times[c] = _median_ms(run, reps)
+    best = min(times, key=times.get)
+    ctx.tune(abi.TUNE_FAST_WINDOW, best)
+    return {"knob": "fast_window", "best": best, "ms": times}

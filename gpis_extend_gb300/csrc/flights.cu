@@ -1991,23 +1991,82 @@ struct EvalSkip3D {
 // lane (the jump-ahead PCG draws any impulse of a cell independently), 32/NMAX
 // cells per pass; shuffles deliver each cell into its owner's registers.  Every
 // lane of the warp must call value() (idle lanes pass live = false).
-template <int NMAX, bool GRID = false, bool NS = false>
+// SM: the three-cell window lives in dynamic shared memory as a ring of slots
+// (kSmem1D bytes per 256-thread block, float4 rows per lane as EvalCoopOct lays
+// them out) instead of 24 registers per lane; a one-cell move then refills one
+// slot without shifting the others.
+constexpr int kC1Threads = 256;
+constexpr size_t kSmem1D = (size_t)3 * 8 * sizeof(float) * kC1Threads;
+
+template <int NMAX, bool GRID = false, bool NS = false, bool SM = false>
 struct EvalCoop1D {
     static constexpr bool kCollective = true;
     // 4 CTAs per SM for the stationary analytic-mean kernel (64 registers, measured 2 %
     // faster than 2 CTAs at 128 registers despite spills: its stalls are dependency
-    // waits that more warps hide); the grid and nonstationary variants keep 2
+    // waits that more warps hide; with the window in shared memory 4 CTAs at 64
+    // registers measured 17.06 against 17.27 ms per step for 3 CTAs at 80); the grid
+    // and nonstationary variants keep 2
     static constexpr int kMinBlocks = (GRID || NS) ? 2 : 4;
     static constexpr bool kGeneral = NS;   // stationary, single octave, 1D otherwise
     static constexpr bool kSkip = !NS;
-    float cache[3][NMAX];
+    float cache[SM ? 1 : 3][SM ? 1 : NMAX];
     int base;
     bool valid;
     const PcgJump *sj;      // the jump table in shared memory
     float last_ls;          // nonstationary: the local scale at the last evaluated point
+    float *cbase;           // SM: the window's shared memory
+    int rot;                // SM: logical cell j (0: ci - 1, 1: ci, 2: ci + 1) sits in slot (rot + j) mod 3
 
-    __device__ __forceinline__ void reset() { valid = false; base = 0; last_ls = 1.0f; }
-    __device__ __forceinline__ void bind(const PcgJump *t) { sj = t; }
+    __device__ __forceinline__ void reset() { valid = false; base = 0; last_ls = 1.0f; rot = 0; }
+    __device__ __forceinline__ void bind(const PcgJump *t)
+    {
+        sj = t;
+        if (SM) {
+            extern __shared__ float4 dsm_c1[];
+            cbase = reinterpret_cast<float *>(dsm_c1);
+        }
+    }
+    __device__ __forceinline__ float *slot_ptr(int tid, int slot, int k) const
+    {
+        return cbase + (((slot * 2 + (k >> 2)) * kC1Threads + tid) << 2) + (k & 3);
+    }
+
+    // SM: cooperative generation of one cell per requesting lane, each impulse written
+    // by the lane that draws it straight into the owner's ring slot
+    __device__ __forceinline__ void fill_sm(bool need, int cell, int slot, const LaneField &L, int lane)
+    {
+        unsigned mask = __ballot_sync(FULL, need);
+        const int rq = lane >> 3;
+        const int k = lane & 7;
+        const int warp0 = threadIdx.x & ~31;
+        while (mask) {
+            unsigned pass = 0u, mm = mask;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                pass |= mm & (0u - mm);
+                mm &= mm - 1u;
+            }
+            mask = mm;
+            unsigned pm = pass;
+            for (int r = 0; r < rq; ++r) pm &= pm - 1u;
+            const int owner = pm ? __ffs(pm) - 1 : 0;
+            const int ocell = __shfl_sync(FULL, cell, owner);
+            const uint32_t oseed = __shfl_sync(FULL, L.seed, owner);
+            const int oslot = __shfl_sync(FULL, slot, owner);
+            const uint32_t onimp = __shfl_sync(FULL, L.n_imp, owner);
+            if (pm != 0u) {
+                float v = __int_as_float(0x7f800000);
+                if ((uint32_t)k < onimp) {
+                    const uint32_t s = xxhash2((uint32_t)ocell, oseed) + 1u;
+                    const uint32_t r1 = pcg_draw(sj[2 + 2 * k], s);
+                    const uint32_t r2 = pcg_draw(sj[3 + 2 * k], s);
+                    v = __uint_as_float(__float_as_uint(unit_float(r1)) | (~r2 & 0x80000000u));
+                }
+                *slot_ptr(warp0 + owner, oslot, k) = v;
+            }
+        }
+        __syncwarp();
+    }
 
     template <int S>
     __device__ __forceinline__ void fill_slot(bool need, int cell, const LaneField &L, int lane)
@@ -2076,34 +2135,70 @@ struct EvalCoop1D {
         const bool up = changed && valid && ci == base + 1;
         const bool down = changed && valid && ci == base - 1;
         const bool full = changed && !up && !down;
-        if (up) {
-#pragma unroll
-            for (int k = 0; k < NMAX; ++k) { cache[0][k] = cache[1][k]; cache[1][k] = cache[2][k]; }
-        }
-        if (down) {
-#pragma unroll
-            for (int k = 0; k < NMAX; ++k) { cache[2][k] = cache[1][k]; cache[1][k] = cache[0][k]; }
-        }
-        fill_slot<0>(full || down, ci - 1, L, lane);
-        fill_slot<1>(full, ci, L, lane);
-        fill_slot<2>(full || up, ci + 1, L, lane);
-        if (changed) {
-            base = ci;
-            valid = true;
-            refills += full ? 3u : 1u;
-        }
         float acc0 = 0.0f, acc1 = 0.0f;
+        if constexpr (SM) {
+            int r = rot;
+            if (up) r = r == 2 ? 0 : r + 1;          // the old middle becomes the low cell
+            if (down) r = r == 0 ? 2 : r - 1;
+            if (full) r = 0;
+            const int s0 = r, s1 = r == 2 ? 0 : r + 1, s2 = r == 0 ? 2 : r - 1;
+            fill_sm(full || down, ci - 1, s0, L, lane);
+            fill_sm(full, ci, s1, L, lane);
+            fill_sm(full || up, ci + 1, s2, L, lane);
+            if (changed) {
+                base = ci;
+                rot = r;
+                valid = true;
+                refills += full ? 3u : 1u;
+            }
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const float tl = __fsub_rn(frac, (float)(c - 1));
+            for (int c = 0; c < 3; ++c) {
+                const float tl = __fsub_rn(frac, (float)(c - 1));
+                const int slot = c == 0 ? s0 : (c == 1 ? s1 : s2);
 #pragma unroll
-            for (int k = 0; k < NMAX; ++k) {
-                const float s = cache[c][k];
-                const float tp = __fsub_rn(tl, fabsf(s));
-                const float e = ex2_approx(kexp * (tp * tp));
-                const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(s) & 0x80000000u));
-                if (k & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
-                else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
+                for (int h = 0; h < 2; ++h) {
+                    const float4 q4 = *reinterpret_cast<const float4 *>(slot_ptr(threadIdx.x, slot, 4 * h));
+                    const float qs[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const float sv = qs[j];
+                        const float tp = __fsub_rn(tl, fabsf(sv));
+                        const float e = ex2_approx(kexp * (tp * tp));
+                        const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(sv) & 0x80000000u));
+                        if (j & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
+                        else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
+                    }
+                }
+            }
+        } else {
+            if (up) {
+#pragma unroll
+                for (int k = 0; k < NMAX; ++k) { cache[0][k] = cache[1][k]; cache[1][k] = cache[2][k]; }
+            }
+            if (down) {
+#pragma unroll
+                for (int k = 0; k < NMAX; ++k) { cache[2][k] = cache[1][k]; cache[1][k] = cache[0][k]; }
+            }
+            fill_slot<0>(full || down, ci - 1, L, lane);
+            fill_slot<1>(full, ci, L, lane);
+            fill_slot<2>(full || up, ci + 1, L, lane);
+            if (changed) {
+                base = ci;
+                valid = true;
+                refills += full ? 3u : 1u;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float tl = __fsub_rn(frac, (float)(c - 1));
+#pragma unroll
+                for (int k = 0; k < NMAX; ++k) {
+                    const float sv = cache[c][k];
+                    const float tp = __fsub_rn(tl, fabsf(sv));
+                    const float e = ex2_approx(kexp * (tp * tp));
+                    const float w = __uint_as_float(__float_as_uint(e) | (__float_as_uint(sv) & 0x80000000u));
+                    if (k & 1) acc1 += fabsf(tp) < 1.0f ? w : 0.0f;
+                    else acc0 += fabsf(tp) < 1.0f ? w : 0.0f;
+                }
             }
         }
         float noise = (acc0 + acc1) * inv_norm;
@@ -3353,6 +3448,10 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     } else if (coop && a.all_grid) {
         const void *fn = (const void *)k_march<EvalCoop1D<8, true>, false>;
         k_march<EvalCoop1D<8, true>, false><<<grid(fn), 256, 0, stream>>>(b);
+    } else if (coop && a.fast_window == 0u) {
+        // the impulse window in shared memory (the default)
+        const void *fn = (const void *)k_march<EvalCoop1D<8, false, false, true>, false>;
+        k_march<EvalCoop1D<8, false, false, true>, false><<<grid(fn, kSmem1D), 256, kSmem1D, stream>>>(b);
     } else if (coop) {
         const void *fn = (const void *)k_march<EvalCoop1D<8>, false>;
         k_march<EvalCoop1D<8>, false><<<grid(fn), 256, 0, stream>>>(b);

@@ -57,6 +57,7 @@ struct FlightArgs {
                                 // (the general 3D evaluator, no 3D step skipping)
     uint32_t ctas_per_sm;       // fast-pass persistent grid: CTAs per SM (0: every resident CTA)
     uint32_t prop_cap;          // most steps one evaluation skips before a proposed interval (0: 16)
+    uint32_t fast_window;       // stationary 1D fast pass: 0 impulse window in shared memory, 1 in registers
     const uint32_t *n_dev;      // may be null: the live flight count in device memory (<= n,
                                 // which is then the capacity the grids are sized for)
     const float4 *proposal;     // may be null: per flight the proposed crossing interval

@@ -278,7 +278,7 @@ struct gpis_ctx {
     double prof_ms[3] = {0, 0, 0};
     uint64_t prof_launches[3] = {0, 0, 0};
     // schedule knobs (gpis_tune_set; 0 = default)
-    uint64_t tune[5] = {0, 0, 0, 0, 0};
+    uint64_t tune[6] = {0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -494,6 +494,7 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.n_dev = n_dev;
     a.ctas_per_sm = (uint32_t)ctx->tune[GPIS_TUNE_MARCH_CTAS_PER_SM];
     a.prop_cap = ctx->tune[GPIS_TUNE_PROPOSED_SKIP_CAP] ? (uint32_t)ctx->tune[GPIS_TUNE_PROPOSED_SKIP_CAP] : 16u;
+    a.fast_window = (uint32_t)ctx->tune[GPIS_TUNE_FAST_WINDOW];
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
     a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
     a.seeds = reinterpret_cast<const uint4 *>(in->seeds);
@@ -629,8 +630,9 @@ __attribute__((visibility("hidden"))) int gpis_internal_nee_live(gpis_ctx *ctx, 
 int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value)
 {
     if (!ctx) return fail(GPIS_EINVAL, "null context");
-    if (key > GPIS_TUNE_PROPOSED_SKIP_CAP) return fail(GPIS_EINVAL, "unknown schedule knob");
+    if (key > GPIS_TUNE_FAST_WINDOW) return fail(GPIS_EINVAL, "unknown schedule knob");
     if (key == GPIS_TUNE_HOST_DIRECT && value > 1) return fail(GPIS_ERANGE, "host direct mode is 0 or 1");
+    if (key == GPIS_TUNE_FAST_WINDOW && value > 1) return fail(GPIS_ERANGE, "fast window is 0 or 1");
     if (key == GPIS_TUNE_PROPOSED_SKIP_CAP && value && (value < 8 || value > 256))
         return fail(GPIS_ERANGE, "proposed skip cap must be in [8, 256]");
     if (key == GPIS_TUNE_MARCH_CTAS_PER_SM && value > 64) return fail(GPIS_ERANGE, "CTAs per SM must be <= 64");
@@ -645,7 +647,7 @@ int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value)
 int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value)
 {
     if (!ctx || !value) return fail(GPIS_EINVAL, "null argument");
-    if (key > GPIS_TUNE_PROPOSED_SKIP_CAP) return fail(GPIS_EINVAL, "unknown schedule knob");
+    if (key > GPIS_TUNE_FAST_WINDOW) return fail(GPIS_EINVAL, "unknown schedule knob");
     *value = ctx->tune[key];
     return GPIS_OK;
 }

@@ -295,6 +295,9 @@ int gpis_nee_host(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n)
                                             one evaluation may skip before a flight's
                                             proposed interval, 8..256 (default 16; every
                                             skipped step is still certified)            */
+#define GPIS_TUNE_FAST_WINDOW       5u   /* stationary 1D fast pass: 0 (default) keeps
+                                            each lane's three-cell impulse window in
+                                            shared memory, 1 in registers              */
 int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value);
 int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value);
 

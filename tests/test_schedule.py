@@ -1,6 +1,7 @@
 """Schedule knobs (gpis_tune_set) and the autotuner: no knob changes a result.
-The fast pass's persistent grid, the render's pass size and the host pipeline's
-chunk are varied and every flight record / image must stay bit-identical."""
+The fast pass's persistent grid and impulse window, the render's pass size and
+the host pipeline's chunk are varied and every flight record / image must stay
+bit-identical."""
 import numpy as np
 import pytest
 
@@ -18,6 +19,12 @@ def test_gpu_knobs_keep_results():
         for c in (1, 2, 3):
             assert ctx.tune(abi.TUNE_MARCH_CTAS_PER_SM, c) == c
             assert np.array_equal(ctx.trace_host(prim).view(np.uint32), ref.view(np.uint32)), c
+        # the stationary fast pass's impulse window in registers, then shared memory again
+        for w in (1, 0):
+            ctx.tune(abi.TUNE_FAST_WINDOW, w)
+            assert np.array_equal(ctx.trace_host(prim).view(np.uint32), ref.view(np.uint32)), w
+        with pytest.raises(abi.GpisError):
+            ctx.tune(abi.TUNE_FAST_WINDOW, 2)
         for chunk in (4096, 1 << 14):
             ctx.tune(abi.TUNE_HOST_CHUNK, chunk)
             assert np.array_equal(ctx.trace_host(prim).view(np.uint32), ref.view(np.uint32)), chunk
