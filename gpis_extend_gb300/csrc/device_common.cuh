@@ -423,15 +423,17 @@ __device__ __forceinline__ float cr_expf(float x)
     const float h2h = __fmul_rn(0.5f, s2h), h2l = __fmul_rn(0.5f, s2l);
     const float tail = __fmul_rn(__fmul_rn(r, s2h),
                                  __fmaf_rn(r, __fmaf_rn(r, 0x1.111112p-7f, 0x1.555556p-5f), 0x1.555556p-3f));
-    float ql;
-    const float qh = two_sum(r, h2h, ql);
+    // |h2h| <= 0.003 |r|: the fast two-sum is exact
+    const float qh = __fadd_rn(r, h2h);
+    float ql = __fsub_rn(h2h, __fsub_rn(qh, r));
     ql = __fadd_rn(ql, __fadd_rn(rl, __fadd_rn(h2l, tail)));
     const float2 t = c_exp2_64[k & 63];
     const float ah = __fmul_rn(t.x, qh);
     float al = __fmaf_rn(t.x, qh, -ah);
     al = __fadd_rn(al, __fmaf_rn(t.x, ql, __fmaf_rn(t.y, qh, t.y)));
-    float sl;
-    const float sh = two_sum(t.x, ah, sl);
+    // |ah| < 0.011 <= t.x: the fast two-sum is exact
+    const float sh = __fadd_rn(t.x, ah);
+    const float sl = __fsub_rn(ah, __fsub_rn(sh, t.x));
     const float y = __fadd_rn(sh, __fadd_rn(sl, al));
     return __fmul_rn(y, __int_as_float(((k >> 6) + 127) << 23));
 }

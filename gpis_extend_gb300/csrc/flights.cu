@@ -1177,6 +1177,13 @@ __device__ __forceinline__ void lane_cond_1d(const LaneField &L, int k, float sc
 // The march uses it wherever a sign decision is close: the crossing step, the
 // step before it and every refinement point.
 
+// x / den rounded once; den is 2 ls^2, exactly 2 for a stationary medium, where the
+// product with 0.5 is the same correctly rounded value without the division
+__device__ __forceinline__ float div_den(float x, float den)
+{
+    return den == 2.0f ? __fmul_rn(x, 0.5f) : __fdiv_rn(x, den);
+}
+
 __device__ float noise1d_precise(const DevMedium &m, float z, uint32_t seed, float ls = 1.0f)
 {
     const float kr = m.kr_iso;
@@ -1197,7 +1204,7 @@ __device__ float noise1d_precise(const DevMedium &m, float z, uint32_t seed, flo
             const float tp = __fsub_rn(tl, ti);
             if (fabsf(tp) < 1.0f) {
                 const float ab = __fsub_rn(a, __fmul_rn(kr, ti));
-                const float e = cr_expf(-__fdiv_rn(__fmul_rn(ab, ab), den));
+                const float e = cr_expf(-div_den(__fmul_rn(ab, ab), den));
                 cv = __fadd_rn(cv, (wr >> 31) ? e : -e);
             }
         }
@@ -1246,7 +1253,7 @@ __device__ void noise1d_precise_vd(const DevMedium &m, float z, uint32_t seed, f
             const float tp = __fsub_rn(tl, ti);
             if (fabsf(tp) < 1.0f) {
                 const float ab = __fsub_rn(a, __fmul_rn(kr, ti));
-                const float e = cr_expf(-__fdiv_rn(__fmul_rn(ab, ab), den));
+                const float e = cr_expf(-div_den(__fmul_rn(ab, ab), den));
                 const float gr = rn_mul_div(__fmul_rn(-2.0f, ab), e, den);
                 cv = __fadd_rn(cv, (wr >> 31) ? e : -e);
                 cg = __fadd_rn(cg, (wr >> 31) ? gr : -gr);
