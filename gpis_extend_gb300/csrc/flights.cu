@@ -2529,8 +2529,13 @@ __device__ __forceinline__ unsigned long long warp_sum(uint32_t v)
 // its resume record and left to the resume pass.
 // RESUME = true: the resume pass over the saved flights, with precise decisions,
 // the refinement and, after a rejected crossing candidate, the rest of the march.
+// resident 256-thread blocks per SM the resume pass is compiled for: 4 (64 registers,
+// with spills) hide the precise evaluator's dependent float-float chains better than
+// 2 (128 registers): 15.93 against 16.57 ms per bench step (3: 16.07)
+constexpr int kResumeMinBlocks = 4;
+
 template <class Eval, bool RESUME>
-__global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
+__global__ void __launch_bounds__(256, RESUME ? kResumeMinBlocks : Eval::kMinBlocks) k_march(FlightArgs a)
 {
     const int lane = threadIdx.x & 31;
     uint32_t *work = a.work + (RESUME ? 2 : 0);
