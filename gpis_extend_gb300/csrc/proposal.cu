@@ -5,10 +5,11 @@
 // slope along the ray, then a 3 x 64 GELU MLP over the GRU state and eight
 // per-flight features, emitting an 8-component logistic mixture over
 // u = (t - near) / (far - near) and a miss logit.  Every contraction runs on the
-// tensor cores as BF16 x BF16 -> FP32 (mma.sync m16n8k16); the elementwise parts,
+// tensor cores as BF16 x BF16 -> FP32 (tcgen05 with tensor-memory accumulators; the
+// warp-level mma.sync m16n8k16 kernels remain selectable); the elementwise parts,
 // the loss and Adam are FP32.  Training uses an unfused layer-by-layer forward
-// that keeps its activations and a hand-written backward; inference is one fused
-// kernel per 16 flights a warp with the weights in shared memory.
+// that keeps its activations and a hand-written backward, its GEMMs on tcgen05;
+// inference is one persistent fused tcgen05 kernel with the weights in shared memory.
 //
 // The proposal never changes a flight's result: gpis_flights_submit_proposed lets
 // the march take longer certified skips before the proposed interval, and every
@@ -916,6 +917,129 @@ __global__ void __launch_bounds__(128) k_tc_gemm_check(const bf *A, const bf *B,
     if (tid < 32) umma::tmem_free(tmem, 128);
 }
 
+// ---- training GEMMs on the tensor cores --------------------------------------------------
+// C(m, n) (+)= sum_k A(m, k) B(k, n) with the strides of Gemm, through tcgen05: one
+// 128-thread CTA per 128-row tile of C, slice of 32 (or 16) columns and K chunk
+// (ksplit), so that even these small GEMMs spread over the SMs.  Per 64-deep step of K
+// the threads stage the A tile (128 x 64; rows beyond M are zero) and B^T (32 x 64) in the
+// K-major no-swizzle layout, whatever the operands' strides in global memory; one thread
+// issues the step's K = 16 MMAs into the tensor-memory accumulator (128 lanes x 32 FP32
+// columns) and commits them to an mbarrier, which every thread waits for (bounded) before
+// the next step overwrites the tiles.  The epilogue reads each thread's row (tcgen05.ld
+// 32x32b) and stores, adds or, with several K chunks, atomically adds it into C.
+// N % 16 == 0, N <= 128, K % 16 == 0.
+constexpr int TCG_KC = 64, TCG_NMAX = 128;
+constexpr uint32_t kTcgSmem = 128u * TCG_KC * 2u + 32u * TCG_KC * 2u;
+
+__global__ void __launch_bounds__(128) k_gemm_tc(Gemm g, uint32_t wait_limit, uint32_t *err)
+{
+    extern __shared__ __align__(128) unsigned char gsm[];
+    unsigned char *sa = gsm, *sb = gsm + 128u * TCG_KC * 2u;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x;
+    // the CTA's tile: 128 rows, a slice of 32 (or 16) columns, a K chunk
+    const int N = g.N % 32 == 0 ? 32 : 16;
+    const int nslices = g.N / N;
+    const int kc = (int)(blockIdx.x % (unsigned)g.ksplit);
+    const int rest = (int)(blockIdx.x / (unsigned)g.ksplit);
+    const int n0 = (rest % nslices) * N, mt = rest / nslices;
+    const long m0 = (long)mt * 128;
+    const uint32_t cols = 32u;
+    const int ktiles = g.K / 16;
+    const int per = (ktiles + g.ksplit - 1) / g.ksplit;
+    const int kt0 = kc * per, kt1 = min(ktiles, kt0 + per);
+    if (tid == 0) umma::bar_init(&bar, 1);
+    if (tid < 32) umma::tmem_alloc(&tslot, cols);
+    umma::fence_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tslot;
+    const bf zero = __float2bfloat16_rn(0.0f);
+    uint32_t phase = 0;
+    bool fail = false, issued = false;
+    for (int k16 = kt0; k16 < kt1; k16 += TCG_KC / 16) {
+        const int kn = min(TCG_KC, (kt1 - k16) * 16);
+        const long kbase = (long)k16 * 16;
+        // operands contiguous along K (row-major activations, weights as [N][K]) move as
+        // 16-byte core-matrix rows; the others element by element
+        if (g.lak == 1 && g.lam % 8 == 0 && (reinterpret_cast<uintptr_t>(g.A) & 15u) == 0) {
+            const int kq = kn / 8;
+            for (int i = (int)tid; i < 128 * kq; i += 128) {
+                const int r = i / kq, k = (i - r * kq) * 8;
+                const long row = m0 + r;
+                const uint4 v = row < g.M ? *reinterpret_cast<const uint4 *>(g.A + row * g.lam + kbase + k)
+                                          : make_uint4(0u, 0u, 0u, 0u);
+                *reinterpret_cast<uint4 *>(sa + umma::tile_offset((uint32_t)r, (uint32_t)k, TCG_KC)) = v;
+            }
+        } else {
+            for (int i = (int)tid; i < 128 * kn; i += 128) {
+                const int r = i / kn, k = i - r * kn;
+                const long row = m0 + r;
+                const bf v = row < g.M ? g.A[row * g.lam + (kbase + k) * g.lak] : zero;
+                *reinterpret_cast<bf *>(sa + umma::tile_offset((uint32_t)r, (uint32_t)k, TCG_KC)) = v;
+            }
+        }
+        if (g.lbk == 1 && g.lbn % 8 == 0 && (reinterpret_cast<uintptr_t>(g.B) & 15u) == 0) {
+            const int kq = kn / 8;
+            for (int i = (int)tid; i < N * kq; i += 128) {
+                const int c = i / kq, k = (i - c * kq) * 8;
+                *reinterpret_cast<uint4 *>(sb + umma::tile_offset((uint32_t)c, (uint32_t)k, TCG_KC)) =
+                    *reinterpret_cast<const uint4 *>(g.B + (long)(n0 + c) * g.lbn + kbase + k);
+            }
+        } else {
+            for (int i = (int)tid; i < N * kn; i += 128) {
+                const int c = i / kn, k = i - c * kn;
+                *reinterpret_cast<bf *>(sb + umma::tile_offset((uint32_t)c, (uint32_t)k, TCG_KC)) =
+                    g.B[(kbase + k) * g.lbk + (long)(n0 + c) * g.lbn];
+            }
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+        if (tid == 0) {
+            for (int kb = 0; kb < kn / 16; ++kb)
+                umma::mma(tmem, umma::tile_desc(sa, 0, (uint32_t)kb, TCG_KC), umma::tile_desc(sb, 0, (uint32_t)kb, TCG_KC),
+                          umma::idesc_bf16_m128((uint32_t)N), issued || kb > 0);
+            umma::commit(&bar);
+        }
+        issued = true;
+        const bool done = umma::bar_wait(&bar, phase, wait_limit);
+        if (umma::sync_or(1, 128, !done)) {
+            fail = true;
+            break;
+        }
+        phase ^= 1u;
+        umma::fence_after_sync();
+    }
+    if (fail) {
+        // wait (default bound) for the MMAs committed before the tensor memory is released
+        if (tid == 0) atomicExch(err, 1u);
+        umma::bar_wait(&bar, phase, kTcWaitLimit);
+    } else if (issued) {
+        const uint32_t w = tid >> 5;
+        const long row = m0 + tid;
+        float *c = g.C + row * g.ldc + n0;
+        float v[32];
+        umma::ld32(tmem + ((w * 32u) << 16), v);
+        if (row < g.M) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                if (j < N) {
+                    if (g.ksplit > 1) atomicAdd(c + j, v[j]);
+                    else if (g.accumulate) c[j] += v[j];
+                    else c[j] = v[j];
+                }
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (tid < 32) umma::tmem_free(tmem, cols);
+}
+
 }  // namespace prop
 }  // namespace gpis
 
@@ -999,10 +1123,18 @@ int ensure_batch(gpis_proposal *p, uint32_t n)
     return GPIS_OK;
 }
 
-void gemm(cudaStream_t s, const bf *A, long lam, long lak, const bf *B, long lbk, long lbn, float *C, long ldc, int M,
-          int N, int K, int accumulate, int ksplit = 1)
+// The training GEMMs: tcgen05 (k_gemm_tc) unless the proposal selects the warp-level
+// mma.sync kernels (GPIS_PROPOSAL_KERNEL_MMA) or N is outside its shapes.
+void gemm(gpis_proposal *p, cudaStream_t s, const bf *A, long lam, long lak, const bf *B, long lbk, long lbn, float *C,
+          long ldc, int M, int N, int K, int accumulate, int ksplit = 1)
 {
     Gemm g{A, lam, lak, B, lbk, lbn, C, ldc, M, N, K, accumulate, ksplit};
+    if (p->kernel != GPIS_PROPOSAL_KERNEL_MMA && N % 16 == 0 && N <= TCG_NMAX) {
+        const int nslices = N % 32 == 0 ? N / 32 : N / 16;
+        const unsigned blocks = (unsigned)(((long)M + 127) / 128 * nslices * ksplit);
+        k_gemm_tc<<<blocks, 128, kTcgSmem, s>>>(g, p->wait_limit, p->tc_err_dev);
+        return;
+    }
     const long warps = (long)(M / 16) * (N / 8) * ksplit;
     k_gemm<<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(g);
 }
@@ -1017,23 +1149,23 @@ void forward(gpis_proposal *p, const float *feat, uint32_t n, cudaStream_t s)
     for (int j = 0; j < NHIST; ++j) {
         const bf *x = p->xb + (size_t)j * n * NIN;
         const bf *hb = p->hb + (size_t)j * n * HID;
-        gemm(s, x, NIN, 1, wb + O_WIH, 1, NIN, p->gi, 3 * HID, n, 3 * HID, NIN, 0);
-        gemm(s, hb, HID, 1, wb + O_WHH, 1, HID, p->gh, 3 * HID, n, 3 * HID, HID, 0);
+        gemm(p, s, x, NIN, 1, wb + O_WIH, 1, NIN, p->gi, 3 * HID, n, 3 * HID, NIN, 0);
+        gemm(p, s, hb, HID, 1, wb + O_WHH, 1, HID, p->gh, 3 * HID, n, 3 * HID, HID, 0);
         const size_t o = (size_t)j * n * HID;
         k_gru_cell<<<nb((size_t)n * HID), 256, 0, s>>>(p->gi, p->gh, p->p, p->h + o, n, p->r + o, p->z + o, p->nn + o,
                                                         p->ghn + o, p->h + o + (size_t)n * HID, p->hb + o + (size_t)n * HID,
                                                         j == NHIST - 1 ? p->ub : nullptr);
     }
-    gemm(s, p->ub, MLPIN, 1, wb + O_W1, 1, MLPIN, p->a1, WID, n, WID, MLPIN, 0);
+    gemm(p, s, p->ub, MLPIN, 1, wb + O_W1, 1, MLPIN, p->a1, WID, n, WID, MLPIN, 0);
     k_bias_gelu<<<nb((size_t)n * WID), 256, 0, s>>>(p->a1, p->p + O_B1, n, WID, p->y1);
-    gemm(s, p->y1, WID, 1, wb + O_W2, 1, WID, p->a2, WID, n, WID, WID, 0);
+    gemm(p, s, p->y1, WID, 1, wb + O_W2, 1, WID, p->a2, WID, n, WID, WID, 0);
     k_bias_gelu<<<nb((size_t)n * WID), 256, 0, s>>>(p->a2, p->p + O_B2, n, WID, p->y2);
-    gemm(s, p->y2, WID, 1, wb + O_W3, 1, WID, p->a3, WID, n, WID, WID, 0);
+    gemm(p, s, p->y2, WID, 1, wb + O_W3, 1, WID, p->a3, WID, n, WID, WID, 0);
     k_bias_gelu<<<nb((size_t)n * WID), 256, 0, s>>>(p->a3, p->p + O_B3, n, WID, p->y3);
-    gemm(s, p->y3, WID, 1, wb + O_W4, 1, WID, p->o, NOUT, n, NOUT, WID, 0);
+    gemm(p, s, p->y3, WID, 1, wb + O_W4, 1, WID, p->o, NOUT, n, NOUT, WID, 0);
 }
 
-int ksplit_for(uint32_t n) { return (int)std::max(1u, std::min(64u, n / 256)); }
+int ksplit_for(uint32_t n) { return (int)std::max(1u, std::min(64u, n / 128)); }
 
 // loss and gradient of the mean loss into p->g (zeroed here)
 void backward(gpis_proposal *p, const float2 *tgt, uint32_t n, cudaStream_t s)
@@ -1045,19 +1177,19 @@ void backward(gpis_proposal *p, const float2 *tgt, uint32_t n, cudaStream_t s)
     cudaMemsetAsync(p->loss, 0, sizeof(float), s);
     k_loss<<<nb(n), 256, 0, s>>>(p->o, p->p + O_B4, tgt, n, 1.0f / (float)n, p->dof, p->dob, p->loss);
     // output layer
-    gemm(s, p->dob, 1, NOUT, p->y3, WID, 1, G + O_W4, WID, NOUT, WID, n, 1, ks);
+    gemm(p, s, p->dob, 1, NOUT, p->y3, WID, 1, G + O_W4, WID, NOUT, WID, n, 1, ks);
     k_colsum<<<64, 256, 0, s>>>(p->dof, n, NOUT, NOUT, G + O_B4);
-    gemm(s, p->dob, NOUT, 1, wb + O_W4, WID, 1, p->dy, WID, n, WID, NOUT, 0);
+    gemm(p, s, p->dob, NOUT, 1, wb + O_W4, WID, 1, p->dy, WID, n, WID, NOUT, 0);
     // hidden layers 3, 2, 1
     const float *acts[3] = {p->a3, p->a2, p->a1};
     const bf *ins[3] = {p->y2, p->y1, p->ub};
     const int ow[3] = {O_W3, O_W2, O_W1}, ob[3] = {O_B3, O_B2, O_B1}, inw[3] = {WID, WID, MLPIN};
     for (int l = 0; l < 3; ++l) {
         k_gelu_back<<<nb((size_t)n * WID), 256, 0, s>>>(p->dy, acts[l], n, WID, p->daf, p->dab);
-        gemm(s, p->dab, 1, WID, ins[l], inw[l], 1, G + ow[l], inw[l], WID, inw[l], n, 1, ks);
+        gemm(p, s, p->dab, 1, WID, ins[l], inw[l], 1, G + ow[l], inw[l], WID, inw[l], n, 1, ks);
         k_colsum<<<64, 256, 0, s>>>(p->daf, n, WID, WID, G + ob[l]);
-        if (l < 2) gemm(s, p->dab, WID, 1, wb + ow[l], WID, 1, p->dy, WID, n, WID, WID, 0);
-        else gemm(s, p->dab, WID, 1, wb + ow[l], MLPIN, 1, p->du, MLPIN, n, MLPIN, WID, 0);
+        if (l < 2) gemm(p, s, p->dab, WID, 1, wb + ow[l], WID, 1, p->dy, WID, n, WID, WID, 0);
+        else gemm(p, s, p->dab, WID, 1, wb + ow[l], MLPIN, 1, p->du, MLPIN, n, MLPIN, WID, 0);
     }
     // GRU, through time
     const float *dh = p->du;
@@ -1068,11 +1200,11 @@ void backward(gpis_proposal *p, const float2 *tgt, uint32_t n, cudaStream_t s)
                                                         n, p->dgif, p->dgib, p->dghf, p->dghb, p->dh);
         const bf *x = p->xb + (size_t)j * n * NIN;
         const bf *hb = p->hb + o;
-        gemm(s, p->dgib, 1, 3 * HID, x, NIN, 1, G + O_WIH, NIN, 3 * HID, NIN, n, 1, ks);
-        gemm(s, p->dghb, 1, 3 * HID, hb, HID, 1, G + O_WHH, HID, 3 * HID, HID, n, 1, ks);
+        gemm(p, s, p->dgib, 1, 3 * HID, x, NIN, 1, G + O_WIH, NIN, 3 * HID, NIN, n, 1, ks);
+        gemm(p, s, p->dghb, 1, 3 * HID, hb, HID, 1, G + O_WHH, HID, 3 * HID, HID, n, 1, ks);
         k_colsum<<<64, 192, 0, s>>>(p->dgif, n, 3 * HID, 3 * HID, G + O_BIH);
         k_colsum<<<64, 192, 0, s>>>(p->dghf, n, 3 * HID, 3 * HID, G + O_BHH);
-        gemm(s, p->dghb, 3 * HID, 1, wb + O_WHH, HID, 1, p->dh, HID, n, HID, 3 * HID, 1);
+        gemm(p, s, p->dghb, 3 * HID, 1, wb + O_WHH, HID, 1, p->dh, HID, n, HID, 3 * HID, 1);
         dh = p->dh;
         ldh = HID;
     }
@@ -1180,7 +1312,10 @@ int gpis_proposal_create(const float *params, gpis_proposal **out)
     if (!out) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
     *out = nullptr;
     gpis_proposal *p = new gpis_proposal;
-    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+    // a blocking stream: the training kernels run after the work the caller queued on
+    // the legacy default stream (the batch it gathered) and that stream's later work
+    // (which may reuse the batch's memory) waits for them
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamDefault) != cudaSuccess ||
         cudaMalloc(&p->p, N_PARAMS * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&p->g, N_PARAMS * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&p->m1, N_PARAMS * sizeof(float)) != cudaSuccess ||
@@ -1228,10 +1363,24 @@ int gpis_proposal_get_params(gpis_proposal *p, float *params)
     return GPIS_OK;
 }
 
+// a tensor-core wait that ran out in an earlier call (inference or training): reported
+// once, as GPIS_EIO
+static int check_tc_flag(gpis_proposal *p)
+{
+    volatile uint32_t *flag = p->tc_err_host;
+    if (*flag) {
+        *flag = 0;
+        return gpis_internal_set_error(GPIS_EIO, "proposal: tensor-core completion wait timed out");
+    }
+    return GPIS_OK;
+}
+
 static int check_batch(gpis_proposal *p, const float *feat, uint32_t n)
 {
     if (!p || !feat) return gpis_internal_set_error(GPIS_EINVAL, "null argument");
     if (n == 0 || n % 16) return gpis_internal_set_error(GPIS_EINVAL, "the batch must be a positive multiple of 16");
+    const int rc = check_tc_flag(p);
+    if (rc) return rc;
     return ensure_batch(p, n);
 }
 
@@ -1245,7 +1394,7 @@ int gpis_proposal_forward(gpis_proposal *p, const float *features, uint32_t n, f
     k_add_bias<<<nb((size_t)n * NOUT), 256, 0, p->stream>>>(p->o, p->p + O_B4, n, outputs);
     PTRY(cudaStreamSynchronize(p->stream), "proposal forward");
     PTRY(cudaGetLastError(), "proposal forward kernels");
-    return GPIS_OK;
+    return check_tc_flag(p);
 }
 
 int gpis_proposal_gradient(gpis_proposal *p, const float *features, const float *targets, uint32_t n, float *grad,
@@ -1258,6 +1407,8 @@ int gpis_proposal_gradient(gpis_proposal *p, const float *features, const float 
     backward(p, reinterpret_cast<const float2 *>(targets), n, p->stream);
     PTRY(cudaStreamSynchronize(p->stream), "proposal gradient");
     PTRY(cudaGetLastError(), "proposal gradient kernels");
+    rc = check_tc_flag(p);
+    if (rc) return rc;
     PTRY(cudaMemcpy(grad, p->g, N_PARAMS * sizeof(float), cudaMemcpyDeviceToHost), "read gradient");
     float l = 0.0f;
     PTRY(cudaMemcpy(&l, p->loss, sizeof(float), cudaMemcpyDeviceToHost), "read loss");
@@ -1284,6 +1435,7 @@ int gpis_proposal_train_step(gpis_proposal *p, const float *features, const floa
         PTRY(cudaMemcpyAsync(&l, p->loss, sizeof(float), cudaMemcpyDeviceToHost, s), "read loss");
         PTRY(cudaStreamSynchronize(s), "proposal training step");
         *loss = l / (float)n;
+        return check_tc_flag(p);
     }
     return GPIS_OK;
 }

@@ -495,7 +495,10 @@ int gpis_proposal_features(gpis_ctx *ctx, const gpis_flight_soa *in, float *feat
                            void *cuda_stream);
 /* Training on device batches: features (24 per flight), targets (u*, hit) per
  * flight; n a positive multiple of 16.  train_step: one Adam step (lr), loss =
- * mean negative log-likelihood before the step (NULL: no synchronization).
+ * mean negative log-likelihood before the step (NULL: no synchronization: the
+ * step runs on the proposal's own blocking stream, ordered with the legacy
+ * default stream; a caller that fills or reuses the batch on another stream
+ * synchronizes first).
  * gradient: the gradient of the mean loss (host vector) without a step.
  * forward: the 32 raw outputs per flight (device).  Blocking.               */
 int gpis_proposal_train_step(gpis_proposal *prop, const float *features, const float *targets, uint32_t n,
@@ -511,12 +514,14 @@ int gpis_proposal_infer(gpis_proposal *prop, const gpis_flight_soa *in, const fl
                         uint32_t n, void *cuda_stream);
 /* The fused inference kernel: tcgen05 MMAs with tensor-memory accumulators, two
  * 128-flight tiles per block (default) or one, or warp-level mma.sync (also
- * taken when features is not 16-byte aligned).                              */
+ * taken when features is not 16-byte aligned).  The training GEMMs (forward,
+ * gradient, train_step) run on tcgen05 too, unless GPIS_PROPOSAL_KERNEL_MMA
+ * selects the warp-level mma.sync kernels for them as well.                  */
 #define GPIS_PROPOSAL_KERNEL_TC2 0
 #define GPIS_PROPOSAL_KERNEL_TC1 1
 #define GPIS_PROPOSAL_KERNEL_MMA 2
 int gpis_proposal_set_kernel(gpis_proposal *prop, int kernel);
-/* Polls of the tensor-memory inference kernel's bounded completion wait per
+/* Polls of the tensor-memory kernels' bounded completion wait per
  * MMA round (default GPIS_PROPOSAL_WAIT_DEFAULT; each poll is one
  * mbarrier.try_wait).  When a round's wait runs out, the kernel's threads stop
  * together, wait for the MMAs already committed with the default bound, free

@@ -134,6 +134,33 @@ def test_gpu_forward_and_gradient_match_reference(gpu):
 
 
 @pytest.mark.gpu
+def test_gpu_training_gemms_tcgen05_match_mma_sync(gpu):
+    """The training GEMMs on tcgen05 (tensor-memory accumulators) against the warp-level
+    mma.sync kernels: the same BF16 operands accumulated in FP32 in another order, so
+    the outputs agree to 1e-5 relative and every gradient tensor to 1e-4 relative L2."""
+    torch, runtime = gpu
+    rng = np.random.default_rng(14)
+    n = 1008
+    f = torch.from_numpy(random_features(n, rng)).cuda()
+    tg = torch.from_numpy(random_targets(n, rng)).cuda()
+    params = proposal.init_params(8)
+    got = {}
+    for k in ("tc2", "mma"):
+        with runtime.Proposal(params) as prop:
+            prop.set_kernel(k)
+            out = prop.forward(f).cpu().numpy()
+            grad, loss = prop.gradient(f, tg)
+        got[k] = (out, grad, loss)
+    (o1, g1, l1), (o2, g2, l2) = got["tc2"], got["mma"]
+    assert np.max(np.abs(o1 - o2)) <= 1e-5 * (1 + np.max(np.abs(o2)))
+    assert abs(l1 - l2) <= 1e-5 * (1 + abs(l2))
+    a, b = R.unflatten(g1.astype(np.float64)), R.unflatten(g2.astype(np.float64))
+    for name, _ in R.PARAMS:
+        rel = np.linalg.norm(a[name] - b[name]) / max(np.linalg.norm(b[name]), 1e-12)
+        assert rel <= 1e-4, (name, rel)
+
+
+@pytest.mark.gpu
 def test_gpu_adam_step_matches_reference(gpu):
     torch, runtime = gpu
     rng = np.random.default_rng(6)
@@ -211,6 +238,19 @@ def test_gpu_tensor_core_wait_time_out_is_reported(gpu, kernel):
         assert "timed out" in str(e.value)
         again = prop.infer(dev, f).cpu().numpy()
         torch.cuda.synchronize()
+        if kernel == "tc2":
+            # the training GEMMs' wait: the gradient call that timed out reports it
+            rng = np.random.default_rng(1)
+            ft = torch.from_numpy(random_features(256, rng)).cuda()
+            tt = torch.from_numpy(random_targets(256, rng)).cuda()
+            g0, _ = prop.gradient(ft, tt)
+            prop.set_wait_limit(0)
+            with pytest.raises(abi.GpisError) as e2:
+                prop.gradient(ft, tt)
+            assert e2.value.code == abi.GPIS_EIO
+            prop.set_wait_limit()
+            g1, _ = prop.gradient(ft, tt)
+            assert np.allclose(g0, g1, rtol=1e-5, atol=1e-7)
     assert np.array_equal(again.view(np.uint32), good.view(np.uint32))
 
 
