@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <climits>
+#include <type_traits>
 
 #include "flights.cuh"
 
@@ -1022,9 +1023,12 @@ __device__ __forceinline__ void prepare_one(const FlightArgs &a, uint32_t i)
     s[3] = make_float4(__uint_as_float(fl.noise_seed), __uint_as_float(flags), 0.0f, 0.0f);
 }
 
-// 8 blocks of 128 per SM (at most 64 registers): 1.14 against 1.38 ms per bench step at
-// 4 blocks and 128 registers, the precise conditioning's FP64 work needs the warps
-__global__ void __launch_bounds__(128, 8) k_prepare(FlightArgs a)
+// MINB blocks of 128 per SM: 8 (at most 64 registers) for batches of 1D media, 1.14
+// against 1.38 ms per bench step at 4 blocks and 128 registers (the precise
+// conditioning's FP64 work needs the warps); 4 when 3D media are present, whose 27-cell
+// evaluations spill heavily at 64 registers
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_prepare(FlightArgs a)
 {
     const uint32_t n = live_n(a);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) prepare_one(a, i);
@@ -1492,7 +1496,7 @@ __device__ __forceinline__ float norm3(const DevMedium &m, bool iso, float kr, f
 // One level: the normalized noise value (and world gradient) at p with the
 // conditioning splats of c (null: none) about the flight's origin o.
 template <bool GRAD, bool PRECISE>
-__device__ void noise3d_level_gen(const DevMedium &m, const float p[3], const float d[3], const CondRec *c,
+__device__ __noinline__ void noise3d_level_gen(const DevMedium &m, const float p[3], const float d[3], const CondRec *c,
                                   const float o[3], const Lv3 &lv, uint32_t seed, float &v, float g[3])
 {
     const bool iso = (m.flags & MF_ISO3D) != 0;
@@ -1877,6 +1881,15 @@ struct EvalGeneric {
         refills += 27;
         return L.sigma * noise + lane_mean(L, px, py, pz, id);
     }
+};
+
+// The resume pass of batches whose media all use 1D noise: the generic evaluator
+// compiled for 4 blocks of 256 per SM (64 registers, with spills), which hides the
+// precise evaluator's dependent float-float chains better than 2 blocks at 128
+// registers (15.93 against 16.57 ms per bench step; 3 blocks: 16.07).  3D media keep
+// 2 blocks: their 27-cell evaluations spill too much at 64 registers.
+struct EvalGeneric4 : EvalGeneric {
+    static constexpr int kMinBlocks = 4;
 };
 
 // 3D stationary single-octave media with step skipping.  The value is EvalGeneric's
@@ -2529,13 +2542,8 @@ __device__ __forceinline__ unsigned long long warp_sum(uint32_t v)
 // its resume record and left to the resume pass.
 // RESUME = true: the resume pass over the saved flights, with precise decisions,
 // the refinement and, after a rejected crossing candidate, the rest of the march.
-// resident 256-thread blocks per SM the resume pass is compiled for: 4 (64 registers,
-// with spills) hide the precise evaluator's dependent float-float chains better than
-// 2 (128 registers): 15.93 against 16.57 ms per bench step (3: 16.07)
-constexpr int kResumeMinBlocks = 4;
-
 template <class Eval, bool RESUME>
-__global__ void __launch_bounds__(256, RESUME ? kResumeMinBlocks : Eval::kMinBlocks) k_march(FlightArgs a)
+__global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
 {
     const int lane = threadIdx.x & 31;
     uint32_t *work = a.work + (RESUME ? 2 : 0);
@@ -2694,7 +2702,7 @@ __global__ void __launch_bounds__(256, RESUME ? kResumeMinBlocks : Eval::kMinBlo
         // is the precise one too (their fast evaluator's normalisation and level
         // weights round differently)
         const bool precise = (RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE)) ||
-                             (!Eval::kCollective && phase == PH_FAR && general_3d(*L.m));
+                             (std::is_same<Eval, EvalGeneric>::value && phase == PH_FAR && general_3d(*L.m));
         if constexpr (IsSkip3D<Eval>::value) {
             // a marching step of a 3D medium asks for the field's range over the next
             // steps: about half of |f| at the last step, and at least two steps
@@ -2966,8 +2974,10 @@ __device__ __forceinline__ void finish_one(const FlightArgs &a, uint32_t i)
     a.out[2 * i + 1] = r1;
 }
 
-// 8 blocks of 128 per SM: 0.62 against 0.79 ms per bench step at 128 registers
-__global__ void __launch_bounds__(128, 8) k_finish(FlightArgs a)
+// MINB blocks of 128 per SM: 8 for batches of 1D media (0.62 against 0.79 ms per bench
+// step at 128 registers), 4 when 3D media are present
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_finish(FlightArgs a)
 {
     const uint32_t n = live_n(a);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) finish_one(a, i);
@@ -3428,7 +3438,10 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     const bool coop_plain = a.one_d && a.max_imp <= 8 && a.max_oct == 1 && !a.any_ns && !a.all_grid && !a.any_mr;
     FlightArgs b = a;
     if (!coop_plain) b.setup = nullptr;     // the march kernels read set-up records only when written
-    if (b.any_cond || b.setup) k_prepare<<<blocks, 128, 0, stream>>>(b);
+    if (b.any_cond || b.setup) {
+        if (a.one_d) k_prepare<8><<<blocks, 128, 0, stream>>>(b);
+        else k_prepare<4><<<blocks, 128, 0, stream>>>(b);
+    }
     if (ev) cudaEventRecord(ev[1], stream);
     cudaError_t err = cudaMemsetAsync(b.work, 0, 4 * sizeof(uint32_t), stream);
     if (err != cudaSuccess) return err;
@@ -3478,13 +3491,17 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
         const void *fn = (const void *)k_march<EvalGeneric, false>;
         k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(b);
     }
-    {
+    if (a.one_d) {
+        const void *fn = (const void *)k_march<EvalGeneric4, true>;
+        k_march<EvalGeneric4, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
+    } else {
         const void *fn = (const void *)k_march<EvalGeneric, true>;
         k_march<EvalGeneric, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
     }
     if (ev) cudaEventRecord(ev[3], stream);
     if (ev) cudaEventRecord(ev[4], stream);
-    k_finish<<<blocks, 128, 0, stream>>>(b);
+    if (a.one_d) k_finish<8><<<blocks, 128, 0, stream>>>(b);
+    else k_finish<4><<<blocks, 128, 0, stream>>>(b);
     if (ev) cudaEventRecord(ev[5], stream);
     return cudaGetLastError();
 }
