@@ -750,7 +750,15 @@ def main():
             "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, best of 5, measured in this run",
             "ops32": {"per_eval": ops_eval, "achieved": ops_achieved, "peak": ops_peak, "unit": "Tops/s",
                       "frac": (ops_achieved / ops_peak) if ops_peak else None,
-                      "peak_source": f"{sms} SMs x {roofline.LANES_PER_SM} 32-bit lanes x the sampled SM clock"}}
+                      "peak_source": f"{sms} SMs x {roofline.LANES_PER_SM} 32-bit lanes x the sampled SM clock",
+                      "note": "the reference formulation's operations: it regenerates the three cells at every "
+                              "evaluation; the kernels regenerate "
+                              f"{cnt['cell_refills'] / max(1.0, evals_march):.3f} cells per evaluation, so this "
+                              "rate overstates the work executed; the utilisation is issue_active"},
+            # the fast pass's issue-slot utilisation and DRAM bytes per flight from the
+            # committed ncu capture (profiles/march_fast_pass_2p21.md), not measured here
+            "issue_active_ncu": {"fast_pass": 0.763, "resume_pass": 0.459,
+                                 "source": "profiles/march_fast_pass_2p21.md, march_resume_pass_2p21.md"}}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
