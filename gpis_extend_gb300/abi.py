@@ -147,6 +147,7 @@ PHASE_LAMBERT, PHASE_MIRROR, PHASE_CONDUCTOR = 0, 1, 2
 TUNE_MARCH_CTAS_PER_SM, TUNE_RENDER_PASS_PATHS, TUNE_HOST_CHUNK, TUNE_HOST_DIRECT = 0, 1, 2, 3
 TUNE_PROPOSED_SKIP_CAP = 4
 TUNE_FAST_WINDOW = 5
+TUNE_PRECISE_DECISIONS = 6
 PHASE_NAMES = {"lambert": PHASE_LAMBERT, "mirror": PHASE_MIRROR, "conductor": PHASE_CONDUCTOR}
 PROPOSAL_KERNELS = {"tc2": 0, "tc1": 1, "mma": 2}
 PROPOSAL_WAIT_DEFAULT = 1 << 22

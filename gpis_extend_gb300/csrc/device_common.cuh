@@ -338,7 +338,7 @@ __device__ __forceinline__ float ex2_approx(float x)
 // rounded value on about 1e-8 of the arguments in [-90, 0] (checked exhaustively
 // on every third float there).  Arguments below -87 (results near the denormal
 // range, which never decide a sum) take expf.
-static __constant__ float2 c_exp2_64[64] = {
+static __device__ const float2 g_exp2_64[64] = {
     {0x1.0000000000000p+0f, 0x0.0p+0f},
     {0x1.02c9a40000000p+0f, -0x1.887fa00000000p-28f},
     {0x1.059b0e0000000p+0f, -0x1.9d4f520000000p-25f},
@@ -427,7 +427,7 @@ __device__ __forceinline__ float cr_expf(float x)
     const float qh = __fadd_rn(r, h2h);
     float ql = __fsub_rn(h2h, __fsub_rn(qh, r));
     ql = __fadd_rn(ql, __fadd_rn(rl, __fadd_rn(h2l, tail)));
-    const float2 t = c_exp2_64[k & 63];
+    const float2 t = __ldg(&g_exp2_64[k & 63]);
     const float ah = __fmul_rn(t.x, qh);
     float al = __fmaf_rn(t.x, qh, -ah);
     al = __fadd_rn(al, __fmaf_rn(t.x, ql, __fmaf_rn(t.y, qh, t.y)));

@@ -25,6 +25,8 @@
 #include <climits>
 #include <type_traits>
 
+#include <cooperative_groups.h>
+
 #include "flights.cuh"
 
 namespace gpis {
@@ -208,8 +210,9 @@ __device__ __forceinline__ float inv_norm_1d(const DevMedium &m, float ls)
 // ---- 1D noise, generic impulse count (no cache) --------------------------------
 // Returns the raw (unnormalized) sum and its derivative w.r.t. the iso coordinate;
 // ls is the local kernel scale (splattingKernel1D takes it at the query point).
-template <bool DERIV>
-__device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, float &v, float &dv, float ls = 1.0f)
+template <bool DERIV, bool MARGIN = false>
+__device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, float &v, float &dv, float ls = 1.0f,
+                                float *margin = nullptr)
 {
     const float tg = __fdiv_rn(z, m.kr_iso);
     const float fl = floorf(tg);
@@ -218,6 +221,9 @@ __device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, floa
     const float il2 = 1.0f / (ls * ls);
     const float kexp = m.kexp1d * il2;
     float sv = 0.0f, sd = 0.0f;
+    // MARGIN: the distance in cells from the query to the nearest support edge of
+    // an impulse of the three cells or to its cell's faces
+    float mg = fminf(frac, 1.0f - frac);
     for (int dx = -1; dx <= 1; ++dx) {
         const float tl = __fsub_rn(frac, (float)dx);
         const uint32_t s = xxhash2((uint32_t)(ci + dx), seed) + 1u;
@@ -225,6 +231,7 @@ __device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, floa
             const float ti = unit_float(pcg_draw(c_jump[2 + 2 * k], s));
             const uint32_t wr = pcg_draw(c_jump[3 + 2 * k], s);
             const float tp = __fsub_rn(tl, ti);
+            if (MARGIN) mg = fminf(mg, fabsf(fabsf(tp) - 1.0f));
             if (fabsf(tp) < 1.0f) {
                 const float e = ex2_approx(kexp * (tp * tp));
                 const float w = (wr >> 31) ? 1.0f : -1.0f;
@@ -235,6 +242,8 @@ __device__ void noise1d_generic(const DevMedium &m, float z, uint32_t seed, floa
     }
     v = sv;
     dv = sd;
+    // less 16 ulps of the cell coordinate for the rounding of the points and of z
+    if (MARGIN) *margin = mg - 0x1p-19f * (fabsf(tg) + 1.0f);
 }
 
 // ---- 3D world-space noise, generic (no cache) ----------------------------------
@@ -1892,6 +1901,74 @@ struct EvalGeneric4 : EvalGeneric {
     static constexpr int kMinBlocks = 4;
 };
 
+// Certified crossing decisions of the resume pass.  The refinement after a crossing
+// (SparseConvolutionNoiseMedium.cpp:296-330) decides the sign of the field at
+// t = ta + fac * step, fac = f(ta) / (f(ta) - f(tb)), and then fac <= 0.01 after each
+// x0.9 back-off.  The reference takes those values in float at its own points.  For
+// 1D stationary single-octave media with an analytic mean the pass decides them on
+// EvalGeneric's fast values instead whenever the decision is certain:
+//  * a fast value differs from the reference's float value at the same point by less
+//    than kPreciseBand (the margin the fast pass's sign decisions use), so fac is
+//    within dfac = 1.1 eps (|f(ta)| + |f(tb)|) / (f(ta) - f(tb))^2 of the reference's
+//    (for |f(ta) - f(tb)| >= 64 eps) and the refinement point within step * dfac;
+//  * the two points differ by d dt plus the rounding of each (pu: four float ulps of
+//    the largest coordinate); between them the field moves by at most the ray's
+//    slope bound (the step-skipping Lipschitz constant) times dt plus the gradient
+//    bound times pu, both of which hold away from the splats' truncation edges, and
+//    no truncation edge or cell face lies between them when the query's margin to
+//    the nearest one exceeds their distance in cells.
+// A sign is certain when |f| exceeds 2 eps plus that movement with the margin clear;
+// a back-off comparison when |fac - 0.01| exceeds dfac.  Anything else restarts the
+// crossing at tb with the precise evaluator, as without certification.
+__device__ __forceinline__ bool cert_medium(const DevMedium &m)
+{
+    return (m.flags & MF_ONE_D) && m.n_oct == 1 && !(m.flags & MF_MULTIRES) && m.ls_kind == 0u &&
+           m.mean_kind != GPIS_MEAN_GRID && m.skip_mean_lip >= 0.0f;
+}
+
+// true when the sign of the reference's value at its refinement point is that of
+// the fast value f at this one (dt: the bound on their distance in t)
+__device__ __forceinline__ bool cert_sign(const DevMedium &m, const LaneField &L, const float d[3], const float p[3],
+                                          float step, float f, float margin, float dt, float eps)
+{
+    float lip, j0, j1;
+    skip_params(m, d, L.sigma, L.cond, L.vs, L.gsz, step, lip, j0, j1);
+    const float lmax = fmaxf(fabsf(m.l_inv[0]), fmaxf(fabsf(m.l_inv[1]), fabsf(m.l_inv[2])));
+    const float lx = m.l_inv[0] * d[0], ly = m.l_inv[1] * d[1], lz = m.l_inv[2] * d[2];
+    const float dz = sqrtf(lx * lx + ly * ly + lz * lz) * 1.0001f / m.kr_iso;   // cells per unit of t
+    const float cslope = L.cond ? 0.42888194f * fabsf(L.vs) + 0.5f * fabsf(L.gsz) : 0.0f;
+    const float grad = (m.skip_mean_lip + fabsf(L.sigma) * (m.skip_noise_lip + cslope) * lmax) * 1.01f;
+    const float pu = 0x1p-21f * fmaxf(fabsf(p[0]), fmaxf(fabsf(p[1]), fabsf(p[2])));
+    const float move = lip * dt + grad * pu;
+    const float cells = dz * dt + lmax * 1.0001f / m.kr_iso * pu;
+    return lip >= 0.0f && fabsf(f) > 2.0f * eps + move && margin > cells && isfinite(move) && isfinite(cells);
+}
+
+// EvalGeneric's value of such a medium, with the query's margin in cells
+__device__ __forceinline__ float value_1d_cert(const LaneField &L, float px, float py, float pz, int &id, float &margin)
+{
+    const DevMedium &m = *L.m;
+    const float ls = ns_scale(m, px, pz);
+    const float z = ray_coord_oct(m, L.n, px, py, pz, oct_scale(m, 0));
+    float v, dv;
+    noise1d_generic<false, true>(m, z, L.seed + oct_seed(m, 0), v, dv, ls, &margin);
+    float nk = v * inv_norm_1d(m, ls);
+    if (L.cond) {
+        const Cov1D c = cov1d(z - L.ozc, splat_cov_1d(ls, L.ls_o));
+        nk += L.vs * c.k0 + L.gsz * c.k1;
+    }
+    return oct_sigma(m, 0) * nk + lane_mean(L, px, py, pz, id);
+}
+
+// the bound on fac's distance from the reference's (false: too close to call)
+__device__ __forceinline__ bool cert_fac(float pf, float fb, float eps, float &dfac)
+{
+    const float den = fabsf(pf - fb);
+    if (!(den >= 64.0f * eps)) return false;
+    dfac = 1.1f * eps * (fabsf(pf) + fabsf(fb)) / (den * den) + 0x1p-40f;
+    return isfinite(dfac);
+}
+
 // 3D stationary single-octave media with step skipping.  The value is EvalGeneric's
 // (the same arithmetic); a march step that plans a segment [p, p + D d] also gets the
 // range of the field over it: the raw noise sum's range (noise3d_core), the
@@ -2512,12 +2589,29 @@ constexpr int kMaxSkipProposed = 16;
 // (the fast evaluator differs from the precise one by a few 1e-8).
 constexpr float kPreciseBand = 1e-6f;
 
-// Saved march state of a flight handed to the resume pass (phase 0: none).
+// FlightArgs::work: the passes' fetch counters (fast 0, certified 1, precise 2),
+// then the lengths of the two hand-off queues.
+constexpr int kWorkQueueLen = 3;
+
+// Appends v to a hand-off queue: one atomic per group of lanes that push together.
+__device__ __forceinline__ void queue_push(uint32_t *q, uint32_t *len, uint32_t v)
+{
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(len, g.size());
+    base = g.shfl(base, 0);
+    q[base + g.thread_rank()] = v;
+}
+
+// Saved march state of a flight handed to the resume pass (phase 0: none); bit 26
+// marks a crossing that the certified pass could not decide.
+constexpr uint32_t kResumeNoCert = 1u << 26;
 __device__ __forceinline__ uint4 pack_resume(float th, float tl, float pf, uint32_t steps, int sign0,
-                                             bool pf_precise, int phase)
+                                             bool pf_precise, int phase, bool no_cert = false)
 {
     const uint32_t bits = (steps & 0xFFFFFFu) | (sign0 < 0 ? (1u << 24) : 0u) | (pf_precise ? (1u << 25) : 0u) |
-                          ((uint32_t)phase << 28);
+                          (no_cert ? kResumeNoCert : 0u) | ((uint32_t)phase << 28);
     return make_uint4(__float_as_uint(th), __float_as_uint(tl), __float_as_uint(pf), bits);
 }
 
@@ -2542,11 +2636,16 @@ __device__ __forceinline__ unsigned long long warp_sum(uint32_t v)
 // its resume record and left to the resume pass.
 // RESUME = true: the resume pass over the saved flights, with precise decisions,
 // the refinement and, after a rejected crossing candidate, the rest of the march.
-template <class Eval, bool RESUME>
+// RESUME: the resume pass; with CERT the certified pass before it, which takes the
+// saved crossings of the media cert_medium accepts, decides them on fast values
+// where that is certain and hands the rest on (kResumeNoCert) to the precise pass,
+// so that no warp runs both evaluators.
+template <class Eval, bool RESUME, bool CERT = false>
 __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
 {
+    static_assert(!CERT || RESUME, "the certified pass is a resume pass");
     const int lane = threadIdx.x & 31;
-    uint32_t *work = a.work + (RESUME ? 2 : 0);
+    uint32_t *work = a.work + (RESUME ? (CERT ? 1 : 2) : 0);
     const unsigned lt_mask = (1u << lane) - 1u;
     // 0.9 and 0.01 as float-float pairs (the reference's double constants)
     const FF kNine = {0.9f, -2.38418579e-08f};
@@ -2574,8 +2673,16 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     // its truncation-jump allowance, fixed and per step
     float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
     float prop_a = -INFINITY;   // start of the proposed crossing interval (learned proposal)
+    // certified pass: the bound on fac's distance from the reference's (cert_fac)
+    float dfac = 0.0f;
     const int prop_cap = a.prop_cap ? (int)a.prop_cap : kMaxSkipProposed;
-    const uint32_t n_live = live_n(a);
+    // the flights this pass takes: every flight, or the queue the pass before filled
+    const int q_in = RESUME && a.queue ? a.queue_in : 0;
+    const uint32_t *queue_in = q_in ? a.queue + (size_t)(q_in - 1) * a.n : nullptr;
+    const uint32_t n_live = q_in ? a.work[kWorkQueueLen + q_in - 1] : live_n(a);
+    // the queue this pass hands its saved flights on to
+    uint32_t *queue_out = a.queue ? a.queue + (CERT ? (size_t)a.n : 0) : nullptr;
+    uint32_t *queue_len = a.work + kWorkQueueLen + (CERT ? 1 : 0);
 
     for (;;) {
         const bool need = phase == PH_IDLE && !drained;
@@ -2586,10 +2693,11 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
             if (lane == leader) base = atomicAdd(work, (uint32_t)__popc(need_mask));
             base = __shfl_sync(FULL, base, leader);
             if (need) {
-                const uint32_t idx = base + (uint32_t)__popc(need_mask & lt_mask);
-                if (idx >= n_live) {
+                const uint32_t item = base + (uint32_t)__popc(need_mask & lt_mask);
+                if (item >= n_live) {
                     drained = true;
                 } else {
+                    const uint32_t idx = q_in ? queue_in[item] : item;
                     fid = idx;
                     if (!RESUME) c_flights++;
                     prop_a = (!RESUME && a.proposal) ? a.proposal[idx].x : -INFINITY;
@@ -2600,6 +2708,10 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     if (RESUME) rs = a.resume[idx];
                     if (RESUME && (rs.w >> 28) == 0u) {
                         // finished by the fast pass
+                    } else if (CERT && ((rs.w >> 28) != (uint32_t)PH_MARCH_P || (rs.w & kResumeNoCert) || !mok ||
+                                        !cert_medium(m))) {
+                        // left to the precise pass
+                        if (queue_out) queue_push(queue_out, queue_len, idx);
                     } else if (Eval::kSkip && !RESUME && a.setup) {
                         // the set-up k_prepare computed for this flight
                         const float4 s0 = a.setup[4 * (size_t)idx], s1 = a.setup[4 * (size_t)idx + 1];
@@ -2701,8 +2813,11 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
         // the value at farT of isotropic, nonstationary or multi-resolution 3D media
         // is the precise one too (their fast evaluator's normalisation and level
         // weights round differently)
-        const bool precise = (RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE)) ||
+        const bool decide = RESUME && (phase == PH_F0_P || phase == PH_MARCH_P || phase == PH_PF || phase == PH_REFINE);
+        const bool cert_eval = CERT && decide;
+        const bool precise = (!CERT && decide) ||
                              (std::is_same<Eval, EvalGeneric>::value && phase == PH_FAR && general_3d(*L.m));
+        float margin = 0.0f;
         if constexpr (IsSkip3D<Eval>::value) {
             // a marching step of a 3D medium asks for the field's range over the next
             // steps: about half of |f| at the last step, and at least two steps
@@ -2720,9 +2835,17 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 ev3.plan(len >= 2.0f * step ? len : 0.0f);
             }
         }
-        const float f = precise ? field_precise(L, p[0], p[1], p[2], id)
-                                : (use3 ? ev3.value(L, d, p[0], p[1], p[2], id, c_refills, live)
-                                        : eval_at(ev, L, d, p, id, c_refills, live));
+        float f;
+        if (CERT) {
+            // every phase on the one evaluator (its value is EvalGeneric's), so that
+            // the lanes of a warp never run two
+            f = value_1d_cert(L, p[0], p[1], p[2], id, margin);
+            c_refills += 3;
+        } else {
+            f = precise ? field_precise(L, p[0], p[1], p[2], id)
+                        : (use3 ? ev3.value(L, d, p[0], p[1], p[2], id, c_refills, live)
+                                : eval_at(ev, L, d, p, id, c_refills, live));
+        }
         if (Eval::kCollective && !live) continue;
         gpid = id;
         const int sg = f < 0.0f ? -1 : 1;
@@ -2732,7 +2855,34 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
         uint32_t status = GPIS_FLIGHT_OK;
 
         bool pend = false;
-        if (!isfinite(f)) {
+        // a certified decision that is not certain hands the crossing on to the
+        // precise pass, from tb
+        bool restart = false;
+        if (cert_eval) {
+            if (!isfinite(f)) {
+                restart = true;
+            } else if (phase == PH_MARCH_P) {
+                restart = fabsf(f) < kPreciseBand;
+            } else if (phase == PH_REFINE) {
+                const float dt = step * dfac + 0x1p-44f * fabsf(ttest.h);
+                restart = !cert_sign(*L.m, L, d, p, step, f, margin, dt, kPreciseBand);
+                // the back-off comparison that follows a sign change
+                if (!restart && sg != sign0) {
+                    const FF nf = ff_mul(fac, kNine);
+                    restart = fabsf(__fsub_rn(nf.h, kHundredthH)) <= 0.9f * dfac * 1.01f + 0x1p-40f;
+                }
+            }
+        }
+        if (CERT && restart) {
+            // (t stays at tb through the refinement)
+            if (phase != PH_MARCH_P) {
+                steps--;
+                c_steps--;
+                pf_precise = false;
+                phase = PH_MARCH_P;
+            }
+            pend = true;
+        } else if (!isfinite(f)) {
             // a non-finite field value ends the flight (RaySegmentBatch.cu:228-229, 238-239)
             done = true;
             status = GPIS_FLIGHT_INVALID_INPUT;
@@ -2754,10 +2904,11 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 phase = PH_FAR;
                 th = far_t;
             }
-        } else if (phase == PH_MARCH && (fabsf(f) < kPreciseBand || (sg != sign0 && (first || steps != 0)))) {
-            // close to zero or a candidate crossing: decide on the precise value
+        } else if (phase == PH_MARCH && (fabsf(f) < kPreciseBand || (sg != sign0 && (first || steps != 0) && !CERT))) {
+            // close to zero or a candidate crossing: decide on the precise value (a
+            // certified resume lane decides a crossing on this value)
             phase = PH_MARCH_P;
-            pend = !RESUME;
+            pend = !RESUME || CERT;
         } else if (phase == PH_MARCH || phase == PH_MARCH_P) {
             steps++;
             c_steps++;
@@ -2785,6 +2936,14 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     tprev = ttest;
                     refine_iter = 0;
                     phase = PH_REFINE;
+                    if (CERT && !cert_fac(pf, fb, kPreciseBand, dfac)) {
+                        // too close to call: the precise pass, from tb
+                        steps--;
+                        c_steps--;
+                        pf_precise = false;
+                        phase = PH_MARCH_P;
+                        pend = true;
+                    }
                 }
             } else {
                 pf = f;
@@ -2849,7 +3008,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 }
             }
         } else if (phase == PH_PF) {
-            // f: precise value at the previous point; fb: precise value at tb
+            // f: precise (or certified fast) value at the previous point; fb: the same at tb
             pf = f;
             float e;
             const float dh = two_sum(pf, -fb, e);
@@ -2858,6 +3017,13 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
             tprev = ttest;
             refine_iter = 0;
             phase = PH_REFINE;
+            if (CERT && !cert_fac(pf, fb, kPreciseBand, dfac)) {
+                steps--;
+                c_steps--;
+                pf_precise = false;
+                phase = PH_MARCH_P;
+                pend = true;
+            }
         } else if (phase == PH_REFINE) {
             c_refine++;
             refine_iter++;
@@ -2866,6 +3032,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 hit = true;
             } else {
                 fac = ff_mul(fac, kNine);
+                if (CERT) dfac *= 0.9f * 1.0001f;
                 // 0.9^44 < 0.01: the back-off ends within 44 evaluations for any
                 // factor <= 1; the explicit bound also covers a non-finite factor.
                 if (ff_le(fac, kHundredthH, kHundredthL) || !(fac.h == fac.h) || refine_iter >= 64) {
@@ -2891,12 +3058,14 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
             v_out = f;
         }
         if (pend) {
-            a.resume[fid] = pack_resume(th, tl, pf, steps, sign0, pf_precise, phase);
+            // (a value the certified pass took is never a precise one)
+            a.resume[fid] = pack_resume(th, tl, pf, steps, sign0, pf_precise && !CERT, phase, CERT);
+            if (queue_out) queue_push(queue_out, queue_len, fid);
             phase = PH_IDLE;
         } else if (done) {
             write_status(a, fid, t_out, v_out, trans, steps, status | ((uint32_t)gpid << 8));
             a.t_end[fid] = (double)t_end.h + (double)t_end.l;
-            if (!RESUME) a.resume[fid] = make_uint4(0u, 0u, 0u, 0u);
+            if (!RESUME || CERT) a.resume[fid] = make_uint4(0u, 0u, 0u, 0u);
             phase = PH_IDLE;
         }
     }
@@ -3443,7 +3612,7 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
         else k_prepare<4><<<blocks, 128, 0, stream>>>(b);
     }
     if (ev) cudaEventRecord(ev[1], stream);
-    cudaError_t err = cudaMemsetAsync(b.work, 0, 4 * sizeof(uint32_t), stream);
+    cudaError_t err = cudaMemsetAsync(b.work, 0, kWorkCounters * sizeof(uint32_t), stream);
     if (err != cudaSuccess) return err;
     // persistent grids: exactly the CTAs that are resident at once, never more
     // warps than flights
@@ -3490,6 +3659,15 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     } else {
         const void *fn = (const void *)k_march<EvalGeneric, false>;
         k_march<EvalGeneric, false><<<grid(fn), 256, 0, stream>>>(b);
+    }
+    // the resume passes take the flights the pass before handed on (queue 1: the
+    // fast pass's, 2: the certified pass's)
+    b.queue_in = 1;
+    if (coop_plain && !a.precise_only) {
+        // crossings of stationary single-octave media decided on certified fast values
+        const void *fn = (const void *)k_march<EvalGeneric4, true, true>;
+        k_march<EvalGeneric4, true, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
+        b.queue_in = 2;
     }
     if (a.one_d) {
         const void *fn = (const void *)k_march<EvalGeneric4, true>;

@@ -27,6 +27,9 @@ struct CondRec {
 static_assert(sizeof(CondRec) == 80 && offsetof(CondRec, tgn) == 64, "conditioning record layout (k_prepare "
                                                                       "writes 1D single-octave records by float4)");
 
+// counters per FlightArgs::work block
+constexpr int kWorkCounters = 8;
+
 struct FlightArgs {
     const float4 *origin_near;
     const float4 *dir_far;
@@ -39,9 +42,13 @@ struct FlightArgs {
     uint32_t n;
     CondRec *cond;              // scratch, n records
     double *t_end;              // scratch, n values (double march parameter at the end point)
-    uint32_t *work;             // scratch, 4 counters zeroed before the march: the fast pass's
-                                // and the resume pass's work counters (0 and 2)
+    uint32_t *work;             // scratch, kWorkCounters counters zeroed before the march: the
+                                // passes' work counters and the hand-off queues' lengths
     uint4 *resume;              // scratch, n saved march states
+    uint32_t *queue;            // scratch, 2 n flight indices (may be null: the resume passes then
+                                // scan every flight): the flights the fast pass hands on, then
+                                // those the certified resume pass hands on
+    int queue_in;               // set by launch_flights for each resume pass
     float4 *setup;              // scratch, 4 per flight: the fast pass's per-flight set-up, written by
                                 // k_prepare when the stationary cooperative evaluator runs (else unused)
     unsigned long long *counters;  // gpis_counters block (8 x u64)
@@ -58,6 +65,7 @@ struct FlightArgs {
     uint32_t ctas_per_sm;       // fast-pass persistent grid: CTAs per SM (0: every resident CTA)
     uint32_t prop_cap;          // most steps one evaluation skips before a proposed interval (0: 16)
     uint32_t fast_window;       // stationary 1D fast pass: 0 impulse window in shared memory, 1 in registers
+    uint32_t precise_only;      // 1: no certified resume pass (every crossing on the precise evaluator)
     const uint32_t *n_dev;      // may be null: the live flight count in device memory (<= n,
                                 // which is then the capacity the grids are sized for)
     const float4 *proposal;     // may be null: per flight the proposed crossing interval

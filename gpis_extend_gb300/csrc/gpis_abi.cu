@@ -260,6 +260,7 @@ struct gpis_ctx {
     double *d_tend = nullptr;
     uint4 *d_resume = nullptr;
     float4 *d_setup = nullptr;
+    uint32_t *d_queue = nullptr;
     uint32_t *d_work = nullptr;
     unsigned long long *d_counters = nullptr;
     size_t cap = 0;
@@ -278,7 +279,7 @@ struct gpis_ctx {
     double prof_ms[3] = {0, 0, 0};
     uint64_t prof_launches[3] = {0, 0, 0};
     // schedule knobs (gpis_tune_set; 0 = default)
-    uint64_t tune[6] = {0, 0, 0, 0, 0, 0};
+    uint64_t tune[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -292,6 +293,7 @@ void release(gpis_ctx *c)
     cudaFree(c->d_tend);
     cudaFree(c->d_resume);
     cudaFree(c->d_setup);
+    cudaFree(c->d_queue);
     cudaFree(c->d_work);
     cudaFree(c->d_counters);
     cudaFree(c->d_stage);
@@ -325,15 +327,18 @@ int ensure_scratch(gpis_ctx *c, size_t n)
     cudaFree(c->d_tend);
     cudaFree(c->d_resume);
     cudaFree(c->d_setup);
+    cudaFree(c->d_queue);
     c->d_cond = nullptr;
     c->d_tend = nullptr;
     c->d_resume = nullptr;
     c->d_setup = nullptr;
+    c->d_queue = nullptr;
     c->cap = 0;
     CUDA_TRY(cudaMalloc(&c->d_cond, cap * sizeof(gpis::CondRec)), "allocate conditioning scratch");
     CUDA_TRY(cudaMalloc(&c->d_tend, cap * sizeof(double)), "allocate end-parameter scratch");
     CUDA_TRY(cudaMalloc(&c->d_resume, cap * sizeof(uint4)), "allocate resume scratch");
     CUDA_TRY(cudaMalloc(&c->d_setup, cap * 4 * sizeof(float4)), "allocate set-up scratch");
+    CUDA_TRY(cudaMalloc(&c->d_queue, cap * 2 * sizeof(uint32_t)), "allocate hand-off queues");
     c->cap = cap;
     return GPIS_OK;
 }
@@ -458,7 +463,7 @@ int gpis_ctx_create(const gpis_medium_desc *media, int n_media, gpis_ctx **out)
             rc = cuda_fail(e, "upload media");
             break;
         }
-        if ((e = cudaMalloc(&c->d_work, 4 * kMaxChunks * sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(e, "allocate work counters"); break; }
+        if ((e = cudaMalloc(&c->d_work, gpis::kWorkCounters * kMaxChunks * sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(e, "allocate work counters"); break; }
         if ((e = cudaMalloc(&c->d_counters, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "allocate counters"); break; }
         if ((e = cudaMemset(c->d_counters, 0, sizeof(gpis_counters))) != cudaSuccess) { rc = cuda_fail(e, "clear counters"); break; }
         if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(e, "create stream"); break; }
@@ -495,6 +500,7 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.ctas_per_sm = (uint32_t)ctx->tune[GPIS_TUNE_MARCH_CTAS_PER_SM];
     a.prop_cap = ctx->tune[GPIS_TUNE_PROPOSED_SKIP_CAP] ? (uint32_t)ctx->tune[GPIS_TUNE_PROPOSED_SKIP_CAP] : 16u;
     a.fast_window = (uint32_t)ctx->tune[GPIS_TUNE_FAST_WINDOW];
+    a.precise_only = (uint32_t)ctx->tune[GPIS_TUNE_PRECISE_DECISIONS];
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);
     a.dir_far = reinterpret_cast<const float4 *>(in->dir_far);
     a.seeds = reinterpret_cast<const uint4 *>(in->seeds);
@@ -509,6 +515,7 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.work = work;
     a.resume = ctx->d_resume + offset;
     a.setup = ctx->d_setup + 4 * offset;
+    a.queue = ctx->d_queue + 2 * offset;
     a.counters = ctx->d_counters;
     a.any_cond = ctx->any_cond;
     a.one_d = ctx->all_one_d;
@@ -630,9 +637,10 @@ __attribute__((visibility("hidden"))) int gpis_internal_nee_live(gpis_ctx *ctx, 
 int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value)
 {
     if (!ctx) return fail(GPIS_EINVAL, "null context");
-    if (key > GPIS_TUNE_FAST_WINDOW) return fail(GPIS_EINVAL, "unknown schedule knob");
+    if (key > GPIS_TUNE_PRECISE_DECISIONS) return fail(GPIS_EINVAL, "unknown schedule knob");
     if (key == GPIS_TUNE_HOST_DIRECT && value > 1) return fail(GPIS_ERANGE, "host direct mode is 0 or 1");
     if (key == GPIS_TUNE_FAST_WINDOW && value > 1) return fail(GPIS_ERANGE, "fast window is 0 or 1");
+    if (key == GPIS_TUNE_PRECISE_DECISIONS && value > 1) return fail(GPIS_ERANGE, "precise decisions is 0 or 1");
     if (key == GPIS_TUNE_PROPOSED_SKIP_CAP && value && (value < 8 || value > 256))
         return fail(GPIS_ERANGE, "proposed skip cap must be in [8, 256]");
     if (key == GPIS_TUNE_MARCH_CTAS_PER_SM && value > 64) return fail(GPIS_ERANGE, "CTAs per SM must be <= 64");
@@ -647,7 +655,7 @@ int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value)
 int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value)
 {
     if (!ctx || !value) return fail(GPIS_EINVAL, "null argument");
-    if (key > GPIS_TUNE_FAST_WINDOW) return fail(GPIS_EINVAL, "unknown schedule knob");
+    if (key > GPIS_TUNE_PRECISE_DECISIONS) return fail(GPIS_EINVAL, "unknown schedule knob");
     *value = ctx->tune[key];
     return GPIS_OK;
 }
@@ -796,7 +804,7 @@ int gpis_flights_trace_host(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis
         CUDA_TRY(cudaStreamWaitEvent(cs, ctx->ev_chunks[2 * k], 0), "wait for copies");
         gpis_flight_soa din{d_on + 4 * o, d_df + 4 * o, d_sd + 4 * o, d_pv + 4 * o, in->medium ? d_md + o : nullptr};
         gpis_result_soa dout{d_rec + 8 * o};
-        int rc = submit_slice(ctx, &din, &dout, (uint32_t)m, cs, o, ctx->d_work + 4 * k);
+        int rc = submit_slice(ctx, &din, &dout, (uint32_t)m, cs, o, ctx->d_work + gpis::kWorkCounters * k);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(ctx->ev_chunks[2 * k + 1], cs), "record kernel event");
     }

@@ -26,9 +26,9 @@ extern "C" int gpis_internal_set_error(int code, const char *msg);
 
 namespace {
 
-// Layout of the working array: the medium table, four work counters, the
-// counter block, then the per-flight conditioning records, end parameters,
-// saved march states and fast-pass set-up records.
+// Layout of the working array: the medium table, the work counters, the counter
+// block, then the per-flight conditioning records, end parameters, saved march
+// states, fast-pass set-up records and the two hand-off queues.
 constexpr size_t kMax = GPIS_STATIC_MAX_FLIGHTS;
 constexpr size_t kOffMedium = 0;
 constexpr size_t kOffWork = 1024;
@@ -37,8 +37,10 @@ constexpr size_t kOffCond = kOffCounters + 256;
 constexpr size_t kOffTEnd = kOffCond + kMax * sizeof(gpis::CondRec);
 constexpr size_t kOffResume = kOffTEnd + kMax * sizeof(double);
 constexpr size_t kOffSetup = kOffResume + kMax * sizeof(uint4);
-constexpr size_t kBytes = kOffSetup + kMax * 4 * sizeof(float4);
+constexpr size_t kOffQueue = kOffSetup + kMax * 4 * sizeof(float4);
+constexpr size_t kBytes = kOffQueue + kMax * 2 * sizeof(uint32_t);
 static_assert(sizeof(gpis::DevMedium) <= kOffWork, "medium table must fit its slot");
+static_assert(gpis::kWorkCounters * sizeof(uint32_t) <= kOffCounters - kOffWork, "work counters must fit their slot");
 
 // The working memory.  In host code this name is only a stand-in for the
 // device array: its device address comes from cudaGetSymbolAddress.
@@ -132,6 +134,7 @@ extern "C" int gpis_flights_submit_static(const gpis_medium_desc *medium, const 
     a.work = reinterpret_cast<uint32_t *>(b + kOffWork);
     a.resume = reinterpret_cast<uint4 *>(b + kOffResume);
     a.setup = reinterpret_cast<float4 *>(b + kOffSetup);
+    a.queue = reinterpret_cast<uint32_t *>(b + kOffQueue);
     a.counters = reinterpret_cast<unsigned long long *>(b + kOffCounters);
     a.any_cond = cond;
     a.one_d = (m.flags & gpis::MF_ONE_D) != 0;

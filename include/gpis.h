@@ -298,6 +298,14 @@ int gpis_nee_host(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n)
 #define GPIS_TUNE_FAST_WINDOW       5u   /* stationary 1D fast pass: 0 (default) keeps
                                             each lane's three-cell impulse window in
                                             shared memory, 1 in registers              */
+#define GPIS_TUNE_PRECISE_DECISIONS 6u   /* 1: every crossing of a stationary 1D single-
+                                            octave medium is decided on the precise
+                                            evaluator; 0 (default): on fast values where
+                                            error bounds make the decision certain (the
+                                            refinement point may then differ from the
+                                            reference's by that bound, far below the
+                                            march's tolerance), the precise evaluator
+                                            for the rest                                */
 int gpis_tune_set(gpis_ctx *ctx, uint32_t key, uint64_t value);
 int gpis_tune_get(gpis_ctx *ctx, uint32_t key, uint64_t *value);
 
