@@ -2486,8 +2486,10 @@ struct EvalCoopOct {
 // refinement point.
 enum : int { PH_IDLE = 0, PH_F0, PH_F0_P, PH_MARCH, PH_MARCH_P, PH_PF, PH_REFINE, PH_FAR };
 
-// most march steps one evaluation may skip (fast pass)
-constexpr int kMaxSkip = 8;
+// most march steps one evaluation may skip (fast pass; the skipped steps cost one
+// jump when t_direct_ok holds, a loop that the warp runs for its longest lane
+// otherwise)
+constexpr int kMaxSkip = 16;
 // at most this many steps skipped per evaluation of a 3D medium (the segment also ends
 // inside the query's cell)
 constexpr int kMaxSkip3D = 32;
@@ -2583,7 +2585,7 @@ __device__ __forceinline__ float eval_at(EvalSkip3D &ev, const LaneField &L, con
 }
 // before a proposed crossing interval the cap is this by default (every skipped step is
 // still certified; GPIS_TUNE_PROPOSED_SKIP_CAP sets it)
-constexpr int kMaxSkipProposed = 16;
+constexpr int kMaxSkipProposed = 32;
 
 // Fast values farther than this from zero have the sign of the precise value
 // (the fast evaluator differs from the precise one by a few 1e-8).
@@ -2618,6 +2620,33 @@ __device__ __forceinline__ uint4 pack_resume(float th, float tl, float pf, uint3
 __device__ __forceinline__ bool t_less(float hi, float lo, float far_t)
 {
     return hi < far_t || (hi == far_t && lo < 0.0f);
+}
+
+// The march parameter after k steps, t0 + k step, straight from k: with t0 and step
+// floats the exact sum is a multiple of q = min(ulp(t0), ulp(step)); while every t
+// of the flight spans at most 45 bits above q, the product's two parts, their sum
+// with t0 and the low parts' sum are all exact, so the result is the normalised
+// float-float of the exact sum, which is what k sequential ff_add steps produce
+// under the same condition (t_direct_ok).
+__device__ __forceinline__ bool t_direct_ok(float t0, float step, float far_t)
+{
+    if (!(step > 0.0f) || !isfinite(t0) || !isfinite(far_t)) return false;
+    const int top = ilogbf(fmaxf(fabsf(far_t), fabsf(t0)) + 4.0f * step);
+    const int es = ilogbf(step);
+    const int q = (t0 == 0.0f ? es : min(ilogbf(t0), es)) - 23;
+    return top - q <= 44;
+}
+
+__device__ __forceinline__ void t_after(float t0, float step, uint32_t k, float &hi, float &lo)
+{
+    const float kf = (float)k;   // exact: k < 2^24
+    const float p = __fmul_rn(kf, step);
+    const float pe = __fmaf_rn(kf, step, -p);
+    float e;
+    const float s = two_sum(t0, p, e);
+    const float l = __fadd_rn(e, pe);
+    hi = __fadd_rn(s, l);
+    lo = __fsub_rn(l, __fsub_rn(hi, s));
 }
 
 __device__ __forceinline__ unsigned long long warp_sum(uint32_t v)
@@ -2672,6 +2701,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     // step skipping (fast pass): the field's Lipschitz constant along this ray and
     // its truncation-jump allowance, fixed and per step
     float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
+    bool t_direct = false;      // fast pass: skipped steps jump to t0 + k step (t_direct_ok)
     float prop_a = -INFINITY;   // start of the proposed crossing interval (learned proposal)
     // certified pass: the bound on fac's distance from the reference's (cert_fac)
     float dfac = 0.0f;
@@ -2753,6 +2783,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                             skip_j0 = s2.y;
                             skip_j1 = s2.z;
                             max_steps = m.max_steps;
+                            t_direct = t_direct_ok(t0, step, far_t);
                             th = near_t;
                             tl = 0.0f;
                             steps = 0;
@@ -2778,6 +2809,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                         skip_lip = -1.0f;
                         if (Eval::kSkip && !RESUME)
                             skip_params(m, d, L.sigma, L.cond, L.vs, L.gsz, step, skip_lip, skip_j0, skip_j1);
+                        t_direct = !RESUME && t_direct_ok(t0, step, far_t);
                         th = near_t;
                         tl = 0.0f;
                         steps = 0;
@@ -2960,8 +2992,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                 if (Eval::kSkip && !RESUME && skip_lip >= 0.0f) {
                     const float af = fabsf(f) * (1.0f - 1e-6f) - 1e-5f - skip_j0;
                     const float per = skip_lip * step + skip_j1;
-                    // at most kMaxSkip per evaluation: the lanes of a warp skip different
-                    // counts, so the warp runs the longest lane's loop
+                    // at most kMaxSkip per evaluation
                     const float cap = th < prop_a ? (float)prop_cap : (float)kMaxSkip;
                     if (af > per) skip = (int)fminf(af / per, cap);
                 }
@@ -2983,6 +3014,19 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                     else if (use3)
                         skip = ev3.skips(f, step, kMaxSkip3D);
                     if (skip > 0) pf_precise = false;
+                }
+                if (!RESUME && t_direct && skip > 0 && steps + (uint32_t)skip < max_steps) {
+                    // the skipped steps in one jump when it stays before farT (else step by step)
+                    float nh, nl;
+                    t_after(t0, step, steps + (uint32_t)skip, nh, nl);
+                    if (t_less(nh, nl, far_t)) {
+                        th = nh;
+                        tl = nl;
+                        steps += (uint32_t)skip;
+                        c_steps += (uint32_t)skip;
+                        c_skipped += (uint32_t)skip;
+                        skip = 0;
+                    }
                 }
                 for (;;) {
                     if (!t_less(th, tl, far_t)) {

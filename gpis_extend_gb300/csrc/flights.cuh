@@ -63,7 +63,7 @@ struct FlightArgs {
     int any_gen3d;              // some 3D medium is isotropic, nonstationary or multi-resolution
                                 // (the general 3D evaluator, no 3D step skipping)
     uint32_t ctas_per_sm;       // fast-pass persistent grid: CTAs per SM (0: every resident CTA)
-    uint32_t prop_cap;          // most steps one evaluation skips before a proposed interval (0: 16)
+    uint32_t prop_cap;          // most steps one evaluation skips before a proposed interval (0: 32)
     uint32_t fast_window;       // stationary 1D fast pass: 0 impulse window in shared memory, 1 in registers
     uint32_t precise_only;      // 1: no certified resume pass (every crossing on the precise evaluator)
     const uint32_t *n_dev;      // may be null: the live flight count in device memory (<= n,

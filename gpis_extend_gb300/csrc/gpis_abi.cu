@@ -498,7 +498,7 @@ int submit_slice(gpis_ctx *ctx, const gpis_flight_soa *in, const gpis_result_soa
     a.proposal = reinterpret_cast<const float4 *>(proposal);
     a.n_dev = n_dev;
     a.ctas_per_sm = (uint32_t)ctx->tune[GPIS_TUNE_MARCH_CTAS_PER_SM];
-    a.prop_cap = ctx->tune[GPIS_TUNE_PROPOSED_SKIP_CAP] ? (uint32_t)ctx->tune[GPIS_TUNE_PROPOSED_SKIP_CAP] : 16u;
+    a.prop_cap = ctx->tune[GPIS_TUNE_PROPOSED_SKIP_CAP] ? (uint32_t)ctx->tune[GPIS_TUNE_PROPOSED_SKIP_CAP] : 32u;
     a.fast_window = (uint32_t)ctx->tune[GPIS_TUNE_FAST_WINDOW];
     a.precise_only = (uint32_t)ctx->tune[GPIS_TUNE_PRECISE_DECISIONS];
     a.origin_near = reinterpret_cast<const float4 *>(in->origin_near);

@@ -293,7 +293,7 @@ int gpis_nee_host(gpis_ctx *ctx, const gpis_nee_soa *in, float *out, uint32_t n)
                                             chunked copies                             */
 #define GPIS_TUNE_PROPOSED_SKIP_CAP 4u   /* gpis_flights_submit_proposed: the most steps
                                             one evaluation may skip before a flight's
-                                            proposed interval, 8..256 (default 16; every
+                                            proposed interval, 8..256 (default 32; every
                                             skipped step is still certified)            */
 #define GPIS_TUNE_FAST_WINDOW       5u   /* stationary 1D fast pass: 0 (default) keeps
                                             each lane's three-cell impulse window in
