@@ -1892,10 +1892,11 @@ struct EvalGeneric {
     }
 };
 
-// The resume pass of batches whose media all use 1D noise: the generic evaluator
-// compiled for 4 blocks of 256 per SM (64 registers, with spills), which hides the
-// precise evaluator's dependent float-float chains better than 2 blocks at 128
-// registers (15.93 against 16.57 ms per bench step; 3 blocks: 16.07).  3D media keep
+// The resume passes of batches whose media all use 1D noise: the generic evaluator
+// compiled for 4 blocks of 256 per SM (64 registers, with spills).  For the precise
+// pass that decides every crossing it hides the precise evaluator's dependent
+// float-float chains better than 2 blocks at 128 registers (15.93 against 16.57 ms
+// per bench step; 3 blocks: 16.07); the certified pass runs it too.  3D media keep
 // 2 blocks: their 27-cell evaluations spill too much at 64 registers.
 struct EvalGeneric4 : EvalGeneric {
     static constexpr int kMinBlocks = 4;
@@ -2100,12 +2101,12 @@ constexpr size_t kSmem1D = (size_t)3 * 8 * sizeof(float) * kC1Threads;
 template <int NMAX, bool GRID = false, bool NS = false, bool SM = false>
 struct EvalCoop1D {
     static constexpr bool kCollective = true;
-    // 4 CTAs per SM for the stationary analytic-mean kernel (64 registers, measured 2 %
-    // faster than 2 CTAs at 128 registers despite spills: its stalls are dependency
-    // waits that more warps hide; with the window in shared memory 4 CTAs at 64
-    // registers measured 17.06 against 17.27 ms per step for 3 CTAs at 80); the grid
-    // and nonstationary variants keep 2
-    static constexpr int kMinBlocks = (GRID || NS) ? 2 : 4;
+    // CTAs per SM for the stationary analytic-mean kernel: with the window in shared
+    // memory 3 (80 registers; 14.34 ms per bench step against 14.72 for 4 CTAs at 64
+    // registers, whose spills feed long-scoreboard stalls, and 15.44 for 2 at 128),
+    // with the window in registers 4 (64 registers, 2 % faster than 2 CTAs at 128
+    // despite spills); the grid and nonstationary variants keep 2
+    static constexpr int kMinBlocks = (GRID || NS) ? 2 : (SM ? 3 : 4);
     static constexpr bool kGeneral = NS;   // stationary, single octave, 1D otherwise
     static constexpr bool kSkip = !NS;
     float cache[SM ? 1 : 3][SM ? 1 : NMAX];
@@ -3713,10 +3714,12 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
         k_march<EvalGeneric4, true, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
         b.queue_in = 2;
     }
-    if (a.one_d) {
+    if (a.one_d && b.queue_in != 2) {
         const void *fn = (const void *)k_march<EvalGeneric4, true>;
         k_march<EvalGeneric4, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
     } else {
+        // 3D media, and what the certified pass leaves (a fifth of the crossings: 2
+        // CTAs at 128 registers without spills, 0.7 % faster per bench step than 4)
         const void *fn = (const void *)k_march<EvalGeneric, true>;
         k_march<EvalGeneric, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
     }
