@@ -742,7 +742,7 @@ def main():
             "frac": (achieved / peak) if peak else None, "traffic": traffic,
             "traffic_source": ((tr or {}).get("source", "") + "; DRAM bytes per flight of that capture times "
                                "the flights of one launch, not measured in this run") if traffic else None,
-            "kernel": "k_march<EvalCoop1D<8>> fast pass + k_march<EvalGeneric> resume pass",
+            "kernel": "k_march<EvalCoop1D<8>> fast pass + certified and precise resume passes",
             "march_ms_per_launch": march_ms,
             "kernel_ms_per_step": [k / max(1, args.steps) for k in kms],
             "flops_per_eval": roofline.flops_per_eval_1d(8),
@@ -755,10 +755,9 @@ def main():
                               "evaluation; the kernels regenerate "
                               f"{cnt['cell_refills'] / max(1.0, evals_march):.3f} cells per evaluation, so this "
                               "rate overstates the work executed; the utilisation is issue_active"},
-            # the fast pass's issue-slot utilisation and DRAM bytes per flight from the
-            # committed ncu capture (profiles/march_fast_pass_2p21.md), not measured here
-            "issue_active_ncu": {"fast_pass": 0.763, "resume_pass": 0.459,
-                                 "source": "profiles/march_fast_pass_2p21.md, march_resume_pass_2p21.md"}}
+            # the passes' issue-slot utilisation from the committed ncu capture, not
+            # measured here
+            "issue_active_ncu": dict((tr or {}).get("issue_active") or {}, source=(tr or {}).get("source"))}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -2702,7 +2702,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
     // step skipping (fast pass): the field's Lipschitz constant along this ray and
     // its truncation-jump allowance, fixed and per step
     float skip_lip = -1.0f, skip_j0 = 0.0f, skip_j1 = 0.0f;
-    bool t_direct = false;      // fast pass: skipped steps jump to t0 + k step (t_direct_ok)
+    bool t_direct = false;      // skipped steps jump to t0 + k step (t_direct_ok)
     float prop_a = -INFINITY;   // start of the proposed crossing interval (learned proposal)
     // certified pass: the bound on fac's distance from the reference's (cert_fac)
     float dfac = 0.0f;
@@ -2810,7 +2810,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                         skip_lip = -1.0f;
                         if (Eval::kSkip && !RESUME)
                             skip_params(m, d, L.sigma, L.cond, L.vs, L.gsz, step, skip_lip, skip_j0, skip_j1);
-                        t_direct = !RESUME && t_direct_ok(t0, step, far_t);
+                        t_direct = t_direct_ok(t0, step, far_t);
                         th = near_t;
                         tl = 0.0f;
                         steps = 0;
@@ -3016,7 +3016,7 @@ __global__ void __launch_bounds__(256, Eval::kMinBlocks) k_march(FlightArgs a)
                         skip = ev3.skips(f, step, kMaxSkip3D);
                     if (skip > 0) pf_precise = false;
                 }
-                if (!RESUME && t_direct && skip > 0 && steps + (uint32_t)skip < max_steps) {
+                if (t_direct && skip > 0 && steps + (uint32_t)skip < max_steps) {
                     // the skipped steps in one jump when it stays before farT (else step by step)
                     float nh, nl;
                     t_after(t0, step, steps + (uint32_t)skip, nh, nl);
@@ -3652,6 +3652,12 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     const bool coop_plain = a.one_d && a.max_imp <= 8 && a.max_oct == 1 && !a.any_ns && !a.all_grid && !a.any_mr;
     FlightArgs b = a;
     if (!coop_plain) b.setup = nullptr;     // the march kernels read set-up records only when written
+    // hand-off queues only with the certified pass: a precise pass that takes a queue
+    // loads its flights in the order they were saved, scattered, and measured slower
+    // than one that scans every resume record in flight order (the uneven image batch
+    // 512 against 496 ms)
+    const bool certify = coop_plain && !a.precise_only;
+    if (!certify) b.queue = nullptr;
     if (b.any_cond || b.setup) {
         if (a.one_d) k_prepare<8><<<blocks, 128, 0, stream>>>(b);
         else k_prepare<4><<<blocks, 128, 0, stream>>>(b);
@@ -3708,13 +3714,13 @@ cudaError_t launch_flights(const FlightArgs &a, int num_sms, cudaStream_t stream
     // the resume passes take the flights the pass before handed on (queue 1: the
     // fast pass's, 2: the certified pass's)
     b.queue_in = 1;
-    if (coop_plain && !a.precise_only) {
+    if (certify) {
         // crossings of stationary single-octave media decided on certified fast values
         const void *fn = (const void *)k_march<EvalGeneric4, true, true>;
         k_march<EvalGeneric4, true, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
         b.queue_in = 2;
     }
-    if (a.one_d && b.queue_in != 2) {
+    if (a.one_d && !certify) {
         const void *fn = (const void *)k_march<EvalGeneric4, true>;
         k_march<EvalGeneric4, true><<<grid(fn, 0, false), 256, 0, stream>>>(b);
     } else {
