@@ -367,7 +367,7 @@ int gpis_se_splat_1d(const float *queries, const float *centers, float *values,
  * cudaFree can), or a plugin host that owns all device memory and forbids
  * plugins to allocate.  The same flight kernels as gpis_flights_submit run on
  * one medium description (no grid mean), with all working memory in a fixed
- * array of this library (about 11 MB for GPIS_STATIC_MAX_FLIGHTS flights)
+ * array of this library (about 12 MB for GPIS_STATIC_MAX_FLIGHTS flights)
  * that every GPU which loads the library keeps until the process exits.  The
  * caller provides device flight and result streams as for gpis_flights_submit.
  * Larger batches fail with GPIS_ERANGE.  The first call on a device, with that
