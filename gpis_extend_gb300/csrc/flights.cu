@@ -28,6 +28,7 @@
 #include <cooperative_groups.h>
 
 #include "flights.cuh"
+#include "ffmath.cuh"
 
 namespace gpis {
 
@@ -386,19 +387,37 @@ __device__ __forceinline__ void normal_draws(uint32_t seed, int pair, float &z0,
 
 // Box-Muller as the reference evaluates it, in double (Gaussian.cpp:23-35; PI is
 // the float constant of Angle.hpp:8, so 2*PI is formed in float before it meets
-// the double u2): the pair of draws `pair` of the normal-seed stream.  One pair per
-// conditioned flight (its conditioning gradient), where the transverse draws enter
-// the along-ray coefficient through the rounding of the frame transforms.
-__device__ __forceinline__ void normal_draws_double(uint32_t seed, int pair, double &z0, double &z1)
+// the double u2), of the uniform draws u1f, u2f.  Out of line: normal_pair_scaled
+// takes it only when its float-float evaluation cannot decide the rounding.
+__device__ __noinline__ void normal_draws_double(float u1f, float u2f, double &z0, double &z1)
 {
-    const double u1 = (double)unit_float(pcg_draw(c_jump[2 + 2 * pair], seed));
-    const double u2 = (double)unit_float(pcg_draw(c_jump[3 + 2 * pair], seed));
+    const double u1 = (double)u1f;
+    const double u2 = (double)u2f;
     const double r = sqrt(-2.0 * log(1.0 - u1));
     const float two_pi = 2.0f * 3.1415926536f;
     double sn, cs;
     sincos((double)two_pi * u2, &sn, &cs);
     z0 = r * cs;
     z1 = r * sn;
+}
+
+// The pair of draws `pair` of the normal-seed stream as the reference's double
+// Box-Muller gives it, divided by sqrt(2)_f and by sc in double and rounded to
+// float (the conditioning gradient of a conditioned flight, where the transverse
+// draws enter the along-ray coefficient through the rounding of the frame
+// transforms): float-float with a test of the rounding (ffm_normal_pair), the
+// double evaluation for the draws it cannot decide (about 2e-4 of the pairs).
+__device__ __forceinline__ void normal_pair_scaled(uint32_t seed, int pair, float sc, float &g0, float &g1)
+{
+    const float u1 = unit_float(pcg_draw(c_jump[2 + 2 * pair], seed));
+    const float u2 = unit_float(pcg_draw(c_jump[3 + 2 * pair], seed));
+    if (ffm_normal_pair(u1, u2, sc, g0, g1)) return;
+    double z0, z1;
+    normal_draws_double(u1, u2, z0, z1);
+    const double s2 = 1.4142135381698608;   // (double)sqrtf(2.f)
+    const double xs = 1.0 / (double)sc;
+    g0 = (float)(z0 / s2 * xs);
+    g1 = (float)(z1 / s2 * xs);
 }
 
 // correlatedGradientMoments (SparseConvolutionNoise.cpp:13-22)
@@ -537,14 +556,12 @@ __device__ void noise_gradient_mr(const DevMedium &m, const FlightIn &fl, const 
             noise1d_precise_vd(m, z, fl.noise_seed + lv.seed[j], 1.0f, v[j], dv[j]);
         }
         value = __fadd_rn(__fmul_rn(lv.w[0], v[0]), __fmul_rn(lv.w[1], v[1]));
-        const double s2 = 1.4142135381698608;   // (double)sqrtf(2.f)
         float gw[2][3];
 #pragma unroll 1
         for (int j = 0; j < 2; ++j) {
-            double z0, z1;
-            normal_draws_double(fl.normal_seed, j, z0, z1);
-            const float gq[3] = {__fadd_rn((float)(z0 / s2 * 1.0), 0.0f), __fadd_rn((float)(z1 / s2 * 1.0), 0.0f),
-                                 __fadd_rn(0.0f, dv[j])};
+            float g0, g1;
+            normal_pair_scaled(fl.normal_seed, j, 1.0f, g0, g1);
+            const float gq[3] = {__fadd_rn(g0, 0.0f), __fadd_rn(g1, 0.0f), __fadd_rn(0.0f, dv[j])};
             Frame fj;
             ray_frame_level(m, fl.d, lv.s[j], fj);
 #pragma unroll
@@ -696,11 +713,8 @@ __device__ __forceinline__ void noise_gradient_oct(const DevMedium &m, const Fli
         // inverse length scales (evaluateGradientNoise1D, SparseConvolutionNoise.cpp:
         // 178-296; TangentFrame::toGlobal; transformGradLocaltoWorld)
         const float scx = splat_cov_1d(ls, ls);
-        const double xs = 1.0 / (double)scx;
-        double z0, z1;
-        normal_draws_double(nseed, 0, z0, z1);
-        const double s2 = 1.4142135381698608;   // (double)sqrtf(2.f)
-        const float gx0 = (float)(z0 / s2 * xs), gy0 = (float)(z1 / s2 * xs);
+        float gx0, gy0;
+        normal_pair_scaled(nseed, 0, scx, gx0, gy0);
         const float gq[3] = {__fadd_rn(gx0, gcx), __fadd_rn(gy0, gcy), __fadd_rn(0.0f, dv)};
         const float sdiv = m.ls_kind ? m.ls_max : 1.0f;
 #pragma unroll
